@@ -1,0 +1,127 @@
+// Shared device/host helpers for the JSCC OSEM kernels (sm_103a).
+//
+// Error model: every extern "C" entry point returns a jscc status code and
+// leaves a human-readable message in a thread-local buffer that
+// jscc_last_error() returns. No entry point allocates device memory: callers
+// pass outputs and a workspace sized by the matching *_workspace_bytes call.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <atomic>
+#include <cstdio>
+#include <cstdarg>
+
+#include "../../include/jscc_gb300.h"
+
+namespace jscc {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+std::atomic<unsigned long long>& launch_counter();
+
+#define JSCC_REQUIRE(cond, ...)                                   \
+  do {                                                            \
+    if (!(cond)) {                                                \
+      ::jscc::set_error(__VA_ARGS__);                             \
+      return JSCC_ERR_INVALID;                                    \
+    }                                                             \
+  } while (0)
+
+#define JSCC_CUDA_CHECK(expr)                                                  \
+  do {                                                                         \
+    cudaError_t _e = (expr);                                                   \
+    if (_e != cudaSuccess) {                                                   \
+      ::jscc::set_error("%s failed: %s (%s:%d)", #expr, cudaGetErrorString(_e), \
+                        __FILE__, __LINE__);                                   \
+      return JSCC_ERR_CUDA;                                                    \
+    }                                                                          \
+  } while (0)
+
+// Checks the launch just issued and counts it.
+#define JSCC_LAUNCH_CHECK()                                   \
+  do {                                                        \
+    ::jscc::launch_counter().fetch_add(1);                    \
+    JSCC_CUDA_CHECK(cudaGetLastError());                      \
+  } while (0)
+
+// Optional per-kernel timing with CUDA events recorded on the launch stream
+// (off by default; enabled by jscc_kernel_timing_enable for measurement runs,
+// never while a stream is being captured into a graph).
+bool timing_enabled();
+void timing_begin(cudaStream_t st);
+void timing_end(const char* name, cudaStream_t st);
+
+#define JSCC_TIMED(name, st, ...)                      \
+  do {                                                 \
+    const bool _t = ::jscc::timing_enabled();          \
+    if (_t) ::jscc::timing_begin(st);                  \
+    __VA_ARGS__;                                       \
+    if (_t) ::jscc::timing_end(name, st);              \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int num_sms();
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Carves aligned sub-buffers out of a caller-provided workspace.
+struct Carver {
+  char* base;
+  size_t cap;
+  size_t off = 0;
+  Carver(void* b, size_t c) : base(static_cast<char*>(b)), cap(c) {}
+  template <typename T>
+  T* take(size_t count) {
+    off = align_up(off, 256);
+    T* p = reinterpret_cast<T*>(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+  bool ok() const { return off <= cap; }
+};
+
+// ---------------------------------------------------------------- device helpers
+__device__ __forceinline__ float warp_sum(float v) {
+  // Fixed xor-butterfly: the same lanes combine in the same order on every call.
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Streaming 128-bit load that does not pollute L1 (data read once per pass).
+__device__ __forceinline__ float4 ld_stream_f4(const float* p) {
+  float4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ uint4 ld_stream_u4(const void* p) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u & 0xffff0000u); }
+
+// Element loaders used by the generic (unaligned / tail) paths.
+__device__ __forceinline__ float load_elem(const float* p, int64_t i) { return __ldg(p + i); }
+__device__ __forceinline__ float load_elem(const __nv_bfloat16* p, int64_t i) {
+  return __bfloat162float(p[i]);
+}
+
+}  // namespace jscc

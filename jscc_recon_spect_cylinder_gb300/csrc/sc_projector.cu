@@ -1,0 +1,489 @@
+// Single-photon (self-collimation, SC) projector: w += scale * sum_r P_r^-1 A^T (y_r / A P_r x).
+//
+// Reference semantics: recon_osem_plane.py:28-30 (get_weight_single) inside the
+// rotation loop of osem_bin_mode (recon_osem_plane.py:49-53); the clamped form of
+// recon_osem_local_cntstat.py:6-8.
+//
+// GB300 design
+//  * All rotations of one call share the subset matrix A, so the R rotated images
+//    are gathered once into X[R][V] and A is streamed once per pass for up to 8
+//    rotations (a skinny GEMM instead of R GEMVs).
+//  * Forward pass: CTA per row block, 128-bit streaming loads of A that bypass L1,
+//    X re-read from L1/L2, fixed-order CTA reduction, ratio epilogue fused.
+//  * Back pass: CTA per (1024-column tile x row chunk); each thread owns 4 (fp32)
+//    or 8 (bf16) adjacent columns and walks its rows in order; partial column sums
+//    go to the workspace.
+//  * Reduce pass: one thread per output voxel sums the chunk partials in chunk
+//    order, applies the inverse rotation gather and accumulates into `weight`.
+//  No float atomics anywhere: every sum has one fixed order, so results are
+//  bit-reproducible run to run.
+#include "jscc_common.cuh"
+
+namespace jscc {
+
+constexpr int kRotBlock = 8;          // rotations handled per pass over A
+constexpr int kColTile = 1024;        // columns per back-pass CTA
+constexpr int kTargetCtas = 1216;     // back-pass grid target (8 CTAs x 152 SMs)
+constexpr int kFwdThreads = 256;
+
+__device__ unsigned int g_bad_index_count = 0;  // out-of-range rotation indices seen
+
+// ------------------------------------------------------------------ gather
+__global__ void sc_gather_rot_kernel(const float* __restrict__ img, const int64_t* __restrict__ rotmat,
+                                     int64_t ld_rot, int r0, int nr, int64_t V, int64_t ldx,
+                                     float* __restrict__ xr) {
+  const int64_t total = (int64_t)nr * V;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / V);
+    const int64_t j = t - (int64_t)r * V;
+    int64_t src = j;
+    if (rotmat != nullptr) {
+      src = rotmat[j * ld_rot + r0 + r] - 1;
+      if (src < 0 || src >= V) {
+        atomicAdd(&g_bad_index_count, 1u);
+        xr[(int64_t)r * ldx + j] = 0.f;
+        continue;
+      }
+    }
+    xr[(int64_t)r * ldx + j] = img[src];
+  }
+}
+
+// ------------------------------------------------------------------ forward
+template <typename T>
+struct VecTraits;
+template <>
+struct VecTraits<float> {
+  static constexpr int kVec = 4;  // elements per 16-byte load
+};
+template <>
+struct VecTraits<__nv_bfloat16> {
+  static constexpr int kVec = 8;
+};
+
+template <typename T>
+__device__ __forceinline__ void load_vec(const T* p, float (&v)[VecTraits<T>::kVec]);
+
+template <>
+__device__ __forceinline__ void load_vec<float>(const float* p, float (&v)[4]) {
+  float4 a = ld_stream_f4(p);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+template <>
+__device__ __forceinline__ void load_vec<__nv_bfloat16>(const __nv_bfloat16* p, float (&v)[8]) {
+  uint4 u = ld_stream_u4(p);
+  v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x);
+  v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
+  v[4] = bf16_lo(u.z); v[5] = bf16_hi(u.z);
+  v[6] = bf16_lo(u.w); v[7] = bf16_hi(u.w);
+}
+
+// ratio[b][r] = proj[b, r0 + r] / f(b, r), f = A[b,:] . X[r,:]
+template <typename T, int ROWS, int RB, bool VEC>
+__global__ void __launch_bounds__(kFwdThreads)
+sc_forward_ratio_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx,
+                        int64_t n_bins, int64_t V, const float* __restrict__ xr, int64_t ldx, int nr,
+                        const float* __restrict__ proj, int64_t ld_proj, int r0, int use_floor,
+                        float floor_v, float* __restrict__ ratio) {
+  constexpr int NV = VecTraits<T>::kVec;
+  constexpr int NW = kFwdThreads / 32;
+  __shared__ float red[NW][ROWS * RB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t nblk = (n_bins + ROWS - 1) / ROWS;
+
+  for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int64_t b0 = blk * ROWS;
+    float acc[ROWS][RB];
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+      for (int r = 0; r < RB; ++r) acc[i][r] = 0.f;
+
+    const T* rowp[ROWS];
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i) {
+      int64_t b = b0 + i;
+      const int64_t bb = b < n_bins ? b : n_bins - 1;  // clamped; masked below
+      rowp[i] = A + (row_idx ? row_idx[bb] : bb) * lda;
+    }
+
+    int64_t tail_start = 0;
+    if (VEC) {
+      const int64_t nvec = V / NV;
+      tail_start = nvec * NV;
+#pragma unroll 2
+      for (int64_t v = tid; v < nvec; v += kFwdThreads) {
+        float a[ROWS][NV];
+#pragma unroll
+        for (int i = 0; i < ROWS; ++i) load_vec<T>(rowp[i] + v * NV, a[i]);
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+          if (r < nr) {
+            const float* xp = xr + (int64_t)r * ldx + v * NV;
+            float x[NV];
+#pragma unroll
+            for (int k = 0; k < NV; k += 4) {
+              float4 q = __ldg(reinterpret_cast<const float4*>(xp + k));
+              x[k] = q.x; x[k + 1] = q.y; x[k + 2] = q.z; x[k + 3] = q.w;
+            }
+#pragma unroll
+            for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+              for (int k = 0; k < NV; ++k) acc[i][r] = fmaf(a[i][k], x[k], acc[i][r]);
+          }
+        }
+      }
+    }
+    for (int64_t j = tail_start + tid; j < V; j += kFwdThreads) {
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        if (r < nr) {
+          const float x = __ldg(xr + (int64_t)r * ldx + j);
+#pragma unroll
+          for (int i = 0; i < ROWS; ++i) acc[i][r] = fmaf(load_elem(rowp[i], j), x, acc[i][r]);
+        }
+      }
+    }
+
+    // fixed-order CTA reduction
+#pragma unroll
+    for (int i = 0; i < ROWS; ++i)
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        float s = warp_sum(acc[i][r]);
+        if (lane == 0) red[warp][i * RB + r] = s;
+      }
+    __syncthreads();
+    if (tid < ROWS * RB) {
+      const int i = tid / RB, r = tid % RB;
+      const int64_t b = b0 + i;
+      if (b < n_bins && r < nr) {
+        float f = 0.f;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) f += red[w][tid];
+        if (use_floor) f = fmaxf(f, floor_v);
+        const int64_t pb = row_idx ? row_idx[b] : b;
+        ratio[b * RB + r] = proj[pb * ld_proj + r0 + r] / f;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ back (partials)
+// part[chunk][r][col] = sum_{b in chunk} A[b, col] * ratio[b][r]
+template <typename T, int RB, bool VEC>
+__global__ void __launch_bounds__(kColTile / VecTraits<T>::kVec)
+sc_back_partial_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx,
+                       int64_t n_bins, int64_t V,
+                       const float* __restrict__ ratio, int nr, int64_t rows_per_chunk,
+                       float* __restrict__ part, int64_t ldp) {
+  constexpr int NV = VecTraits<T>::kVec;
+  const int64_t col = (int64_t)blockIdx.x * kColTile + (int64_t)threadIdx.x * NV;
+  const int64_t b_begin = (int64_t)blockIdx.y * rows_per_chunk;
+  int64_t b_end = b_begin + rows_per_chunk;
+  if (b_end > n_bins) b_end = n_bins;
+  if (col >= V) return;
+  const bool full = VEC && (col + NV <= V);
+
+  float acc[RB][NV];
+#pragma unroll
+  for (int r = 0; r < RB; ++r)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[r][k] = 0.f;
+
+  if (full) {
+    int64_t b = b_begin;
+    for (; b + 4 <= b_end; b += 4) {
+      float a[4][NV];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        load_vec<T>(A + (row_idx ? row_idx[b + u] : b + u) * lda + col, a[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int r = 0; r < RB; ++r) {
+          if (r < nr) {
+            const float q = __ldg(ratio + (b + u) * RB + r);
+#pragma unroll
+            for (int k = 0; k < NV; ++k) acc[r][k] = fmaf(a[u][k], q, acc[r][k]);
+          }
+        }
+      }
+    }
+    for (; b < b_end; ++b) {
+      float a[NV];
+      load_vec<T>(A + (row_idx ? row_idx[b] : b) * lda + col, a);
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        if (r < nr) {
+          const float q = __ldg(ratio + b * RB + r);
+#pragma unroll
+          for (int k = 0; k < NV; ++k) acc[r][k] = fmaf(a[k], q, acc[r][k]);
+        }
+      }
+    }
+  } else {
+    const int ncol = (int)((V - col) < NV ? (V - col) : NV);
+    for (int64_t b = b_begin; b < b_end; ++b) {
+      const T* rowb = A + (row_idx ? row_idx[b] : b) * lda;
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        if (r < nr) {
+          const float q = __ldg(ratio + b * RB + r);
+#pragma unroll
+          for (int k = 0; k < NV; ++k)
+            if (k < ncol) acc[r][k] = fmaf(load_elem(rowb, col + k), q, acc[r][k]);
+        }
+      }
+    }
+  }
+
+  const int ncol = (int)((V - col) < NV ? (V - col) : NV);
+#pragma unroll
+  for (int r = 0; r < RB; ++r) {
+    if (r < nr) {
+      float* dst = part + ((int64_t)blockIdx.y * RB + r) * ldp + col;
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (k < ncol) dst[k] = acc[r][k];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ reduce + inverse rotation
+__global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
+                                         int nr, int rb_stride, const int64_t* __restrict__ rotinv,
+                                         int64_t ld_rot, int r0, int64_t V, int has_scale,
+                                         float scale, float* __restrict__ weight) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    float acc = weight[j];
+    for (int r = 0; r < nr; ++r) {
+      int64_t src = j;
+      if (rotinv != nullptr) {
+        src = rotinv[j * ld_rot + r0 + r] - 1;
+        if (src < 0 || src >= V) {
+          atomicAdd(&g_bad_index_count, 1u);
+          continue;
+        }
+      }
+      float s = 0.f;
+      for (int c = 0; c < chunks; ++c) s += part[((int64_t)c * rb_stride + r) * ldp + src];
+      acc = has_scale ? __fadd_rn(acc, __fmul_rn(scale, s)) : __fadd_rn(acc, s);
+    }
+    weight[j] = acc;
+  }
+}
+
+// ------------------------------------------------------------------ host planning
+struct ScPlan {
+  int rb;                  // rotation block (1, 2, 4, 8)
+  int64_t ldx;             // padded voxel stride of X / partials
+  int64_t col_tiles;
+  int64_t chunks;
+  int64_t rows_per_chunk;
+  size_t ws_bytes;
+};
+
+static int pow2_block(int n_rot) {
+  int rb = 1;
+  while (rb < n_rot && rb < kRotBlock) rb <<= 1;
+  return rb;
+}
+
+static ScPlan plan_sc(int64_t n_bins, int64_t V, int32_t n_rot) {
+  ScPlan p{};
+  p.rb = pow2_block(n_rot < 1 ? 1 : n_rot);
+  p.ldx = (int64_t)align_up((size_t)(V > 0 ? V : 1), 8);
+  p.col_tiles = (V + kColTile - 1) / kColTile;
+  if (p.col_tiles < 1) p.col_tiles = 1;
+  int64_t chunks = (kTargetCtas + p.col_tiles - 1) / p.col_tiles;
+  int64_t max_chunks = (n_bins + 15) / 16;  // at least 16 rows per chunk
+  if (max_chunks < 1) max_chunks = 1;
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks < 1) chunks = 1;
+  p.rows_per_chunk = (n_bins + chunks - 1) / chunks;
+  if (p.rows_per_chunk < 1) p.rows_per_chunk = 1;
+  p.chunks = (n_bins + p.rows_per_chunk - 1) / p.rows_per_chunk;
+  if (p.chunks < 1) p.chunks = 1;
+  size_t bytes = 0;
+  bytes += align_up((size_t)p.rb * p.ldx * sizeof(float), 256);                   // X
+  bytes += align_up((size_t)(n_bins > 0 ? n_bins : 1) * p.rb * sizeof(float), 256);  // ratio
+  bytes += align_up((size_t)p.chunks * p.rb * p.ldx * sizeof(float), 256);          // partials
+  p.ws_bytes = bytes + 256;
+  return p;
+}
+
+template <typename T, int RB>
+static int launch_sc_block(const T* A, int64_t lda, const int64_t* row_idx, int64_t n_bins, int64_t V,
+                           const float* proj,
+                           int64_t ld_proj, int64_t ld_rot, int r0, int nr, const int64_t* rotinv,
+                           int use_floor, float floor_v, int has_scale, float scale,
+                           float* weight, const ScPlan& p, float* xr, float* ratio, float* part,
+                           cudaStream_t st) {
+  constexpr int NV = VecTraits<T>::kVec;
+  const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) &&
+                      (reinterpret_cast<uintptr_t>(A) % 16 == 0);
+  const int sms = num_sms();
+  // forward: 2 rows per CTA for large problems, 1 row otherwise
+  {
+    const bool big = n_bins >= 4096;
+    const int rows = big ? 2 : 1;
+    int64_t nblk = (n_bins + rows - 1) / rows;
+    int64_t grid = nblk;
+    const int64_t cap = (int64_t)sms * 8;
+    if (grid > cap) grid = cap;
+    JSCC_TIMED("sc_forward_ratio", st, {
+      if (big) {
+        if (vec_ok)
+          sc_forward_ratio_kernel<T, 2, RB, true><<<(unsigned)grid, kFwdThreads, 0, st>>>(
+              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+        else
+          sc_forward_ratio_kernel<T, 2, RB, false><<<(unsigned)grid, kFwdThreads, 0, st>>>(
+              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+      } else {
+        if (vec_ok)
+          sc_forward_ratio_kernel<T, 1, RB, true><<<(unsigned)grid, kFwdThreads, 0, st>>>(
+              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+        else
+          sc_forward_ratio_kernel<T, 1, RB, false><<<(unsigned)grid, kFwdThreads, 0, st>>>(
+              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+      }
+    });
+    JSCC_LAUNCH_CHECK();
+  }
+  {
+    dim3 grid((unsigned)p.col_tiles, (unsigned)p.chunks);
+    const int threads = kColTile / NV;
+    JSCC_TIMED("sc_back_partial", st, {
+      if (vec_ok)
+        sc_back_partial_kernel<T, RB, true><<<grid, threads, 0, st>>>(
+            A, lda, row_idx, n_bins, V, ratio, nr, p.rows_per_chunk, part, p.ldx);
+      else
+        sc_back_partial_kernel<T, RB, false><<<grid, threads, 0, st>>>(
+            A, lda, row_idx, n_bins, V, ratio, nr, p.rows_per_chunk, part, p.ldx);
+    });
+    JSCC_LAUNCH_CHECK();
+  }
+  {
+    int64_t blocks = (V + 255) / 256;
+    if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+    if (blocks < 1) blocks = 1;
+    JSCC_TIMED("sc_reduce_scatter", st,
+               sc_reduce_scatter_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+                   part, p.ldx, (int)p.chunks, nr, RB, rotinv, ld_rot, r0, V, has_scale, scale,
+                   weight));
+    JSCC_LAUNCH_CHECK();
+  }
+  return JSCC_OK;
+}
+
+template <typename T>
+static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int64_t n_bins, int64_t V,
+                           const float* proj,
+                           int64_t ld_proj, int n_rot, const float* img, const int64_t* rotmat,
+                           const int64_t* rotinv, int64_t ld_rot, int use_floor, float floor_v, int has_scale,
+                           float scale, float* weight, const ScPlan& p, float* xr, float* ratio,
+                           float* part, cudaStream_t st) {
+  const int sms = num_sms();
+  for (int r0 = 0; r0 < n_rot; r0 += p.rb) {
+    const int nr = (n_rot - r0) < p.rb ? (n_rot - r0) : p.rb;
+    {
+      int64_t total = (int64_t)nr * V;
+      int64_t blocks = (total + 255) / 256;
+      if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+      if (blocks < 1) blocks = 1;
+      JSCC_TIMED("sc_gather_rot", st,
+                 sc_gather_rot_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, rotmat, ld_rot, r0, nr,
+                                                                        V, p.ldx, xr));
+      JSCC_LAUNCH_CHECK();
+    }
+    int rc;
+    switch (p.rb) {
+      case 1:
+        rc = launch_sc_block<T, 1>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
+                                   use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
+                                   st);
+        break;
+      case 2:
+        rc = launch_sc_block<T, 2>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
+                                   use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
+                                   st);
+        break;
+      case 4:
+        rc = launch_sc_block<T, 4>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
+                                   use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
+                                   st);
+        break;
+      default:
+        rc = launch_sc_block<T, 8>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
+                                   use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
+                                   st);
+        break;
+    }
+    if (rc != JSCC_OK) return rc;
+  }
+  return JSCC_OK;
+}
+
+}  // namespace jscc
+
+using namespace jscc;
+
+extern "C" {
+
+size_t jscc_sc_weight_workspace_bytes(int64_t n_bins, int64_t n_vox, int32_t n_rot) {
+  return plan_sc(n_bins, n_vox, n_rot).ws_bytes;
+}
+
+int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox,
+                   const float* proj, int64_t ld_proj, int32_t n_rot, const float* img,
+                   const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
+                   int32_t use_floor, float floor_v, float scale, float* weight, void* workspace,
+                   size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0, "jscc_sc_weight: negative size");
+  JSCC_REQUIRE(n_rot >= 1, "jscc_sc_weight: n_rot must be >= 1 (got %d)", n_rot);
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16,
+               "jscc_sc_weight: unsupported a_dtype %d", a_dtype);
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;  // nothing to add
+  JSCC_REQUIRE(A && proj && img && weight, "jscc_sc_weight: null pointer argument");
+  JSCC_REQUIRE(lda >= n_vox, "jscc_sc_weight: lda (%lld) < n_vox (%lld)", (long long)lda,
+               (long long)n_vox);
+  JSCC_REQUIRE(ld_proj >= n_rot, "jscc_sc_weight: ld_proj (%lld) < n_rot (%d)",
+               (long long)ld_proj, n_rot);
+  JSCC_REQUIRE((rotmat == nullptr && rotmat_inv == nullptr) || ld_rot >= n_rot,
+               "jscc_sc_weight: ld_rot (%lld) < n_rot (%d)", (long long)ld_rot, n_rot);
+  const ScPlan p = plan_sc(n_bins, n_vox, n_rot);
+  JSCC_REQUIRE(workspace != nullptr && workspace_bytes >= p.ws_bytes,
+               "jscc_sc_weight: workspace too small (%zu < %zu bytes)", workspace_bytes,
+               p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  float* xr = cv.take<float>((size_t)p.rb * p.ldx);
+  float* ratio = cv.take<float>((size_t)n_bins * p.rb);
+  float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  JSCC_REQUIRE(cv.ok(), "jscc_sc_weight: workspace carve overflow");
+  const int has_scale = scale != 1.0f;
+  cudaStream_t st = as_stream(stream);
+  if (a_dtype == JSCC_DTYPE_F32)
+    return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, proj,
+                                  ld_proj,
+                                  n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor, floor_v, has_scale,
+                                  scale, weight, p, xr, ratio, part, st);
+  return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins,
+                                        n_vox,
+                                        proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
+                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, st);
+}
+
+int jscc_take_bad_index_count(unsigned int* out) {
+  unsigned int h = 0, zero = 0;
+  JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_bad_index_count, sizeof(h)));
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_bad_index_count, &zero, sizeof(zero)));
+  if (out) *out = h;
+  return JSCC_OK;
+}
+
+}  // extern "C"

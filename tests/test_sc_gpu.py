@@ -1,0 +1,242 @@
+"""GPU parity of the SC projector (kernel b) and EM update against the oracle and the
+reference's golden outputs. Float32 path: rel-L2 <= 1e-5 (spec tolerance for the
+FP32 path); BF16-stored matrix: rel-L2 <= 1e-2 against the FP64 oracle after the
+stated iterations (BF16 storage error ~2^-9 per element, averaged by the projections)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import osem_sc
+
+pytestmark = pytest.mark.gpu
+
+TOL_F32 = 1e-5
+TOL_BF16 = 1e-2
+
+
+def _to(dev, *arrs, dtype=None):
+    out = []
+    for a in arrs:
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        if dtype is not None and t.is_floating_point():
+            t = t.to(dtype)
+        out.append(t.to(dev))
+    return out
+
+
+def test_get_weight_single_golden(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_local_cntstat as loc
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+    g = golden("sc_osem")
+    A, y = _to(cuda, g["A0"], g["y0"][:, :1])
+    x = torch.ones((A.size(1), 1), device=cuda)
+    assert rel_l2(rop.get_weight_single(A, y, x).cpu(), g["w_single"]) < TOL_F32
+    assert rel_l2(loc.get_weight_single(A, y, x).cpu(), g["w_single_local"]) < TOL_F32
+
+
+def test_osem_bin_mode_golden_two_energies(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+    g = golden("sc_osem")
+    S = int(g["n_subsets"])
+    perm = torch.from_numpy(g["perm"])
+    subsets = rop.split_tensor_even(perm, S, dim=0)
+    A0, A1, y0, y1, r0, r1, i0, i1, s = _to(cuda, g["A0"], g["A1"], g["y0"], g["y1"], g["rot0"], g["rot1"],
+                                            g["inv0"], g["inv1"], g["s"])
+    A_l = [[A0[ids.to(cuda)], A1[ids.to(cuda)]] for ids in subsets]
+    y_l = [[y0[ids.to(cuda)], y1[ids.to(cuda)]] for ids in subsets]
+    img = torch.ones((A0.size(1), 1), device=cuda)
+    img = rop.osem_bin_mode(A_l, y_l, [r0, r1], [i0, i1], img, s, r0.size(1))
+    assert rel_l2(img.cpu(), g["img_iter1"]) < TOL_F32
+    img = rop.osem_bin_mode(A_l, y_l, [r0, r1], [i0, i1], img, s, r0.size(1))
+    assert rel_l2(img.cpu(), g["img_iter2"]) < TOL_F32
+
+
+def test_local_bin_mode_replayed_permutations(cuda, golden):
+    """osem_bin_mode_local with the reference's CPU-generator permutations replayed."""
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_local_cntstat as loc
+
+    g = golden("sc_osem")
+    S = int(g["n_subsets"])
+    A, y, r, i, s = _to(cuda, g["A0"], g["y0"], g["rot0"], g["inv0"], g["s0"])
+    img = torch.ones((A.size(1), 1), device=cuda)
+    img_idx = img.clone()
+    for perm in g["local_perms"]:
+        chunks = list(torch.chunk(torch.from_numpy(perm).to(cuda), S, dim=0))
+        img = loc.osem_bin_mode_local([[A[c]] for c in chunks], [[y[c]] for c in chunks], [r], [i], img, s)
+        img_idx = loc.osem_bin_mode_local_indexed([A], [y], chunks, [r], [i], img_idx, s)
+    assert rel_l2(img.cpu(), g["local_img_iter2"]) < TOL_F32
+    # row-index form is bit-identical to the copied-subset form
+    assert torch.equal(img, img_idx)
+
+
+def test_config1_sc_osem_vs_fp64_oracle(cuda):
+    """Config-1 SC problem (40 x 120 grid, 1,024 pixels x 10 views, flat form),
+    10 subsets x 20 iterations, FP32 kernels vs FP64 oracle."""
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    prob = synthetic.sc_problem()
+    B, V = prob.sysmat.shape
+    assert (B, V) == (10240, 4800)
+    S, iters = 10, 20
+    torch.manual_seed(synthetic.SEED)
+    perm = torch.randperm(B)
+    subsets = rop.split_tensor_even(perm, S, dim=0)
+    A = prob.sysmat.to(cuda)
+    y = prob.proj.to(cuda)
+    A_l = [[A[ids.to(cuda)]] for ids in subsets]
+    y_l = [[y[ids.to(cuda)]] for ids in subsets]
+    rot, inv, s = prob.rotmat.to(cuda), prob.rotmat_inv.to(cuda), prob.s_map.to(cuda)
+    img = torch.ones((V, 1), device=cuda)
+    A_np, y_np = prob.sysmat.numpy(), prob.proj.numpy()
+    A_l_np = [[A_np[ids.numpy()]] for ids in subsets]
+    y_l_np = [[y_np[ids.numpy()]] for ids in subsets]
+    ref = np.ones((V, 1))
+    for _ in range(iters):
+        img = rop.osem_bin_mode(A_l, y_l, [rot], [inv], img, s, 1)
+        ref = osem_sc.osem_bin_mode(A_l_np, y_l_np, [prob.rotmat.numpy()], [prob.rotmat_inv.numpy()], ref,
+                                    prob.s_map.numpy(), 1)
+    err = rel_l2(img.cpu(), ref)
+    assert err < TOL_F32, err
+
+    # BF16-stored matrix, FP32 accumulation: stated tolerance against the FP64 oracle
+    A_bf = [[a[0].to(torch.bfloat16)] for a in A_l]
+    img_bf = torch.ones((V, 1), device=cuda)
+    for _ in range(iters):
+        img_bf = rop.osem_bin_mode(A_bf, y_l, [rot], [inv], img_bf, s, 1)
+    err_bf = rel_l2(img_bf.cpu(), ref)
+    assert err_bf < TOL_BF16, err_bf
+
+
+@pytest.mark.parametrize("views", [3, 4, 10])
+def test_rotated_form_multi_rotation_blocks(cuda, views):
+    """Rotation tables (cyclic per ring), R = 3 / 4 / 10 (10 > one rotation block of 8)."""
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    prob = synthetic.sc_problem(n_r=10, n_theta=60, n_phi=128, views=views, flat=False, total_counts=1e5)
+    A, y = prob.sysmat.to(cuda), prob.proj.to(cuda)
+    rot, inv, s = prob.rotmat.to(cuda), prob.rotmat_inv.to(cuda), prob.s_map.to(cuda)
+    img = rop.osem_bin_mode([[A]], [[y]], [rot], [inv], torch.ones((A.size(1), 1), device=cuda), s, views)
+    ref = osem_sc.osem_bin_mode([[prob.sysmat.numpy()]], [[prob.proj.numpy()]], [prob.rotmat.numpy()],
+                                [prob.rotmat_inv.numpy()], np.ones((A.size(1), 1)), prob.s_map.numpy(), views)
+    assert rel_l2(img.cpu(), ref) < TOL_F32
+
+
+@pytest.mark.parametrize("n_bins,n_vox", [(1, 1), (3, 5), (17, 1023), (33, 4097), (5000, 37)])
+def test_ragged_and_unaligned_shapes(cuda, n_bins, n_vox):
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    g = torch.Generator().manual_seed(n_bins * 7 + n_vox)
+    A = torch.rand((n_bins, n_vox), generator=g) + 0.01
+    y = torch.rand((n_bins, 1), generator=g) * 10
+    x = torch.rand((n_vox, 1), generator=g) + 0.1
+    ref = osem_sc.get_weight_single(A.numpy(), y.numpy(), x.numpy())
+    w = ops.sc_weight(A.to(cuda), y.to(cuda), x.to(cuda))
+    assert rel_l2(w.cpu(), ref) < TOL_F32
+    # leading dimension larger than the row (unaligned rows force the scalar path)
+    A_pad = torch.zeros((n_bins, n_vox + 3))
+    A_pad[:, :n_vox] = A
+    w2 = ops.sc_weight(A_pad.to(cuda)[:, :n_vox], y.to(cuda), x.to(cuda))
+    assert rel_l2(w2.cpu(), ref) < TOL_F32
+
+
+def test_deterministic_bitwise(cuda):
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    g = torch.Generator().manual_seed(5)
+    A = (torch.rand((3000, 5000), generator=g) + 0.01).to(cuda)
+    y = (torch.rand((3000, 1), generator=g) * 10).to(cuda)
+    x = (torch.rand((5000, 1), generator=g) + 0.1).to(cuda)
+    w1 = ops.sc_weight(A, y, x)
+    w2 = ops.sc_weight(A, y, x)
+    assert torch.equal(w1, w2)
+
+
+def test_em_update_golden(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    g = golden("dense_compton")
+    im, w, s = _to(cuda, g["safe_img"], g["safe_w"], g["safe_s"])
+    out = ops.em_update(im, w, s, safe=True)
+    np.testing.assert_array_equal(out.cpu().numpy(), g["safe_out"])
+    # plain update rounds exactly like (img * w) / s in float32
+    a = torch.rand(1000, 1, device=cuda)
+    b = torch.rand(1000, 1, device=cuda)
+    c = torch.rand(1000, 1, device=cuda) + 0.5
+    assert torch.equal(ops.em_update(a, b, c, safe=False), a * b / c)
+    assert torch.equal(ops.em_update(a, b, c, safe=False, coef=1.5, weight_b=c, coef_b=0.5),
+                       a * (1.5 * b + 0.5 * c) / c)
+
+
+def test_dense_compton_list_and_joint_golden(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+    g = golden("dense_compton")
+    S, D = int(g["n_subsets"]), int(g["n_divide"])
+    R = g["rot"].shape[1]
+    V = g["s"].shape[0]
+    t_all = [torch.from_numpy(g["t"][i]) for i in range(R)]
+    t_list = [[[[None] for _ in range(D)] for _ in range(R)] for _ in range(S)]
+    for i in range(R):
+        for j, ts in enumerate(rop.split_tensor_even(t_all[i], S, dim=0)):
+            for k, tk in enumerate(rop.split_tensor_even(ts, D, dim=0)):
+                # half the blocks stay in host memory, as the reference's pinned spill
+                t_list[j][i][k][0] = tk.to(cuda) if (i + j + k) % 2 == 0 else tk
+    rot, inv, s, s_d, A, y = _to(cuda, g["rot"], g["inv"], g["s"], g["s_d"], g["A"], g["y"])
+    img = rop.osem_list_mode(t_list, [rot], [inv], torch.ones((V, 1), device=cuda), s_d, R)
+    assert rel_l2(img.cpu(), g["img_list"]) < TOL_F32
+    subsets = rop.split_tensor_even(torch.arange(A.size(0)), S, dim=0)
+    A_l = [[A[ids.to(cuda)]] for ids in subsets]
+    y_l = [[y[ids.to(cuda)]] for ids in subsets]
+    img = rop.osem_joint_mode(A_l, y_l, t_list, [rot], [inv], torch.ones((V, 1), device=cuda),
+                              0.5 * s + 1.5 * s_d, 0.5, R)
+    assert rel_l2(img.cpu(), g["img_joint"]) < TOL_F32
+    w = rop.get_weight_compton(t_all[0], torch.ones((V, 1), device=cuda))
+    assert rel_l2(w.cpu(), g["w_compton"]) < TOL_F32
+
+
+def test_bad_rotation_index_is_counted_not_faulting(cuda):
+    """An out-of-range 1-based index is skipped by the kernel's own bounds check and
+    reported through jscc_take_bad_index_count."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops
+
+    V = 64
+    A = torch.rand((32, V), device=cuda) + 0.1
+    y = torch.rand((32, 1), device=cuda)
+    x = torch.rand((V, 1), device=cuda) + 0.1
+    rot = torch.arange(1, V + 1, device=cuda).unsqueeze(1)
+    bad = rot.clone()
+    bad[5, 0] = V + 10
+    bad[6, 0] = 0
+    _lib.take_bad_index_count()
+    ops.sc_weight(A, y, x, bad, rot)
+    torch.cuda.synchronize()
+    assert _lib.take_bad_index_count() == 2
+
+
+def test_full_size_invariant_config3_sc(cuda):
+    """Size-independent property at the config-3 SC size (81,920 x 36,000; fp32
+    11.8 GB): with positive projections, x . A^T(y / A x) = sum(y) exactly in real
+    arithmetic; float32 accumulation keeps it to ~1e-5."""
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    B, V = 81920, 36000
+    g = torch.Generator(device=cuda).manual_seed(3)
+    A = torch.rand((B, V), device=cuda, generator=g)
+    y = torch.rand((B, 1), device=cuda, generator=g) * 100
+    x = torch.rand((V, 1), device=cuda, generator=g) + 0.5
+    w = ops.sc_weight(A, y, x)
+    lhs = (x.double() * w.double()).sum().item()
+    rhs = y.double().sum().item()
+    assert abs(lhs - rhs) / rhs < 1e-5
+    del A
+    A16 = torch.rand((B, V), device=cuda, generator=g).to(torch.bfloat16)
+    w16 = ops.sc_weight(A16, y, x)
+    lhs16 = (x.double() * w16.double()).sum().item()
+    assert abs(lhs16 - rhs) / rhs < 1e-5
