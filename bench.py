@@ -63,7 +63,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (OSError, FileNotFoundError):
             self.proc = None
             return
@@ -118,6 +118,8 @@ class Sc3Workload:
 
     def __init__(self, device, n_r=100, n_theta=360, radius=100.0, det_radius=120.0, n_phi=128, n_axial=32,
                  axial_pitch=2.0, views=20, subsets=8, counts=1e7, seed=None):
+        if views != 20 or subsets != 8:
+            self.name = f"sc-channel-{views}views-{subsets}subsets"
         from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
         from jscc_recon_spect_cylinder_gb300 import synthetic
 
@@ -170,13 +172,21 @@ class Sc3Workload:
         rows = float(np.mean(self.rows_per_subset))
         mat = rows * self.V * b
         return {
-            "sc_forward_ratio": mat + self.V * 4 + rows * 8,   # A once, image, proj in + ratio out
-            "sc_back_partial": mat + rows * 4,                  # A once, ratio in
+            "sc_forward_split": mat + self.V * 4,   # A once + image
+            "sc_back_partial": mat + rows * 4,      # A once + ratio
         }
 
     def bytes_per_step(self, dtype):
         kb = self.kernel_bytes(dtype)
-        return self.subsets * (kb["sc_forward_ratio"] + kb["sc_back_partial"])
+        return self.subsets * (kb["sc_forward_split"] + kb["sc_back_partial"])
+
+
+def make_workload(name, dev):
+    if name == "sc3":
+        return Sc3Workload(dev)
+    if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
+        return Sc3Workload(dev, views=2, subsets=1)
+    raise ValueError(name)
 
 
 # ----------------------------------------------------------------------------- timing
@@ -303,7 +313,7 @@ def reference_arm(args):
     if rank != 0:
         return
     dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
-    work = Sc3Workload(dev)
+    work = make_workload(args.workload, dev)
     rates = []
     for i in range(args.warmup + args.steps):
         r = cpu_port_rate(work, budget_s=max(2.0, 20.0 / max(1, args.steps)))
@@ -332,7 +342,7 @@ def ours_arm(args):
     from jscc_recon_spect_cylinder_gb300 import _lib
 
     _lib.load()
-    work = Sc3Workload(dev)
+    work = make_workload(args.workload, dev)
     sampler = ClockSampler(local)
     sampler.start()
     ms_bf16, launches, img_bf16 = timed_steps(work, "bf16", args.steps, args.warmup, world)
@@ -369,6 +379,7 @@ def ours_arm(args):
             if not args.no_errors else None
         e2e = run_e2e(work, "bf16", 30) if not args.no_e2e else None
         cpu = cpu_port_rate(work) if (world == 1 and not args.no_cpu_baseline) else None
+        errors_iters = args.steps + args.warmup
         line = {
             "metric": "OSEM subset-iters/s: BF16-stored vs plain FP32 (SC channel of config 3), 1xGB300",
             "value": value, "unit": "subset-iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -380,6 +391,7 @@ def ours_arm(args):
             "fp32": {"value": value_f32, "ms_per_step": ms_f32 / args.steps},
             "speedup_bf16_vs_fp32": value / value_f32,
             "errors_vs_fp64": errors,
+            "errors_after_iterations": errors_iters,
             "gpu_launches": launches,
             "clocks": clocks,
             "roofline": roofline,
@@ -397,10 +409,10 @@ def ours_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sc3"], default="sc3")
+    ap.add_argument("--workload", choices=["sc3", "sc3-small"], default="sc3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")

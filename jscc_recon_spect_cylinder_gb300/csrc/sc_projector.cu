@@ -79,6 +79,33 @@ __device__ __forceinline__ void load_vec<__nv_bfloat16>(const __nv_bfloat16* p, 
   v[6] = bf16_lo(u.w); v[7] = bf16_hi(u.w);
 }
 
+// acc + sum_k a[k] * x[k] over one 16-byte vector of A held as raw bits.
+template <typename T>
+__device__ __forceinline__ float fma_raw(const uint4& u, const float* x, float acc);
+template <>
+__device__ __forceinline__ float fma_raw<float>(const uint4& u, const float* x, float acc) {
+  const float4 xv = *reinterpret_cast<const float4*>(x);
+  acc = fmaf(__uint_as_float(u.x), xv.x, acc);
+  acc = fmaf(__uint_as_float(u.y), xv.y, acc);
+  acc = fmaf(__uint_as_float(u.z), xv.z, acc);
+  acc = fmaf(__uint_as_float(u.w), xv.w, acc);
+  return acc;
+}
+template <>
+__device__ __forceinline__ float fma_raw<__nv_bfloat16>(const uint4& u, const float* x, float acc) {
+  const float4 x0 = *reinterpret_cast<const float4*>(x);
+  const float4 x1 = *reinterpret_cast<const float4*>(x + 4);
+  acc = fmaf(bf16_lo(u.x), x0.x, acc);
+  acc = fmaf(bf16_hi(u.x), x0.y, acc);
+  acc = fmaf(bf16_lo(u.y), x0.z, acc);
+  acc = fmaf(bf16_hi(u.y), x0.w, acc);
+  acc = fmaf(bf16_lo(u.z), x1.x, acc);
+  acc = fmaf(bf16_hi(u.z), x1.y, acc);
+  acc = fmaf(bf16_lo(u.w), x1.z, acc);
+  acc = fmaf(bf16_hi(u.w), x1.w, acc);
+  return acc;
+}
+
 // ratio[b][r] = proj[b, r0 + r] / f(b, r), f = A[b,:] . X[r,:]
 template <typename T, int ROWS, int RB, bool VEC>
 __global__ void __launch_bounds__(kFwdThreads)
@@ -168,6 +195,134 @@ sc_forward_ratio_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __r
       }
     }
     __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------ forward, balanced split
+// The subset matrix is viewed as n_bins x nvr vector units (nvr = ceil(V / NV)). Every
+// warp of the persistent grid owns one contiguous range of L units (the last warp
+// fewer), so all warps stream the same number of bytes. A range crosses at most a
+// few row boundaries; for each row piece the warp writes one partial dot product
+// per rotation to part[g][k][RB]. sc_finish_ratio_kernel sums a row's partials in
+// warp order. The rotated image(s) are staged in shared memory when they fit.
+template <typename T, int RB, bool VEC, bool SMEM_X, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+sc_forward_split_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx,
+                        int64_t n_bins, int64_t V, const float* __restrict__ xr, int64_t ldx_src,
+                        int64_t ldx, int nr, int64_t nvr, int64_t L, int maxp,
+                        float* __restrict__ part) {
+  constexpr int NV = VEC ? VecTraits<T>::kVec : 1;
+  constexpr int WARPS = THREADS / 32;
+  extern __shared__ float4 xs4[];
+  float* xs = reinterpret_cast<float*>(xs4);
+  const int lane = threadIdx.x & 31;
+  const int64_t g = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+  if (SMEM_X) {
+    for (int r = 0; r < nr; ++r)
+      for (int64_t i = threadIdx.x; i < V; i += THREADS) xs[(int64_t)r * ldx + i] = __ldg(xr + r * ldx_src + i);
+    __syncthreads();
+  } else {
+    ldx = ldx_src;
+  }
+  const float* xsrc = SMEM_X ? xs : xr;
+  const int64_t U = n_bins * nvr;
+  int64_t u = g * L;
+  const int64_t u_end = (u + L < U) ? u + L : U;
+  int64_t row = u < U ? u / nvr : 0;
+  int k = 0;
+  while (u < u_end) {
+    const int64_t row_end = (row + 1) * nvr;
+    const int64_t piece_end = row_end < u_end ? row_end : u_end;
+    const T* rowp = A + (row_idx ? row_idx[row] : row) * lda;
+    const int64_t ubase = row * nvr;
+    float acc[RB];
+#pragma unroll
+    for (int r = 0; r < RB; ++r) acc[r] = 0.f;
+    int64_t uu = u + lane;
+    if constexpr (VEC) {
+      // 4 independent 16-byte loads in flight per lane; raw registers, converted on use.
+      // Only whole vectors here (32-bit column arithmetic); the row's partial last
+      // vector, if any, is left to the loop below.
+      const int64_t full_end_u = ubase + V / NV;
+      const int64_t fe = piece_end < full_end_u ? piece_end : full_end_u;
+      if (uu + 96 < fe) {
+        const T* rp = rowp;
+        const float* xp0 = xsrc;
+        int col = (int)(uu - ubase) * NV;
+        const int n_iter = (int)((fe - uu - 96 + 127) / 128);
+        for (int it = 0; it < n_iter; ++it, col += 128 * NV) {
+          uint4 raw[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) raw[q] = ld_stream_u4(rp + col + 32 * NV * q);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int r = 0; r < RB; ++r)
+              if (r < nr) acc[r] = fma_raw<T>(raw[q], xp0 + (int64_t)r * ldx + col + 32 * NV * q, acc[r]);
+        }
+        uu += (int64_t)n_iter * 128;
+      }
+    }
+    for (; uu < piece_end; uu += 32) {
+      const int64_t col = (uu - ubase) * NV;
+      bool done = false;
+      if constexpr (VEC) {
+        if (col + NV <= V) {
+          float a[NV];
+          load_vec<T>(rowp + col, a);
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            if (r < nr) {
+              const float* xp = xsrc + (int64_t)r * ldx + col;
+#pragma unroll
+              for (int kk = 0; kk < NV; ++kk) acc[r] = fmaf(a[kk], xp[kk], acc[r]);
+            }
+          }
+          done = true;
+        }
+      }
+      if (!done) {
+        const int64_t cend = (col + NV < V) ? col + NV : V;
+        for (int64_t c = col; c < cend; ++c) {
+          const float av = load_elem(rowp, c);
+#pragma unroll
+          for (int r = 0; r < RB; ++r)
+            if (r < nr) acc[r] = fmaf(av, xsrc[(int64_t)r * ldx + c], acc[r]);
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RB; ++r) {
+      const float sum = warp_sum(acc[r]);
+      if (lane == 0) part[((g * maxp) + k) * RB + r] = sum;
+    }
+    ++k;
+    ++row;
+    u = piece_end;
+  }
+}
+
+// ratio[b][r] = proj[b, r0 + r] / f, f = sum of the row's partials in warp order.
+template <int RB>
+__global__ void sc_finish_ratio_kernel(const float* __restrict__ part, int64_t n_bins, int64_t nvr,
+                                       int64_t L, int maxp, const int64_t* __restrict__ row_idx,
+                                       const float* __restrict__ proj, int64_t ld_proj, int r0, int nr,
+                                       int use_floor, float floor_v, float* __restrict__ ratio) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_bins * RB;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / RB;
+    const int r = (int)(t % RB);
+    if (r >= nr) continue;
+    const int64_t g0 = (b * nvr) / L;
+    const int64_t g1 = ((b + 1) * nvr - 1) / L;
+    float f = 0.f;
+    for (int64_t g = g0; g <= g1; ++g) {
+      const int64_t first_row = (g * L) / nvr;
+      f += part[((g * maxp) + (b - first_row)) * RB + r];
+    }
+    if (use_floor) f = fmaxf(f, floor_v);
+    const int64_t pb = row_idx ? row_idx[b] : b;
+    ratio[b * RB + r] = proj[pb * ld_proj + r0 + r] / f;
   }
 }
 
@@ -281,9 +436,11 @@ __global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t
 struct ScPlan {
   int rb;                  // rotation block (1, 2, 4, 8)
   int64_t ldx;             // padded voxel stride of X / partials
-  int64_t col_tiles;
-  int64_t chunks;
+  int64_t col_tiles;       // back pass: 1024-column tiles
+  int64_t chunks;          // back pass: row chunks
   int64_t rows_per_chunk;
+  int64_t fwd_warps;       // forward pass: warps of the persistent grid (32 per SM)
+  int fwd_maxp;            // forward pass: row pieces per warp (upper bound)
   size_t ws_bytes;
 };
 
@@ -308,7 +465,10 @@ static ScPlan plan_sc(int64_t n_bins, int64_t V, int32_t n_rot) {
   if (p.rows_per_chunk < 1) p.rows_per_chunk = 1;
   p.chunks = (n_bins + p.rows_per_chunk - 1) / p.rows_per_chunk;
   if (p.chunks < 1) p.chunks = 1;
+  p.fwd_warps = (int64_t)num_sms() * 32;
+  p.fwd_maxp = (int)((n_bins + p.fwd_warps - 1) / p.fwd_warps) + 2;
   size_t bytes = 0;
+  bytes += align_up((size_t)p.fwd_warps * p.fwd_maxp * p.rb * sizeof(float), 256);  // fwd partials
   bytes += align_up((size_t)p.rb * p.ldx * sizeof(float), 256);                   // X
   bytes += align_up((size_t)(n_bins > 0 ? n_bins : 1) * p.rb * sizeof(float), 256);  // ratio
   bytes += align_up((size_t)p.chunks * p.rb * p.ldx * sizeof(float), 256);          // partials
@@ -322,36 +482,63 @@ static int launch_sc_block(const T* A, int64_t lda, const int64_t* row_idx, int6
                            int64_t ld_proj, int64_t ld_rot, int r0, int nr, const int64_t* rotinv,
                            int use_floor, float floor_v, int has_scale, float scale,
                            float* weight, const ScPlan& p, float* xr, float* ratio, float* part,
-                           cudaStream_t st) {
+                           float* fpart, const float* xsrc_direct, cudaStream_t st) {
   constexpr int NV = VecTraits<T>::kVec;
   const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) &&
                       (reinterpret_cast<uintptr_t>(A) % 16 == 0);
   const int sms = num_sms();
-  // forward: 2 rows per CTA for large problems, 1 row otherwise
+  // forward: balanced contiguous split over warps, then fixed-order row finish
   {
-    const bool big = n_bins >= 4096;
-    const int rows = big ? 2 : 1;
-    int64_t nblk = (n_bins + rows - 1) / rows;
-    int64_t grid = nblk;
-    const int64_t cap = (int64_t)sms * 8;
-    if (grid > cap) grid = cap;
-    JSCC_TIMED("sc_forward_ratio", st, {
-      if (big) {
-        if (vec_ok)
-          sc_forward_ratio_kernel<T, 2, RB, true><<<(unsigned)grid, kFwdThreads, 0, st>>>(
-              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
-        else
-          sc_forward_ratio_kernel<T, 2, RB, false><<<(unsigned)grid, kFwdThreads, 0, st>>>(
-              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+    constexpr int NVv = VecTraits<T>::kVec;
+    const int64_t nvr = vec_ok ? (V + NVv - 1) / NVv : V;
+    const int64_t U = n_bins * nvr;
+    const int64_t G = p.fwd_warps;
+    const int64_t L = (U + G - 1) / G;
+    const size_t xbytes = (size_t)nr * p.ldx * sizeof(float);
+    // identity rotation: read the image directly (no gather pass)
+    const bool direct = xsrc_direct != nullptr;
+    const float* xsrc = direct ? xsrc_direct : xr;
+    const int64_t xld = direct ? 0 : p.ldx;
+    const bool smem_x = RB <= 2 && xbytes <= 200 * 1024;
+    cudaError_t attr_err = cudaSuccess;
+    if (RB <= 2) {
+      const unsigned grid = (unsigned)(G / 32);
+      const size_t sh = smem_x ? xbytes : 0;
+      if (vec_ok && smem_x) {
+        attr_err = cudaFuncSetAttribute(sc_forward_split_kernel<T, RB, true, true, 1024>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+        JSCC_TIMED("sc_forward_split", st,
+                   sc_forward_split_kernel<T, RB, true, true, 1024><<<grid, 1024, sh, st>>>(
+                       A, lda, row_idx, n_bins, V, xsrc, xld, p.ldx, nr, nvr, L, p.fwd_maxp, fpart));
+      } else if (vec_ok) {
+        JSCC_TIMED("sc_forward_split", st,
+                   sc_forward_split_kernel<T, RB, true, false, 1024><<<grid, 1024, 0, st>>>(
+                       A, lda, row_idx, n_bins, V, xsrc, xld, p.ldx, nr, nvr, L, p.fwd_maxp, fpart));
       } else {
-        if (vec_ok)
-          sc_forward_ratio_kernel<T, 1, RB, true><<<(unsigned)grid, kFwdThreads, 0, st>>>(
-              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
-        else
-          sc_forward_ratio_kernel<T, 1, RB, false><<<(unsigned)grid, kFwdThreads, 0, st>>>(
-              A, lda, row_idx, n_bins, V, xr, p.ldx, nr, proj, ld_proj, r0, use_floor, floor_v, ratio);
+        JSCC_TIMED("sc_forward_split", st,
+                   sc_forward_split_kernel<T, RB, false, false, 1024><<<grid, 1024, 0, st>>>(
+                       A, lda, row_idx, n_bins, V, xsrc, xld, p.ldx, nr, nvr, L, p.fwd_maxp, fpart));
       }
-    });
+    } else {
+      const unsigned grid = (unsigned)(G / 8);
+      if (vec_ok)
+        JSCC_TIMED("sc_forward_split", st,
+                   sc_forward_split_kernel<T, RB, true, false, 256><<<grid, 256, 0, st>>>(
+                       A, lda, row_idx, n_bins, V, xsrc, xld, p.ldx, nr, nvr, L, p.fwd_maxp, fpart));
+      else
+        JSCC_TIMED("sc_forward_split", st,
+                   sc_forward_split_kernel<T, RB, false, false, 256><<<grid, 256, 0, st>>>(
+                       A, lda, row_idx, n_bins, V, xsrc, xld, p.ldx, nr, nvr, L, p.fwd_maxp, fpart));
+    }
+    JSCC_CUDA_CHECK(attr_err);
+    JSCC_LAUNCH_CHECK();
+    int64_t blocks = (n_bins * RB + 255) / 256;
+    if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+    if (blocks < 1) blocks = 1;
+    JSCC_TIMED("sc_finish_ratio", st,
+               sc_finish_ratio_kernel<RB><<<(unsigned)blocks, 256, 0, st>>>(
+                   fpart, n_bins, nvr, L, p.fwd_maxp, row_idx, proj, ld_proj, r0, nr, use_floor,
+                   floor_v, ratio));
     JSCC_LAUNCH_CHECK();
   }
   {
@@ -386,11 +573,14 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
                            int64_t ld_proj, int n_rot, const float* img, const int64_t* rotmat,
                            const int64_t* rotinv, int64_t ld_rot, int use_floor, float floor_v, int has_scale,
                            float scale, float* weight, const ScPlan& p, float* xr, float* ratio,
-                           float* part, cudaStream_t st) {
+                           float* part, float* fpart, cudaStream_t st) {
   const int sms = num_sms();
   for (int r0 = 0; r0 < n_rot; r0 += p.rb) {
     const int nr = (n_rot - r0) < p.rb ? (n_rot - r0) : p.rb;
-    {
+    const float* direct = nullptr;
+    if (rotmat == nullptr && nr == 1 && (reinterpret_cast<uintptr_t>(img) % 16 == 0)) {
+      direct = img;
+    } else {
       int64_t total = (int64_t)nr * V;
       int64_t blocks = (total + 255) / 256;
       if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
@@ -405,22 +595,22 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
       case 1:
         rc = launch_sc_block<T, 1>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   st);
+                                   fpart, direct, st);
         break;
       case 2:
         rc = launch_sc_block<T, 2>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   st);
+                                   fpart, direct, st);
         break;
       case 4:
         rc = launch_sc_block<T, 4>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   st);
+                                   fpart, direct, st);
         break;
       default:
         rc = launch_sc_block<T, 8>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   st);
+                                   fpart, direct, st);
         break;
     }
     if (rc != JSCC_OK) return rc;
@@ -464,6 +654,7 @@ int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* r
   float* xr = cv.take<float>((size_t)p.rb * p.ldx);
   float* ratio = cv.take<float>((size_t)n_bins * p.rb);
   float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  float* fpart = cv.take<float>((size_t)p.fwd_warps * p.fwd_maxp * p.rb);
   JSCC_REQUIRE(cv.ok(), "jscc_sc_weight: workspace carve overflow");
   const int has_scale = scale != 1.0f;
   cudaStream_t st = as_stream(stream);
@@ -471,11 +662,11 @@ int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* r
     return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, proj,
                                   ld_proj,
                                   n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor, floor_v, has_scale,
-                                  scale, weight, p, xr, ratio, part, st);
+                                  scale, weight, p, xr, ratio, part, fpart, st);
   return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins,
                                         n_vox,
                                         proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
-                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, st);
+                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st);
 }
 
 int jscc_take_bad_index_count(unsigned int* out) {

@@ -6,6 +6,8 @@ the reference: images are ``[V, 1]`` float32, rotation tables ``[V, R]`` int64
 """
 from __future__ import annotations
 
+import weakref
+
 import torch
 
 from . import _lib
@@ -32,6 +34,23 @@ def _f32_contig(t: torch.Tensor) -> torch.Tensor:
     return t.contiguous()
 
 
+_IDENTITY_CACHE: "weakref.WeakKeyDictionary[torch.Tensor, dict]" = weakref.WeakKeyDictionary()
+
+
+def _is_identity(t: torch.Tensor, rot_start: int, n_rot: int) -> bool:
+    """True when columns rot_start..rot_start+n_rot-1 of a 1-based table are all the
+    identity. Checked once per (table object, version, column range); the first
+    check synchronises the device, so call once before capturing a CUDA graph."""
+    per_table = _IDENTITY_CACHE.setdefault(t, {})
+    key = (t._version, rot_start, n_rot)
+    hit = per_table.get(key)
+    if hit is None:
+        ar = torch.arange(1, t.size(0) + 1, device=t.device, dtype=t.dtype).unsqueeze(1)
+        hit = bool((t[:, rot_start:rot_start + n_rot] == ar).all().item())
+        per_table[key] = hit
+    return hit
+
+
 def _index_table(t: torch.Tensor | None, n_vox: int, name: str) -> torch.Tensor | None:
     if t is None:
         return None
@@ -56,11 +75,14 @@ def sc_weight(
     scale: float = 1.0,
     out: torch.Tensor | None = None,
     row_idx: torch.Tensor | None = None,
+    proj_col: int | None = None,
 ) -> torch.Tensor:
     """``out += scale * sum_r rotinv_r( A^T (proj[:, r] / A rot_r(img)) )``.
 
     ``row_idx`` (int64, 0-based, on the device) restricts A and proj to those rows
-    without copying them; ids must be in range.
+    without copying them; ids must be in range. ``proj_col`` overrides the first
+    projection column used (default ``rot_start``), e.g. 0 for a single shared
+    column of ones in the dense-T Compton weight.
 
     Rotations ``r = rot_start .. rot_start + n_rot - 1`` use column ``r`` of
     ``proj``, ``rotmat`` and ``rotmat_inv`` (no copies are made). With ``rotmat``
@@ -97,7 +119,8 @@ def sc_weight(
             n_rot = rotmat.size(1) - rot_start
         if rot_start < 0 or n_rot < 1 or rot_start + n_rot > rotmat.size(1):
             raise ValueError(f"rotation range [{rot_start}, {rot_start + (n_rot or 0)}) out of range")
-    if rot_start + n_rot > p.size(1):
+    col0 = rot_start if proj_col is None else proj_col
+    if col0 < 0 or col0 + n_rot > p.size(1):
         raise ValueError("proj has fewer columns than the requested rotations")
     x = img.reshape(-1)
     if x.dtype != torch.float32 or not x.is_contiguous():
@@ -111,7 +134,7 @@ def sc_weight(
     lib = _lib.load()
     nbytes = lib.jscc_sc_weight_workspace_bytes(n_bins, n_vox, n_rot)
     ws = _lib.workspace.get(dev, nbytes)
-    p_ptr = p.data_ptr() + rot_start * p.element_size() * p.stride(1)
+    p_ptr = p.data_ptr() + col0 * p.element_size() * p.stride(1)
     rm_ptr = None if rotmat is None else rotmat.data_ptr() + rot_start * 8
     ri_ptr = None if rotmat_inv is None else rotmat_inv.data_ptr() + rot_start * 8
     if rotmat is not None and rotmat.stride(0) != rotmat_inv.stride(0):
@@ -119,6 +142,8 @@ def sc_weight(
         rotmat = rotmat.contiguous()
         rm_ptr = rotmat.data_ptr() + rot_start * 8
         ri_ptr = rotmat_inv.data_ptr() + rot_start * 8
+    if rotmat is not None and _is_identity(rotmat, rot_start, n_rot) and _is_identity(rotmat_inv, rot_start, n_rot):
+        rm_ptr = ri_ptr = None  # identity views: no gather / scatter passes
     ld_rot = 0 if rotmat is None else rotmat.stride(0)
     rc = lib.jscc_sc_weight(
         A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins, n_vox,

@@ -101,7 +101,7 @@ def _accumulate_compton_dense(weight, t_list, rotmat_all, rotmat_inv_all, img, r
                     continue
                 t_dev = t_tmp if t_tmp.device == img.device else t_tmp.to(img.device, non_blocking=True)
                 ops.sc_weight(t_dev, _ones_col(t_dev.size(0), img.device), img, rotmat, rotmat_inv,
-                              rot_start=i, n_rot=1, out=weight)
+                              rot_start=i, n_rot=1, out=weight, proj_col=0)
 
 
 def _apply_denoiser(img, model_denoiser):
