@@ -6,8 +6,6 @@ the reference: images are ``[V, 1]`` float32, rotation tables ``[V, R]`` int64
 """
 from __future__ import annotations
 
-import weakref
-
 import torch
 
 from . import _lib
@@ -34,14 +32,14 @@ def _f32_contig(t: torch.Tensor) -> torch.Tensor:
     return t.contiguous()
 
 
-_IDENTITY_CACHE: "weakref.WeakKeyDictionary[torch.Tensor, dict]" = weakref.WeakKeyDictionary()
-
-
 def _is_identity(t: torch.Tensor, rot_start: int, n_rot: int) -> bool:
     """True when columns rot_start..rot_start+n_rot-1 of a 1-based table are all the
     identity. Checked once per (table object, version, column range); the first
     check synchronises the device, so call once before capturing a CUDA graph."""
-    per_table = _IDENTITY_CACHE.setdefault(t, {})
+    per_table = getattr(t, "_jscc_identity", None)
+    if per_table is None:
+        per_table = {}
+        t._jscc_identity = per_table  # lives and dies with the table object
     key = (t._version, rot_start, n_rot)
     hit = per_table.get(key)
     if hit is None:
