@@ -112,6 +112,35 @@ JSCC_API int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const i
                    int32_t use_floor, float floor, float scale, float* weight, void* workspace,
                    size_t workspace_bytes, void* stream);
 
+/*
+ * jscc_sc_weight without a workspace: the same computation and arguments minus
+ * (workspace, workspace_bytes). No counterpart in the reference (its PyTorch code
+ * allocates freely); it exists for callers that cannot allocate device memory — a
+ * host framework that owns all GPU memory through its own pool and forbids
+ * allocations from plugins, a runtime reaching this library over a bare FFI with
+ * no device allocator, or a latency-critical loop that must avoid cudaMalloc's
+ * implicit synchronisation.
+ *
+ * Scratch lives in one fixed device array of JSCC_SC_NOALLOC_SCRATCH_BYTES (16 MiB)
+ * inside this library; every GPU that loads the library holds it until the process
+ * exits. Problems whose scratch need (jscc_sc_weight_workspace_bytes) exceeds it are
+ * rejected with JSCC_ERR_INVALID and a message; use jscc_sc_weight for those. The
+ * 16 MiB covers e.g. a 10,240-bin x 36,000-voxel subset block with one rotation
+ * (about 5 MiB); scratch grows with the rotations handled per pass (up to 8).
+ * The first call on each device looks up the array's device address (with that
+ * device current); make that first call before any stream capture. All calls share
+ * the one array, so calls that can overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. Nothing in the scratch needs
+ * clearing between calls: each call writes every scratch byte it later reads.
+ * Calls no cudaMalloc / cudaFree and no allocating library routine.
+ */
+#define JSCC_SC_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+JSCC_API int jscc_sc_weight_noalloc(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, const float* proj, int64_t ld_proj,
+                   int32_t n_rot, const float* img, const int64_t* rotmat,
+                   const int64_t* rotmat_inv, int64_t ld_rot, int32_t use_floor, float floor,
+                   float scale, float* weight, void* stream);
+
 /* ------------------------------------------------------------ EM update */
 
 #define JSCC_EM_PLAIN 0 /* img * w / s                         (recon_osem_plane.py:54, :73, :118) */

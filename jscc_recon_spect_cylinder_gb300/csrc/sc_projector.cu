@@ -19,6 +19,8 @@
 //  bit-reproducible run to run.
 #include "jscc_common.cuh"
 
+#include <mutex>
+
 namespace jscc {
 
 constexpr int kRotBlock = 8;          // rotations handled per pass over A
@@ -678,3 +680,98 @@ int jscc_take_bad_index_count(unsigned int* out) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// No-allocation variant of jscc_sc_weight.
+//
+// Some callers cannot hand this library a workspace: a host framework that owns all
+// device memory through its own pool and forbids allocations from plugins, a language
+// runtime driving the library through a bare FFI without any device allocator, or a
+// latency-critical loop that must not pay cudaMalloc's implicit synchronisation. For
+// them the scratch of the SC weight lives in one fixed file-scope device array,
+// allocated when the library's device code is loaded on a GPU and held until the
+// process exits.
+//
+// The array's name is only a host-side stand-in in host code: its device address is
+// obtained once per device with cudaGetSymbolAddress (the first call on each device
+// does this, with that device current) and that address is what the kernels get.
+// Every call shares the one array: calls that may overlap on the GPU (different
+// streams, or concurrent host threads) race on it and must be serialised by the
+// caller. No byte of the scratch needs to start at zero: each call writes every
+// scratch element before it reads it.
+// ============================================================================
+
+namespace jscc {
+
+static __device__ __align__(256) unsigned char g_sc_noalloc_scratch[JSCC_SC_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch_address(void** out) {
+  int dev = -1;
+  JSCC_CUDA_CHECK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("jscc_sc_weight_noalloc: device ordinal %d outside the supported range", dev);
+    return JSCC_ERR_INVALID;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_sc_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error("jscc_sc_weight_noalloc: cudaGetSymbolAddress of the scratch array failed on device %d: %s",
+                dev, cudaGetErrorString(e));
+      return JSCC_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return JSCC_OK;
+}
+
+}  // namespace jscc
+
+extern "C" int jscc_sc_weight_noalloc(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                                      int64_t n_bins, int64_t n_vox, const float* proj, int64_t ld_proj,
+                                      int32_t n_rot, const float* img, const int64_t* rotmat,
+                                      const int64_t* rotmat_inv, int64_t ld_rot, int32_t use_floor,
+                                      float floor_v, float scale, float* weight, void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0, "jscc_sc_weight_noalloc: negative size");
+  JSCC_REQUIRE(n_rot >= 1, "jscc_sc_weight_noalloc: n_rot must be >= 1 (got %d)", n_rot);
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16,
+               "jscc_sc_weight_noalloc: unsupported a_dtype %d", a_dtype);
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(A && proj && img && weight, "jscc_sc_weight_noalloc: null pointer argument");
+  JSCC_REQUIRE(lda >= n_vox, "jscc_sc_weight_noalloc: lda (%lld) < n_vox (%lld)", (long long)lda,
+               (long long)n_vox);
+  JSCC_REQUIRE(ld_proj >= n_rot, "jscc_sc_weight_noalloc: ld_proj (%lld) < n_rot (%d)",
+               (long long)ld_proj, n_rot);
+  JSCC_REQUIRE((rotmat == nullptr && rotmat_inv == nullptr) || ld_rot >= n_rot,
+               "jscc_sc_weight_noalloc: ld_rot (%lld) < n_rot (%d)", (long long)ld_rot, n_rot);
+  const ScPlan p = plan_sc(n_bins, n_vox, n_rot);
+  JSCC_REQUIRE(p.ws_bytes <= (size_t)JSCC_SC_NOALLOC_SCRATCH_BYTES,
+               "jscc_sc_weight_noalloc: this problem (%lld bins x %lld voxels, %d rotations) needs %zu "
+               "bytes of scratch but the fixed scratch array holds %zu bytes; call jscc_sc_weight with a "
+               "caller-provided workspace instead",
+               (long long)n_bins, (long long)n_vox, n_rot, p.ws_bytes,
+               (size_t)JSCC_SC_NOALLOC_SCRATCH_BYTES);
+  void* scratch = nullptr;
+  const int rc = noalloc_scratch_address(&scratch);
+  if (rc != JSCC_OK) return rc;
+  Carver cv(scratch, (size_t)JSCC_SC_NOALLOC_SCRATCH_BYTES);
+  float* xr = cv.take<float>((size_t)p.rb * p.ldx);
+  float* ratio = cv.take<float>((size_t)n_bins * p.rb);
+  float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  float* fpart = cv.take<float>((size_t)p.fwd_warps * p.fwd_maxp * p.rb);
+  JSCC_REQUIRE(cv.ok(), "jscc_sc_weight_noalloc: scratch carve overflow");
+  const int has_scale = scale != 1.0f;
+  cudaStream_t st = as_stream(stream);
+  if (a_dtype == JSCC_DTYPE_F32)
+    return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, proj, ld_proj,
+                                  n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor, floor_v, has_scale, scale,
+                                  weight, p, xr, ratio, part, fpart, st);
+  return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox,
+                                        proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
+                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st);
+}
