@@ -131,9 +131,164 @@ def golden_dense_compton(ref):
          safe_out=_np(safe))
 
 
+# ----------------------------------------------------------------------------- Compton
+def _planar_detector_subset(ref_dir: Path, per_layer=48, seed=5):
+    """A subset of the shipped 4-layer planar detector (Factors/511keV_RotateNum10/Detector.csv):
+    `per_layer` pixels from each |y| layer, so the strict crystal-variance branch applies."""
+    det = np.genfromtxt(ref_dir / "Factors" / "511keV_RotateNum10" / "Detector.csv", delimiter=",",
+                        dtype=np.float32)[:, 1:4]
+    rng = np.random.default_rng(seed)
+    layers = np.unique(np.abs(det[:, 1]))
+    pick = []
+    for y in layers:
+        ids = np.nonzero(np.abs(det[:, 1]) == y)[0]
+        pick.append(rng.choice(ids, per_layer, replace=False))
+    return det[np.sort(np.concatenate(pick))]
+
+
+def _cylinder_detector(n_phi=24, n_axial=2):
+    scat = synthetic.cylinder_pixels(120.0, n_phi, n_axial, 4.0).float().numpy()
+    absb = synthetic.cylinder_pixels(150.0, n_phi, n_axial, 4.0).float().numpy()
+    return np.concatenate((scat, absb), axis=0).astype(np.float32), scat.shape[0]
+
+
+def _events(det, n_front, E, e0, seed):
+    """Seeded list (cp1, e1, cp2, e2), 1-based ids: first hit among the first n_front
+    detectors, second hit among the rest; e1 from a Compton-like spread."""
+    rng = np.random.default_rng(seed)
+    cp1 = rng.integers(1, n_front + 1, E)
+    cp2 = rng.integers(n_front + 1, det.shape[0] + 1, E)
+    e1 = rng.uniform(0.06, 0.9 * (2 * e0 ** 2 / (0.511 + 2 * e0)), E)
+    e2 = e0 - e1
+    return np.stack((cp1, e1, cp2, e2), axis=1).astype(np.float32)
+
+
+def golden_compton(ref):
+    """Strict and legacy T builders on (a) a 4-layer planar detector subset of the shipped
+    geometry and (b) a cylinder detector (isotropic-fallback sigma_pos)."""
+    strict = ref["process_list_plane_strict"]
+    legacy = ref["process_list_plane"]
+    out = {}
+    grid = synthetic.polar_grid(8, 24, 20.0)
+    coor = grid.coor.numpy()
+    for tag, (det, n_front), e0, dr in (
+        ("planar", (_planar_detector_subset(REF_DIR), 96), 0.511, 0.0),
+        ("cyl", _cylinder_detector(), 0.662, 0.5),
+    ):
+        g = torch.Generator().manual_seed(11)
+        sysmat = (torch.rand((det.shape[0], coor.shape[0]), generator=g) * 1e-3).numpy()
+        lst = _events(det, n_front, 160, e0, seed=len(tag))
+        res = 0.1 * (0.662 / e0) ** 0.5
+        tmax = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
+        args = (dr, dr, e0, res, tmax, 0.05, e0 - 0.06)
+        torch.manual_seed(77)
+        L = torch.from_numpy(lst.copy())
+        with torch.no_grad():
+            t, tc, ts = strict.get_compton_backproj_list_single(torch.from_numpy(sysmat), torch.from_numpy(det),
+                                                                torch.from_numpy(coor), L, *args, "cpu")
+        smeared = L.numpy().copy()  # the strict builder smears the caller's list in place
+        torch.manual_seed(77)
+        n1 = torch.randn(lst.shape[0]).numpy()
+        n2 = torch.randn(lst.shape[0]).numpy()
+        torch.manual_seed(78)
+        L2 = torch.from_numpy(lst.copy())
+        with torch.no_grad():
+            lt, ltc, lts = legacy.get_compton_backproj_list_single(torch.from_numpy(sysmat), torch.from_numpy(det),
+                                                                   torch.from_numpy(coor), L2, 1.0 + dr, 1.0 + dr,
+                                                                   e0, res, tmax, 0.05, e0 - 0.06, "cpu")
+        out.update({f"{tag}_det": det, f"{tag}_sysmat": sysmat, f"{tag}_list": lst, f"{tag}_smeared": smeared,
+                    f"{tag}_noise1": n1, f"{tag}_noise2": n2, f"{tag}_args": np.array(args),
+                    f"{tag}_t": t.numpy(), f"{tag}_tc": tc.numpy(), f"{tag}_ts": ts.numpy(),
+                    f"{tag}_legacy_smeared": L2.numpy().copy(), f"{tag}_legacy_t": lt.numpy(),
+                    f"{tag}_legacy_tc": ltc.numpy(), f"{tag}_legacy_ts": lts.numpy()})
+    save("compton_builders", coor=coor, **out)
+
+
+def golden_sparse(ref):
+    """Sparse projector on the shipped 511keV_RotateNum10 grid and on a small synthetic grid
+    (stride reduction), its operators, the sparse builder and both sparse weights."""
+    cso = ref["compton_sparse_ops"]
+    rsp = ref["recon_osem_plane_sparse"]
+    loc = ref["recon_osem_local_sparse_jsccsd_only"]
+    psp = ref["process_list_plane_sparse"]
+    out = {}
+    coor_r10 = torch.from_numpy(np.genfromtxt(REF_DIR / "Factors" / "511keV_RotateNum10" / "coor_polar_full.csv",
+                                              delimiter=",", dtype=np.float32))
+    p10 = cso.build_compton_sparse_projector(coor_r10, theta_stride=2, z_stride=2, rotate_num=10)
+    g = torch.Generator().manual_seed(3)
+    rows = torch.rand((3, p10.coarse_pixel_num), generator=g)
+    frows = torch.rand((3, p10.fine_pixel_num), generator=g)
+    img_f = torch.rand((p10.fine_pixel_num, 1), generator=g)
+    img_c = torch.rand((p10.coarse_pixel_num, 1), generator=g)
+    for name in ("layer_reduce", "layer_expand", "z_reduce", "z_expand"):
+        m = getattr(p10, name).numpy()
+        nz = np.nonzero(m)
+        out[f"r10_{name}_idx"] = np.stack(nz).astype(np.int32)
+        out[f"r10_{name}_val"] = m[nz]
+        out[f"r10_{name}_shape"] = np.array(m.shape)
+    out.update({
+        "r10_coor_full": coor_r10.numpy(), "r10_coor_coarse": p10.coor_coarse.numpy(),
+        "r10_ring_strides": np.array(p10.ring_strides),
+        "r10_dims": np.array([p10.fine_layer_num, p10.fine_z_num, p10.coarse_layer_num, p10.coarse_z_num]),
+        "r10_rows_c": rows.numpy(), "r10_rows_f": frows.numpy(), "r10_img_f": img_f.numpy(),
+        "r10_img_c": img_c.numpy(),
+        "r10_up": cso.upsample_coarse_rows_to_fine(rows, p10).numpy(),
+        "r10_adj": cso.project_fine_rows_to_coarse_adjoint(frows, p10).numpy(),
+        "r10_red": cso.reduce_fine_rows_to_coarse(frows, p10).numpy(),
+        "r10_img_red": cso.reduce_fine_image_to_coarse(img_f, p10).numpy(),
+        "r10_img_up": cso.upsample_coarse_weight_to_fine(img_c, p10).numpy(),
+    })
+    # small synthetic grid: 6 rings x 24 theta x 4 z planes; theta stride 4 with 4 views -> 3
+    planes = [synthetic.polar_grid(6, 24, 20.0, z=z).coor for z in (-6.0, -2.0, 2.0, 6.0)]
+    coor = torch.cat(planes, dim=0)
+    p = cso.build_compton_sparse_projector(coor, theta_stride=4, z_stride=2, rotate_num=4)
+    det, n_front = _planar_detector_subset(REF_DIR, per_layer=32, seed=9), 64
+    e0 = 0.511
+    sysmat = (torch.rand((det.shape[0], coor.shape[0]), generator=g) * 1e-3)
+    lst = _events(det, n_front, 200, e0, seed=21)
+    res = 0.1 * (0.662 / e0) ** 0.5
+    tmax = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
+    args = (0.0, 0.0, e0, res, tmax, 0.05, e0 - 0.06)
+    torch.manual_seed(91)
+    with torch.no_grad():
+        ev_rows, _, _ = psp.get_compton_backproj_list_single_sparse(sysmat, torch.from_numpy(det), p,
+                                                                     torch.from_numpy(lst.copy()), *args, "cpu")
+    torch.manual_seed(91)
+    n1 = torch.randn(lst.shape[0])
+    n2 = torch.randn(lst.shape[0])
+    # the smeared list exactly as the sparse builder forms it on CPU (same torch expression,
+    # process_list_plane_sparse.py:45-48), so tests can feed it to the inner builder
+    Lt = torch.from_numpy(lst.copy())
+    e1s = Lt[:, 1] + (Lt[:, 1] * res / 2.355 * (e0 / Lt[:, 1]) ** 0.5) * n1
+    e2s = Lt[:, 3] + (Lt[:, 3] * res / 2.355 * (e0 / Lt[:, 3]) ** 0.5) * n2
+    smeared = lst.copy()
+    smeared[:, 1] = e1s.numpy()
+    smeared[:, 3] = e2s.numpy()
+    n1, n2 = n1.numpy(), n2.numpy()
+    x = torch.rand((coor.shape[0], 1), generator=g) + 0.2
+    with torch.no_grad():
+        t_fine, valid = cso.materialize_sparse_event_rows_to_fine(ev_rows, sysmat, p)
+        w_grouped = rsp.get_weight_compton_sparse(ev_rows, sysmat, x, p)
+        w_mat = loc.get_weight_compton_sparse(ev_rows, sysmat, x, p)
+    out.update({
+        "s_coor": coor.numpy(), "s_coor_coarse": p.coor_coarse.numpy(), "s_ring_strides": np.array(p.ring_strides),
+        "s_dims": np.array([p.fine_layer_num, p.fine_z_num, p.coarse_layer_num, p.coarse_z_num]),
+        "s_layer_expand": p.layer_expand.numpy(), "s_z_expand": p.z_expand.numpy(),
+        "s_layer_reduce": p.layer_reduce.numpy(), "s_z_reduce": p.z_reduce.numpy(),
+        "s_det": det, "s_sysmat": sysmat.numpy(), "s_list": lst, "s_smeared": smeared, "s_noise1": n1,
+        "s_noise2": n2,
+        "s_args": np.array(args), "s_event_rows": ev_rows.numpy(), "s_x": x.numpy(),
+        "s_t_fine": t_fine.numpy(), "s_valid": valid.numpy(), "s_w_grouped": w_grouped.numpy(),
+        "s_w_mat": w_mat.numpy(),
+    })
+    save("sparse_ops", **out)
+
+
 GENERATORS = {
     "sc_osem": golden_sc,
     "dense_compton": golden_dense_compton,
+    "compton_builders": golden_compton,
+    "sparse_ops": golden_sparse,
 }
 
 
@@ -149,11 +304,16 @@ def load_reference(ref_dir: Path):
     return mods
 
 
+REF_DIR = Path("/root/reference")
+
+
 def main():
+    global REF_DIR
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=str(REF_DIR))
     ap.add_argument("--only", nargs="*")
     args = ap.parse_args()
+    REF_DIR = Path(args.ref)
     torch.set_num_threads(1)
     ref = load_reference(Path(args.ref))
     for name, fn in GENERATORS.items():

@@ -88,3 +88,119 @@ def test_safe_em_update_matches_reference(golden):
     g = golden("dense_compton")
     out = osem_sc.safe_em_update(g["safe_img"], g["safe_w"], g["safe_s"])
     np.testing.assert_allclose(out, g["safe_out"], rtol=1e-7, atol=0)
+
+
+# ----------------------------------------------------------------------------- Compton builders
+from oracle import compton as oc  # noqa: E402
+from oracle import sparse as osp  # noqa: E402
+
+
+def test_smearing_replays_reference(golden):
+    g = golden("compton_builders")
+    for tag in ("planar", "cyl"):
+        a = g[f"{tag}_args"]
+        e0, res = float(a[2]), float(a[3])
+        L = g[f"{tag}_list"]
+        e1 = oc.smear_energies(L[:, 1], g[f"{tag}_noise1"], e0, res)
+        e2 = oc.smear_energies(L[:, 3], g[f"{tag}_noise2"], e0, res)
+        np.testing.assert_allclose(e1, g[f"{tag}_smeared"][:, 1], rtol=2.5e-7, atol=0)
+        np.testing.assert_allclose(e2, g[f"{tag}_smeared"][:, 3], rtol=2.5e-7, atol=0)
+
+
+def _rows_close(a, b, rtol):
+    assert a.shape == b.shape, (a.shape, b.shape)
+    scale = np.maximum(np.abs(b).max(axis=1, keepdims=True), 1e-30)
+    err = np.abs(a - b) / scale
+    assert err.max() < rtol, err.max()
+
+
+def test_strict_builder_matches_reference(golden):
+    g = golden("compton_builders")
+    for tag in ("planar", "cyl"):
+        a = g[f"{tag}_args"]
+        dr1, dr2, e0, res, tmax, tmin, tsum = [float(v) for v in a]
+        for dtype, tol in ((np.float32, 2e-5), (np.float64, 2e-4)):
+            t, tc, ts, kept = oc.strict_builder(g[f"{tag}_sysmat"], g[f"{tag}_det"], g["coor"], g[f"{tag}_smeared"],
+                                                dr1, dr2, e0, res, tmax, tmin, tsum, dtype=dtype)
+            _rows_close(t, g[f"{tag}_t"], tol)
+            _rows_close(tc, g[f"{tag}_tc"], tol)
+            _rows_close(ts, g[f"{tag}_ts"], 1e-6)
+
+
+def test_legacy_builder_matches_reference(golden):
+    g = golden("compton_builders")
+    for tag in ("planar", "cyl"):
+        a = g[f"{tag}_args"]
+        dr, e0, res, tmax, tmin, tsum = 1.0 + float(a[0]), float(a[2]), float(a[3]), float(a[4]), float(a[5]), \
+            float(a[6])
+        t, tc, ts, _ = oc.legacy_builder(g[f"{tag}_sysmat"], g[f"{tag}_det"], g["coor"], g[f"{tag}_legacy_smeared"],
+                                         dr, dr, e0, res, tmax, tmin, tsum, dtype=np.float32)
+        # the legacy sigma formulas (atan, 1/sin theta derivatives, no clamps) amplify
+        # float32 rounding more than the strict ones
+        _rows_close(t, g[f"{tag}_legacy_t"], 1e-4)
+        _rows_close(tc, g[f"{tag}_legacy_tc"], 1e-4)
+
+
+# ----------------------------------------------------------------------------- sparse projector
+def _dense_from(g, name):
+    shape = tuple(g[f"r10_{name}_shape"])
+    m = np.zeros(shape, np.float32)
+    i = g[f"r10_{name}_idx"]
+    m[i[0], i[1]] = g[f"r10_{name}_val"]
+    return m
+
+
+def test_projector_matches_reference_on_shipped_geometry(golden):
+    g = golden("sparse_ops")
+    p = osp.build_projector(g["r10_coor_full"], theta_stride=2, z_stride=2, rotate_num=10)
+    assert tuple(p.ring_strides) == tuple(g["r10_ring_strides"])
+    assert [p.fine_layer_num, p.fine_z_num, p.coarse_layer_num, p.coarse_z_num] == list(g["r10_dims"])
+    for name in ("layer_reduce", "layer_expand", "z_reduce", "z_expand"):
+        np.testing.assert_array_equal(getattr(p, name), _dense_from(g, name))
+    np.testing.assert_allclose(p.coor_coarse, g["r10_coor_coarse"], rtol=0, atol=2e-5)
+    np.testing.assert_allclose(osp.upsample_rows(g["r10_rows_c"], p), g["r10_up"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(osp.adjoint_rows(g["r10_rows_f"], p), g["r10_adj"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(osp.reduce_rows(g["r10_rows_f"], p), g["r10_red"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(osp.reduce_image(g["r10_img_f"], p), g["r10_img_red"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(osp.upsample_weight_image(g["r10_img_c"], p), g["r10_img_up"], rtol=1e-5, atol=1e-6)
+
+
+def test_upsample_adjoint_pair_is_exact_in_fp64(golden):
+    g = golden("sparse_ops")
+    p = osp.build_projector(g["r10_coor_full"], theta_stride=2, z_stride=2, rotate_num=10)
+    rng = np.random.default_rng(0)
+    c = rng.random((2, p.coarse_pixel_num))
+    f = rng.random((2, p.fine_pixel_num))
+    lhs = np.sum(osp.upsample_rows(c, p) * f)
+    rhs = np.sum(c * osp.adjoint_rows(f, p))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-13
+
+
+def test_ring_stride_reduction_and_small_projector(golden):
+    g = golden("sparse_ops")
+    p = osp.build_projector(g["s_coor"], theta_stride=4, z_stride=2, rotate_num=4)
+    assert tuple(p.ring_strides) == tuple(g["s_ring_strides"]) == (3,) * 6
+    np.testing.assert_array_equal(p.layer_expand, g["s_layer_expand"])
+    np.testing.assert_array_equal(p.z_expand, g["s_z_expand"])
+    np.testing.assert_array_equal(p.layer_reduce, g["s_layer_reduce"])
+    np.testing.assert_array_equal(p.z_reduce, g["s_z_reduce"])
+
+
+def test_sparse_builder_and_weights_match_reference(golden):
+    g = golden("sparse_ops")
+    p = osp.build_projector(g["s_coor"], theta_stride=4, z_stride=2, rotate_num=4)
+    p.coor_coarse = g["s_coor_coarse"]  # use the reference's float32 coarse coordinates
+    a = [float(v) for v in g["s_args"]]
+    rows, _ = osp.sparse_builder(g["s_sysmat"], g["s_det"], p, g["s_smeared"], *a, dtype=np.float64)
+    ref = g["s_event_rows"]
+    np.testing.assert_array_equal(rows[:, 0], ref[:, 0])
+    _rows_close(rows[:, 1:], ref[:, 1:], 2e-4)
+    t, valid = osp.materialize(ref, g["s_sysmat"], p)
+    np.testing.assert_array_equal(valid, g["s_valid"])
+    _rows_close(t, g["s_t_fine"], 1e-5)
+    w_m = osp.weight_materialize(ref, g["s_sysmat"], g["s_x"], p)
+    w_g = osp.weight_grouped(ref, g["s_sysmat"], g["s_x"], p)
+    assert rel_l2(w_m, g["s_w_mat"]) < 1e-5
+    assert rel_l2(w_g, g["s_w_grouped"]) < 1e-5
+    # grouped and materialise forms agree (row-scale invariance of the list-mode weight)
+    assert rel_l2(w_g, w_m) < 1e-5
