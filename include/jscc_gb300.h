@@ -141,6 +141,149 @@ JSCC_API int jscc_sc_weight_noalloc(const void* A, int32_t a_dtype, int64_t lda,
                    const int64_t* rotmat_inv, int64_t ld_rot, int32_t use_floor, float floor,
                    float scale, float* weight, void* stream);
 
+/* ------------------------------------------------------- Compton cone (kernel a) */
+
+#define JSCC_CONE_STRICT 0 /* process_list_plane_strict.py (kinematic filter, clamped angles) */
+#define JSCC_CONE_LEGACY 1 /* process_list_plane.py (derivative sigma_E, atan sigma_pos, no clamps) */
+#define JSCC_CONE_RECORD_FLOATS 16 /* floats per event record (64 bytes, 16-byte aligned) */
+
+/*
+ * Event selection and per-event record of the Compton cone kernel, for a list that
+ * is already energy-smeared (the caller smears with the reference's torch.randn draws).
+ * Keeps event i when, with float32 arithmetic in the reference's operation order,
+ *   e1 < thr_max, e1 > thr_min, e2 > thr_min, e1 + e2 > thr_sum
+ *   (strict only) -1 + 1e-6 < 1 - 0.511 e1 / ((e0 - e1) e0) < 1 - 1e-6
+ *   |y(cp1) - y(cp2)| > 0.1
+ * (process_list_plane_strict.py:164-189, :30-36; process_list_plane.py:30-46). For kept
+ * events it writes the 16-float record (first-hit position, pos2 - pos1, |pos2 - pos1|,
+ * Compton angle (FP64 when theta_fp64), sigma_E branches (:39-52), Klein-Nishina factor,
+ * per-axis sigma1^2 + sigma2^2 from the given tables (:59-96), and a cos(beta) window of
+ * +-window_sigmas bounding sigmas; window_sigmas <= 0 disables pruning) and
+ * row_id = cp1 - 1. Detector ids outside [1, n_det] drop the event and are counted
+ * (jscc_take_bad_detector_count).
+ * list: [n_events, ld_list] float32 rows (cp1, e1, cp2, e2); det_pos [n_det, 3];
+ * sig1_sq / sig2_sq [n_det, 3] (strict) ; keep [n_events] uint8; records 16-byte aligned.
+ */
+JSCC_API int jscc_compton_event_prep(const float* list, int64_t ld_list, int64_t n_events,
+                   const float* det_pos, const float* sig1_sq, const float* sig2_sq,
+                   int64_t n_det, float e0, float ene_resolution, float thr_max,
+                   float thr_min, float thr_sum, int32_t model, int32_t theta_fp64,
+                   float window_sigmas, float delta_r1, float delta_r2, uint8_t* keep,
+                   float* records, int32_t* row_id, void* stream);
+
+/*
+ * Materialised cone rows for the T builders (process_list_plane_strict.py:201-240,
+ * process_list_plane.py:56-95, process_list_plane_sparse.py:78-106):
+ *   t_compton[i, j] = cone(record i, coor j)            (every pair, no window)
+ *   t[i, j]         = t_compton[i, j] * eff[row_id[i], j]  (eff may be NULL: t = t_compton)
+ * coor [V, 3] float32; eff rows of ld_eff elements (float32 or bf16); either output may
+ * be NULL. At most 65,535 events per call.
+ */
+JSCC_API int jscc_compton_cone_rows(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t V, int32_t model, const void* eff,
+                   int32_t eff_dtype, int64_t ld_eff, float* t_compton, float* t,
+                   void* stream);
+
+/*
+ * Per-event row statistics of t = cone * eff without storing the row: s1 = sum_j t,
+ * s2 = sum_j t^2, nan_flag = any NaN. Feeds the NaN/zero-row filter and the
+ * effective-support filter (process_list_plane_strict.py:137-148, :241-246) of the
+ * fused path. use_window applies the record's cos(beta) window (strict model only).
+ */
+JSCC_API int jscc_compton_row_stats(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t V, int32_t model, int32_t use_window,
+                   const void* eff, int32_t eff_dtype, int64_t ld_eff, float* s1, float* s2,
+                   int32_t* nan_flag, void* stream);
+
+JSCC_API size_t jscc_compton_weight_workspace_bytes(int64_t n_ev, int64_t n_vox);
+
+/*
+ * Fused list-mode Compton weight with T recomputed on the fly (never stored):
+ *   x_r = img[rotmat[:, 0] - 1]            (identity when rotmat == NULL)
+ *   f_i = sum_j t_ij x_r[j],  t_ij = cone(record i, coor j) * eff[row_id[i], j]
+ *   u_j = sum_i t_ij / f_i
+ *   weight[j] += scale * u[rotmat_inv[j * ld_rot] - 1]
+ * Replaces get_weight_compton (recon_osem_plane.py:33-42) over the rows of the strict or
+ * legacy builder, inside osem_list_mode / osem_joint_mode (:63-125): the builder's row
+ * normalisation does not change the weight. Events must already be filtered (event_prep
+ * + row_stats). use_window prunes pairs outside the record's window (t < exp(-K^2/2)).
+ */
+JSCC_API int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t n_vox, int32_t model, int32_t use_window,
+                   const void* eff, int32_t eff_dtype, int64_t ld_eff, const float* img,
+                   const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
+                   float* weight, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Detector ids outside the table seen by jscc_compton_event_prep since the last call
+ * (synchronous device read; resets the count). */
+JSCC_API int jscc_take_bad_detector_count(unsigned int* out);
+
+/* ------------------------------------------ sparse coarse<->fine Compton rows (kernel c) */
+
+/*
+ * Separable sparse map of rows, the form of every operator of compton_sparse_ops.py:
+ *   out[r][zo * n_lo + lo] = sum_{a in Z[zo]} z_w[a] * sum_{b in L[lo]} l_w[b] * in[rr][z_idx[a] * n_li + l_idx[b]]
+ * with rr = row_idx ? row_idx[r] : r and Z, L given as CSR tables (z_ptr [n_zo + 1],
+ * l_ptr [n_lo + 1]) built from the reference's dense layer/z matrices:
+ *   upsample_coarse_rows_to_fine  (:331-342): L = rows of layer_expand, Z = rows of z_expand
+ *   project_fine_rows_to_coarse_adjoint (:345-356): L, Z = columns of layer_expand, z_expand
+ *   reduce_fine_rows_to_coarse    (:317-328): L = rows of layer_reduce, Z = rows of z_reduce
+ *   reduce_fine_image_to_coarse / upsample_coarse_weight_to_fine (:293-314): one-row forms
+ * in: float32 or bf16 rows of ld_in elements; out: float32 rows of ld_out elements.
+ * At most 65,535 rows per call.
+ */
+JSCC_API int jscc_sparse_map(const void* in, int32_t in_dtype, int64_t ld_in, const int32_t* row_idx,
+                   int64_t n_rows, float* out, int64_t ld_out, const int32_t* z_ptr,
+                   const int32_t* z_idx, const float* z_w, int32_t n_zo, int32_t n_zi,
+                   const int32_t* l_ptr, const int32_t* l_idx, const float* l_w, int32_t n_lo,
+                   int32_t n_li, void* stream);
+
+/* pack_sparse_event_rows (compton_sparse_ops.py:359-368): rows[i] = (float(cp1[i]), t_compton[i, :]). */
+JSCC_API int jscc_sparse_pack(const int64_t* cp1, const float* t_compton, int64_t ld_tc, int64_t n_events,
+                   int64_t n_coarse, float* rows, int64_t ld_rows, void* stream);
+
+/* unpack_sparse_event_rows (:371-377), id column: cp1[i] = round-half-even(rows[i, 0]). */
+JSCC_API int jscc_sparse_unpack_ids(const float* rows, int64_t ld_rows, int64_t n_events, int64_t* cp1,
+                   void* stream);
+
+/*
+ * First half of materialize_sparse_event_rows_to_fine (:380-400): for packed rows
+ * (cp1, t_compton[V_c]) with upsample taps (two z taps per fine plane: z_taps/z_tw
+ * [n_zf, 2]; two layer taps per fine layer: l_taps/l_tw [n_lf, 2]; a missing tap has
+ * weight 0), writes fine[i, j] = nan_to_num(up(t_compton_i)[j] * sysmat[clamp(cp1_i - 1), j])
+ * and row_sum[i] = sum_j fine[i, j]. The caller keeps rows with a finite positive sum
+ * and divides them by it.
+ */
+JSCC_API int jscc_sparse_materialize(const float* rows, int64_t ld_rows, int64_t n_events,
+                   const void* sysmat, int32_t sysmat_dtype, int64_t ld_sysmat, int64_t n_det,
+                   const int32_t* z_taps, const float* z_tw, int32_t n_zf, const int32_t* l_taps,
+                   const float* l_tw, int32_t n_lf, int32_t n_lc, float* fine, int64_t ld_fine,
+                   float* row_sum, void* stream);
+
+#define JSCC_SPARSE_MATERIALIZE 0 /* recon_osem_local_sparse_jsccsd_only.py:13-19 */
+#define JSCC_SPARSE_GROUPED 1     /* recon_osem_plane_sparse.py:22-57 */
+
+JSCC_API size_t jscc_sparse_weight_workspace_bytes(int64_t n_events, int64_t n_fine);
+
+/*
+ * Fused sparse list-mode weight; fine rows are formed on the fly from the packed coarse
+ * rows and never stored:
+ *   v_ij = up(t_compton_i)[j] * sysmat[clamp(cp1_i - 1), j]
+ *   MATERIALIZE: v = nan_to_num(v); S_i = sum_j v_ij; rows with a non-finite or
+ *                non-positive S_i are dropped; c_i = 1 / max((sum_j v_ij x_j) / S_i, 1e-12) / S_i
+ *   GROUPED:     c_i = 1 / max(sum_j v_ij x_j, 1e-12)
+ *   weight[j] += scale * nan_to_num(sum_i v_ij c_i)   (after the inverse rotation)
+ * x is img gathered by rotmat[:, 0] (identity when NULL). Replaces get_weight_compton_sparse
+ * in both reference forms and the rotation handling around it (recon_osem_plane_sparse.py:73-80,
+ * recon_osem_local_sparse_jsccsd_only.py:362-377).
+ */
+JSCC_API int jscc_sparse_weight(const float* rows, int64_t ld_rows, int64_t n_events, const void* sysmat,
+                   int32_t sysmat_dtype, int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps,
+                   const float* z_tw, int32_t n_zf, const int32_t* l_taps, const float* l_tw,
+                   int32_t n_lf, int32_t n_lc, int32_t mode, const float* img,
+                   const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
+                   float* weight, void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------ EM update */
 
 #define JSCC_EM_PLAIN 0 /* img * w / s                         (recon_osem_plane.py:54, :73, :118) */

@@ -6,7 +6,13 @@ Drop-in modules mirroring the reference's module names and signatures:
 reference module                        this package
 =====================================  =============================================
 recon_osem_plane                        .recon_osem_plane
+recon_osem_plane_sparse                 .recon_osem_plane_sparse
 recon_osem_local_cntstat                .recon_osem_local_cntstat
+recon_osem_local_sparse_jsccsd_only     .recon_osem_local_sparse_jsccsd_only
+process_list_plane_strict               .process_list_plane_strict
+process_list_plane                      .process_list_plane
+process_list_plane_sparse               .process_list_plane_sparse
+compton_sparse_ops                      .compton_sparse_ops
 =====================================  =============================================
 
 All compute runs in ``lib/libjscc_gb300.so`` (C-ABI in include/jscc_gb300.h). Importing
@@ -21,7 +27,13 @@ __version__ = "0.1.0"
 
 _MIRRORED = (
     "recon_osem_plane",
+    "recon_osem_plane_sparse",
     "recon_osem_local_cntstat",
+    "recon_osem_local_sparse_jsccsd_only",
+    "process_list_plane_strict",
+    "process_list_plane",
+    "process_list_plane_sparse",
+    "compton_sparse_ops",
 )
 
 

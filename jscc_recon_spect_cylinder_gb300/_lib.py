@@ -25,6 +25,13 @@ DTYPE_BF16 = 1
 EM_PLAIN = 0
 EM_SAFE = 1
 
+CONE_STRICT = 0
+CONE_LEGACY = 1
+CONE_RECORD_FLOATS = 16
+
+SPARSE_MATERIALIZE = 0
+SPARSE_GROUPED = 1
+
 _lib = None
 _lock = threading.Lock()
 
@@ -48,6 +55,47 @@ _SIGNATURES: dict[str, tuple] = {
         c_int,
         [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_void_p, c_int64, c_int32,
          c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_float, c_float, c_void_p, c_void_p],
+    ),
+    "jscc_compton_event_prep": (
+        c_int,
+        [c_void_p, c_int64, c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_float, c_float, c_float, c_float,
+         c_float, c_int32, c_int32, c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_void_p],
+    ),
+    "jscc_compton_cone_rows": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p, c_int32, c_int64, c_void_p, c_void_p,
+         c_void_p],
+    ),
+    "jscc_compton_row_stats": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+         c_void_p, c_void_p, c_void_p],
+    ),
+    "jscc_compton_weight_workspace_bytes": (c_size_t, [c_int64, c_int64]),
+    "jscc_compton_weight": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+         c_void_p, c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "jscc_take_bad_detector_count": (c_int, [POINTER(c_uint)]),
+    "jscc_sparse_map": (
+        c_int,
+        [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int32,
+         c_int32, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_void_p],
+    ),
+    "jscc_sparse_pack": (c_int, [c_void_p, c_void_p, c_int64, c_int64, c_int64, c_void_p, c_int64, c_void_p]),
+    "jscc_sparse_unpack_ids": (c_int, [c_void_p, c_int64, c_int64, c_void_p, c_void_p]),
+    "jscc_sparse_materialize": (
+        c_int,
+        [c_void_p, c_int64, c_int64, c_void_p, c_int32, c_int64, c_int64, c_void_p, c_void_p, c_int32, c_void_p,
+         c_void_p, c_int32, c_int32, c_void_p, c_int64, c_void_p, c_void_p],
+    ),
+    "jscc_sparse_weight_workspace_bytes": (c_size_t, [c_int64, c_int64]),
+    "jscc_sparse_weight": (
+        c_int,
+        [c_void_p, c_int64, c_int64, c_void_p, c_int32, c_int64, c_int64, c_void_p, c_void_p, c_int32, c_void_p,
+         c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_float, c_void_p, c_void_p,
+         c_size_t, c_void_p],
     ),
     "jscc_em_update": (
         c_int,
@@ -101,6 +149,12 @@ def launch_count() -> int:
 
 def reset_launch_count() -> None:
     load().jscc_reset_launch_count()
+
+
+def take_bad_detector_count() -> int:
+    out = c_uint(0)
+    check(load().jscc_take_bad_detector_count(ctypes.byref(out)), "jscc_take_bad_detector_count")
+    return int(out.value)
 
 
 def take_bad_index_count() -> int:

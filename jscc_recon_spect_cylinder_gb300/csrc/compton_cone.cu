@@ -1,0 +1,602 @@
+// Compton cone kernel (kernel a): per-event preparation, materialised T rows for the
+// builders, and the fused list-mode weight w = T^T (1 / (T x)) with T recomputed on the fly.
+//
+// Reference semantics
+//   strict:  process_list_plane_strict.py:151-253 (filters :164-189, theta :24-27, sigma_E
+//            :39-52, sigma_pos :59-134, kernel :228), t = cone * sysmat[cp1 - 1] (:240)
+//   legacy:  process_list_plane.py:17-107 (derivative sigma_E :66-74, atan sigma_pos :77-80)
+//   weight:  recon_osem_plane.py:33-42 (get_weight_compton) over the builder's rows; rows are
+//            normalised there, and the list-mode weight is invariant to a row's scale, so the
+//            fused form skips the normalisation.
+//
+// GB300 design
+//   * One 64-byte record per event (positions, Compton angle, sigma branches, Klein-Nishina
+//     factor, per-axis position variance, cos(beta) window). The Compton angle and its
+//     energy-sigma branches are computed in FP64 on request (the 1/(E0 - E1) difference
+//     loses bits in FP32 near the Compton edge); event-selection decisions are made in
+//     FP32 with the reference's operation order so the surviving event set is identical.
+//   * Window: sigma_pos is bounded per event by sqrt(max_k s_k) / d12 (|grad beta| = 1/d12)
+//     and sigma_E by max(sigma+, sigma-), so |beta - theta| > K sigma_max implies
+//     t < exp(-K^2/2). Pairs whose cos(beta) falls outside the window skip acos/exp and
+//     the efficiency load (K = window_sigmas; K <= 0 evaluates every pair).
+//   * Forward: CTA = 256 threads x EB events; every thread walks voxels, keeps EB partial
+//     sums in registers, fixed-order CTA reduction at the end.
+//   * Back: CTA = 256 voxels x one event chunk; partial column sums per chunk to the
+//     workspace, then the chunk-ordered reduce of sc_projector.cu (shared kernel).
+//   No float atomics; results are bit-reproducible.
+#include "jscc_common.cuh"
+
+namespace jscc {
+
+// Shared with sc_projector.cu.
+__global__ void sc_gather_rot_kernel(const float* __restrict__ img, const int64_t* __restrict__ rotmat,
+                                     int64_t ld_rot, int r0, int nr, int64_t V, int64_t ldx,
+                                     float* __restrict__ xr);
+__global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
+                                         int nr, int rb_stride, const int64_t* __restrict__ rotinv,
+                                         int64_t ld_rot, int r0, int64_t V, int has_scale,
+                                         float scale, float* __restrict__ weight);
+
+__device__ unsigned int g_bad_detector_count = 0;
+
+struct alignas(16) ConeEvent {
+  float p1x, p1y, p1z;     // first-hit position
+  float vx, vy, vz;        // v12 = pos2 - pos1
+  float d12;               // |v12|
+  float theta;             // Compton angle
+  float sig_plus, sig_minus;
+  float kn;                // e0 / (e0 - e1) + (e0 - e1) / e0
+  float s0, s1, s2;        // strict: sigma1^2 + sigma2^2 per axis; legacy: delta_r1, q, cos(theta)
+  float cos_lo, cos_hi;    // cos(beta) window
+};
+static_assert(sizeof(ConeEvent) == 64, "record layout");
+
+constexpr float kEE = 0.511f;
+
+// ------------------------------------------------------------------ event preparation
+__device__ __forceinline__ float compton_cos_f32(float e1, float e0) {
+  // 1 - ((ee * e1) / ((e0 - e1) * e0)), each operation rounded as the reference's tensor ops
+  return __fsub_rn(1.0f, __fdiv_rn(__fmul_rn(kEE, e1), __fmul_rn(__fsub_rn(e0, e1), e0)));
+}
+
+__device__ __forceinline__ double compton_theta_f64(double e1, double e0) {
+  double c = 1.0 - (0.511 * e1) / ((e0 - e1) * e0);
+  c = fmin(fmax(c, -1.0 + 1e-7), 1.0 - 1e-7);
+  return acos(c);
+}
+
+__device__ __forceinline__ float compton_theta_f32(float e1, float e0) {
+  float c = compton_cos_f32(e1, e0);
+  c = fminf(fmaxf(c, -1.0f + 1e-7f), 1.0f - 1e-7f);
+  return acosf(c);
+}
+
+__global__ void compton_event_prep_kernel(const float* __restrict__ list, int64_t ld_list, int64_t n,
+                                          const float* __restrict__ det, const float* __restrict__ sig1,
+                                          const float* __restrict__ sig2, int64_t n_det, float e0, float res,
+                                          float thr_max, float thr_min, float thr_sum, int model, int theta_fp64,
+                                          float window_k, float dr1, float dr2, uint8_t* __restrict__ keep,
+                                          ConeEvent* __restrict__ rec, int32_t* __restrict__ row_id) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float* L = list + i * ld_list;
+    const int cp1 = (int)L[0];  // torch .int(): truncation toward zero
+    const int cp2 = (int)L[2];
+    const float e1 = L[1], e2 = L[3];
+    bool k = (e1 < thr_max) && (e1 > thr_min) && (e2 > thr_min) && (__fadd_rn(e1, e2) > thr_sum);
+    if (model == 0) {
+      const float c = compton_cos_f32(e1, e0);
+      k = k && (c > -1.0f + 1e-6f) && (c < 1.0f - 1e-6f);
+    }
+    if (cp1 < 1 || cp1 > n_det || cp2 < 1 || cp2 > n_det) {
+      if (k) atomicAdd(&g_bad_detector_count, 1u);
+      k = false;
+    }
+    if (k) {
+      const float y1 = det[(int64_t)(cp1 - 1) * 3 + 1], y2 = det[(int64_t)(cp2 - 1) * 3 + 1];
+      k = fabsf(__fsub_rn(y1, y2)) > 0.1f;
+    }
+    keep[i] = k ? 1 : 0;
+    row_id[i] = k ? cp1 - 1 : 0;
+    if (!k) continue;
+    ConeEvent r;
+    const float* a = det + (int64_t)(cp1 - 1) * 3;
+    const float* b = det + (int64_t)(cp2 - 1) * 3;
+    r.p1x = a[0]; r.p1y = a[1]; r.p1z = a[2];
+    r.vx = __fsub_rn(b[0], a[0]);
+    r.vy = __fsub_rn(b[1], a[1]);
+    r.vz = __fsub_rn(b[2], a[2]);
+    r.d12 = sqrtf(r.vx * r.vx + r.vy * r.vy + r.vz * r.vz);
+    if (model == 0) {
+      // sigma_E: e1 -/+ e1 * res / 2.355 * sqrt(e0 / e1), clamped to (1e-7, e0 - 1e-7)
+      if (theta_fp64) {
+        const double E0 = (double)e0, E1 = (double)e1;
+        const double th = compton_theta_f64(E1, E0);
+        const double se = E1 * (double)res / 2.355 * sqrt(E0 / E1);
+        const double lo = fmin(fmax(E1 - se, 1e-7), E0 - 1e-7);
+        const double hi = fmin(fmax(E1 + se, 1e-7), E0 - 1e-7);
+        r.theta = (float)th;
+        r.sig_minus = (float)fmax(th - compton_theta_f64(lo, E0), 1e-7);
+        r.sig_plus = (float)fmax(compton_theta_f64(hi, E0) - th, 1e-7);
+        r.kn = (float)(E0 / (E0 - E1) + (E0 - E1) / E0);
+      } else {
+        const float th = compton_theta_f32(e1, e0);
+        const float se = e1 * res / 2.355f * sqrtf(e0 / e1);
+        const float lo = fminf(fmaxf(e1 - se, 1e-7f), e0 - 1e-7f);
+        const float hi = fminf(fmaxf(e1 + se, 1e-7f), e0 - 1e-7f);
+        r.theta = th;
+        r.sig_minus = fmaxf(th - compton_theta_f32(lo, e0), 1e-7f);
+        r.sig_plus = fmaxf(compton_theta_f32(hi, e0) - th, 1e-7f);
+        r.kn = e0 / (e0 - e1) + (e0 - e1) / e0;
+      }
+      const float* q1 = sig1 + (int64_t)(cp1 - 1) * 3;
+      const float* q2 = sig2 + (int64_t)(cp2 - 1) * 3;
+      r.s0 = q1[0] + q2[0];
+      r.s1 = q1[1] + q2[1];
+      r.s2 = q1[2] + q2[2];
+      if (window_k > 0.f) {
+        const float d12c = fmaxf(r.d12, 1e-7f);
+        const float smax = fmaxf(fmaxf(r.s0, r.s1), r.s2);
+        const float sp2 = smax / (d12c * d12c);
+        const float se = fmaxf(r.sig_plus, r.sig_minus);
+        // 1 % margin on the bound for rounding in the per-pair terms
+        const float sig_max = 1.01f * sqrtf(fmaxf(sp2 + se * se, 1e-12f));
+        const float hi_ang = fminf(r.theta + window_k * sig_max, 3.14159265f);
+        const float lo_ang = fmaxf(r.theta - window_k * sig_max, 0.f);
+        r.cos_lo = hi_ang >= 3.14159265f ? -2.f : cosf(hi_ang);
+        r.cos_hi = lo_ang <= 0.f ? 2.f : cosf(lo_ang);
+      } else {
+        r.cos_lo = -2.f;
+        r.cos_hi = 2.f;
+      }
+    } else {
+      // legacy: unclamped theta and first/second-derivative sigma_E (process_list_plane.py:64-74)
+      const float th = acosf(compton_cos_f32(e1, e0));
+      const float er = e1 * res / 2.355f * sqrtf(e0 / e1);
+      const float st = sinf(th), ct = cosf(th);
+      const float dm = e0 - e1;
+      const float dth = (1.0f / fabsf(st)) * kEE / (dm * dm);
+      const float d2th = kEE / (st * dm * dm * dm) * (2.0f - ct / (st * st) * kEE / dm);
+      r.theta = th;
+      r.sig_plus = fabsf(dth * er + 0.5f * d2th * er * er);
+      r.sig_minus = fabsf(dth * er - 0.5f * d2th * er * er);
+      r.kn = e0 / dm + dm / e0;
+      r.s0 = dr1;
+      r.s1 = dr1 / dr2;
+      r.s2 = ct;
+      r.cos_lo = -2.f;
+      r.cos_hi = 2.f;
+    }
+    rec[i] = r;
+  }
+}
+
+// ------------------------------------------------------------------ per-pair kernel value
+// Returns the cone value t_ij (no efficiency factor). WINDOW: skip outside the cos window.
+template <int MODEL, bool WINDOW>
+__device__ __forceinline__ float cone_value(const ConeEvent& e, float cx, float cy, float cz) {
+  const float ax = e.p1x - cx, ay = e.p1y - cy, az = e.p1z - cz;
+  const float dot = ax * e.vx + ay * e.vy + az * e.vz;
+  const float d01sq = ax * ax + ay * ay + az * az;
+  const float d01 = sqrtf(d01sq);
+  if (MODEL == 0) {
+    const float bcos = dot / fmaxf(d01 * e.d12, 1e-7f);
+    if (WINDOW && (bcos < e.cos_lo || bcos > e.cos_hi)) return 0.f;
+    const float c = fminf(fmaxf(bcos, -1.0f + 1e-7f), 1.0f - 1e-7f);
+    const float beta = acosf(c);
+    const float delta = beta - e.theta;
+    const float sig_e = delta >= 0.f ? e.sig_plus : e.sig_minus;
+    // sigma_pos: grad beta w.r.t. the first hit (inter-crystal leg) and second hit
+    const float i01 = 1.0f / fmaxf(d01, 1e-7f);
+    const float i12 = 1.0f / fmaxf(e.d12, 1e-7f);
+    const float ux = ax * i01, uy = ay * i01, uz = az * i01;
+    const float wx = e.vx * i12, wy = e.vy * i12, wz = e.vz * i12;
+    const float cb = ux * wx + uy * wy + uz * wz;
+    const float sb2 = fmaxf(1.0f - cb * cb, 1e-12f);
+    const float jx = (ux - cb * wx) * i12, jy = (uy - cb * wy) * i12, jz = (uz - cb * wz) * i12;
+    const float sp2 = (jx * jx * e.s0 + jy * jy * e.s1 + jz * jz * e.s2) / sb2;
+    const float sig_pos = sqrtf(fmaxf(sp2, 1e-12f));
+    const float sig2 = fmaxf(sig_pos * sig_pos + sig_e * sig_e, 1e-12f);
+    const float sinb2 = (1.0f - c) * (1.0f + c);
+    return expf(-(delta * delta) / (2.0f * sig2)) * (e.kn - sinb2);
+  } else {
+    const float beta = acosf(dot / (d01 * e.d12));
+    const float delta = beta - e.theta;
+    const float sig_e = delta >= 0.f ? e.sig_plus : e.sig_minus;
+    const float p = d01 / e.d12;
+    const float q = e.s1;
+    const float sig_pos = atanf(e.s0 / d01) * sqrtf(1.0f + p * p * (1.0f + q * q) + 2.0f * p * e.s2);
+    const float sig = sqrtf(sig_pos * sig_pos + sig_e * sig_e);
+    const float sb = sinf(beta);
+    return expf(-(delta * delta) / (2.0f * sig * sig)) * (e.kn - sb * sb);
+  }
+}
+
+template <typename TE>
+__device__ __forceinline__ float eff_load(const TE* p, int64_t i);
+template <>
+__device__ __forceinline__ float eff_load<float>(const float* p, int64_t i) { return __ldg(p + i); }
+template <>
+__device__ __forceinline__ float eff_load<__nv_bfloat16>(const __nv_bfloat16* p, int64_t i) {
+  return __bfloat162float(p[i]);
+}
+
+// ------------------------------------------------------------------ materialised rows
+template <int MODEL, typename TE>
+__global__ void cone_rows_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                                 const float* __restrict__ coor, int64_t V, const TE* __restrict__ eff,
+                                 int64_t ld_eff, float* __restrict__ tc_out, float* __restrict__ t_out) {
+  const int64_t i = blockIdx.y;
+  if (i >= n_ev) return;
+  const ConeEvent e = rec[i];
+  const TE* er = eff ? eff + (int64_t)row_id[i] * ld_eff : nullptr;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V; j += (int64_t)gridDim.x * blockDim.x) {
+    const float t = cone_value<MODEL, false>(e, coor[3 * j], coor[3 * j + 1], coor[3 * j + 2]);
+    if (tc_out) tc_out[i * V + j] = t;
+    if (t_out) t_out[i * V + j] = er ? t * eff_load(er, j) : t;
+  }
+}
+
+// ------------------------------------------------------------------ fused forward
+// f[i] = sum_j t_ij eff_ij x_j; optional stats s1[i] = sum t_ij eff_ij, s2[i] = sum (t eff)^2,
+// nan[i] = any NaN.
+constexpr int kConeThreads = 256;
+
+template <int MODEL, bool WINDOW, int EB, bool STATS, typename TE>
+__global__ void __launch_bounds__(kConeThreads)
+cone_forward_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                    const float* __restrict__ coor, int64_t V, const float* __restrict__ x,
+                    const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ f_out,
+                    float* __restrict__ s1_out, float* __restrict__ s2_out, int32_t* __restrict__ nan_out) {
+  __shared__ ConeEvent sev[EB];
+  __shared__ int64_t srow[EB];
+  __shared__ float red[kConeThreads / 32][EB * (STATS ? 4 : 1)];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t i0 = (int64_t)blockIdx.x * EB;
+  if (tid < EB) {
+    const int64_t i = i0 + tid < n_ev ? i0 + tid : n_ev - 1;
+    sev[tid] = rec[i];
+    srow[tid] = (int64_t)row_id[i] * ld_eff;
+  }
+  __syncthreads();
+  const int ne = (n_ev - i0) < EB ? (int)(n_ev - i0) : EB;
+  float af[EB], a1[EB], a2[EB], an[EB];
+#pragma unroll
+  for (int e = 0; e < EB; ++e) af[e] = a1[e] = a2[e] = an[e] = 0.f;
+  for (int64_t j = tid; j < V; j += kConeThreads) {
+    const float cx = coor[3 * j], cy = coor[3 * j + 1], cz = coor[3 * j + 2];
+    const float xj = x ? __ldg(x + j) : 0.f;
+#pragma unroll
+    for (int e = 0; e < EB; ++e) {
+      if (e < ne) {
+        float t = cone_value<MODEL, WINDOW>(sev[e], cx, cy, cz);
+        if (t != 0.f) {
+          t = eff ? t * eff_load(eff + srow[e], j) : t;
+          af[e] = fmaf(t, xj, af[e]);
+          if (STATS) {
+            a1[e] += t;
+            a2[e] = fmaf(t, t, a2[e]);
+            if (isnan(t)) an[e] = 1.f;
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < EB; ++e) {
+    const float v = warp_sum(af[e]);
+    if (lane == 0) red[warp][e] = v;
+    if (STATS) {
+      const float v1 = warp_sum(a1[e]);
+      const float v2 = warp_sum(a2[e]);
+      float vn = an[e];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) vn = fmaxf(vn, __shfl_xor_sync(0xffffffffu, vn, o));
+      if (lane == 0) {
+        red[warp][EB + e] = v1;
+        red[warp][2 * EB + e] = v2;
+        red[warp][3 * EB + e] = vn;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < ne) {
+    float f = 0.f, s1 = 0.f, s2 = 0.f, sn = 0.f;
+#pragma unroll
+    for (int w = 0; w < kConeThreads / 32; ++w) {
+      f += red[w][tid];
+      if (STATS) {
+        s1 += red[w][EB + tid];
+        s2 += red[w][2 * EB + tid];
+        sn = fmaxf(sn, red[w][3 * EB + tid]);
+      }
+    }
+    if (f_out) f_out[i0 + tid] = f;
+    if (STATS) {
+      s1_out[i0 + tid] = s1;
+      s2_out[i0 + tid] = s2;
+      nan_out[i0 + tid] = sn > 0.f ? 1 : 0;
+    }
+  }
+}
+
+// q[i] = 1 / f[i] (get_weight_compton divides by the forward projection without a floor)
+__global__ void cone_ratio_kernel(const float* __restrict__ f, int64_t n, float* __restrict__ q) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    q[i] = 1.0f / f[i];
+}
+
+// ------------------------------------------------------------------ fused back projection
+// part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i
+constexpr int kBackStage = 64;
+
+template <int MODEL, bool WINDOW, typename TE>
+__global__ void __launch_bounds__(kConeThreads)
+cone_back_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                 int64_t ev_per_chunk, const float* __restrict__ q, const float* __restrict__ coor, int64_t V,
+                 const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp) {
+  __shared__ ConeEvent sev[kBackStage];
+  __shared__ int64_t srow[kBackStage];
+  __shared__ float sq[kBackStage];
+  const int tid = threadIdx.x;
+  const int64_t j = (int64_t)blockIdx.x * kConeThreads + tid;
+  const int64_t e_begin = (int64_t)blockIdx.y * ev_per_chunk;
+  int64_t e_end = e_begin + ev_per_chunk;
+  if (e_end > n_ev) e_end = n_ev;
+  float cx = 0.f, cy = 0.f, cz = 0.f;
+  if (j < V) {
+    cx = coor[3 * j];
+    cy = coor[3 * j + 1];
+    cz = coor[3 * j + 2];
+  }
+  float acc = 0.f;
+  for (int64_t s = e_begin; s < e_end; s += kBackStage) {
+    const int n = (e_end - s) < kBackStage ? (int)(e_end - s) : kBackStage;
+    __syncthreads();
+    if (tid < n) {
+      sev[tid] = rec[s + tid];
+      srow[tid] = (int64_t)row_id[s + tid] * ld_eff;
+      sq[tid] = q[s + tid];
+    }
+    __syncthreads();
+    if (j < V) {
+      for (int e = 0; e < n; ++e) {
+        float t = cone_value<MODEL, WINDOW>(sev[e], cx, cy, cz);
+        if (t != 0.f) {
+          t = eff ? t * eff_load(eff + srow[e], j) : t;
+          acc = fmaf(t, sq[e], acc);
+        }
+      }
+    }
+  }
+  if (j < V) part[(int64_t)blockIdx.y * ldp + j] = acc;
+}
+
+// ------------------------------------------------------------------ host planning
+struct ConePlan {
+  int64_t chunks;
+  int64_t ev_per_chunk;
+  int64_t ldp;
+  int64_t ldx;
+  size_t ws_bytes;
+};
+
+static ConePlan plan_cone(int64_t n_ev, int64_t V) {
+  ConePlan p{};
+  const int64_t tiles = (V + kConeThreads - 1) / kConeThreads;
+  const int64_t target = 2432;  // back-pass CTAs: 16 x 152 SMs
+  int64_t chunks = (target + tiles - 1) / (tiles > 0 ? tiles : 1);
+  const int64_t max_chunks = (n_ev + 63) / 64;  // >= 64 events per chunk
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks < 1) chunks = 1;
+  p.ev_per_chunk = (n_ev + chunks - 1) / chunks;
+  if (p.ev_per_chunk < 1) p.ev_per_chunk = 1;
+  p.chunks = (n_ev + p.ev_per_chunk - 1) / p.ev_per_chunk;
+  if (p.chunks < 1) p.chunks = 1;
+  p.ldp = (int64_t)align_up((size_t)(V > 0 ? V : 1), 8);
+  p.ldx = p.ldp;
+  size_t b = 0;
+  b += align_up((size_t)p.ldx * sizeof(float), 256);                       // rotated image
+  b += align_up((size_t)(n_ev > 0 ? n_ev : 1) * sizeof(float), 256) * 2;  // f, q
+  b += align_up((size_t)p.chunks * p.ldp * sizeof(float), 256);            // partials
+  p.ws_bytes = b + 256;
+  return p;
+}
+
+template <int MODEL, bool WINDOW, typename TE>
+static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t n_ev, const float* coor, int64_t V,
+                              const float* x, const TE* eff, int64_t ld_eff, float* f, float* q, float* part,
+                              const ConePlan& p, cudaStream_t st) {
+  constexpr int EB = 16;
+  const unsigned fgrid = (unsigned)((n_ev + EB - 1) / EB);
+  JSCC_TIMED("cone_forward", st,
+             (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
+                 rec, rid, n_ev, coor, V, x, eff, ld_eff, f, nullptr, nullptr, nullptr)));
+  JSCC_LAUNCH_CHECK();
+  int64_t rb = (n_ev + 255) / 256;
+  if (rb > 4096) rb = 4096;
+  JSCC_TIMED("cone_ratio", st, (cone_ratio_kernel<<<(unsigned)rb, 256, 0, st>>>(f, n_ev, q)));
+  JSCC_LAUNCH_CHECK();
+  dim3 bgrid((unsigned)((V + kConeThreads - 1) / kConeThreads), (unsigned)p.chunks);
+  JSCC_TIMED("cone_back", st,
+             (cone_back_kernel<MODEL, WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
+                 rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+}  // namespace jscc
+
+using namespace jscc;
+
+extern "C" {
+
+int jscc_compton_event_prep(const float* list, int64_t ld_list, int64_t n_events, const float* det_pos,
+                            const float* sig1_sq, const float* sig2_sq, int64_t n_det, float e0,
+                            float ene_resolution, float thr_max, float thr_min, float thr_sum, int32_t model,
+                            int32_t theta_fp64, float window_sigmas, float delta_r1, float delta_r2,
+                            uint8_t* keep, float* records, int32_t* row_id, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_det >= 0, "jscc_compton_event_prep: negative size");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_event_prep: bad model %d",
+               model);
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(list && det_pos && keep && records && row_id, "jscc_compton_event_prep: null pointer argument");
+  JSCC_REQUIRE(model == JSCC_CONE_LEGACY || (sig1_sq && sig2_sq),
+               "jscc_compton_event_prep: strict model needs the position-variance tables");
+  JSCC_REQUIRE(ld_list >= 4, "jscc_compton_event_prep: ld_list < 4");
+  JSCC_REQUIRE(reinterpret_cast<uintptr_t>(records) % 16 == 0, "jscc_compton_event_prep: records not 16-byte aligned");
+  cudaStream_t st = as_stream(stream);
+  int64_t blocks = (n_events + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  JSCC_TIMED("compton_event_prep", st,
+             (compton_event_prep_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+                 list, ld_list, n_events, det_pos, sig1_sq, sig2_sq, n_det, e0, ene_resolution, thr_max, thr_min,
+                 thr_sum, model, theta_fp64, window_sigmas, delta_r1, delta_r2, keep,
+                 reinterpret_cast<ConeEvent*>(records), row_id)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_compton_cone_rows(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t V,
+                           int32_t model, const void* eff, int32_t eff_dtype, int64_t ld_eff, float* t_compton,
+                           float* t, void* stream) {
+  JSCC_REQUIRE(n_ev >= 0 && V >= 0, "jscc_compton_cone_rows: negative size");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_cone_rows: bad model");
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_cone_rows: bad dtype");
+  if (n_ev == 0 || V == 0) return JSCC_OK;
+  JSCC_REQUIRE(records && coor && (t_compton || t), "jscc_compton_cone_rows: null pointer argument");
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= V), "jscc_compton_cone_rows: efficiency rows need row ids and ld >= V");
+  JSCC_REQUIRE(n_ev <= 65535, "jscc_compton_cone_rows: at most 65,535 events per call (got %lld)", (long long)n_ev);
+  cudaStream_t st = as_stream(stream);
+  const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
+  int64_t bx = (V + 255) / 256;
+  if (bx > 64) bx = 64;
+  dim3 grid((unsigned)bx, (unsigned)n_ev);
+  if (eff_dtype == JSCC_DTYPE_F32) {
+    const float* e = static_cast<const float*>(eff);
+    if (model == JSCC_CONE_STRICT)
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<0, float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, V, e,
+                                                                                        ld_eff, t_compton, t)));
+    else
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<1, float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, V, e,
+                                                                                        ld_eff, t_compton, t)));
+  } else {
+    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
+    if (model == JSCC_CONE_STRICT)
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<0, __nv_bfloat16><<<grid, 256, 0, st>>>(
+                                      rec, row_id, n_ev, coor, V, e, ld_eff, t_compton, t)));
+    else
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<1, __nv_bfloat16><<<grid, 256, 0, st>>>(
+                                      rec, row_id, n_ev, coor, V, e, ld_eff, t_compton, t)));
+  }
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_compton_row_stats(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t V,
+                           int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                           float* s1, float* s2, int32_t* nan_flag, void* stream) {
+  JSCC_REQUIRE(n_ev >= 0 && V >= 0, "jscc_compton_row_stats: negative size");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_row_stats: bad model");
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_row_stats: bad dtype");
+  if (n_ev == 0) return JSCC_OK;
+  JSCC_REQUIRE(records && coor && s1 && s2 && nan_flag, "jscc_compton_row_stats: null pointer argument");
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= V), "jscc_compton_row_stats: efficiency rows need row ids and ld >= V");
+  cudaStream_t st = as_stream(stream);
+  const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
+  constexpr int EB = 8;
+  const unsigned grid = (unsigned)((n_ev + EB - 1) / EB);
+#define JSCC_STATS_LAUNCH(M, W, TE)                                                                            \
+  JSCC_TIMED("cone_row_stats", st,                                                                             \
+             (cone_forward_kernel<M, W, EB, true, TE><<<grid, kConeThreads, 0, st>>>(                          \
+                 rec, row_id, n_ev, coor, V, nullptr, static_cast<const TE*>(eff), ld_eff, nullptr, s1, s2,    \
+                 nan_flag)))
+  if (eff_dtype == JSCC_DTYPE_F32) {
+    if (model == JSCC_CONE_LEGACY) JSCC_STATS_LAUNCH(1, false, float);
+    else if (use_window) JSCC_STATS_LAUNCH(0, true, float);
+    else JSCC_STATS_LAUNCH(0, false, float);
+  } else {
+    if (model == JSCC_CONE_LEGACY) JSCC_STATS_LAUNCH(1, false, __nv_bfloat16);
+    else if (use_window) JSCC_STATS_LAUNCH(0, true, __nv_bfloat16);
+    else JSCC_STATS_LAUNCH(0, false, __nv_bfloat16);
+  }
+#undef JSCC_STATS_LAUNCH
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+size_t jscc_compton_weight_workspace_bytes(int64_t n_ev, int64_t n_vox) { return plan_cone(n_ev, n_vox).ws_bytes; }
+
+int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t n_vox,
+                        int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                        const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
+                        float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0, "jscc_compton_weight: negative size");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_weight: bad model");
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_weight: bad dtype");
+  if (n_ev == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(records && coor && img && weight, "jscc_compton_weight: null pointer argument");
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= n_vox), "jscc_compton_weight: efficiency rows need row ids, ld >= V");
+  JSCC_REQUIRE((rotmat == nullptr) == (rotmat_inv == nullptr), "jscc_compton_weight: give both rotation tables");
+  const ConePlan p = plan_cone(n_ev, n_vox);
+  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "jscc_compton_weight: workspace too small (%zu < %zu)",
+               workspace_bytes, p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  float* xr = cv.take<float>((size_t)p.ldx);
+  float* f = cv.take<float>((size_t)n_ev);
+  float* q = cv.take<float>((size_t)n_ev);
+  float* part = cv.take<float>((size_t)p.chunks * p.ldp);
+  JSCC_REQUIRE(cv.ok(), "jscc_compton_weight: workspace carve overflow");
+  cudaStream_t st = as_stream(stream);
+  const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
+  const float* x = img;
+  if (rotmat) {
+    int64_t blocks = (n_vox + 255) / 256;
+    if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+    JSCC_TIMED("sc_gather_rot", st,
+               (sc_gather_rot_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, rotmat, ld_rot, 0, 1, n_vox, p.ldx, xr)));
+    JSCC_LAUNCH_CHECK();
+    x = xr;
+  }
+  int rc;
+  const bool win = use_window != 0 && model == JSCC_CONE_STRICT;
+  if (eff_dtype == JSCC_DTYPE_F32) {
+    const float* e = static_cast<const float*>(eff);
+    if (model == JSCC_CONE_LEGACY)
+      rc = launch_cone_weight<1, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+    else if (win)
+      rc = launch_cone_weight<0, true, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+    else
+      rc = launch_cone_weight<0, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+  } else {
+    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
+    if (model == JSCC_CONE_LEGACY)
+      rc = launch_cone_weight<1, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
+                                                       st);
+    else if (win)
+      rc = launch_cone_weight<0, true, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
+                                                      st);
+    else
+      rc = launch_cone_weight<0, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
+                                                       st);
+  }
+  if (rc != JSCC_OK) return rc;
+  int64_t blocks = (n_vox + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  const int has_scale = scale != 1.0f;
+  JSCC_TIMED("sc_reduce_scatter", st,
+             (sc_reduce_scatter_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldp, (int)p.chunks, 1, 1, rotmat_inv,
+                                                                          ld_rot, 0, n_vox, has_scale, scale,
+                                                                          weight)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_take_bad_detector_count(unsigned int* out) {
+  unsigned int h = 0, zero = 0;
+  JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_bad_detector_count, sizeof(h)));
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_bad_detector_count, &zero, sizeof(zero)));
+  if (out) *out = h;
+  return JSCC_OK;
+}
+
+}  // extern "C"

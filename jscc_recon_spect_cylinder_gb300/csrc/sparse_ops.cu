@@ -1,0 +1,491 @@
+// Sparse Compton rows on a coarse polar grid (kernel c): separable coarse<->fine maps,
+// pack/unpack, materialisation and the fused sparse list-mode weight.
+//
+// Reference semantics: compton_sparse_ops.py. The reference applies its operators as
+// dense matrix products (layer_expand is [fine layers x coarse layers] block-diagonal,
+// z_expand [fine z x coarse z]); every row of those matrices has at most two non-zeros
+// (two-tap periodic interpolation in theta, two-tap linear interpolation in z), and the
+// reduce matrices sample (theta) or interpolate (z). Here each map is a pair of small CSR
+// tables built from the reference's own matrices by the host, so each output element
+// costs a handful of loads instead of a full matrix row: O(V) per row instead of O(V_f V_c).
+//
+// out[r][zo * n_lo + lo] = sum_{(zi, wz) in Z[zo]} wz * sum_{(li, wl) in L[lo]} wl * in[r][zi * n_li + li]
+// (layer sum first, then z, as the reference's two matmuls).
+#include "jscc_common.cuh"
+
+namespace jscc {
+
+// ------------------------------------------------------------------ separable map
+template <typename TI>
+__device__ __forceinline__ float ld_any(const TI* p, int64_t i);
+template <>
+__device__ __forceinline__ float ld_any<float>(const float* p, int64_t i) { return __ldg(p + i); }
+template <>
+__device__ __forceinline__ float ld_any<__nv_bfloat16>(const __nv_bfloat16* p, int64_t i) {
+  return __bfloat162float(p[i]);
+}
+
+template <typename TI>
+__global__ void sparse_map_kernel(const TI* __restrict__ in, int64_t ld_in, const int32_t* __restrict__ row_idx,
+                                  int64_t n_rows, float* __restrict__ out, int64_t ld_out,
+                                  const int32_t* __restrict__ zp, const int32_t* __restrict__ zi,
+                                  const float* __restrict__ zw, int n_zo, const int32_t* __restrict__ lp,
+                                  const int32_t* __restrict__ li, const float* __restrict__ lw, int n_lo, int n_li) {
+  const int64_t r = blockIdx.y;
+  if (r >= n_rows) return;
+  const TI* src = in + (row_idx ? (int64_t)row_idx[r] : r) * ld_in;
+  const int64_t n_out = (int64_t)n_zo * n_lo;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out; o += (int64_t)gridDim.x * blockDim.x) {
+    const int zo = (int)(o / n_lo), lo = (int)(o % n_lo);
+    float acc = 0.f;
+    for (int a = zp[zo]; a < zp[zo + 1]; ++a) {
+      const int64_t base = (int64_t)zi[a] * n_li;
+      float s = 0.f;
+      for (int b = lp[lo]; b < lp[lo + 1]; ++b) s = fmaf(lw[b], ld_any(src, base + li[b]), s);
+      acc = fmaf(zw[a], s, acc);
+    }
+    out[r * ld_out + o] = acc;
+  }
+}
+
+// ------------------------------------------------------------------ pack / unpack
+__global__ void sparse_pack_kernel(const int64_t* __restrict__ cp1, const float* __restrict__ tc, int64_t ld_tc,
+                                   int64_t n, int64_t vc, float* __restrict__ out, int64_t ld_out) {
+  const int64_t i = blockIdx.y;
+  if (i >= n) return;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= vc; c += (int64_t)gridDim.x * blockDim.x)
+    out[i * ld_out + c] = c == 0 ? (float)cp1[i] : tc[i * ld_tc + c - 1];
+}
+
+__global__ void sparse_unpack_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n,
+                                     int64_t* __restrict__ cp1) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    cp1[i] = (int64_t)rintf(rows[i * ld_rows]);  // torch.round: half to even
+}
+
+// ------------------------------------------------------------------ fine value of a sparse row
+// Upsample taps: fine j = zf * n_lf + lf has z taps (zt[2 zf], zt[2 zf + 1]) with weights
+// zwt[...] and layer taps (lt[2 lf], lt[2 lf + 1]) with weights lwt[...]; a missing tap has
+// weight 0 and a valid index.
+struct UpTaps {
+  const int32_t* zt;
+  const float* zwt;
+  const int32_t* lt;
+  const float* lwt;
+  int n_lf;
+  int n_lc;
+};
+
+__device__ __forceinline__ float up_value(const float* __restrict__ tc, const UpTaps& t, int zf, int lf) {
+  const int l0 = t.lt[2 * lf], l1 = t.lt[2 * lf + 1];
+  const float w0 = t.lwt[2 * lf], w1 = t.lwt[2 * lf + 1];
+  const int z0 = t.zt[2 * zf], z1 = t.zt[2 * zf + 1];
+  const float u0 = t.zwt[2 * zf], u1 = t.zwt[2 * zf + 1];
+  const float* r0 = tc + (int64_t)z0 * t.n_lc;
+  const float* r1 = tc + (int64_t)z1 * t.n_lc;
+  float a = w0 * __ldg(r0 + l0);
+  if (w1 != 0.f) a = fmaf(w1, __ldg(r0 + l1), a);
+  float v = u0 * a;
+  if (u1 != 0.f) {
+    float b = w0 * __ldg(r1 + l0);
+    if (w1 != 0.f) b = fmaf(w1, __ldg(r1 + l1), b);
+    v = fmaf(u1, b, v);
+  }
+  return v;
+}
+
+__device__ __forceinline__ float finite_or_zero(float v) { return isfinite(v) ? v : 0.f; }
+
+// ------------------------------------------------------------------ materialise
+// fine[i][j] = nan_to_num(up(tc_i)[j] * sysmat[clamp(cp1_i - 1)][j]); rsum[i] = sum_j fine[i][j]
+template <typename TE>
+__global__ void __launch_bounds__(256)
+sparse_materialize_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, int64_t vf,
+                          const TE* __restrict__ eff, int64_t ld_eff, int64_t n_det, UpTaps taps,
+                          float* __restrict__ fine, int64_t ld_fine, float* __restrict__ rsum) {
+  __shared__ float red[8];
+  const int64_t i = blockIdx.x;
+  if (i >= n) return;
+  const float* row = rows + i * ld_rows;
+  int64_t g = (int64_t)rintf(row[0]) - 1;
+  g = g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+  const float* tc = row + 1;
+  const TE* er = eff + g * ld_eff;
+  float s = 0.f;
+  for (int64_t j = threadIdx.x; j < vf; j += blockDim.x) {
+    const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
+    const float v = finite_or_zero(up_value(tc, taps, zf, lf) * ld_any(er, j));
+    fine[i * ld_fine + j] = v;
+    s += v;
+  }
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    rsum[i] = t;
+  }
+}
+
+// ------------------------------------------------------------------ fused sparse weight
+constexpr int kSpThreads = 256;
+
+// f[i] = sum_j v_ij x_j, s[i] = sum_j v_ij, v = up(tc_i) * eff_g(i) (nan_to_num in MATERIALIZE mode)
+template <int EB, bool MATERIALIZE, typename TE>
+__global__ void __launch_bounds__(kSpThreads)
+sparse_forward_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, int64_t vf,
+                      const float* __restrict__ x, const TE* __restrict__ eff, int64_t ld_eff, int64_t n_det,
+                      UpTaps taps, float* __restrict__ f_out, float* __restrict__ s_out) {
+  __shared__ int64_t sg[EB];
+  __shared__ float red[kSpThreads / 32][2 * EB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t i0 = (int64_t)blockIdx.x * EB;
+  const int ne = (n - i0) < EB ? (int)(n - i0) : EB;
+  if (tid < EB) {
+    const int64_t i = i0 + tid < n ? i0 + tid : n - 1;
+    int64_t g = (int64_t)rintf(rows[i * ld_rows]) - 1;
+    sg[tid] = g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+  }
+  __syncthreads();
+  float af[EB], as[EB];
+#pragma unroll
+  for (int e = 0; e < EB; ++e) af[e] = as[e] = 0.f;
+  for (int64_t j = tid; j < vf; j += kSpThreads) {
+    const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
+    const float xj = __ldg(x + j);
+#pragma unroll
+    for (int e = 0; e < EB; ++e) {
+      if (e < ne) {
+        const float* tc = rows + (i0 + e) * ld_rows + 1;
+        float v = up_value(tc, taps, zf, lf);
+        if (v != 0.f) {
+          v *= ld_any(eff + sg[e] * ld_eff, j);
+          if (MATERIALIZE) v = finite_or_zero(v);
+          af[e] = fmaf(v, xj, af[e]);
+          as[e] += v;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < EB; ++e) {
+    const float a = warp_sum(af[e]);
+    const float b = warp_sum(as[e]);
+    if (lane == 0) {
+      red[warp][e] = a;
+      red[warp][EB + e] = b;
+    }
+  }
+  __syncthreads();
+  if (tid < ne) {
+    float fa = 0.f, sa = 0.f;
+#pragma unroll
+    for (int w = 0; w < kSpThreads / 32; ++w) {
+      fa += red[w][tid];
+      sa += red[w][EB + tid];
+    }
+    f_out[i0 + tid] = fa;
+    s_out[i0 + tid] = sa;
+  }
+}
+
+// coef[i]: MATERIALIZE: valid = isfinite(s) && s > 0; coef = (1 / max(f / s, 1e-12)) / s, else 0
+//          GROUPED:     coef = 1 / max(f, 1e-12)
+template <bool MATERIALIZE>
+__global__ void sparse_coef_kernel(const float* __restrict__ f, const float* __restrict__ s, int64_t n,
+                                   float* __restrict__ coef) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (MATERIALIZE) {
+      const float si = s[i];
+      const bool valid = isfinite(si) && si > 0.f;
+      coef[i] = valid ? (1.0f / fmaxf(f[i] / si, 1e-12f)) / si : 0.f;
+    } else {
+      coef[i] = 1.0f / fmaxf(f[i], 1e-12f);
+    }
+  }
+}
+
+constexpr int kSpStage = 64;
+
+// part[chunk][j] = sum_{i in chunk} v_ij coef_i
+template <bool MATERIALIZE, typename TE>
+__global__ void __launch_bounds__(kSpThreads)
+sparse_back_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, int64_t ev_per_chunk, int64_t vf,
+                   const float* __restrict__ coef, const TE* __restrict__ eff, int64_t ld_eff, int64_t n_det,
+                   UpTaps taps, float* __restrict__ part, int64_t ldp) {
+  __shared__ int64_t sg[kSpStage];
+  __shared__ float sc[kSpStage];
+  const int tid = threadIdx.x;
+  const int64_t j = (int64_t)blockIdx.x * kSpThreads + tid;
+  const int64_t e_begin = (int64_t)blockIdx.y * ev_per_chunk;
+  int64_t e_end = e_begin + ev_per_chunk;
+  if (e_end > n) e_end = n;
+  const int zf = j < vf ? (int)(j / taps.n_lf) : 0, lf = j < vf ? (int)(j % taps.n_lf) : 0;
+  float acc = 0.f;
+  for (int64_t s0 = e_begin; s0 < e_end; s0 += kSpStage) {
+    const int cnt = (e_end - s0) < kSpStage ? (int)(e_end - s0) : kSpStage;
+    __syncthreads();
+    if (tid < cnt) {
+      int64_t g = (int64_t)rintf(rows[(s0 + tid) * ld_rows]) - 1;
+      sg[tid] = g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+      sc[tid] = coef[s0 + tid];
+    }
+    __syncthreads();
+    if (j < vf) {
+      for (int e = 0; e < cnt; ++e) {
+        const float ce = sc[e];
+        if (ce == 0.f) continue;
+        const float* tc = rows + (s0 + e) * ld_rows + 1;
+        float v = up_value(tc, taps, zf, lf);
+        if (v != 0.f) {
+          v *= ld_any(eff + sg[e] * ld_eff, j);
+          if (MATERIALIZE) v = finite_or_zero(v);
+          acc = fmaf(v, ce, acc);
+        }
+      }
+    }
+  }
+  if (j < vf) part[(int64_t)blockIdx.y * ldp + j] = acc;
+}
+
+// weight[j] += scale * nan_to_num(sum_c part[c][src(j)]), src = rotmat_inv[j, 0] - 1 or j
+__global__ void sparse_reduce_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
+                                     const int64_t* __restrict__ rotinv, int64_t ld_rot, int64_t V, int has_scale,
+                                     float scale, float* __restrict__ weight) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V; j += (int64_t)gridDim.x * blockDim.x) {
+    int64_t src = j;
+    if (rotinv) {
+      src = rotinv[j * ld_rot] - 1;
+      if (src < 0 || src >= V) continue;
+    }
+    float s = 0.f;
+    for (int c = 0; c < chunks; ++c) s += part[(int64_t)c * ldp + src];
+    s = finite_or_zero(s);
+    weight[j] = has_scale ? __fadd_rn(weight[j], __fmul_rn(scale, s)) : __fadd_rn(weight[j], s);
+  }
+}
+
+// Shared with sc_projector.cu.
+__global__ void sc_gather_rot_kernel(const float* __restrict__ img, const int64_t* __restrict__ rotmat,
+                                     int64_t ld_rot, int r0, int nr, int64_t V, int64_t ldx,
+                                     float* __restrict__ xr);
+
+struct SpPlan {
+  int64_t chunks, ev_per_chunk, ldp;
+  size_t ws_bytes;
+};
+
+static SpPlan plan_sparse(int64_t n, int64_t vf) {
+  SpPlan p{};
+  const int64_t tiles = (vf + kSpThreads - 1) / kSpThreads;
+  int64_t chunks = (2432 + tiles - 1) / (tiles > 0 ? tiles : 1);
+  const int64_t max_chunks = (n + 63) / 64;
+  if (chunks > max_chunks) chunks = max_chunks;
+  if (chunks < 1) chunks = 1;
+  p.ev_per_chunk = (n + chunks - 1) / chunks;
+  if (p.ev_per_chunk < 1) p.ev_per_chunk = 1;
+  p.chunks = (n + p.ev_per_chunk - 1) / p.ev_per_chunk;
+  if (p.chunks < 1) p.chunks = 1;
+  p.ldp = (int64_t)align_up((size_t)(vf > 0 ? vf : 1), 8);
+  size_t b = 0;
+  b += align_up((size_t)p.ldp * sizeof(float), 256);                     // rotated image
+  b += align_up((size_t)(n > 0 ? n : 1) * sizeof(float), 256) * 3;      // f, s, coef
+  b += align_up((size_t)p.chunks * p.ldp * sizeof(float), 256);          // partials
+  p.ws_bytes = b + 256;
+  return p;
+}
+
+template <bool MAT, typename TE>
+static void launch_sparse_weight(const float* rows, int64_t ld_rows, int64_t n, int64_t vf, const float* x,
+                                 const TE* eff, int64_t ld_eff, int64_t n_det, const UpTaps& taps, float* f, float* s,
+                                 float* coef, float* part, const SpPlan& p, cudaStream_t st) {
+  constexpr int EB = 8;
+  JSCC_TIMED("sparse_forward", st,
+             (sparse_forward_kernel<EB, MAT, TE><<<(unsigned)((n + EB - 1) / EB), kSpThreads, 0, st>>>(
+                 rows, ld_rows, n, vf, x, eff, ld_eff, n_det, taps, f, s)));
+  launch_counter().fetch_add(1);
+  int64_t cb = (n + 255) / 256;
+  if (cb > 4096) cb = 4096;
+  JSCC_TIMED("sparse_coef", st, (sparse_coef_kernel<MAT><<<(unsigned)cb, 256, 0, st>>>(f, s, n, coef)));
+  launch_counter().fetch_add(1);
+  dim3 bgrid((unsigned)((vf + kSpThreads - 1) / kSpThreads), (unsigned)p.chunks);
+  JSCC_TIMED("sparse_back", st,
+             (sparse_back_kernel<MAT, TE><<<bgrid, kSpThreads, 0, st>>>(rows, ld_rows, n, p.ev_per_chunk, vf, coef,
+                                                                        eff, ld_eff, n_det, taps, part, p.ldp)));
+  launch_counter().fetch_add(1);
+}
+
+}  // namespace jscc
+
+using namespace jscc;
+
+extern "C" {
+
+int jscc_sparse_map(const void* in, int32_t in_dtype, int64_t ld_in, const int32_t* row_idx, int64_t n_rows,
+                    float* out, int64_t ld_out, const int32_t* z_ptr, const int32_t* z_idx, const float* z_w,
+                    int32_t n_zo, int32_t n_zi, const int32_t* l_ptr, const int32_t* l_idx, const float* l_w,
+                    int32_t n_lo, int32_t n_li, void* stream) {
+  JSCC_REQUIRE(n_rows >= 0 && n_zo >= 0 && n_lo >= 0 && n_zi >= 0 && n_li >= 0, "jscc_sparse_map: negative size");
+  JSCC_REQUIRE(in_dtype == JSCC_DTYPE_F32 || in_dtype == JSCC_DTYPE_BF16, "jscc_sparse_map: bad dtype");
+  if (n_rows == 0 || (int64_t)n_zo * n_lo == 0) return JSCC_OK;
+  JSCC_REQUIRE(in && out && z_ptr && z_idx && z_w && l_ptr && l_idx && l_w, "jscc_sparse_map: null pointer argument");
+  JSCC_REQUIRE(ld_in >= (int64_t)n_zi * n_li && ld_out >= (int64_t)n_zo * n_lo, "jscc_sparse_map: bad leading dims");
+  JSCC_REQUIRE(n_rows <= 65535, "jscc_sparse_map: at most 65,535 rows per call");
+  cudaStream_t st = as_stream(stream);
+  const int64_t n_out = (int64_t)n_zo * n_lo;
+  int64_t bx = (n_out + 255) / 256;
+  if (bx > 128) bx = 128;
+  dim3 grid((unsigned)bx, (unsigned)n_rows);
+  if (in_dtype == JSCC_DTYPE_F32)
+    JSCC_TIMED("sparse_map", st,
+               (sparse_map_kernel<float><<<grid, 256, 0, st>>>(static_cast<const float*>(in), ld_in, row_idx, n_rows,
+                                                               out, ld_out, z_ptr, z_idx, z_w, n_zo, l_ptr, l_idx, l_w,
+                                                               n_lo, n_li)));
+  else
+    JSCC_TIMED("sparse_map", st,
+               (sparse_map_kernel<__nv_bfloat16><<<grid, 256, 0, st>>>(
+                   static_cast<const __nv_bfloat16*>(in), ld_in, row_idx, n_rows, out, ld_out, z_ptr, z_idx, z_w, n_zo,
+                   l_ptr, l_idx, l_w, n_lo, n_li)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_sparse_pack(const int64_t* cp1, const float* t_compton, int64_t ld_tc, int64_t n_events, int64_t n_coarse,
+                     float* rows, int64_t ld_rows, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_coarse >= 0, "jscc_sparse_pack: negative size");
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(cp1 && rows && (t_compton || n_coarse == 0), "jscc_sparse_pack: null pointer argument");
+  JSCC_REQUIRE(ld_rows >= n_coarse + 1 && ld_tc >= n_coarse, "jscc_sparse_pack: bad leading dims");
+  JSCC_REQUIRE(n_events <= 65535, "jscc_sparse_pack: at most 65,535 events per call");
+  cudaStream_t st = as_stream(stream);
+  int64_t bx = (n_coarse + 1 + 255) / 256;
+  if (bx > 64) bx = 64;
+  dim3 grid((unsigned)bx, (unsigned)n_events);
+  JSCC_TIMED("sparse_pack", st,
+             (sparse_pack_kernel<<<grid, 256, 0, st>>>(cp1, t_compton, ld_tc, n_events, n_coarse, rows, ld_rows)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_sparse_unpack_ids(const float* rows, int64_t ld_rows, int64_t n_events, int64_t* cp1, void* stream) {
+  JSCC_REQUIRE(n_events >= 0, "jscc_sparse_unpack_ids: negative size");
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(rows && cp1, "jscc_sparse_unpack_ids: null pointer argument");
+  cudaStream_t st = as_stream(stream);
+  int64_t b = (n_events + 255) / 256;
+  if (b > 4096) b = 4096;
+  JSCC_TIMED("sparse_unpack", st, (sparse_unpack_kernel<<<(unsigned)b, 256, 0, st>>>(rows, ld_rows, n_events, cp1)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+static int make_taps(const int32_t* z_taps, const float* z_tw, const int32_t* l_taps, const float* l_tw,
+                     int32_t n_lf, int32_t n_lc, UpTaps* t) {
+  JSCC_REQUIRE(z_taps && z_tw && l_taps && l_tw, "sparse upsample taps missing");
+  JSCC_REQUIRE(n_lf > 0 && n_lc > 0, "sparse upsample layer sizes must be positive");
+  t->zt = z_taps;
+  t->zwt = z_tw;
+  t->lt = l_taps;
+  t->lwt = l_tw;
+  t->n_lf = n_lf;
+  t->n_lc = n_lc;
+  return JSCC_OK;
+}
+
+int jscc_sparse_materialize(const float* rows, int64_t ld_rows, int64_t n_events, const void* sysmat,
+                            int32_t sysmat_dtype, int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps,
+                            const float* z_tw, int32_t n_zf, const int32_t* l_taps, const float* l_tw, int32_t n_lf,
+                            int32_t n_lc, float* fine, int64_t ld_fine, float* row_sum, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_det > 0, "jscc_sparse_materialize: bad sizes");
+  JSCC_REQUIRE(sysmat_dtype == JSCC_DTYPE_F32 || sysmat_dtype == JSCC_DTYPE_BF16, "jscc_sparse_materialize: dtype");
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(rows && sysmat && fine && row_sum, "jscc_sparse_materialize: null pointer argument");
+  UpTaps t;
+  const int rc = make_taps(z_taps, z_tw, l_taps, l_tw, n_lf, n_lc, &t);
+  if (rc != JSCC_OK) return rc;
+  const int64_t vf = (int64_t)n_zf * n_lf;
+  JSCC_REQUIRE(ld_fine >= vf && ld_sysmat >= vf, "jscc_sparse_materialize: bad leading dims");
+  JSCC_REQUIRE(n_events <= 2147483647LL, "jscc_sparse_materialize: too many events");
+  cudaStream_t st = as_stream(stream);
+  if (sysmat_dtype == JSCC_DTYPE_F32)
+    JSCC_TIMED("sparse_materialize", st,
+               (sparse_materialize_kernel<float><<<(unsigned)n_events, 256, 0, st>>>(
+                   rows, ld_rows, n_events, vf, static_cast<const float*>(sysmat), ld_sysmat, n_det, t, fine, ld_fine,
+                   row_sum)));
+  else
+    JSCC_TIMED("sparse_materialize", st,
+               (sparse_materialize_kernel<__nv_bfloat16><<<(unsigned)n_events, 256, 0, st>>>(
+                   rows, ld_rows, n_events, vf, static_cast<const __nv_bfloat16*>(sysmat), ld_sysmat, n_det, t, fine,
+                   ld_fine, row_sum)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+size_t jscc_sparse_weight_workspace_bytes(int64_t n_events, int64_t n_fine) {
+  return plan_sparse(n_events, n_fine).ws_bytes;
+}
+
+int jscc_sparse_weight(const float* rows, int64_t ld_rows, int64_t n_events, const void* sysmat, int32_t sysmat_dtype,
+                       int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
+                       const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc, int32_t mode,
+                       const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
+                       float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_det > 0, "jscc_sparse_weight: bad sizes");
+  JSCC_REQUIRE(mode == JSCC_SPARSE_MATERIALIZE || mode == JSCC_SPARSE_GROUPED, "jscc_sparse_weight: bad mode %d",
+               mode);
+  JSCC_REQUIRE(sysmat_dtype == JSCC_DTYPE_F32 || sysmat_dtype == JSCC_DTYPE_BF16, "jscc_sparse_weight: dtype");
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(rows && sysmat && img && weight, "jscc_sparse_weight: null pointer argument");
+  JSCC_REQUIRE((rotmat == nullptr) == (rotmat_inv == nullptr), "jscc_sparse_weight: give both rotation tables");
+  UpTaps t;
+  int rc = make_taps(z_taps, z_tw, l_taps, l_tw, n_lf, n_lc, &t);
+  if (rc != JSCC_OK) return rc;
+  const int64_t vf = (int64_t)n_zf * n_lf;
+  JSCC_REQUIRE(ld_sysmat >= vf, "jscc_sparse_weight: ld_sysmat < fine voxels");
+  const SpPlan p = plan_sparse(n_events, vf);
+  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "jscc_sparse_weight: workspace too small (%zu < %zu)",
+               workspace_bytes, p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  float* xr = cv.take<float>((size_t)p.ldp);
+  float* f = cv.take<float>((size_t)n_events);
+  float* s = cv.take<float>((size_t)n_events);
+  float* coef = cv.take<float>((size_t)n_events);
+  float* part = cv.take<float>((size_t)p.chunks * p.ldp);
+  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight: workspace carve overflow");
+  cudaStream_t st = as_stream(stream);
+  const float* x = img;
+  if (rotmat) {
+    int64_t blocks = (vf + 255) / 256;
+    if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+    JSCC_TIMED("sc_gather_rot", st,
+               (sc_gather_rot_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, rotmat, ld_rot, 0, 1, vf, p.ldp, xr)));
+    JSCC_LAUNCH_CHECK();
+    x = xr;
+  }
+  const bool mat = mode == JSCC_SPARSE_MATERIALIZE;
+  if (sysmat_dtype == JSCC_DTYPE_F32) {
+    const float* e = static_cast<const float*>(sysmat);
+    if (mat) launch_sparse_weight<true, float>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef, part, p, st);
+    else launch_sparse_weight<false, float>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef, part, p, st);
+  } else {
+    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(sysmat);
+    if (mat)
+      launch_sparse_weight<true, __nv_bfloat16>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef,
+                                                part, p, st);
+    else
+      launch_sparse_weight<false, __nv_bfloat16>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef,
+                                                 part, p, st);
+  }
+  JSCC_CUDA_CHECK(cudaGetLastError());
+  int64_t blocks = (vf + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  const int has_scale = scale != 1.0f;
+  JSCC_TIMED("sparse_reduce", st,
+             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldp, (int)p.chunks, rotmat_inv, ld_rot, vf,
+                                                                     has_scale, scale, weight)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+}  // extern "C"

@@ -184,3 +184,257 @@ def em_update(
     )
     _lib.check(rc, "jscc_em_update")
     return out.view_as(img) if out.shape != img.shape else out
+
+
+# ============================================================================ Compton cone
+def _eff_args(eff: torch.Tensor | None):
+    if eff is None:
+        return None, _lib.DTYPE_F32, 0
+    e = _rows_contig(eff)
+    return e, _dtype_code(e), e.stride(0)
+
+
+def compton_event_prep(list_smeared, detector_pos, sig1_sq, sig2_sq, e0, ene_resolution, thr_max, thr_min, thr_sum,
+                       model=_lib.CONE_STRICT, theta_fp64=True, window_sigmas=0.0, delta_r1=0.0, delta_r2=0.0):
+    """Event selection + 16-float records (jscc_compton_event_prep). Returns
+    ``(keep [E] bool, records [E, 16], row_id [E] int32)`` for all list rows."""
+    dev = _lib.require_cuda(list_smeared, detector_pos, sig1_sq, sig2_sq, what="compton_event_prep")
+    L = _f32_contig(list_smeared)
+    if L.dim() != 2 or L.size(1) < 4:
+        raise ValueError("list must be [events, 4] (cp1, e1, cp2, e2)")
+    det = _f32_contig(detector_pos)
+    s1 = _f32_contig(sig1_sq) if sig1_sq is not None else None
+    s2 = _f32_contig(sig2_sq) if sig2_sq is not None else None
+    n = L.size(0)
+    keep = torch.empty(n, dtype=torch.uint8, device=dev)
+    rec = torch.empty((n, _lib.CONE_RECORD_FLOATS), dtype=torch.float32, device=dev)
+    rid = torch.empty(n, dtype=torch.int32, device=dev)
+    rc = _lib.load().jscc_compton_event_prep(
+        L.data_ptr(), L.stride(0), n, det.data_ptr(), _lib.ptr(s1), _lib.ptr(s2), det.size(0), float(e0),
+        float(ene_resolution), float(thr_max), float(thr_min), float(thr_sum), int(model), 1 if theta_fp64 else 0,
+        float(window_sigmas), float(delta_r1), float(delta_r2), keep.data_ptr(), rec.data_ptr(), rid.data_ptr(),
+        _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_compton_event_prep")
+    return keep.bool(), rec, rid
+
+
+MAX_ROWS_PER_LAUNCH = 65535
+
+
+def compton_cone_rows(records, row_id, coor, model=_lib.CONE_STRICT, eff=None, want_tc=True, want_t=True):
+    """Materialised cone rows: ``(t_compton, t)`` with ``t = t_compton * eff[row_id]``."""
+    dev = _lib.require_cuda(records, row_id, coor, eff, what="compton_cone_rows")
+    c = _f32_contig(coor)
+    V = c.size(0)
+    n = records.size(0)
+    tc = torch.empty((n, V), dtype=torch.float32, device=dev) if want_tc else None
+    t = torch.empty((n, V), dtype=torch.float32, device=dev) if want_t else None
+    e, edt, ld = _eff_args(eff)
+    lib = _lib.load()
+    for a in range(0, n, MAX_ROWS_PER_LAUNCH):
+        b = min(n, a + MAX_ROWS_PER_LAUNCH)
+        rc = lib.jscc_compton_cone_rows(
+            records[a:b].data_ptr(), row_id[a:b].data_ptr(), b - a, c.data_ptr(), V, int(model), _lib.ptr(e), edt, ld,
+            None if tc is None else tc[a:b].data_ptr(), None if t is None else t[a:b].data_ptr(),
+            _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_compton_cone_rows")
+    return tc, t
+
+
+def compton_row_stats(records, row_id, coor, model=_lib.CONE_STRICT, eff=None, use_window=False):
+    """Per-event ``(sum t, sum t^2, any-NaN)`` of ``t = cone * eff`` without storing rows."""
+    dev = _lib.require_cuda(records, row_id, coor, eff, what="compton_row_stats")
+    c = _f32_contig(coor)
+    n = records.size(0)
+    s1 = torch.empty(n, dtype=torch.float32, device=dev)
+    s2 = torch.empty(n, dtype=torch.float32, device=dev)
+    nan = torch.empty(n, dtype=torch.int32, device=dev)
+    e, edt, ld = _eff_args(eff)
+    rc = _lib.load().jscc_compton_row_stats(
+        records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), c.size(0), int(model), 1 if use_window else 0,
+        _lib.ptr(e), edt, ld, s1.data_ptr(), s2.data_ptr(), nan.data_ptr(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_compton_row_stats")
+    return s1, s2, nan.bool()
+
+
+def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
+                   rotmat_inv=None, rot_col=0, scale=1.0, out=None):
+    """``out += scale * rotinv( T^T (1 / T rot(img)) )`` with T recomputed on the fly."""
+    dev = _lib.require_cuda(records, row_id, coor, img, eff, rotmat, rotmat_inv, out, what="compton_weight")
+    c = _f32_contig(coor)
+    V = c.size(0)
+    x = _f32_contig(img.reshape(-1))
+    if x.numel() != V:
+        raise ValueError(f"img has {x.numel()} voxels, coor has {V}")
+    if out is None:
+        out = torch.zeros((V, 1), dtype=torch.float32, device=dev)
+    rotmat = _index_table(rotmat, V, "rotmat")
+    rotmat_inv = _index_table(rotmat_inv, V, "rotmat_inv")
+    rm = ri = None
+    ld_rot = 0
+    if rotmat is not None:
+        if not (_is_identity(rotmat, rot_col, 1) and _is_identity(rotmat_inv, rot_col, 1)):
+            rm = rotmat.data_ptr() + rot_col * 8
+            ri = rotmat_inv.data_ptr() + rot_col * 8
+            ld_rot = rotmat.stride(0)
+    e, edt, ld = _eff_args(eff)
+    n = records.size(0)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
+    rc = lib.jscc_compton_weight(
+        records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), V, int(model), 1 if use_window else 0, _lib.ptr(e),
+        edt, ld, x.data_ptr(), rm, ri, ld_rot, float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(),
+        _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_compton_weight")
+    return out
+
+
+# ============================================================================ sparse rows
+class SparseTables:
+    """Device tables of a ComptonSparseProjector: CSR forms of the four separable maps and
+    the two-tap upsample arrays of the fused kernels, built from the projector's own
+    dense matrices (so the weights are the reference's float32 values)."""
+
+    def __init__(self, layer_reduce, z_reduce, layer_expand, z_expand, device):
+        def csr(m):
+            m = m.detach().to("cpu", torch.float32)
+            nz = m != 0
+            counts = nz.sum(dim=1)
+            ptr = torch.zeros(m.size(0) + 1, dtype=torch.int32)
+            ptr[1:] = torch.cumsum(counts, 0).to(torch.int32)
+            rows, cols = torch.nonzero(nz, as_tuple=True)
+            return (ptr.to(device), cols.to(torch.int32).to(device), m[rows, cols].contiguous().to(device))
+
+        def two_taps(m):
+            # rows of an expand matrix have one or two non-zeros; a single tap is
+            # duplicated with weight 0 so the kernels always read two valid indices
+            m = m.detach().to("cpu", torch.float32)
+            n = m.size(0)
+            nz = m != 0
+            counts = nz.sum(dim=1)
+            if int(counts.max()) > 2 or int(counts.min()) < 1:
+                raise ValueError("expand matrix rows must have one or two taps")
+            rows, cols = torch.nonzero(nz, as_tuple=True)
+            first = torch.zeros(n, dtype=torch.int64)
+            first[1:] = torch.cumsum(counts, 0)[:-1]
+            idx = torch.empty((n, 2), dtype=torch.int32)
+            w = torch.zeros((n, 2), dtype=torch.float32)
+            idx[:, 0] = cols[first].to(torch.int32)
+            w[:, 0] = m[rows[first], cols[first]]
+            two = counts == 2
+            sec = first[two] + 1
+            idx[:, 1] = idx[:, 0]
+            idx[two, 1] = cols[sec].to(torch.int32)
+            w[two, 1] = m[rows[sec], cols[sec]]
+            return idx.to(device), w.to(device)
+
+        self.n_lf, self.n_lc = layer_expand.shape
+        self.n_zf, self.n_zc = z_expand.shape
+        self.up = (csr(z_expand), csr(layer_expand))                 # coarse -> fine rows
+        self.adj = (csr(z_expand.t()), csr(layer_expand.t()))        # fine -> coarse (adjoint)
+        self.red = (csr(z_reduce), csr(layer_reduce))                # fine -> coarse (sample)
+        self.red_t = (csr(z_reduce.t()), csr(layer_reduce.t()))      # coarse -> fine (weight image)
+        self.z_taps, self.z_tw = two_taps(z_expand)
+        self.l_taps, self.l_tw = two_taps(layer_expand)
+
+
+def sparse_map(rows_in, maps, n_zo, n_zi, n_lo, n_li, row_idx=None):
+    """Apply one separable map (``maps = (Z csr, L csr)``) to every row of ``rows_in``
+    (optionally gathered by ``row_idx``). Returns float32 ``[rows, n_zo * n_lo]``."""
+    dev = _lib.require_cuda(rows_in, row_idx, what="sparse_map")
+    src = rows_in if rows_in.dim() == 2 else rows_in.reshape(1, -1)
+    src = _rows_contig(src)
+    if src.dtype not in (torch.float32, torch.bfloat16):
+        src = src.float()
+    n = row_idx.numel() if row_idx is not None else src.size(0)
+    if src.size(1) < n_zi * n_li:
+        raise ValueError("input rows are shorter than the map's input size")
+    rid = row_idx.to(torch.int32).contiguous() if row_idx is not None else None
+    out = torch.empty((n, n_zo * n_lo), dtype=torch.float32, device=dev)
+    (zp, zi, zw), (lp, li, lw) = maps
+    lib = _lib.load()
+    for a in range(0, n, MAX_ROWS_PER_LAUNCH):
+        b = min(n, a + MAX_ROWS_PER_LAUNCH)
+        in_ptr = src.data_ptr() if rid is not None else src[a:b].data_ptr()
+        rc = lib.jscc_sparse_map(
+            in_ptr, _dtype_code(src), src.stride(0), None if rid is None else rid[a:b].data_ptr(), b - a,
+            out[a:b].data_ptr(), out.stride(0), zp.data_ptr(), zi.data_ptr(), zw.data_ptr(), n_zo, n_zi,
+            lp.data_ptr(), li.data_ptr(), lw.data_ptr(), n_lo, n_li, _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_sparse_map")
+    return out
+
+
+def sparse_pack(cp1, t_compton):
+    dev = _lib.require_cuda(cp1, t_compton, what="sparse_pack")
+    tc = _f32_contig(t_compton)
+    ids = cp1.to(torch.int64).contiguous()
+    n, vc = tc.shape
+    rows = torch.empty((n, vc + 1), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    for a in range(0, n, MAX_ROWS_PER_LAUNCH):
+        b = min(n, a + MAX_ROWS_PER_LAUNCH)
+        rc = lib.jscc_sparse_pack(ids[a:b].data_ptr(), tc[a:b].data_ptr(), tc.stride(0), b - a, vc,
+                                  rows[a:b].data_ptr(), rows.stride(0), _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_sparse_pack")
+    return rows
+
+
+def sparse_unpack_ids(rows):
+    dev = _lib.require_cuda(rows, what="sparse_unpack_ids")
+    r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
+    out = torch.empty(r.size(0), dtype=torch.int64, device=dev)
+    rc = _lib.load().jscc_sparse_unpack_ids(r.data_ptr(), r.stride(0), r.size(0), out.data_ptr(),
+                                            _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sparse_unpack_ids")
+    return out
+
+
+def sparse_materialize(rows, sysmat, tables: SparseTables):
+    """``(fine [E, V_f], row_sum [E])`` of materialize_sparse_event_rows_to_fine (before the
+    validity selection and the division by the row sum)."""
+    dev = _lib.require_cuda(rows, sysmat, what="sparse_materialize")
+    r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
+    A = _rows_contig(sysmat)
+    n = r.size(0)
+    vf = tables.n_zf * tables.n_lf
+    fine = torch.empty((n, vf), dtype=torch.float32, device=dev)
+    rsum = torch.empty(n, dtype=torch.float32, device=dev)
+    rc = _lib.load().jscc_sparse_materialize(
+        r.data_ptr(), r.stride(0), n, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0), tables.z_taps.data_ptr(),
+        tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(), tables.l_tw.data_ptr(), tables.n_lf,
+        tables.n_lc, fine.data_ptr(), fine.stride(0), rsum.data_ptr(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sparse_materialize")
+    return fine, rsum
+
+
+def sparse_weight(rows, sysmat, tables: SparseTables, img, grouped=False, rotmat=None, rotmat_inv=None, rot_col=0,
+                  scale=1.0, out=None):
+    """Fused sparse list-mode weight (MATERIALIZE or GROUPED semantics), accumulated into ``out``."""
+    dev = _lib.require_cuda(rows, sysmat, img, rotmat, rotmat_inv, out, what="sparse_weight")
+    r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
+    A = _rows_contig(sysmat)
+    vf = tables.n_zf * tables.n_lf
+    x = _f32_contig(img.reshape(-1))
+    if x.numel() != vf:
+        raise ValueError(f"img has {x.numel()} voxels, the projector has {vf}")
+    if out is None:
+        out = torch.zeros((vf, 1), dtype=torch.float32, device=dev)
+    rotmat = _index_table(rotmat, vf, "rotmat")
+    rotmat_inv = _index_table(rotmat_inv, vf, "rotmat_inv")
+    rm = ri = None
+    ld_rot = 0
+    if rotmat is not None:
+        if not (_is_identity(rotmat, rot_col, 1) and _is_identity(rotmat_inv, rot_col, 1)):
+            rm = rotmat.data_ptr() + rot_col * 8
+            ri = rotmat_inv.data_ptr() + rot_col * 8
+            ld_rot = rotmat.stride(0)
+    n = r.size(0)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sparse_weight_workspace_bytes(n, vf))
+    rc = lib.jscc_sparse_weight(
+        r.data_ptr(), r.stride(0), n, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0), tables.z_taps.data_ptr(),
+        tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(), tables.l_tw.data_ptr(), tables.n_lf,
+        tables.n_lc, _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE, x.data_ptr(), rm, ri, ld_rot,
+        float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sparse_weight")
+    return out

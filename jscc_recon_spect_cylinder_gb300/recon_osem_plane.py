@@ -354,3 +354,55 @@ def _run_multi_gpu_compton(t_list_all, sysmat_list_all, proj_list_all, rotmat_al
     if getattr(iter_arg, "mode", 0) == 0:
         img_jsccsd = phase(iter_arg.jsccsd, img_jsccsd, img_jsccsd_iter, joint=True)
     return img_jsccd, img_jsccsd
+
+
+# ============================================================================ fused dense Compton path
+# T recomputed on the fly from compact event records (process_list_plane_strict.
+# get_compton_event_params) instead of stored dense blocks; same weight as
+# get_weight_compton over the builder's rows (the list-mode weight is invariant to the
+# builder's row normalisation).
+
+def get_weight_compton_fused(events, coor, sysmat, img, rotmat=None, rotmat_inv=None, rot_col=0, scale=1.0, out=None,
+                             use_window=True):
+    """``T^T (1 / (T x))`` for a block of ComptonEvents; accumulated into ``out``."""
+    if len(events) == 0:
+        return torch.zeros_like(img) if out is None else out
+    return ops.compton_weight(events.records, events.row_id, coor, img, model=events.model, eff=sysmat,
+                              use_window=use_window, rotmat=rotmat, rotmat_inv=rotmat_inv, rot_col=rot_col,
+                              scale=scale, out=out)
+
+
+def _accumulate_compton_fused(weight, ev_list, coor_all, sysmat_all, rotmat_all, rotmat_inv_all, img, rotate_num,
+                              use_window):
+    for i in range(rotate_num):
+        for ev in ev_list[i]:
+            for ev_tmp, coor, sysmat, rotmat, rotmat_inv in zip(ev, coor_all, sysmat_all, rotmat_all, rotmat_inv_all):
+                if ev_tmp is None or len(ev_tmp) == 0:
+                    continue
+                get_weight_compton_fused(ev_tmp, coor, sysmat, img, rotmat, rotmat_inv, rot_col=i, out=weight,
+                                         use_window=use_window)
+
+
+def osem_list_mode_fused(ev_list_all, coor_all, sysmat_all, rotmat_all, rotmat_inv_all, img, s_map, rotate_num,
+                         use_window=True):
+    """osem_list_mode (recon_osem_plane.py:63-80) with T recomputed on the fly;
+    ``ev_list_all[subset][rotation][divide][energy]`` holds ComptonEvents blocks."""
+    for ev_list in ev_list_all:
+        weight = torch.zeros_like(img)
+        _accumulate_compton_fused(weight, ev_list, coor_all, sysmat_all, rotmat_all, rotmat_inv_all, img, rotate_num,
+                                  use_window)
+        img = ops.em_update(img, weight, s_map, safe=False)
+    return img
+
+
+def osem_joint_mode_fused(sysmat_list_all, proj_list_all, ev_list_all, coor_all, sysmat_all, rotmat_all,
+                          rotmat_inv_all, img, s_map, alpha, rotate_num, use_window=True):
+    """osem_joint_mode (recon_osem_plane.py:100-125) with the Compton half on the fly."""
+    for sysmat_list, proj_list, ev_list in zip(sysmat_list_all, proj_list_all, ev_list_all):
+        w_c = torch.zeros_like(img)
+        w_s = torch.zeros_like(img)
+        _accumulate_sc(w_s, sysmat_list, proj_list, rotmat_all, rotmat_inv_all, img, rotate_num)
+        _accumulate_compton_fused(w_c, ev_list, coor_all, sysmat_all, rotmat_all, rotmat_inv_all, img, rotate_num,
+                                  use_window)
+        img = ops.em_update(img, w_c, s_map, safe=False, coef=2 - alpha, weight_b=w_s, coef_b=alpha)
+    return img

@@ -226,7 +226,12 @@ def golden_sparse(ref):
         out[f"r10_{name}_idx"] = np.stack(nz).astype(np.int32)
         out[f"r10_{name}_val"] = m[nz]
         out[f"r10_{name}_shape"] = np.array(m.shape)
+    rotmat = np.genfromtxt(REF_DIR / "Factors" / "511keV_RotateNum10" / "RotMat_full.csv", delimiter=",",
+                           dtype=np.int64)
+    rotinv = np.genfromtxt(REF_DIR / "Factors" / "511keV_RotateNum10" / "RotMatInv_full.csv", delimiter=",",
+                           dtype=np.int64)
     out.update({
+        "r10_rotmat": rotmat.astype(np.int32), "r10_rotmat_inv": rotinv.astype(np.int32),
         "r10_coor_full": coor_r10.numpy(), "r10_coor_coarse": p10.coor_coarse.numpy(),
         "r10_ring_strides": np.array(p10.ring_strides),
         "r10_dims": np.array([p10.fine_layer_num, p10.fine_z_num, p10.coarse_layer_num, p10.coarse_z_num]),

@@ -1,0 +1,340 @@
+"""GPU parity of the Compton cone kernel (a) and the sparse coarse<->fine kernels (c)
+against the reference's golden outputs and the oracle.
+
+Tolerances: cone rows are compared per row relative to the row maximum (float32 acos /
+exp / sqrt in a different operation order than torch: <= 2e-5 strict, <= 1e-4 legacy);
+weights and images by relative L2 <= 1e-5 (FP32 path)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import compton as oc
+from oracle import sparse as osp
+
+pytestmark = pytest.mark.gpu
+
+TOL_ROW = 2e-5
+TOL_ROW_LEGACY = 1e-4
+TOL_W = 1e-5
+
+
+def _rows_close(a, b, rtol):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    if a.size == 0:
+        return
+    scale = np.maximum(np.abs(b).max(axis=1, keepdims=True), 1e-30)
+    err = np.abs(a - b) / scale
+    assert err.max() < rtol, err.max()
+
+
+def _args(g, tag):
+    return [float(v) for v in g[f"{tag}_args"]]
+
+
+@pytest.mark.parametrize("tag", ["planar", "cyl"])
+def test_strict_builder_golden(cuda, golden, tag):
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+
+    g = golden("compton_builders")
+    dr1, dr2, e0, res, tmax, tmin, tsum = _args(g, tag)
+    L = torch.from_numpy(g[f"{tag}_smeared"]).to(cuda)
+    t, tc, ts, _ = pls.build_rows_from_smeared(torch.from_numpy(g[f"{tag}_sysmat"]).to(cuda),
+                                               torch.from_numpy(g[f"{tag}_det"]).to(cuda),
+                                               torch.from_numpy(g["coor"]).to(cuda), L, dr1, dr2, e0, res, tmax,
+                                               tmin, tsum)
+    _rows_close(t.cpu(), g[f"{tag}_t"], TOL_ROW)
+    _rows_close(tc.cpu(), g[f"{tag}_tc"], TOL_ROW)
+    _rows_close(ts.cpu(), g[f"{tag}_ts"], 1e-6)
+
+
+@pytest.mark.parametrize("tag", ["planar", "cyl"])
+def test_strict_builder_wrapper_smears_in_place(cuda, golden, tag):
+    """The reference's contract: the caller's list is smeared in place with CPU torch.randn
+    draws; outputs are CPU tensors. GPU float32 arithmetic can round the smeared energies
+    differently from the CPU by 1 ulp, so values are compared with a tolerance."""
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+
+    g = golden("compton_builders")
+    a = _args(g, tag)
+    L = torch.from_numpy(g[f"{tag}_list"].copy()).to(cuda)
+    torch.manual_seed(77)
+    t, tc, ts = pls.get_compton_backproj_list_single(torch.from_numpy(g[f"{tag}_sysmat"]).to(cuda),
+                                                     torch.from_numpy(g[f"{tag}_det"]).to(cuda),
+                                                     torch.from_numpy(g["coor"]).to(cuda), L, *a, cuda)
+    assert t.device.type == "cpu"
+    np.testing.assert_allclose(L.cpu().numpy(), g[f"{tag}_smeared"], rtol=3e-7, atol=0)
+    assert t.shape == g[f"{tag}_t"].shape
+    _rows_close(t, g[f"{tag}_t"], 1e-4)
+
+
+@pytest.mark.parametrize("tag", ["planar", "cyl"])
+def test_legacy_builder_golden(cuda, golden, tag):
+    from jscc_recon_spect_cylinder_gb300 import _lib
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+
+    g = golden("compton_builders")
+    dr, e0, res, tmax, tmin, tsum = 1.0 + _args(g, tag)[0], *_args(g, tag)[2:]
+    L = torch.from_numpy(g[f"{tag}_legacy_smeared"]).to(cuda)
+    t, tc, ts, _ = pls.build_rows_from_smeared(torch.from_numpy(g[f"{tag}_sysmat"]).to(cuda),
+                                               torch.from_numpy(g[f"{tag}_det"]).to(cuda),
+                                               torch.from_numpy(g["coor"]).to(cuda), L, dr, dr, e0, res, tmax, tmin,
+                                               tsum, model=_lib.CONE_LEGACY, stability=False)
+    _rows_close(t.cpu(), g[f"{tag}_legacy_t"], TOL_ROW_LEGACY)
+    _rows_close(tc.cpu(), g[f"{tag}_legacy_tc"], TOL_ROW_LEGACY)
+
+
+def _cone_problem(cuda, n_events=3000, n_r=20, n_theta=72, seed=4):
+    """Cylinder detector (isotropic sigma_pos with delta_r = 0.8 mm), 511 keV events."""
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    grid = synthetic.polar_grid(n_r, n_theta, 40.0)
+    scat = synthetic.cylinder_pixels(120.0, 32, 4, 3.0)
+    absb = synthetic.cylinder_pixels(150.0, 32, 4, 3.0)
+    det = torch.cat((scat, absb)).float()
+    g = torch.Generator().manual_seed(seed)
+    sysmat = torch.rand((det.size(0), grid.n_vox), generator=g) * 1e-3 + 1e-5
+    rng = np.random.default_rng(seed)
+    e0 = 0.511
+    cp1 = rng.integers(1, scat.size(0) + 1, n_events)
+    cp2 = rng.integers(scat.size(0) + 1, det.size(0) + 1, n_events)
+    e1 = rng.uniform(0.08, 0.3, n_events)
+    L = np.stack((cp1, e1, cp2, e0 - e1), axis=1).astype(np.float32)
+    res = 0.1 * (0.662 / e0) ** 0.5
+    args = (0.8, 0.8, e0, res, 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001, 0.05, e0 - 0.06)
+    return grid, det, sysmat, L, args
+
+
+def test_fused_cone_weight_matches_stored_t(cuda):
+    """The fused on-the-fly weight equals T^T(1/(Tx)) over the builder's stored rows
+    (row normalisation does not change the list-mode weight); window pruning changes it
+    by far less than float32 rounding."""
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+    grid, det, sysmat, L, args = _cone_problem(cuda)
+    Ld = torch.from_numpy(L).to(cuda)
+    A = sysmat.to(cuda)
+    coor = grid.coor.to(cuda)
+    t, _, _, kept = pls.build_rows_from_smeared(A, det.to(cuda), coor, Ld, *args)
+    ev = pls.get_compton_event_params(A, det.to(cuda), coor, Ld, *args, theta_fp64=False, window_sigmas=9.0)
+    assert torch.equal(ev.list_index, kept)  # identical event selection incl. row filters
+    x = torch.rand((grid.n_vox, 1), generator=torch.Generator().manual_seed(1)).to(cuda) + 0.5
+    w_stored = rop.get_weight_compton(t, x)
+    w_fused = rop.get_weight_compton_fused(ev, coor, A, x)
+    w_exact = rop.get_weight_compton_fused(ev, coor, A, x, use_window=False)
+    assert rel_l2(w_fused.cpu(), w_stored.cpu()) < TOL_W
+    assert rel_l2(w_fused.cpu(), w_exact.cpu()) < 1e-6
+    # against the FP64 oracle on the same events
+    rows64, _, _, _ = oc.strict_builder(sysmat.numpy(), det.numpy(), grid.coor.numpy(), L, *args)
+    from oracle import osem_sc
+
+    w64 = osem_sc.get_weight_compton(rows64, x.cpu().numpy())
+    assert rel_l2(w_fused.cpu(), w64) < 1e-4  # FP32 theta vs FP64 oracle rows
+
+
+def test_fused_list_mode_osem_with_rotations(cuda):
+    """osem_list_mode over stored T and osem_list_mode_fused over event records agree
+    (rotated views, 2 subsets x 2 divides)."""
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    grid, det, sysmat, L, args = _cone_problem(cuda, n_events=2400)
+    R, S, D = 4, 2, 2
+    rot, inv = synthetic.cyclic_rotation_tables(grid.n_r, grid.n_theta, R)
+    rot, inv = rot.to(cuda), inv.to(cuda)
+    A, coor, detc = sysmat.to(cuda), grid.coor.to(cuda), det.to(cuda)
+    chunks = torch.chunk(torch.from_numpy(L).to(cuda), R)
+    t_list = [[[[None] for _ in range(D)] for _ in range(R)] for _ in range(S)]
+    e_list = [[[[None] for _ in range(D)] for _ in range(R)] for _ in range(S)]
+    for r in range(R):
+        t, _, _, _ = pls.build_rows_from_smeared(A, detc, coor, chunks[r].contiguous(), *args)
+        ev = pls.get_compton_event_params(A, detc, coor, chunks[r].contiguous(), *args, theta_fp64=False)
+        assert len(ev) == t.size(0)
+        for j, (ts, es) in enumerate(zip(rop.split_tensor_even(t, S), ev.split(S))):
+            for k, (tk, ek) in enumerate(zip(rop.split_tensor_even(ts, D), es.split(D))):
+                t_list[j][r][k][0] = tk
+                e_list[j][r][k][0] = ek
+    s_d = torch.rand((grid.n_vox, 1), generator=torch.Generator().manual_seed(2)).to(cuda) + 0.5
+    x0 = torch.ones((grid.n_vox, 1), device=cuda)
+    img_t = rop.osem_list_mode(t_list, [rot], [inv], x0, s_d, R)
+    img_f = rop.osem_list_mode_fused(e_list, [coor], [A], [rot], [inv], x0, s_d, R)
+    assert rel_l2(img_f.cpu(), img_t.cpu()) < TOL_W
+
+
+def test_row_stats_match_oracle(cuda):
+    from jscc_recon_spect_cylinder_gb300 import _compton, _lib, ops
+
+    grid, det, sysmat, L, args = _cone_problem(cuda, n_events=500)
+    Ld = torch.from_numpy(L).to(cuda)
+    idx, rec, rid = _compton.select_events(Ld, det.to(cuda), args[0], args[1], *args[2:], theta_fp64=False)
+    ref_idx = oc.event_filter(L, det.numpy(), *args[2:])
+    np.testing.assert_array_equal(idx.cpu().numpy(), ref_idx)
+    s1, s2, nan = ops.compton_row_stats(rec, rid, grid.coor.to(cuda), model=_lib.CONE_STRICT, eff=sysmat.to(cuda))
+    cp1 = L[ref_idx, 0].astype(np.int64)
+    cp2 = L[ref_idx, 2].astype(np.int64)
+    d = det.numpy()
+    tc = oc.cone_rows_strict(d[cp1 - 1], d[cp2 - 1], L[ref_idx, 1], oc.pos_sigma_sq(d, args[0])[cp1 - 1],
+                             oc.pos_sigma_sq(d, args[1])[cp2 - 1], grid.coor.numpy(), args[2], args[3],
+                             dtype=np.float32)
+    t = tc * sysmat.numpy()[cp1 - 1]
+    assert rel_l2(s1.cpu(), t.sum(1)) < 1e-5
+    assert rel_l2(s2.cpu(), (t.astype(np.float64) ** 2).sum(1)) < 1e-5
+    assert not nan.any()
+
+
+def test_bad_detector_ids_are_dropped_and_counted(cuda):
+    from jscc_recon_spect_cylinder_gb300 import _compton, _lib
+
+    grid, det, sysmat, L, args = _cone_problem(cuda, n_events=64)
+    L = L.copy()
+    L[3, 0] = det.size(0) + 5
+    L[7, 2] = 0
+    _lib.take_bad_detector_count()
+    idx, _, _ = _compton.select_events(torch.from_numpy(L).to(cuda), det.to(cuda), args[0], args[1], *args[2:])
+    torch.cuda.synchronize()
+    assert 3 not in idx.tolist() and 7 not in idx.tolist()
+    assert _lib.take_bad_detector_count() >= 1  # counted when the event passed the energy tests
+
+
+def test_empty_and_fully_filtered_lists(cuda):
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_sparse as psp
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    grid, det, sysmat, L, args = _cone_problem(cuda, n_events=10)
+    A, detc, coor = sysmat.to(cuda), det.to(cuda), grid.coor.to(cuda)
+    empty = torch.zeros((0, 4), device=cuda)
+    t, tc, ts, idx = pls.build_rows_from_smeared(A, detc, coor, empty, *args)
+    assert t.shape == (0, grid.n_vox)
+    L2 = torch.from_numpy(L).to(cuda)
+    L2[:, 1] = 5.0  # above every threshold: nothing survives
+    t, _, _, _ = pls.build_rows_from_smeared(A, detc, coor, L2, *args)
+    assert t.shape == (0, grid.n_vox)
+    p = cso.build_compton_sparse_projector(grid.coor, 2, 1)
+    rows = psp.build_sparse_rows_from_smeared(A, detc, p, L2, *args)
+    assert rows.shape == (0, p.coarse_pixel_num + 1)
+
+
+# ----------------------------------------------------------------------------- sparse kernels
+def _r10(cuda, g):
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    return cso.build_compton_sparse_projector(torch.from_numpy(g["r10_coor_full"]), 2, 2, 10)
+
+
+def test_sparse_operators_golden_r10(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    g = golden("sparse_ops")
+    p = _r10(cuda, g).to(cuda)
+    rc = torch.from_numpy(g["r10_rows_c"]).to(cuda)
+    rf = torch.from_numpy(g["r10_rows_f"]).to(cuda)
+    np.testing.assert_allclose(cso.upsample_coarse_rows_to_fine(rc, p).cpu(), g["r10_up"], rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(cso.project_fine_rows_to_coarse_adjoint(rf, p).cpu(), g["r10_adj"], rtol=1e-5,
+                               atol=1e-6)
+    np.testing.assert_allclose(cso.reduce_fine_rows_to_coarse(rf, p).cpu(), g["r10_red"], rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(cso.reduce_fine_image_to_coarse(torch.from_numpy(g["r10_img_f"]).to(cuda), p).cpu(),
+                               g["r10_img_red"], rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(
+        cso.upsample_coarse_weight_to_fine(torch.from_numpy(g["r10_img_c"]).to(cuda), p).cpu(), g["r10_img_up"],
+        rtol=1e-6, atol=1e-7)
+
+
+def test_upsample_adjoint_identity_full_size(cuda):
+    """<U c, f> = <c, U^T f> on a config-3-size grid (100 x 360, theta stride 4): a
+    size-independent property of the pair (float32 accumulation, float64 dot products)."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    grid = synthetic.polar_grid(100, 360, 100.0)
+    p = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1).to(cuda)
+    assert p.coarse_pixel_num == 9000
+    g = torch.Generator(device=cuda).manual_seed(7)
+    c = torch.rand((64, p.coarse_pixel_num), device=cuda, generator=g)
+    f = torch.rand((64, p.fine_pixel_num), device=cuda, generator=g)
+    lhs = (cso.upsample_coarse_rows_to_fine(c, p).double() * f.double()).sum()
+    rhs = (c.double() * cso.project_fine_rows_to_coarse_adjoint(f, p).double()).sum()
+    assert abs((lhs - rhs) / lhs).item() < 1e-6
+
+
+def test_pack_unpack_golden(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    g = golden("sparse_ops")
+    rows = torch.from_numpy(g["s_event_rows"]).to(cuda)
+    cp1, tc = cso.unpack_sparse_event_rows(rows)
+    np.testing.assert_array_equal(cp1.cpu().numpy(), np.round(g["s_event_rows"][:, 0]).astype(np.int64))
+    packed = cso.pack_sparse_event_rows(cp1, tc.contiguous())
+    assert torch.equal(packed, rows)
+
+
+def test_sparse_builder_and_weights_golden(cuda, golden):
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_sparse as psp
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_local_sparse_jsccsd_only as loc
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane_sparse as rsp
+
+    g = golden("sparse_ops")
+    p = cso.build_compton_sparse_projector(torch.from_numpy(g["s_coor"]), 4, 2, 4).to(cuda)
+    A = torch.from_numpy(g["s_sysmat"]).to(cuda)
+    a = [float(v) for v in g["s_args"]]
+    rows = psp.build_sparse_rows_from_smeared(A, torch.from_numpy(g["s_det"]).to(cuda), p,
+                                              torch.from_numpy(g["s_smeared"]).to(cuda), *a)
+    ref = g["s_event_rows"]
+    np.testing.assert_array_equal(rows[:, 0].cpu().numpy(), ref[:, 0])
+    _rows_close(rows[:, 1:].cpu(), ref[:, 1:], TOL_ROW)
+    R = torch.from_numpy(ref).to(cuda)
+    t_fine, valid = cso.materialize_sparse_event_rows_to_fine(R, A, p)
+    np.testing.assert_array_equal(valid.cpu().numpy(), g["s_valid"])
+    _rows_close(t_fine.cpu(), g["s_t_fine"], 1e-5)
+    x = torch.from_numpy(g["s_x"]).to(cuda)
+    assert rel_l2(rsp.get_weight_compton_sparse(R, A, x, p).cpu(), g["s_w_grouped"]) < TOL_W
+    assert rel_l2(loc.get_weight_compton_sparse(R, A, x, p).cpu(), g["s_w_mat"]) < TOL_W
+    # host-resident block (the reference's pinned spill) is copied first
+    assert rel_l2(rsp.get_weight_compton_sparse(R.cpu(), A, x, p).cpu(), g["s_w_grouped"]) < TOL_W
+
+
+def test_sparse_osem_loops_vs_oracle(cuda, golden):
+    """osem_list_mode_sparse / osem_joint_mode_sparse / osem_joint_mode_local_sparse against
+    the FP64 oracle on the golden sparse problem (2 subsets, 1 rotation)."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_local_sparse_jsccsd_only as loc
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane_sparse as rsp
+    from oracle import osem_sc
+
+    g = golden("sparse_ops")
+    pn = osp.build_projector(g["s_coor"], 4, 2, 4)
+    p = cso.build_compton_sparse_projector(torch.from_numpy(g["s_coor"]), 4, 2, 4).to(cuda)
+    A = torch.from_numpy(g["s_sysmat"]).to(cuda)
+    rows = g["s_event_rows"]
+    V = A.size(1)
+    halves = [rows[: rows.shape[0] // 2], rows[rows.shape[0] // 2:]]
+    t_list = [[[[torch.from_numpy(h).to(cuda)]]] for h in halves]
+    ident = torch.arange(1, V + 1, device=cuda).unsqueeze(1)
+    s = torch.from_numpy(g["s_x"]).to(cuda) + 1.0
+    x0 = torch.ones((V, 1), device=cuda)
+    img = rsp.osem_list_mode_sparse(t_list, [A], [p], [ident], [ident], x0, s, 1)
+    ref = np.ones((V, 1))
+    for h in halves:
+        ref = osem_sc.safe_em_update(ref, osp.weight_grouped(h, g["s_sysmat"], ref, pn), s.cpu().numpy())
+    assert rel_l2(img.cpu(), ref) < TOL_W
+    # joint local form: alpha * w_s + (2 - alpha) * w_c, materialise semantics
+    B = A.size(0)
+    y = torch.poisson(A @ torch.ones((V, 1), device=cuda) * 50)
+    sub = [torch.arange(0, B // 2, device=cuda), torch.arange(B // 2, B, device=cuda)]
+    img = loc.osem_joint_mode_local_sparse([[A[i]] for i in sub], [[y[i]] for i in sub], t_list, [A], [p], [ident],
+                                           [ident], x0, s, 0.5, 1, cuda)
+    ref = np.ones((V, 1))
+    An, yn = g["s_sysmat"], y.cpu().numpy()
+    for i, h in zip(sub, halves):
+        ic = i.cpu().numpy()
+        w = 0.5 * osem_sc.get_weight_single(An[ic], yn[ic], ref, floor=1e-12) + \
+            1.5 * osp.weight_materialize(h, An, ref, pn)
+        ref = osem_sc.safe_em_update(ref, w, s.cpu().numpy())
+    assert rel_l2(img.cpu(), ref) < TOL_W
