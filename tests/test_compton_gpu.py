@@ -129,12 +129,21 @@ def test_fused_cone_weight_matches_stored_t(cuda):
     w_exact = rop.get_weight_compton_fused(ev, coor, A, x, use_window=False)
     assert rel_l2(w_fused.cpu(), w_stored.cpu()) < TOL_W
     assert rel_l2(w_fused.cpu(), w_exact.cpu()) < 1e-6
-    # against the FP64 oracle on the same events
-    rows64, _, _, _ = oc.strict_builder(sysmat.numpy(), det.numpy(), grid.coor.numpy(), L, *args)
+    # against the float32 oracle (the reference's arithmetic, pinned by the golden tests)
+    # on the same events. Float32 and float64 evaluations of the reference's formula differ
+    # by ~2e-3 here: where the voxel, the first and the second hit are nearly collinear
+    # (beta ~ 180 deg) 1 - cos^2(beta) cancels to its 1e-12 clamp in float32 and sigma_pos
+    # explodes (process_list_plane_strict.py:113-114); the kernel reproduces the reference.
     from oracle import osem_sc
 
-    w64 = osem_sc.get_weight_compton(rows64, x.cpu().numpy())
-    assert rel_l2(w_fused.cpu(), w64) < 1e-4  # FP32 theta vs FP64 oracle rows
+    ids = ev.list_index.cpu().numpy()
+    cp1, cp2 = L[ids, 0].astype(np.int64), L[ids, 2].astype(np.int64)
+    d = det.numpy()
+    tc32 = oc.cone_rows_strict(d[cp1 - 1], d[cp2 - 1], L[ids, 1], oc.pos_sigma_sq(d, args[0])[cp1 - 1],
+                               oc.pos_sigma_sq(d, args[1])[cp2 - 1], grid.coor.numpy(), args[2], args[3],
+                               dtype=np.float32)
+    w32 = osem_sc.get_weight_compton(tc32 * sysmat.numpy()[cp1 - 1], x.cpu().numpy(), dtype=np.float32)
+    assert rel_l2(w_fused.cpu(), w32) < TOL_W
 
 
 def test_fused_list_mode_osem_with_rotations(cuda):
@@ -173,7 +182,7 @@ def test_row_stats_match_oracle(cuda):
     grid, det, sysmat, L, args = _cone_problem(cuda, n_events=500)
     Ld = torch.from_numpy(L).to(cuda)
     idx, rec, rid = _compton.select_events(Ld, det.to(cuda), args[0], args[1], *args[2:], theta_fp64=False)
-    ref_idx = oc.event_filter(L, det.numpy(), *args[2:])
+    ref_idx = oc.event_filter(L, det.numpy(), args[2], args[4], args[5], args[6])
     np.testing.assert_array_equal(idx.cpu().numpy(), ref_idx)
     s1, s2, nan = ops.compton_row_stats(rec, rid, grid.coor.to(cuda), model=_lib.CONE_STRICT, eff=sysmat.to(cuda))
     cp1 = L[ref_idx, 0].astype(np.int64)
