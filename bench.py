@@ -1,16 +1,19 @@
 """Benchmark of the GB300 OSEM hot path; prints ONE JSON line (rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload sc3] [--no-cpu-baseline] [--no-e2e]
+                    [--workload jsccsd3|sc3|sc3-small] [--no-cpu-baseline] [--no-e2e]
 
-Workload "sc3" (default): the SC channel of the JSCCSD joint configuration — dense
-system matrix of 20 views x 4,096 pixels = 81,920 bins x 36,000 voxels (100 x 360
-polar grid), 8 OSEM subsets. One step = one OSEM iteration (8 subset updates:
-forward projection, ratio, back projection, EM update). Metric: subset-iterations/s
-(higher is better), headline with the matrix stored in BF16 (FP32 accumulation),
-the plain FP32-stored run reported beside it. Inputs are synthetic (seeded) and the
-matrix (5.9 GB BF16 / 11.8 GB FP32) is far larger than L2, so no L2 flush is needed
-between timed iterations.
+Workload "jsccsd3" (default): JSCCSD joint OSEM at the joint configuration's size —
+SC channel 20 views x 4,096 pixels = 81,920 bins x 36,000 voxels (100 x 360 polar grid,
+dense matrix 11.8 GB FP32 / 5.9 GB BF16) plus ~1M forward-simulated 662 keV Compton
+events built into sparse rows on a 4x theta-coarsened 9,000-voxel grid and materialised
+to the fine grid on the fly, alpha = 0.5, 8 subsets. One step = one OSEM iteration
+(8 subset updates). Metric: subset-iterations/s (higher is better); headline with the
+system matrix and the sparse rows stored in BF16 (FP32 accumulation), the plain FP32
+storage run beside it, plus Compton event-voxel pairs/s. Inputs are synthetic (seeded)
+and far larger than L2, so no L2 flush is needed between timed iterations.
+
+Workload "sc3": the SC channel alone; "sc3-small": an 8,192-row SC case for profiling.
 
 Multi-GPU: the path is run as independent replicas (one per rank, no collective on
 the data path); `value` sums the replicas' subset-iterations over the slowest rank's
@@ -110,48 +113,41 @@ def dist_env():
     return world, rank, local
 
 
-# ----------------------------------------------------------------------------- workload
+# ----------------------------------------------------------------------------- workloads
 class Sc3Workload:
-    """SC channel of config 3 (flat form: all 20 views are rows of one matrix)."""
+    """SC channel of the joint configuration alone (flat form: all 20 views are rows of one
+    matrix), subsets copied contiguously as the reference stages them."""
 
-    name = "jsccsd-config3-sc-channel"
-
-    def __init__(self, device, n_r=100, n_theta=360, radius=100.0, det_radius=120.0, n_phi=128, n_axial=32,
-                 axial_pitch=2.0, views=20, subsets=8, counts=1e7, seed=None):
-        if views != 20 or subsets != 8:
-            self.name = f"sc-channel-{views}views-{subsets}subsets"
+    def __init__(self, device, views=20, subsets=8, counts=1e7, seed=None):
         from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
         from jscc_recon_spect_cylinder_gb300 import synthetic
 
+        self.name = "jsccsd-config3-sc-channel" if (views, subsets) == (20, 8) else \
+            f"sc-channel-{views}views-{subsets}subsets"
+        self.metric = "OSEM subset-iters/s: BF16-stored vs plain FP32 (SC channel of config 3), 1xGB300"
+        self.traffic_file = "traffic_sc3.json"
         self.dev = device
         self.subsets = subsets
         seed = synthetic.SEED if seed is None else seed
         gen = torch.Generator(device=device)
         gen.manual_seed(seed)
-        grid = synthetic.polar_grid(n_r, n_theta, radius, device=device)
+        grid = synthetic.polar_grid(100, 360, 100.0, device=device)
         self.V = grid.n_vox
-        pitch = 2.0 * math.pi * det_radius / n_phi
-        blocks = []
-        for v in range(views):
-            pos = synthetic.cylinder_pixels(det_radius, n_phi, n_axial, axial_pitch, phi0=2 * math.pi * v / views,
-                                            device=device)
-            blocks.append(synthetic.sc_system_matrix(grid.coor, pos, pitch * axial_pitch, radius, generator=gen))
-        A = torch.cat(blocks, dim=0)
-        del blocks
+        pitch = 2.0 * math.pi * 120.0 / 128
+        A = torch.cat([synthetic.sc_system_matrix(grid.coor, synthetic.cylinder_pixels(
+            120.0, 128, 32, 2.0, phi0=2 * math.pi * v / views, device=device), pitch * 2.0, 100.0, generator=gen)
+            for v in range(views)], dim=0)
         self.B = A.size(0)
-        x_true = synthetic.hot_rod_phantom(grid.coor.cpu(), radius).to(device)
+        x_true = synthetic.hot_rod_phantom(grid.coor.cpu(), 100.0).to(device)
         self.proj = synthetic.poisson_projection(A, x_true, counts, generator=gen)
         self.s_map = A.sum(dim=0, keepdim=True).transpose(0, 1).contiguous()
         gcpu = torch.Generator().manual_seed(seed)
-        perm = torch.randperm(self.B, generator=gcpu)
-        self.subset_ids = [ids.to(device) for ids in rop.split_tensor_even(perm, subsets, dim=0)]
-        self.A_f32 = [A[ids].contiguous() for ids in self.subset_ids]
+        ids = [i.to(device) for i in rop.split_tensor_even(torch.randperm(self.B, generator=gcpu), subsets, dim=0)]
+        self.A_f32 = [A[i].contiguous() for i in ids]
         del A
         self.A_bf16 = [a.to(torch.bfloat16) for a in self.A_f32]
-        self.y = [self.proj[ids].contiguous() for ids in self.subset_ids]
+        self.y = [self.proj[i].contiguous() for i in ids]
         self.rot = torch.arange(1, self.V + 1, dtype=torch.int64, device=device).unsqueeze(1)
-        self.inv = self.rot.clone()
-        self.rows_per_subset = [a.size(0) for a in self.A_f32]
         torch.cuda.synchronize(device)
 
     def matrices(self, dtype):
@@ -160,28 +156,215 @@ class Sc3Workload:
     def step(self, img, dtype):
         from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
 
-        A = self.matrices(dtype)
-        return rop.osem_bin_mode([[a] for a in A], [[y] for y in self.y], [self.rot], [self.inv], img, self.s_map, 1)
+        return rop.osem_bin_mode([[a] for a in self.matrices(dtype)], [[y] for y in self.y], [self.rot], [self.rot],
+                                 img, self.s_map, 1)
 
     def units_per_step(self):
         return self.subsets
 
     def kernel_bytes(self, dtype):
-        """Algorithmic bytes per launch of the streaming kernels, averaged over subsets."""
         b = 2 if dtype == "bf16" else 4
-        rows = float(np.mean(self.rows_per_subset))
-        mat = rows * self.V * b
-        return {
-            "sc_forward_split": mat + self.V * 4,   # A once + image
-            "sc_back_partial": mat + rows * 4,      # A once + ratio
-        }
+        rows = self.B / self.subsets
+        return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4}
 
-    def bytes_per_step(self, dtype):
-        kb = self.kernel_bytes(dtype)
-        return self.subsets * (kb["sc_forward_split"] + kb["sc_back_partial"])
+    def config(self):
+        return {"workload": self.name, "bins": self.B, "voxels": self.V, "subsets": self.subsets,
+                "matrix_bytes_bf16": self.B * self.V * 2, "l2": "inputs larger than L2 (no flush)"}
+
+    def fp64_reference(self, iters):
+        x = torch.ones((self.V, 1), dtype=torch.float64, device=self.dev)
+        s = self.s_map.double()
+        for _ in range(iters):
+            for A, y in zip(self.A_f32, self.y):
+                A64 = A.double()
+                x = x * (A64.t() @ (y.double() / (A64 @ x))) / s
+                del A64
+        return x
+
+    def extra(self, ms_per_step):
+        return {}
+
+    def e2e(self, iters):
+        """One job through recon_osem_plane.osem_bin_mode with host inputs: pinned host
+        subset matrices (BF16), projections and sensitivity copied in, `iters` iterations,
+        image read back."""
+        from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+        host_A = [a.cpu().pin_memory() for a in self.A_bf16]
+        host_y = [y.cpu().pin_memory() for y in self.y]
+        host_s = self.s_map.cpu().pin_memory()
+        out = torch.empty((self.V, 1)).pin_memory()
+        h2d = sum(a.numel() * a.element_size() for a in host_A) + sum(y.numel() * 4 for y in host_y) + \
+            host_s.numel() * 4 + self.V * 4
+        torch.cuda.synchronize(self.dev)
+        t0 = time.perf_counter()
+        A = [[a.to(self.dev, non_blocking=True)] for a in host_A]
+        y = [[v.to(self.dev, non_blocking=True)] for v in host_y]
+        s = host_s.to(self.dev, non_blocking=True)
+        img = torch.ones((self.V, 1)).pin_memory().to(self.dev, non_blocking=True)
+        rot = torch.arange(1, self.V + 1, dtype=torch.int64).unsqueeze(1).to(self.dev, non_blocking=True)
+        for _ in range(iters):
+            img = rop.osem_bin_mode(A, y, [rot], [rot], img, s, 1)
+        out.copy_(img, non_blocking=True)
+        torch.cuda.synchronize(self.dev)
+        sec = time.perf_counter() - t0
+        return {"value": iters * self.subsets / sec, "unit": "subset-iters/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(self.V * 4),
+                "step": f"one job: stage inputs + {iters} iterations + read image", "seconds": sec}
+
+    def cpu_rate(self, budget_s=10.0):
+        """Oracle port (numpy float32 BLAS, all host cores): subset updates of subset 0."""
+        from oracle import osem_sc
+
+        A = self.A_f32[0].cpu().numpy()
+        y = self.y[0].cpu().numpy()
+        s = self.s_map.cpu().numpy()
+        x = np.ones((self.V, 1), dtype=np.float32)
+        n, t0 = 0, time.perf_counter()
+        while True:
+            x = (x * osem_sc.get_weight_single(A, y, x, dtype=np.float32) / s).astype(np.float32)
+            n += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or n >= 200:
+                break
+        return {"value": n / el, "unit": "subset-iters/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": f"{n} subset updates of subset 0 ({A.shape[0]} x {A.shape[1]} float32, numpy BLAS)",
+                "seconds": el}
+
+
+class JointBench:
+    """workloads.JointWorkload behind the bench interface."""
+
+    def __init__(self, dev, small=False):
+        from jscc_recon_spect_cylinder_gb300 import workloads
+
+        kw = dict(views=2, n_events=60000, subsets=2) if small else {}
+        self.w = workloads.JointWorkload(dev, **kw)
+        self.name = "jsccsd-config3" if not small else "jsccsd-small"
+        self.metric = ("OSEM subset-iters/s: BF16-stored vs plain FP32 joint JSCCSD (SC + sparse Compton, "
+                       "config 3), 1xGB300")
+        self.traffic_file = "traffic_jsccsd3.json"
+        self.dev = dev
+        self.V = self.w.V
+        self.subsets = self.w.subsets
+
+    def step(self, img, dtype):
+        return self.w.step(img, dtype)
+
+    def units_per_step(self):
+        return self.w.subsets
+
+    def kernel_bytes(self, dtype):
+        kb = self.w.sc_kernel_bytes(dtype)
+        kb.update(self.w.sparse_kernel_bytes(dtype))
+        return kb
+
+    def config(self):
+        w = self.w
+        return {"workload": self.name, "sc_bins": w.B, "voxels": w.V, "coarse_voxels": w.Vc,
+                "compton_events_listed": w.n_list, "compton_events_kept": w.n_events, "subsets": w.subsets,
+                "alpha": w.alpha, "views": w.views,
+                "storage": "bf16 system matrix + bf16 sparse rows (int32 ids split out)",
+                "l2": "inputs larger than L2 (no flush)"}
+
+    def fp64_reference(self, iters):
+        return self.w.fp64_reference(iters)
+
+    def extra(self, ms_per_step):
+        pairs = self.w.pair_count_per_step()
+        return {"compton_event_voxel_pairs_per_s": pairs / (ms_per_step / 1e3)}
+
+    def e2e(self, iters):
+        """One job with host inputs: pinned host copies of the BF16 system matrix (also the
+        efficiency table), projections, the BF16 sparse rows + ids, subset ids and the
+        joint sensitivity go to the GPU inside the timed region, `iters` iterations run
+        through the same kernels, and the image is read back."""
+        from jscc_recon_spect_cylinder_gb300 import ops
+
+        w = self.w
+        hA = w.A["bf16"].cpu().pin_memory()
+        hy = w.proj.cpu().pin_memory()
+        hs = w.s_joint.cpu().pin_memory()
+        hids = [i.cpu().pin_memory() for i in w.ids]
+        htc = [t.cpu().pin_memory() for t in w.tc_bf16]
+        hsub = [i.cpu().pin_memory() for i in w.subset_ids]
+        out = torch.empty((w.V, 1)).pin_memory()
+        h2d = hA.numel() * 2 + hy.numel() * 4 + hs.numel() * 4 + sum(i.numel() * 4 for i in hids) + \
+            sum(t.numel() * 2 for t in htc) + sum(i.numel() * 8 for i in hsub) + w.V * 4
+        torch.cuda.synchronize(self.dev)
+        t0 = time.perf_counter()
+        A = hA.to(self.dev, non_blocking=True)
+        y = hy.to(self.dev, non_blocking=True)
+        s = hs.to(self.dev, non_blocking=True)
+        ids = [i.to(self.dev, non_blocking=True) for i in hids]
+        tc = [t.to(self.dev, non_blocking=True) for t in htc]
+        sub = [i.to(self.dev, non_blocking=True) for i in hsub]
+        img = torch.ones((w.V, 1)).pin_memory().to(self.dev, non_blocking=True)
+        for _ in range(iters):
+            for k in range(w.subsets):
+                wt = torch.zeros_like(img)
+                ops.sc_weight(A, y, img, floor=1e-12, scale=w.alpha, out=wt, row_idx=sub[k])
+                ops.sparse_weight_split(ids[k], tc[k], A, w.tables, img, grouped=False, scale=2 - w.alpha, out=wt)
+                img = ops.em_update(img, wt, s, safe=True)
+        out.copy_(img, non_blocking=True)
+        torch.cuda.synchronize(self.dev)
+        sec = time.perf_counter() - t0
+        return {"value": iters * w.subsets / sec, "unit": "subset-iters/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(w.V * 4),
+                "step": f"one job: stage inputs + {iters} iterations + read image", "seconds": sec}
+
+    def cpu_rate(self, budget_s=20.0):
+        """Oracle port on the host cores for one subset update: the SC half with numpy
+        float32 BLAS on subset 0's rows, the Compton half with the oracle's sparse (scipy)
+        restatement of the materialise weight on a sample of subset 0's events, scaled to
+        the subset's event count."""
+        from oracle import osem_sc
+        from oracle import sparse as osp
+        import scipy.sparse as sp
+
+        w = self.w
+        ids = w.subset_ids[0]
+        A = w.A["f32"][ids].cpu().numpy()
+        y = w.proj[ids].cpu().numpy()
+        x = np.ones((w.V, 1), dtype=np.float32)
+        ptr, idx, val = (t.cpu().numpy() for t in w.tables.up[1])
+        U = sp.csr_matrix((val.astype(np.float64), idx, ptr), shape=(w.tables.n_lf, w.tables.n_lc))
+        rows = w.rows_f32[0]
+        n_sample = min(rows.size(0), 2000)
+        sample = rows[torch.randperm(rows.size(0), generator=torch.Generator(device=w.dev).manual_seed(0),
+                                     device=w.dev)[:n_sample]].cpu().numpy()
+        Afull = w.A["f32"]
+        eff = Afull[torch.from_numpy(np.clip(np.round(sample[:, 0]).astype(np.int64) - 1, 0, Afull.size(0) - 1))
+                    .to(w.dev)].cpu().numpy()
+        sample_local = sample.copy()
+        sample_local[:, 0] = np.arange(1, n_sample + 1)
+        t_sc = t_c = 0.0
+        n = 0
+        t_start = time.perf_counter()
+        while True:
+            t0 = time.perf_counter()
+            osem_sc.get_weight_single(A, y, x, floor=1e-12, dtype=np.float32)
+            t1 = time.perf_counter()
+            osp.weight_materialize_csr(sample_local, eff, x, U, dtype=np.float32)
+            t2 = time.perf_counter()
+            t_sc += t1 - t0
+            t_c += (t2 - t1) * (rows.size(0) / n_sample)
+            n += 1
+            if time.perf_counter() - t_start >= budget_s or n >= 20:
+                break
+        per_update = (t_sc + t_c) / n
+        return {"value": 1.0 / per_update, "unit": "subset-iters/s", "cores": os.cpu_count(), "kind": "port",
+                "sample": (f"{n} x (SC half on subset 0: {A.shape[0]} x {A.shape[1]} float32 numpy BLAS; Compton "
+                           f"half: materialise weight of {n_sample} of the subset's {rows.size(0)} events with a "
+                           f"scipy sparse upsample, scaled by events)"),
+                "seconds": time.perf_counter() - t_start}
 
 
 def make_workload(name, dev):
+    if name == "jsccsd3":
+        return JointBench(dev)
+    if name == "jsccsd-small":
+        return JointBench(dev, small=True)
     if name == "sc3":
         return Sc3Workload(dev)
     if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
@@ -235,76 +418,12 @@ def kernel_times(work, dtype, steps):
     return _lib.kernel_timing_collect()
 
 
-def fp64_errors(work, iters, images):
-    """Relative L2 and max-voxel error of each image against an FP64 reconstruction of
-    the same problem (torch float64 on the GPU, same subsets, same order)."""
-    x = torch.ones((work.V, 1), dtype=torch.float64, device=work.dev)
-    s = work.s_map.double()
-    for _ in range(iters):
-        for A, y in zip(work.A_f32, work.y):
-            A64 = A.double()
-            w = A64.t() @ (y.double() / (A64 @ x))
-            x = x * w / s
-            del A64
+def image_errors(ref64, images):
     out = {}
     for k, img in images.items():
-        d = (img.double() - x)
-        out[k] = {"rel_l2": float(d.norm() / x.norm()), "max_voxel_rel": float(d.abs().max() / x.abs().max())}
+        d = img.double() - ref64
+        out[k] = {"rel_l2": float(d.norm() / ref64.norm()), "max_voxel_rel": float(d.abs().max() / ref64.abs().max())}
     return out
-
-
-def run_e2e(work, dtype, iters):
-    """One reconstruction job through the reference-facing API with host inputs:
-    pinned host subset matrices, projections and sensitivity are copied to the GPU
-    inside the timed region, `iters` OSEM iterations run, and the image is read back."""
-    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
-
-    host_A = [a.cpu().pin_memory() for a in work.matrices(dtype)]
-    host_y = [y.cpu().pin_memory() for y in work.y]
-    host_s = work.s_map.cpu().pin_memory()
-    host_img = torch.ones((work.V, 1)).pin_memory()
-    out = torch.empty((work.V, 1)).pin_memory()
-    h2d = sum(a.numel() * a.element_size() for a in host_A) + sum(y.numel() * 4 for y in host_y) + \
-        host_s.numel() * 4 + host_img.numel() * 4
-    d2h = out.numel() * 4
-    torch.cuda.synchronize(work.dev)
-    t0 = time.perf_counter()
-    A = [[a.to(work.dev, non_blocking=True)] for a in host_A]
-    y = [[v.to(work.dev, non_blocking=True)] for v in host_y]
-    s = host_s.to(work.dev, non_blocking=True)
-    img = host_img.to(work.dev, non_blocking=True)
-    rot = torch.arange(1, work.V + 1, dtype=torch.int64).unsqueeze(1).to(work.dev, non_blocking=True)
-    for _ in range(iters):
-        img = rop.osem_bin_mode(A, y, [rot], [rot], img, s, 1)
-    out.copy_(img, non_blocking=True)
-    torch.cuda.synchronize(work.dev)
-    sec = time.perf_counter() - t0
-    return {"value": iters * work.subsets / sec, "unit": "subset-iters/s", "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "step": f"one job: stage inputs + {iters} iterations + read image",
-            "seconds": sec}
-
-
-def cpu_port_rate(work, budget_s=10.0, threads=None):
-    """Oracle (numpy port of recon_osem_plane.get_weight_single + EM update) on the
-    host cores: subset updates of the same workload until ~budget_s of CPU work."""
-    from oracle import osem_sc
-
-    A = work.A_f32[0].cpu().numpy()
-    y = work.y[0].cpu().numpy()
-    s = work.s_map.cpu().numpy()
-    x = np.ones((work.V, 1), dtype=np.float32)
-    osem_sc.get_weight_single(A[:64], y[:64], x, dtype=np.float32)
-    n, t0 = 0, time.perf_counter()
-    while True:
-        w = osem_sc.get_weight_single(A, y, x, dtype=np.float32)
-        x = (x * w / s).astype(np.float32)
-        n += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or n >= 200:
-            break
-    return {"value": n / el, "unit": "subset-iters/s", "cores": threads or os.cpu_count(), "kind": "port",
-            "sample": f"{n} subset updates of subset 0 ({A.shape[0]} x {A.shape[1]} float32, numpy BLAS)",
-            "seconds": el}
 
 
 # ----------------------------------------------------------------------------- arms
@@ -316,18 +435,17 @@ def reference_arm(args):
     work = make_workload(args.workload, dev)
     rates = []
     for i in range(args.warmup + args.steps):
-        r = cpu_port_rate(work, budget_s=max(2.0, 20.0 / max(1, args.steps)))
+        r = work.cpu_rate(budget_s=max(2.0, 60.0 / max(1, args.steps + args.warmup)))
         if i >= args.warmup:
             rates.append(r["value"])
     value = float(np.median(rates))
     line = {
-        "impl": "reference", "metric": "OSEM subset-iters/s (SC channel of config 3)", "value": value,
-        "unit": "subset-iters/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * work.subsets / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": work.name, "bins": work.B, "voxels": work.V, "subsets": work.subsets},
+        "impl": "reference", "metric": work.metric, "value": value, "unit": "subset-iters/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * work.subsets / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": work.config(),
         "cpu_baseline": {"value": value, "unit": "subset-iters/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": "per step: subset updates of subset 0 (numpy float32 BLAS), ~20 s total"},
+                         "sample": r["sample"]},
         "e2e": {"value": value, "unit": "subset-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -355,50 +473,50 @@ def ours_arm(args):
     line = None
     if rank == 0:
         peaks = measured_peaks()
-        kt = kernel_times(work, "bf16", max(3, args.steps))
+        kt = kernel_times(work, "bf16", max(3, min(args.steps, 10)))
         kbytes = work.kernel_bytes("bf16")
         kernels = {}
+        total_ms = sum(tot for _, tot in kt.values())
         for name, (n, tot) in kt.items():
             avg = tot / n
-            entry = {"launches": n, "avg_ms": avg}
+            entry = {"launches": n, "avg_ms": avg, "share": tot / total_ms if total_ms else None}
             if name in kbytes:
                 entry["algorithmic_bytes"] = kbytes[name]
                 entry["achieved_gbs"] = kbytes[name] / (avg / 1e3) / 1e9
             kernels[name] = entry
-        top = max((k for k in kernels if "achieved_gbs" in kernels[k]), key=lambda k: kernels[k]["avg_ms"] *
-                  kernels[k]["launches"])
+        top = max((k for k in kernels if "achieved_gbs" in kernels[k]),
+                  key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
         traffic = None
-        tf = REPO / "profiles" / "traffic_sc3.json"
+        tf = REPO / "profiles" / work.traffic_file
         if tf.exists():
             traffic = json.loads(tf.read_text()).get(top)
         achieved = kernels[top]["achieved_gbs"]
         roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                    "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
-                    "peak_source": peaks["source"]}
-        errors = fp64_errors(work, args.steps + args.warmup, {"bf16": img_bf16, "f32": img_f32}) \
-            if not args.no_errors else None
-        e2e = run_e2e(work, "bf16", 30) if not args.no_e2e else None
-        cpu = cpu_port_rate(work) if (world == 1 and not args.no_cpu_baseline) else None
-        errors_iters = args.steps + args.warmup
+                    "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"]}
+        errors = None
+        err_iters = args.error_iters
+        if not args.no_errors:
+            imgs = {}
+            for dt in ("bf16", "f32"):
+                x = torch.ones((work.V, 1), device=dev)
+                for _ in range(err_iters):
+                    x = work.step(x, dt)
+                imgs[dt] = x
+            errors = image_errors(work.fp64_reference(err_iters), imgs)
+        e2e = work.e2e(30) if not args.no_e2e else None
+        cpu = work.cpu_rate() if (world == 1 and not args.no_cpu_baseline) else None
         line = {
-            "metric": "OSEM subset-iters/s: BF16-stored vs plain FP32 (SC channel of config 3), 1xGB300",
-            "value": value, "unit": "subset-iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_bf16 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": work.name, "bins": work.B, "voxels": work.V, "subsets": work.subsets,
-                       "matrix_bytes_bf16": work.B * work.V * 2, "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "metric": work.metric, "value": value, "unit": "subset-iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_bf16 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": dict(work.config(), parallelism="replicas" if world > 1 else "single"),
             "fp32": {"value": value_f32, "ms_per_step": ms_f32 / args.steps},
             "speedup_bf16_vs_fp32": value / value_f32,
-            "errors_vs_fp64": errors,
-            "errors_after_iterations": errors_iters,
-            "gpu_launches": launches,
-            "clocks": clocks,
-            "roofline": roofline,
-            "kernels": kernels,
-            "e2e": e2e,
-            "cpu_baseline": cpu,
+            "errors_vs_fp64": errors, "errors_after_iterations": err_iters,
+            "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "kernels": kernels,
+            "e2e": e2e, "cpu_baseline": cpu,
         }
+        line.update(work.extra(ms_bf16 / args.steps))
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
@@ -409,13 +527,15 @@ def ours_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["sc3", "sc3-small"], default="sc3")
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small"], default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
+    ap.add_argument("--error-iters", type=int, default=10,
+                    help="iterations (from a uniform image) at which BF16 / FP32 images are compared with FP64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

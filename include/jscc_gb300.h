@@ -284,6 +284,20 @@ JSCC_API int jscc_sparse_weight(const float* rows, int64_t ld_rows, int64_t n_ev
                    const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
                    float* weight, void* workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * jscc_sparse_weight over split storage: row_id [n_events] int32 0-based sysmat rows
+ * (cp1 - 1) and t_coarse [n_events, ld_tc] of tc_dtype (float32 or bf16). Same result as
+ * jscc_sparse_weight on the packed rows; the split is what lets the coarse rows be stored
+ * in BF16 (the packed format keeps cp1 as a float, which BF16 cannot represent).
+ */
+JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype,
+                   int64_t ld_tc, int64_t n_events, const void* sysmat, int32_t sysmat_dtype,
+                   int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw,
+                   int32_t n_zf, const int32_t* l_taps, const float* l_tw, int32_t n_lf,
+                   int32_t n_lc, int32_t mode, const float* img, const int64_t* rotmat,
+                   const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------ EM update */
 
 #define JSCC_EM_PLAIN 0 /* img * w / s                         (recon_osem_plane.py:54, :73, :118) */

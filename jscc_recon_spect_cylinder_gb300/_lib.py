@@ -97,6 +97,12 @@ _SIGNATURES: dict[str, tuple] = {
          c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_float, c_void_p, c_void_p,
          c_size_t, c_void_p],
     ),
+    "jscc_sparse_weight_split": (
+        c_int,
+        [c_void_p, c_void_p, c_int32, c_int64, c_int64, c_void_p, c_int32, c_int64, c_int64, c_void_p, c_void_p,
+         c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_float,
+         c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
     "jscc_em_update": (
         c_int,
         [c_void_p, c_void_p, c_void_p, c_int32, c_float, c_void_p, c_float, c_void_p, c_int64,

@@ -76,22 +76,48 @@ struct UpTaps {
   int n_lc;
 };
 
-__device__ __forceinline__ float up_value(const float* __restrict__ tc, const UpTaps& t, int zf, int lf) {
+template <typename TC>
+__device__ __forceinline__ float up_value(const TC* __restrict__ tc, const UpTaps& t, int zf, int lf) {
   const int l0 = t.lt[2 * lf], l1 = t.lt[2 * lf + 1];
   const float w0 = t.lwt[2 * lf], w1 = t.lwt[2 * lf + 1];
   const int z0 = t.zt[2 * zf], z1 = t.zt[2 * zf + 1];
   const float u0 = t.zwt[2 * zf], u1 = t.zwt[2 * zf + 1];
-  const float* r0 = tc + (int64_t)z0 * t.n_lc;
-  const float* r1 = tc + (int64_t)z1 * t.n_lc;
-  float a = w0 * __ldg(r0 + l0);
-  if (w1 != 0.f) a = fmaf(w1, __ldg(r0 + l1), a);
+  const TC* r0 = tc + (int64_t)z0 * t.n_lc;
+  const TC* r1 = tc + (int64_t)z1 * t.n_lc;
+  float a = w0 * ld_any(r0, l0);
+  if (w1 != 0.f) a = fmaf(w1, ld_any(r0, l1), a);
   float v = u0 * a;
   if (u1 != 0.f) {
-    float b = w0 * __ldg(r1 + l0);
-    if (w1 != 0.f) b = fmaf(w1, __ldg(r1 + l1), b);
+    float b = w0 * ld_any(r1, l0);
+    if (w1 != 0.f) b = fmaf(w1, ld_any(r1, l1), b);
     v = fmaf(u1, b, v);
   }
   return v;
+}
+
+// Event rows in either layout: packed float rows (cp1 as float in column 0, the
+// reference's format) or split storage (0-based sysmat row ids + coarse rows of TC,
+// float32 or bf16 — bf16 cannot hold the ids, hence the split).
+template <typename TC>
+struct SpRows {
+  const float* packed;   // non-null: packed layout
+  const int32_t* ids;    // split layout: row ids (0-based, clamped on use)
+  const TC* tc;          // split layout: coarse rows
+  int64_t ld;            // row stride (elements)
+  int64_t n_det;
+  __device__ __forceinline__ int64_t row_of(int64_t i) const {
+    int64_t g = packed ? (int64_t)rintf(packed[i * ld]) - 1 : (int64_t)ids[i];
+    return g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+  }
+  __device__ __forceinline__ const TC* coarse(int64_t i) const;
+};
+template <>
+__device__ __forceinline__ const float* SpRows<float>::coarse(int64_t i) const {
+  return packed ? packed + i * ld + 1 : tc + i * ld;
+}
+template <>
+__device__ __forceinline__ const __nv_bfloat16* SpRows<__nv_bfloat16>::coarse(int64_t i) const {
+  return tc + i * ld;
 }
 
 __device__ __forceinline__ float finite_or_zero(float v) { return isfinite(v) ? v : 0.f; }
@@ -114,7 +140,7 @@ sparse_materialize_kernel(const float* __restrict__ rows, int64_t ld_rows, int64
   float s = 0.f;
   for (int64_t j = threadIdx.x; j < vf; j += blockDim.x) {
     const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
-    const float v = finite_or_zero(up_value(tc, taps, zf, lf) * ld_any(er, j));
+    const float v = finite_or_zero(up_value<float>(tc, taps, zf, lf) * ld_any(er, j));
     fine[i * ld_fine + j] = v;
     s += v;
   }
@@ -132,11 +158,11 @@ sparse_materialize_kernel(const float* __restrict__ rows, int64_t ld_rows, int64
 constexpr int kSpThreads = 256;
 
 // f[i] = sum_j v_ij x_j, s[i] = sum_j v_ij, v = up(tc_i) * eff_g(i) (nan_to_num in MATERIALIZE mode)
-template <int EB, bool MATERIALIZE, typename TE>
+template <int EB, bool MATERIALIZE, typename TE, typename TC>
 __global__ void __launch_bounds__(kSpThreads)
-sparse_forward_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, int64_t vf,
-                      const float* __restrict__ x, const TE* __restrict__ eff, int64_t ld_eff, int64_t n_det,
-                      UpTaps taps, float* __restrict__ f_out, float* __restrict__ s_out) {
+sparse_forward_kernel(SpRows<TC> rows, int64_t n, int64_t vf, const float* __restrict__ x,
+                      const TE* __restrict__ eff, int64_t ld_eff, UpTaps taps, float* __restrict__ f_out,
+                      float* __restrict__ s_out) {
   __shared__ int64_t sg[EB];
   __shared__ float red[kSpThreads / 32][2 * EB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -144,8 +170,7 @@ sparse_forward_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n
   const int ne = (n - i0) < EB ? (int)(n - i0) : EB;
   if (tid < EB) {
     const int64_t i = i0 + tid < n ? i0 + tid : n - 1;
-    int64_t g = (int64_t)rintf(rows[i * ld_rows]) - 1;
-    sg[tid] = g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+    sg[tid] = rows.row_of(i);
   }
   __syncthreads();
   float af[EB], as[EB];
@@ -157,8 +182,7 @@ sparse_forward_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n
 #pragma unroll
     for (int e = 0; e < EB; ++e) {
       if (e < ne) {
-        const float* tc = rows + (i0 + e) * ld_rows + 1;
-        float v = up_value(tc, taps, zf, lf);
+        float v = up_value<TC>(rows.coarse(i0 + e), taps, zf, lf);
         if (v != 0.f) {
           v *= ld_any(eff + sg[e] * ld_eff, j);
           if (MATERIALIZE) v = finite_or_zero(v);
@@ -209,11 +233,10 @@ __global__ void sparse_coef_kernel(const float* __restrict__ f, const float* __r
 constexpr int kSpStage = 64;
 
 // part[chunk][j] = sum_{i in chunk} v_ij coef_i
-template <bool MATERIALIZE, typename TE>
+template <bool MATERIALIZE, typename TE, typename TC>
 __global__ void __launch_bounds__(kSpThreads)
-sparse_back_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, int64_t ev_per_chunk, int64_t vf,
-                   const float* __restrict__ coef, const TE* __restrict__ eff, int64_t ld_eff, int64_t n_det,
-                   UpTaps taps, float* __restrict__ part, int64_t ldp) {
+sparse_back_kernel(SpRows<TC> rows, int64_t n, int64_t ev_per_chunk, int64_t vf, const float* __restrict__ coef,
+                   const TE* __restrict__ eff, int64_t ld_eff, UpTaps taps, float* __restrict__ part, int64_t ldp) {
   __shared__ int64_t sg[kSpStage];
   __shared__ float sc[kSpStage];
   const int tid = threadIdx.x;
@@ -227,8 +250,7 @@ sparse_back_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, i
     const int cnt = (e_end - s0) < kSpStage ? (int)(e_end - s0) : kSpStage;
     __syncthreads();
     if (tid < cnt) {
-      int64_t g = (int64_t)rintf(rows[(s0 + tid) * ld_rows]) - 1;
-      sg[tid] = g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+      sg[tid] = rows.row_of(s0 + tid);
       sc[tid] = coef[s0 + tid];
     }
     __syncthreads();
@@ -236,8 +258,7 @@ sparse_back_kernel(const float* __restrict__ rows, int64_t ld_rows, int64_t n, i
       for (int e = 0; e < cnt; ++e) {
         const float ce = sc[e];
         if (ce == 0.f) continue;
-        const float* tc = rows + (s0 + e) * ld_rows + 1;
-        float v = up_value(tc, taps, zf, lf);
+        float v = up_value<TC>(rows.coarse(s0 + e), taps, zf, lf);
         if (v != 0.f) {
           v *= ld_any(eff + sg[e] * ld_eff, j);
           if (MATERIALIZE) v = finite_or_zero(v);
@@ -296,14 +317,14 @@ static SpPlan plan_sparse(int64_t n, int64_t vf) {
   return p;
 }
 
-template <bool MAT, typename TE>
-static void launch_sparse_weight(const float* rows, int64_t ld_rows, int64_t n, int64_t vf, const float* x,
-                                 const TE* eff, int64_t ld_eff, int64_t n_det, const UpTaps& taps, float* f, float* s,
-                                 float* coef, float* part, const SpPlan& p, cudaStream_t st) {
+template <bool MAT, typename TE, typename TC>
+static void launch_sparse_weight(const SpRows<TC>& rows, int64_t n, int64_t vf, const float* x, const TE* eff,
+                                 int64_t ld_eff, const UpTaps& taps, float* f, float* s, float* coef, float* part,
+                                 const SpPlan& p, cudaStream_t st) {
   constexpr int EB = 8;
   JSCC_TIMED("sparse_forward", st,
-             (sparse_forward_kernel<EB, MAT, TE><<<(unsigned)((n + EB - 1) / EB), kSpThreads, 0, st>>>(
-                 rows, ld_rows, n, vf, x, eff, ld_eff, n_det, taps, f, s)));
+             (sparse_forward_kernel<EB, MAT, TE, TC><<<(unsigned)((n + EB - 1) / EB), kSpThreads, 0, st>>>(
+                 rows, n, vf, x, eff, ld_eff, taps, f, s)));
   launch_counter().fetch_add(1);
   int64_t cb = (n + 255) / 256;
   if (cb > 4096) cb = 4096;
@@ -311,9 +332,56 @@ static void launch_sparse_weight(const float* rows, int64_t ld_rows, int64_t n, 
   launch_counter().fetch_add(1);
   dim3 bgrid((unsigned)((vf + kSpThreads - 1) / kSpThreads), (unsigned)p.chunks);
   JSCC_TIMED("sparse_back", st,
-             (sparse_back_kernel<MAT, TE><<<bgrid, kSpThreads, 0, st>>>(rows, ld_rows, n, p.ev_per_chunk, vf, coef,
-                                                                        eff, ld_eff, n_det, taps, part, p.ldp)));
+             (sparse_back_kernel<MAT, TE, TC><<<bgrid, kSpThreads, 0, st>>>(rows, n, p.ev_per_chunk, vf, coef, eff,
+                                                                            ld_eff, taps, part, p.ldp)));
   launch_counter().fetch_add(1);
+}
+
+template <typename TC>
+static int sparse_weight_impl(const SpRows<TC>& rows, int64_t n_events, const void* sysmat, int32_t sysmat_dtype,
+                              int64_t ld_sysmat, const UpTaps& t, int64_t vf, int32_t mode, const float* img,
+                              const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
+                              float* weight, void* workspace, size_t workspace_bytes, cudaStream_t st) {
+  const SpPlan p = plan_sparse(n_events, vf);
+  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "jscc_sparse_weight: workspace too small (%zu < %zu)",
+               workspace_bytes, p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  float* xr = cv.take<float>((size_t)p.ldp);
+  float* f = cv.take<float>((size_t)n_events);
+  float* s = cv.take<float>((size_t)n_events);
+  float* coef = cv.take<float>((size_t)n_events);
+  float* part = cv.take<float>((size_t)p.chunks * p.ldp);
+  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight: workspace carve overflow");
+  const float* x = img;
+  if (rotmat) {
+    int64_t blocks = (vf + 255) / 256;
+    if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+    JSCC_TIMED("sc_gather_rot", st,
+               (sc_gather_rot_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, rotmat, ld_rot, 0, 1, vf, p.ldp, xr)));
+    JSCC_LAUNCH_CHECK();
+    x = xr;
+  }
+  const bool mat = mode == JSCC_SPARSE_MATERIALIZE;
+  if (sysmat_dtype == JSCC_DTYPE_F32) {
+    const float* e = static_cast<const float*>(sysmat);
+    if (mat) launch_sparse_weight<true, float, TC>(rows, n_events, vf, x, e, ld_sysmat, t, f, s, coef, part, p, st);
+    else launch_sparse_weight<false, float, TC>(rows, n_events, vf, x, e, ld_sysmat, t, f, s, coef, part, p, st);
+  } else {
+    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(sysmat);
+    if (mat)
+      launch_sparse_weight<true, __nv_bfloat16, TC>(rows, n_events, vf, x, e, ld_sysmat, t, f, s, coef, part, p, st);
+    else
+      launch_sparse_weight<false, __nv_bfloat16, TC>(rows, n_events, vf, x, e, ld_sysmat, t, f, s, coef, part, p, st);
+  }
+  JSCC_CUDA_CHECK(cudaGetLastError());
+  int64_t blocks = (vf + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  const int has_scale = scale != 1.0f;
+  JSCC_TIMED("sparse_reduce", st,
+             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldp, (int)p.chunks, rotmat_inv, ld_rot, vf,
+                                                                     has_scale, scale, weight)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
 }
 
 }  // namespace jscc
@@ -443,49 +511,39 @@ int jscc_sparse_weight(const float* rows, int64_t ld_rows, int64_t n_events, con
   if (rc != JSCC_OK) return rc;
   const int64_t vf = (int64_t)n_zf * n_lf;
   JSCC_REQUIRE(ld_sysmat >= vf, "jscc_sparse_weight: ld_sysmat < fine voxels");
-  const SpPlan p = plan_sparse(n_events, vf);
-  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "jscc_sparse_weight: workspace too small (%zu < %zu)",
-               workspace_bytes, p.ws_bytes);
-  Carver cv(workspace, workspace_bytes);
-  float* xr = cv.take<float>((size_t)p.ldp);
-  float* f = cv.take<float>((size_t)n_events);
-  float* s = cv.take<float>((size_t)n_events);
-  float* coef = cv.take<float>((size_t)n_events);
-  float* part = cv.take<float>((size_t)p.chunks * p.ldp);
-  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight: workspace carve overflow");
-  cudaStream_t st = as_stream(stream);
-  const float* x = img;
-  if (rotmat) {
-    int64_t blocks = (vf + 255) / 256;
-    if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
-    JSCC_TIMED("sc_gather_rot", st,
-               (sc_gather_rot_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, rotmat, ld_rot, 0, 1, vf, p.ldp, xr)));
-    JSCC_LAUNCH_CHECK();
-    x = xr;
+  SpRows<float> r{rows, nullptr, nullptr, ld_rows, n_det};
+  return sparse_weight_impl<float>(r, n_events, sysmat, sysmat_dtype, ld_sysmat, t, vf, mode, img, rotmat, rotmat_inv,
+                                   ld_rot, scale, weight, workspace, workspace_bytes, as_stream(stream));
+}
+
+int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,
+                             int64_t n_events, const void* sysmat, int32_t sysmat_dtype, int64_t ld_sysmat,
+                             int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
+                             const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc, int32_t mode,
+                             const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
+                             float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_det > 0, "jscc_sparse_weight_split: bad sizes");
+  JSCC_REQUIRE(mode == JSCC_SPARSE_MATERIALIZE || mode == JSCC_SPARSE_GROUPED, "jscc_sparse_weight_split: mode");
+  JSCC_REQUIRE(sysmat_dtype == JSCC_DTYPE_F32 || sysmat_dtype == JSCC_DTYPE_BF16, "jscc_sparse_weight_split: dtype");
+  JSCC_REQUIRE(tc_dtype == JSCC_DTYPE_F32 || tc_dtype == JSCC_DTYPE_BF16, "jscc_sparse_weight_split: row dtype");
+  if (n_events == 0) return JSCC_OK;
+  JSCC_REQUIRE(row_id && t_coarse && sysmat && img && weight, "jscc_sparse_weight_split: null pointer argument");
+  JSCC_REQUIRE((rotmat == nullptr) == (rotmat_inv == nullptr), "jscc_sparse_weight_split: give both tables");
+  UpTaps t;
+  int rc = make_taps(z_taps, z_tw, l_taps, l_tw, n_lf, n_lc, &t);
+  if (rc != JSCC_OK) return rc;
+  const int64_t vf = (int64_t)n_zf * n_lf;
+  JSCC_REQUIRE(ld_sysmat >= vf, "jscc_sparse_weight_split: ld_sysmat < fine voxels");
+  JSCC_REQUIRE(ld_tc >= (int64_t)n_lc * (n_zf > 0 ? 1 : 0), "jscc_sparse_weight_split: ld_tc too small");
+  if (tc_dtype == JSCC_DTYPE_F32) {
+    SpRows<float> r{nullptr, row_id, static_cast<const float*>(t_coarse), ld_tc, n_det};
+    return sparse_weight_impl<float>(r, n_events, sysmat, sysmat_dtype, ld_sysmat, t, vf, mode, img, rotmat,
+                                     rotmat_inv, ld_rot, scale, weight, workspace, workspace_bytes, as_stream(stream));
   }
-  const bool mat = mode == JSCC_SPARSE_MATERIALIZE;
-  if (sysmat_dtype == JSCC_DTYPE_F32) {
-    const float* e = static_cast<const float*>(sysmat);
-    if (mat) launch_sparse_weight<true, float>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef, part, p, st);
-    else launch_sparse_weight<false, float>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef, part, p, st);
-  } else {
-    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(sysmat);
-    if (mat)
-      launch_sparse_weight<true, __nv_bfloat16>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef,
-                                                part, p, st);
-    else
-      launch_sparse_weight<false, __nv_bfloat16>(rows, ld_rows, n_events, vf, x, e, ld_sysmat, n_det, t, f, s, coef,
-                                                 part, p, st);
-  }
-  JSCC_CUDA_CHECK(cudaGetLastError());
-  int64_t blocks = (vf + 255) / 256;
-  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
-  const int has_scale = scale != 1.0f;
-  JSCC_TIMED("sparse_reduce", st,
-             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldp, (int)p.chunks, rotmat_inv, ld_rot, vf,
-                                                                     has_scale, scale, weight)));
-  JSCC_LAUNCH_CHECK();
-  return JSCC_OK;
+  SpRows<__nv_bfloat16> r{nullptr, row_id, static_cast<const __nv_bfloat16*>(t_coarse), ld_tc, n_det};
+  return sparse_weight_impl<__nv_bfloat16>(r, n_events, sysmat, sysmat_dtype, ld_sysmat, t, vf, mode, img, rotmat,
+                                           rotmat_inv, ld_rot, scale, weight, workspace, workspace_bytes,
+                                           as_stream(stream));
 }
 
 }  // extern "C"

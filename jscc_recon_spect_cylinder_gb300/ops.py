@@ -438,3 +438,45 @@ def sparse_weight(rows, sysmat, tables: SparseTables, img, grouped=False, rotmat
         float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
     _lib.check(rc, "jscc_sparse_weight")
     return out
+
+
+def split_sparse_rows(rows, dtype=torch.bfloat16):
+    """Packed rows [E, 1 + V_c] -> (row_id int32 0-based, coarse rows [E, V_c] of ``dtype``)."""
+    ids = (sparse_unpack_ids(rows) - 1).to(torch.int32)
+    return ids, rows[:, 1:].to(dtype).contiguous()
+
+
+def sparse_weight_split(row_id, t_coarse, sysmat, tables: SparseTables, img, grouped=False, rotmat=None,
+                        rotmat_inv=None, rot_col=0, scale=1.0, out=None):
+    """sparse_weight over split storage (int32 row ids + float32/bf16 coarse rows)."""
+    dev = _lib.require_cuda(row_id, t_coarse, sysmat, img, rotmat, rotmat_inv, out, what="sparse_weight_split")
+    tc = _rows_contig(t_coarse)
+    A = _rows_contig(sysmat)
+    vf = tables.n_zf * tables.n_lf
+    x = _f32_contig(img.reshape(-1))
+    if x.numel() != vf:
+        raise ValueError(f"img has {x.numel()} voxels, the projector has {vf}")
+    if tc.size(1) < tables.n_lc * tables.n_zc:
+        raise ValueError("coarse rows are shorter than the projector's coarse grid")
+    if out is None:
+        out = torch.zeros((vf, 1), dtype=torch.float32, device=dev)
+    rotmat = _index_table(rotmat, vf, "rotmat")
+    rotmat_inv = _index_table(rotmat_inv, vf, "rotmat_inv")
+    rm = ri = None
+    ld_rot = 0
+    if rotmat is not None and not (_is_identity(rotmat, rot_col, 1) and _is_identity(rotmat_inv, rot_col, 1)):
+        rm = rotmat.data_ptr() + rot_col * 8
+        ri = rotmat_inv.data_ptr() + rot_col * 8
+        ld_rot = rotmat.stride(0)
+    ids = row_id.to(torch.int32).contiguous()
+    n = ids.numel()
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sparse_weight_workspace_bytes(n, vf))
+    rc = lib.jscc_sparse_weight_split(
+        ids.data_ptr(), tc.data_ptr(), _dtype_code(tc), tc.stride(0), n, A.data_ptr(), _dtype_code(A), A.stride(0),
+        A.size(0), tables.z_taps.data_ptr(), tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(),
+        tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE,
+        x.data_ptr(), rm, ri, ld_rot, float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(),
+        _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sparse_weight_split")
+    return out

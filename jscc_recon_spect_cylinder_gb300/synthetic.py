@@ -180,3 +180,67 @@ def sc_problem(n_r=40, n_theta=120, disk_radius=50.0, det_radius=120.0, n_phi=10
         s += colsum[:, inv[:, r] - 1].transpose(0, 1)
     s = s / R
     return ScProblem(grid, A, proj, rot, inv, s, x)
+
+
+# ----------------------------------------------------------------------------- Compton lists
+def _kn_cos_theta(n, e0, generator, device):
+    """Scatter-angle cosines from the Klein-Nishina distribution (rejection sampling)."""
+    k = e0 / 0.511
+    out = torch.empty(n, dtype=torch.float64, device=device)
+    filled = 0
+    while filled < n:
+        m = 2 * (n - filled) + 1024
+        c = torch.rand(m, generator=generator, device=device, dtype=torch.float64) * 2 - 1
+        ratio = 1.0 / (1.0 + k * (1.0 - c))
+        f = ratio * ratio * (ratio + 1.0 / ratio - (1.0 - c * c))   # (E'/E)^2 (E'/E + E/E' - sin^2)
+        u = torch.rand(m, generator=generator, device=device, dtype=torch.float64) * 2.0
+        acc = c[u < f]
+        take = min(acc.numel(), n - filled)
+        out[filled:filled + take] = acc[:take]
+        filled += take
+    return out
+
+
+def compton_list(coor, activity, scat_pos, abs_radius, abs_n_phi, abs_n_axial, abs_pitch, e0, n_events, generator,
+                 cp1_offset=0, cp2_offset=0, abs_phi0=0.0):
+    """Forward-simulated two-interaction events (cp1, e1, cp2, e2) with 1-based ids.
+
+    Source voxel ~ activity; first interaction at a uniformly chosen scatter pixel; scatter
+    angle from Klein-Nishina around the source -> pixel direction, uniform azimuth; the
+    scattered ray is intersected with the absorber cylinder (radius abs_radius, pixels of
+    cylinder_pixels(abs_radius, abs_n_phi, abs_n_axial, abs_pitch, abs_phi0)); rays that miss
+    its axial extent are dropped, so fewer than n_events may be returned. e1 = e0 - E'.
+    Energy blur is left to the T builder (the reference smears in the builder)."""
+    dev = coor.device
+    n = int(n_events)
+    src = coor[torch.multinomial(activity.flatten().double(), n, replacement=True, generator=generator)].double()
+    i1 = torch.randint(scat_pos.size(0), (n,), generator=generator, device=dev)
+    p1 = scat_pos[i1].double()
+    d0 = p1 - src
+    d0 = d0 / d0.norm(dim=1, keepdim=True)
+    cos_t = _kn_cos_theta(n, e0, generator, dev)
+    sin_t = torch.sqrt((1 - cos_t * cos_t).clamp_min(0))
+    phi = torch.rand(n, generator=generator, device=dev, dtype=torch.float64) * (2 * math.pi)
+    helper = torch.where(d0[:, 2:3].abs() < 0.9, torch.tensor([0.0, 0.0, 1.0], device=dev, dtype=torch.float64),
+                         torch.tensor([1.0, 0.0, 0.0], device=dev, dtype=torch.float64))
+    u = torch.linalg.cross(d0, helper)
+    u = u / u.norm(dim=1, keepdim=True)
+    w = torch.linalg.cross(d0, u)
+    d1 = cos_t[:, None] * d0 + sin_t[:, None] * (torch.cos(phi)[:, None] * u + torch.sin(phi)[:, None] * w)
+    # ray p1 + s d1 against the cylinder x^2 + y^2 = R^2 (outward root)
+    a = d1[:, 0] ** 2 + d1[:, 1] ** 2
+    b = 2 * (p1[:, 0] * d1[:, 0] + p1[:, 1] * d1[:, 1])
+    c = p1[:, 0] ** 2 + p1[:, 1] ** 2 - abs_radius ** 2
+    disc = (b * b - 4 * a * c).clamp_min(0)
+    s = (-b + torch.sqrt(disc)) / (2 * a.clamp_min(1e-12))
+    p2 = p1 + s[:, None] * d1
+    half = abs_n_axial * abs_pitch / 2.0
+    ok = (a > 1e-9) & (s > 0) & (p2[:, 2].abs() < half)
+    ang = torch.remainder(torch.atan2(p2[:, 1], p2[:, 0]) - abs_phi0, 2 * math.pi)
+    iphi = torch.clamp((ang / (2 * math.pi) * abs_n_phi).floor().long(), 0, abs_n_phi - 1)
+    iz = torch.clamp(((p2[:, 2] + half) / abs_pitch).floor().long(), 0, abs_n_axial - 1)
+    cp2 = iz * abs_n_phi + iphi
+    e_sc = e0 / (1.0 + (e0 / 0.511) * (1.0 - cos_t))
+    e1 = e0 - e_sc
+    lst = torch.stack(((i1 + 1 + cp1_offset).double(), e1, (cp2 + 1 + cp2_offset).double(), e_sc), dim=1)
+    return lst[ok].to(torch.float32)

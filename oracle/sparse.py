@@ -318,3 +318,31 @@ def sparse_builder(sysmat, detector_pos, p, list_smeared, delta_r1, delta_r2, e0
     stable = (1.0 / np.sum(tn ** 2, axis=1)) >= oc.MIN_EVENT_EFFECTIVE_SUPPORT
     rows = pack_rows(cp1[keep][stable], tcn[stable].astype(np.float32))
     return rows, idx[keep][stable]
+
+
+# ----------------------------------------------------------------------------- sparse restatement
+def upsample_matrix_csr(p):
+    """The upsample operator as one scipy CSR matrix U [V_f, V_c] = kron(z_expand, layer_expand),
+    the same linear map as upsample_rows (validated against it in tests), for CPU runs where
+    the reference's dense products are prohibitive."""
+    import scipy.sparse as sp
+
+    return sp.kron(sp.csr_matrix(p.z_expand.astype(np.float64)), sp.csr_matrix(p.layer_expand.astype(np.float64)),
+                   format="csr")
+
+
+def weight_materialize_csr(rows, sysmat, x, U, dtype=np.float64):
+    """weight_materialize with the upsample applied as a sparse matrix product."""
+    x = np.asarray(x, dtype=dtype).reshape(-1, 1)
+    rows = np.asarray(rows)
+    if rows.shape[0] == 0:
+        return np.zeros_like(x)
+    cp1 = np.clip(np.round(rows[:, 0]).astype(np.int64) - 1, 0, sysmat.shape[0] - 1)
+    up = np.asarray((U @ np.asarray(rows[:, 1:], dtype=dtype).T).T, dtype=dtype)
+    t = np.nan_to_num(up * np.asarray(sysmat[cp1], dtype=dtype), nan=0.0, posinf=0.0, neginf=0.0)
+    s = t.sum(axis=1, keepdims=True)
+    valid = np.isfinite(s[:, 0]) & (s[:, 0] > 0)
+    t = t[valid] / s[valid]
+    with np.errstate(divide="ignore"):
+        w = t.T @ (dtype(1.0) / np.maximum(t @ x, dtype(1e-12)))
+    return np.nan_to_num(w, nan=0.0, posinf=0.0, neginf=0.0)

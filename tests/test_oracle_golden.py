@@ -204,3 +204,14 @@ def test_sparse_builder_and_weights_match_reference(golden):
     assert rel_l2(w_g, g["s_w_grouped"]) < 1e-5
     # grouped and materialise forms agree (row-scale invariance of the list-mode weight)
     assert rel_l2(w_g, w_m) < 1e-5
+
+
+def test_sparse_restatement_matches_dense_operators(golden):
+    g = golden("sparse_ops")
+    p = osp.build_projector(g["s_coor"], theta_stride=4, z_stride=2, rotate_num=4)
+    U = osp.upsample_matrix_csr(p)
+    rows = g["s_event_rows"]
+    np.testing.assert_allclose((U @ rows[:, 1:].astype(np.float64).T).T, osp.upsample_rows(rows[:, 1:], p),
+                               rtol=1e-12, atol=1e-15)
+    w = osp.weight_materialize_csr(rows, g["s_sysmat"], g["s_x"], U)
+    assert rel_l2(w, g["s_w_mat"]) < 1e-5
