@@ -408,8 +408,13 @@ def sparse_materialize(rows, sysmat, tables: SparseTables):
 
 
 def sparse_weight(rows, sysmat, tables: SparseTables, img, grouped=False, rotmat=None, rotmat_inv=None, rot_col=0,
-                  scale=1.0, out=None):
-    """Fused sparse list-mode weight (MATERIALIZE or GROUPED semantics), accumulated into ``out``."""
+                  scale=1.0, out=None, method="auto"):
+    """Fused sparse list-mode weight (MATERIALIZE or GROUPED semantics), accumulated into
+    ``out``. method "auto" uses the grouped coarse-space kernel when the grids fit in
+    shared memory, "event" the per-event fine-space kernels."""
+    if method != "event" and grouped_fits(tables):
+        return sparse_weight_grouped(sysmat, tables, img, rows=rows, grouped=grouped, rotmat=rotmat,
+                                     rotmat_inv=rotmat_inv, rot_col=rot_col, scale=scale, out=out)
     dev = _lib.require_cuda(rows, sysmat, img, rotmat, rotmat_inv, out, what="sparse_weight")
     r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
     A = _rows_contig(sysmat)
@@ -447,8 +452,11 @@ def split_sparse_rows(rows, dtype=torch.bfloat16):
 
 
 def sparse_weight_split(row_id, t_coarse, sysmat, tables: SparseTables, img, grouped=False, rotmat=None,
-                        rotmat_inv=None, rot_col=0, scale=1.0, out=None):
+                        rotmat_inv=None, rot_col=0, scale=1.0, out=None, method="auto"):
     """sparse_weight over split storage (int32 row ids + float32/bf16 coarse rows)."""
+    if method != "event" and grouped_fits(tables):
+        return sparse_weight_grouped(sysmat, tables, img, row_id=row_id, t_coarse=t_coarse, grouped=grouped,
+                                     rotmat=rotmat, rotmat_inv=rotmat_inv, rot_col=rot_col, scale=scale, out=out)
     dev = _lib.require_cuda(row_id, t_coarse, sysmat, img, rotmat, rotmat_inv, out, what="sparse_weight_split")
     tc = _rows_contig(t_coarse)
     A = _rows_contig(sysmat)
@@ -479,4 +487,106 @@ def sparse_weight_split(row_id, t_coarse, sysmat, tables: SparseTables, img, gro
         x.data_ptr(), rm, ri, ld_rot, float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(),
         _lib.stream_handle(dev))
     _lib.check(rc, "jscc_sparse_weight_split")
+    return out
+
+
+# ============================================================================ grouped sparse weight
+class GroupPlan:
+    """Grouping of a block of sparse events by first-hit row for jscc_sparse_weight_grouped:
+    stable order by row, group offsets / rows, and contiguous group ranges per CTA balanced
+    by cost (one fine-grid pass per group + coarse passes per event)."""
+
+    def __init__(self, row_ids: torch.Tensor, n_fine: int, n_coarse: int, n_ctas: int):
+        ids = row_ids.to(torch.int64)
+        order = torch.argsort(ids, stable=True)
+        sorted_ids = ids[order]
+        rows, counts = torch.unique_consecutive(sorted_ids, return_counts=True)
+        offsets = torch.zeros(rows.numel() + 1, dtype=torch.int64, device=ids.device)
+        offsets[1:] = torch.cumsum(counts, 0)
+        cost = 3.0 * n_fine + counts.double() * (3.0 * n_coarse)
+        ccost = torch.cumsum(cost, 0)
+        targets = ccost[-1] * torch.arange(1, n_ctas, device=ids.device, dtype=torch.float64) / n_ctas
+        cuts = torch.searchsorted(ccost, targets)
+        begin = torch.zeros(n_ctas + 1, dtype=torch.int64, device=ids.device)
+        begin[1:-1] = cuts
+        begin[-1] = rows.numel()
+        begin = torch.cummax(begin, 0).values
+        self.order = order.to(torch.int32).contiguous()
+        self.offsets = offsets.to(torch.int32).contiguous()
+        self.rows = rows.to(torch.int32).contiguous()
+        self.cta_begin = begin.to(torch.int32).contiguous()
+        self.n_groups = int(rows.numel())
+        self.n_ctas = n_ctas
+
+
+def _group_plan(key_tensor, row_ids_fn, tables, n_ctas):
+    """GroupPlan cached on ``key_tensor`` (keyed by its version and the grid sizes)."""
+    cache = getattr(key_tensor, "_jscc_group_plan", None)
+    key = (key_tensor._version, tables.n_zf * tables.n_lf, tables.n_zc * tables.n_lc, n_ctas)
+    if cache is not None and cache[0] == key:
+        return cache[1]
+    plan = GroupPlan(row_ids_fn(), key[1], key[2], n_ctas)
+    key_tensor._jscc_group_plan = (key, plan)
+    return plan
+
+
+def grouped_fits(tables: SparseTables) -> bool:
+    vf = tables.n_zf * tables.n_lf
+    vc = tables.n_zc * tables.n_lc
+    return ((vf + 3) // 4 * 4 + 2 * ((vc + 3) // 4 * 4)) * 4 <= 227 * 1024
+
+
+def _sms(dev):
+    return torch.cuda.get_device_properties(dev).multi_processor_count
+
+
+def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=None, t_coarse=None, grouped=False,
+                          rotmat=None, rotmat_inv=None, rot_col=0, scale=1.0, out=None):
+    """Grouped coarse-space sparse weight over packed ``rows`` or split (``row_id``,
+    ``t_coarse``) storage; accumulated into ``out``. Same result as sparse_weight."""
+    dev = _lib.require_cuda(sysmat, img, rows, row_id, t_coarse, rotmat, rotmat_inv, out,
+                            what="sparse_weight_grouped")
+    A = _rows_contig(sysmat)
+    vf = tables.n_zf * tables.n_lf
+    x = _f32_contig(img.reshape(-1))
+    if x.numel() != vf:
+        raise ValueError(f"img has {x.numel()} voxels, the projector has {vf}")
+    if out is None:
+        out = torch.zeros((vf, 1), dtype=torch.float32, device=dev)
+    n_ctas = _sms(dev)
+    if rows is not None:
+        r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
+        n = r.size(0)
+        if n == 0:
+            return out
+        plan = _group_plan(r, lambda: torch.clamp(sparse_unpack_ids(r) - 1, 0, A.size(0) - 1), tables, n_ctas)
+        packed, ids_p, tc_p, tc_dt, ld = r.data_ptr(), None, None, _lib.DTYPE_F32, r.stride(0)
+    else:
+        tc = _rows_contig(t_coarse)
+        ids = row_id.to(torch.int32).contiguous()
+        n = ids.numel()
+        if n == 0:
+            return out
+        plan = _group_plan(ids, lambda: torch.clamp(ids.long(), 0, A.size(0) - 1), tables, n_ctas)
+        packed, ids_p, tc_p, tc_dt, ld = None, ids.data_ptr(), tc.data_ptr(), _dtype_code(tc), tc.stride(0)
+    rotmat = _index_table(rotmat, vf, "rotmat")
+    rotmat_inv = _index_table(rotmat_inv, vf, "rotmat_inv")
+    rm = ri = None
+    ld_rot = 0
+    if rotmat is not None and not (_is_identity(rotmat, rot_col, 1) and _is_identity(rotmat_inv, rot_col, 1)):
+        rm = rotmat.data_ptr() + rot_col * 8
+        ri = rotmat_inv.data_ptr() + rot_col * 8
+        ld_rot = rotmat.stride(0)
+    (azp, azi, azw), (alp, ali, alw) = tables.adj
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, n_ctas))
+    rc = lib.jscc_sparse_weight_grouped(
+        ids_p, tc_p, tc_dt, ld, packed, n, plan.order.data_ptr(), plan.offsets.data_ptr(), plan.rows.data_ptr(),
+        plan.n_groups, plan.cta_begin.data_ptr(), n_ctas, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
+        tables.z_taps.data_ptr(), tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(),
+        tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, azp.data_ptr(), azi.data_ptr(), azw.data_ptr(),
+        tables.n_zc, alp.data_ptr(), ali.data_ptr(), alw.data_ptr(),
+        _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE, x.data_ptr(), rm, ri, ld_rot, float(scale),
+        out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sparse_weight_grouped")
     return out

@@ -347,3 +347,36 @@ def test_sparse_osem_loops_vs_oracle(cuda, golden):
             1.5 * osp.weight_materialize(h, An, ref, pn)
         ref = osem_sc.safe_em_update(ref, w, s.cpu().numpy())
     assert rel_l2(img.cpu(), ref) < TOL_W
+
+
+@pytest.mark.parametrize("grouped", [False, True])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+def test_grouped_kernel_matches_event_kernel(cuda, golden, grouped, dtype):
+    """The grouped coarse-space kernel and the per-event fine-space kernel compute the same
+    weight (packed and split storage, both semantics, rotated view, FP32 and BF16 rows)."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import ops, synthetic
+
+    g = golden("sparse_ops")
+    p = cso.build_compton_sparse_projector(torch.from_numpy(g["s_coor"]), 4, 2, 4)
+    tb = cso.tables(p, cuda)
+    A = torch.from_numpy(g["s_sysmat"]).to(cuda)
+    rows = torch.from_numpy(g["s_event_rows"]).to(cuda)
+    rows = torch.cat([rows] * 7)  # repeated first-hit rows -> real groups
+    V = A.size(1)
+    x = torch.from_numpy(g["s_x"]).to(cuda)
+    w_ev = ops.sparse_weight(rows, A, tb, x, grouped=grouped, method="event")
+    w_gr = ops.sparse_weight(rows, A, tb, x, grouped=grouped)
+    assert rel_l2(w_gr.cpu(), w_ev.cpu()) < TOL_W
+    ids, tc = ops.split_sparse_rows(rows, dtype)
+    w_sp_ev = ops.sparse_weight_split(ids, tc, A, tb, x, grouped=grouped, method="event")
+    w_sp_gr = ops.sparse_weight_split(ids, tc, A, tb, x, grouped=grouped)
+    assert rel_l2(w_sp_gr.cpu(), w_sp_ev.cpu()) < TOL_W
+    # rotated view: 24 theta per ring, 4 views of 6 steps
+    rot, inv = synthetic.cyclic_rotation_tables(6 * 4, 24, 4)
+    rot, inv = rot.to(cuda), inv.to(cuda)
+    a = ops.sparse_weight(rows, A, tb, x, grouped=grouped, rotmat=rot, rotmat_inv=inv, rot_col=2, method="event")
+    b = ops.sparse_weight(rows, A, tb, x, grouped=grouped, rotmat=rot, rotmat_inv=inv, rot_col=2)
+    assert rel_l2(b.cpu(), a.cpu()) < TOL_W
+    # deterministic
+    assert torch.equal(ops.sparse_weight(rows, A, tb, x, grouped=grouped), w_gr)
