@@ -95,6 +95,26 @@ __device__ __forceinline__ float up_value(const TC* __restrict__ tc, const UpTap
   return v;
 }
 
+// The same two-tap upsample from a coarse row held in SHARED memory (plain loads: the
+// read-only global path of ld_any must not be used on a shared-memory address).
+__device__ __forceinline__ float up_value_shared(const float* tc, const UpTaps& t, int zf, int lf) {
+  const int l0 = t.lt[2 * lf], l1 = t.lt[2 * lf + 1];
+  const float w0 = t.lwt[2 * lf], w1 = t.lwt[2 * lf + 1];
+  const int z0 = t.zt[2 * zf], z1 = t.zt[2 * zf + 1];
+  const float u0 = t.zwt[2 * zf], u1 = t.zwt[2 * zf + 1];
+  const float* r0 = tc + (int64_t)z0 * t.n_lc;
+  const float* r1 = tc + (int64_t)z1 * t.n_lc;
+  float a = w0 * r0[l0];
+  if (w1 != 0.f) a = fmaf(w1, r0[l1], a);
+  float v = u0 * a;
+  if (u1 != 0.f) {
+    float b = w0 * r1[l0];
+    if (w1 != 0.f) b = fmaf(w1, r1[l1], b);
+    v = fmaf(u1, b, v);
+  }
+  return v;
+}
+
 // Event rows in either layout: packed float rows (cp1 as float in column 0, the
 // reference's format) or split storage (0-based sysmat row ids + coarse rows of TC,
 // float32 or bf16 — bf16 cannot hold the ids, hence the split).
@@ -482,7 +502,7 @@ sparse_grouped_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const 
     // w += A_g * up(q)
     for (int64_t j = tid; j < vf; j += kGrpThreads) {
       const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
-      const float u = up_value<float>(bq, taps, zf, lf);
+      const float u = up_value_shared(bq, taps, zf, lf);
       if (u != 0.f) w[j] = fmaf(ld_any(er, j), u, w[j]);
     }
   }
