@@ -405,14 +405,16 @@ static int sparse_weight_impl(const SpRows<TC>& rows, int64_t n_events, const vo
 }
 
 // ------------------------------------------------------------------ grouped coarse-space weight
-// Events sharing a first-hit row g share that sysmat row, so with v_ij = up(tc_i)[j] A[g, j]:
-//   f_i = sum_j v_ij x_j = tc_i . adj(A_g * x)          (adjoint of the upsample, coarse space)
-//   S_i = sum_j v_ij     = tc_i . adj(A_g)
-//   w_j += sum_i v_ij c_i = A[g, j] * up(sum_i c_i tc_i)[j]
-// so the fine-grid work is done once per group instead of once per event. A persistent
-// grid: CTA k owns a contiguous range of groups (balanced by cost on the host) and keeps
-// its partial weight over the whole fine grid in shared memory; partials are reduced in
-// CTA order afterwards. Events are visited through `order` (event indices sorted by row).
+// Events sharing a first-hit row g share that sysmat row, so with v_ij = up(t_i)[j] A[g, j]:
+//   f_i = sum_j v_ij x_j = t_i . adj(A_g * x)          (adjoint of the upsample, coarse grid)
+//   S_i = sum_j v_ij     = t_i . adj(A_g)              (fixed per event: computed once)
+//   w_j += sum_i v_ij c_i = A[g, j] * up(q_g)[j],  q_g = sum_{i in g} c_i t_i
+// Two kernels, both deterministic:
+//   group_coef:    one CTA per group (grid-stride): adj(A_g * x) in shared memory, per-event
+//                  coarse dots -> c_i, then q_g written to the workspace;
+//   group_scatter: one thread per fine voxel (its taps in registers) x a chunk of groups,
+//                  partial sums per chunk, reduced in chunk order by sparse_reduce.
+// Events are visited through `order` (event indices sorted by row).
 struct MapCsr {
   const int32_t* zp;
   const int32_t* zi;
@@ -424,90 +426,168 @@ struct MapCsr {
   int n_li;   // fine layers (inputs)
 };
 
-constexpr int kGrpThreads = 1024;
+constexpr int kGcThreads = 256;
 
-template <bool MATERIALIZE, typename TE, typename TC>
-__global__ void __launch_bounds__(kGrpThreads, 1)
-sparse_grouped_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
-                      const int32_t* __restrict__ grow, const int32_t* __restrict__ cta_gbeg, int64_t vf, int64_t vc,
-                      const float* __restrict__ x, const TE* __restrict__ eff, int64_t ld_eff, UpTaps taps,
-                      MapCsr adj, float* __restrict__ coef, float* __restrict__ part, int64_t ldp) {
+// MODE 0: materialise semantics (needs S), 1: grouped semantics, 2: compute S (x = 1, no q)
+template <int MODE, typename TE, typename TC>
+__global__ void __launch_bounds__(kGcThreads)
+sparse_group_coef_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
+                         const int32_t* __restrict__ grow, int n_groups, int64_t vc, const float* __restrict__ x,
+                         const TE* __restrict__ eff, int64_t ld_eff, MapCsr adj, float* __restrict__ s_ev,
+                         float* __restrict__ coef, float* __restrict__ q, int64_t ldq) {
   extern __shared__ float4 sm4[];
-  float* w = reinterpret_cast<float*>(sm4);               // [vf]
-  float* bq = w + ((vf + 3) & ~(int64_t)3);               // [vc]  adj(A_g x), then q
-  float* ag = bq + ((vc + 3) & ~(int64_t)3);              // [vc]  adj(A_g)
+  float* b = reinterpret_cast<float*>(sm4);  // [vc]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int64_t j = tid; j < vf; j += kGrpThreads) w[j] = 0.f;
-  const int g0 = cta_gbeg[blockIdx.x], g1 = cta_gbeg[blockIdx.x + 1];
-  for (int gi = g0; gi < g1; ++gi) {
-    const int64_t g = grow[gi];
-    const TE* er = eff + g * ld_eff;
+  for (int gi = blockIdx.x; gi < n_groups; gi += gridDim.x) {
+    const TE* er = eff + (int64_t)grow[gi] * ld_eff;
     const int e0 = goff[gi], e1 = goff[gi + 1];
     __syncthreads();
-    // adjoint of (A_g * x) and of A_g
-    for (int64_t c = tid; c < vc; c += kGrpThreads) {
+    for (int64_t c = tid; c < vc; c += kGcThreads) {
       const int zo = (int)(c / adj.n_lo), lo = (int)(c % adj.n_lo);
-      float sb = 0.f, sa = 0.f;
+      float sb = 0.f;
       for (int a = adj.zp[zo]; a < adj.zp[zo + 1]; ++a) {
         const int64_t base = (int64_t)adj.zi[a] * adj.n_li;
-        float tb = 0.f, ta = 0.f;
-        for (int b = adj.lp[lo]; b < adj.lp[lo + 1]; ++b) {
-          const int64_t j = base + adj.li[b];
+        float tb = 0.f;
+        for (int k = adj.lp[lo]; k < adj.lp[lo + 1]; ++k) {
+          const int64_t j = base + adj.li[k];
           const float av = ld_any(er, j);
-          ta = fmaf(adj.lw[b], av, ta);
-          tb = fmaf(adj.lw[b], av * __ldg(x + j), tb);
+          tb = fmaf(adj.lw[k], MODE == 2 ? av : av * __ldg(x + j), tb);
         }
         sb = fmaf(adj.zw[a], tb, sb);
-        sa = fmaf(adj.zw[a], ta, sa);
       }
-      bq[c] = sb;
-      ag[c] = sa;
+      b[c] = sb;
     }
     __syncthreads();
-    // per-event coarse dots -> c_i
-    for (int e = e0 + warp; e < e1; e += kGrpThreads / 32) {
+    for (int e = e0 + warp; e < e1; e += kGcThreads / 32) {
       const int64_t i = order[e];
       const TC* tc = rows.coarse(i);
-      float f = 0.f, s = 0.f;
-      for (int64_t c = lane; c < vc; c += 32) {
-        const float t = ld_any(tc, c);
-        f = fmaf(t, bq[c], f);
-        s = fmaf(t, ag[c], s);
-      }
+      float f = 0.f;
+      for (int64_t c = lane; c < vc; c += 32) f = fmaf(ld_any(tc, c), b[c], f);
       f = warp_sum(f);
-      s = warp_sum(s);
       if (lane == 0) {
-        float ci;
-        if (MATERIALIZE) {
-          const bool valid = isfinite(s) && s > 0.f;
-          ci = valid ? (1.0f / fmaxf(f / s, 1e-12f)) / s : 0.f;
+        if (MODE == 2) {
+          s_ev[i] = f;
+        } else if (MODE == 0) {
+          const float si = s_ev[i];
+          coef[i] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
         } else {
-          ci = 1.0f / fmaxf(f, 1e-12f);
+          coef[i] = 1.0f / fmaxf(f, 1e-12f);
         }
-        coef[i] = ci;
       }
     }
+    if (MODE == 2) continue;
     __syncthreads();
-    // q = sum_i c_i tc_i (coarse), reusing bq
-    for (int64_t c = tid; c < vc; c += kGrpThreads) {
-      float q = 0.f;
+    float* qg = q + (int64_t)gi * ldq;
+    for (int64_t c = tid; c < vc; c += kGcThreads) {
+      float acc = 0.f;
       for (int e = e0; e < e1; ++e) {
         const int64_t i = order[e];
         const float ci = coef[i];
-        if (ci != 0.f) q = fmaf(ci, ld_any(rows.coarse(i), c), q);
+        if (ci != 0.f) acc = fmaf(ci, ld_any(rows.coarse(i), c), acc);
       }
-      bq[c] = q;
-    }
-    __syncthreads();
-    // w += A_g * up(q)
-    for (int64_t j = tid; j < vf; j += kGrpThreads) {
-      const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
-      const float u = up_value_shared(bq, taps, zf, lf);
-      if (u != 0.f) w[j] = fmaf(ld_any(er, j), u, w[j]);
+      qg[c] = acc;
     }
   }
-  __syncthreads();
-  for (int64_t j = tid; j < vf; j += kGrpThreads) part[(int64_t)blockIdx.x * ldp + j] = w[j];
+}
+
+// part[chunk][j] = sum_{groups in chunk} A[g, j] * up(q_g)[j]
+template <typename TE>
+__global__ void __launch_bounds__(256)
+sparse_group_scatter_kernel(const float* __restrict__ q, int64_t ldq, const int32_t* __restrict__ grow, int n_groups,
+                            int groups_per_chunk, int64_t vf, const TE* __restrict__ eff, int64_t ld_eff, UpTaps taps,
+                            float* __restrict__ part, int64_t ldp) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= vf) return;
+  const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
+  const int l0 = taps.lt[2 * lf], l1 = taps.lt[2 * lf + 1];
+  const float w0 = taps.lwt[2 * lf], w1 = taps.lwt[2 * lf + 1];
+  const int z0 = taps.zt[2 * zf], z1 = taps.zt[2 * zf + 1];
+  const float u0 = taps.zwt[2 * zf], u1 = taps.zwt[2 * zf + 1];
+  const int64_t c00 = (int64_t)z0 * taps.n_lc + l0, c01 = (int64_t)z0 * taps.n_lc + l1;
+  const int64_t c10 = (int64_t)z1 * taps.n_lc + l0, c11 = (int64_t)z1 * taps.n_lc + l1;
+  const int g_begin = blockIdx.y * groups_per_chunk;
+  const int g_end = (g_begin + groups_per_chunk) < n_groups ? g_begin + groups_per_chunk : n_groups;
+  float acc = 0.f;
+#pragma unroll 4
+  for (int gi = g_begin; gi < g_end; ++gi) {
+    const float* qg = q + (int64_t)gi * ldq;
+    float a = w0 * __ldg(qg + c00);
+    a = fmaf(w1, __ldg(qg + c01), a);
+    float v = u0 * a;
+    if (u1 != 0.f) {
+      float bb = w0 * __ldg(qg + c10);
+      bb = fmaf(w1, __ldg(qg + c11), bb);
+      v = fmaf(u1, bb, v);
+    }
+    if (v != 0.f) acc = fmaf(ld_any(eff + (int64_t)grow[gi] * ld_eff, j), v, acc);
+  }
+  part[(int64_t)blockIdx.y * ldp + j] = acc;
+}
+
+static int64_t group_chunks(int64_t n_groups, int64_t vf) {
+  const int64_t tiles = (vf + 255) / 256;
+  int64_t chunks = (2432 + tiles - 1) / (tiles > 0 ? tiles : 1);  // ~16 CTAs x 152 SMs
+  const int64_t max_chunks = (n_groups + 31) / 32;                 // >= 32 groups per chunk
+  if (chunks > max_chunks) chunks = max_chunks;
+  return chunks < 1 ? 1 : chunks;
+}
+
+
+template <typename TE, typename TC>
+static int grouped_launch(const SpRows<TC>& rows, int64_t n_events, const int32_t* order, const int32_t* goff,
+                          const int32_t* grow, int32_t n_groups, const TE* eff, int64_t ld_eff, const UpTaps& taps,
+                          const MapCsr& adj, int64_t vf, int64_t vc, int32_t mode, const float* x, float* s_ev,
+                          const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight, void* workspace,
+                          size_t workspace_bytes, cudaStream_t st) {
+  const int64_t ldp = (int64_t)align_up((size_t)vf, 8);
+  const int64_t ldq = (int64_t)align_up((size_t)vc, 8);
+  Carver cv(workspace, workspace_bytes);
+  cv.take<float>((size_t)ldp);  // rotated image slot (used by the caller)
+  float* coef = cv.take<float>((size_t)n_events);
+  float* q = cv.take<float>((size_t)n_groups * ldq);
+  const int64_t chunks = group_chunks(n_groups, vf);
+  float* part = cv.take<float>((size_t)chunks * ldp);
+  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
+  const size_t smem = align_up((size_t)vc, 4) * sizeof(float);
+  JSCC_REQUIRE(smem <= 227 * 1024, "jscc_sparse_weight_grouped: coarse grid (%zu bytes) exceeds shared memory", smem);
+  int64_t grid = (int64_t)num_sms() * ((227 * 1024) / (smem + 1024) < 8 ? (227 * 1024) / (smem + 1024) : 8);
+  if (grid < 1) grid = 1;
+  if (grid > n_groups) grid = n_groups;
+  cudaError_t attr = cudaSuccess;
+#define JSCC_GC(MODE)                                                                                            \
+  do {                                                                                                           \
+    attr = cudaFuncSetAttribute(sparse_group_coef_kernel<MODE, TE, TC>,                                          \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                         \
+    if (attr == cudaSuccess)                                                                                     \
+      JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
+                 (sparse_group_coef_kernel<MODE, TE, TC><<<(unsigned)grid, kGcThreads, smem, st>>>(              \
+                     rows, order, goff, grow, n_groups, vc, x, eff, ld_eff, adj, s_ev, coef, q, ldq)));          \
+  } while (0)
+  if (mode == JSCC_SPARSE_MATERIALIZE) {
+    JSCC_GC(2);  // S_i = t_i . adj(A_g)
+    JSCC_CUDA_CHECK(attr);
+    JSCC_LAUNCH_CHECK();
+    JSCC_GC(0);
+  } else {
+    JSCC_GC(1);
+  }
+#undef JSCC_GC
+  JSCC_CUDA_CHECK(attr);
+  JSCC_LAUNCH_CHECK();
+  const int gpc = (int)((n_groups + chunks - 1) / chunks);
+  dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
+  JSCC_TIMED("sparse_group_scatter", st,
+             (sparse_group_scatter_kernel<TE><<<sgrid, 256, 0, st>>>(q, ldq, grow, n_groups, gpc, vf, eff, ld_eff, taps,
+                                                                     part, ldp)));
+  JSCC_LAUNCH_CHECK();
+  int64_t blocks = (vf + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  const int has_scale = scale != 1.0f;
+  JSCC_TIMED("sparse_reduce", st,
+             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, (int)chunks, rotmat_inv, ld_rot, vf,
+                                                                     has_scale, scale, weight)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
 }
 
 }  // namespace jscc
@@ -673,29 +753,32 @@ int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coarse, int32_
 }
 
 
-size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int32_t n_ctas) {
+size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse, int32_t n_groups) {
   const int64_t ldp = (int64_t)align_up((size_t)(n_fine > 0 ? n_fine : 1), 8);
+  const int64_t ldq = (int64_t)align_up((size_t)(n_coarse > 0 ? n_coarse : 1), 8);
+  const int64_t chunks = group_chunks(n_groups, n_fine);
   return align_up((size_t)ldp * sizeof(float), 256) + align_up((size_t)(n_events > 0 ? n_events : 1) * 4, 256) +
-         align_up((size_t)(n_ctas > 0 ? n_ctas : 1) * ldp * sizeof(float), 256) + 256;
+         align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) +
+         align_up((size_t)chunks * ldp * sizeof(float), 256) + 256;
 }
 
 int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,
                                const float* packed_rows, int64_t n_events, const int32_t* order,
                                const int32_t* group_offsets, const int32_t* group_rows, int32_t n_groups,
-                               const int32_t* cta_group_begin, int32_t n_ctas, const void* sysmat,
-                               int32_t sysmat_dtype, int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps,
-                               const float* z_tw, int32_t n_zf, const int32_t* l_taps, const float* l_tw,
-                               int32_t n_lf, int32_t n_lc, const int32_t* adj_z_ptr, const int32_t* adj_z_idx,
-                               const float* adj_z_w, int32_t n_zc, const int32_t* adj_l_ptr, const int32_t* adj_l_idx,
-                               const float* adj_l_w, int32_t mode, const float* img, const int64_t* rotmat,
-                               const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight,
-                               void* workspace, size_t workspace_bytes, void* stream) {
-  JSCC_REQUIRE(n_events >= 0 && n_det > 0 && n_groups >= 0 && n_ctas > 0, "jscc_sparse_weight_grouped: bad sizes");
+                               float* event_sums, const void* sysmat, int32_t sysmat_dtype, int64_t ld_sysmat,
+                               int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
+                               const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc,
+                               const int32_t* adj_z_ptr, const int32_t* adj_z_idx, const float* adj_z_w, int32_t n_zc,
+                               const int32_t* adj_l_ptr, const int32_t* adj_l_idx, const float* adj_l_w, int32_t mode,
+                               const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
+                               float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_events >= 0 && n_det > 0 && n_groups >= 0, "jscc_sparse_weight_grouped: bad sizes");
   JSCC_REQUIRE(mode == JSCC_SPARSE_MATERIALIZE || mode == JSCC_SPARSE_GROUPED, "jscc_sparse_weight_grouped: mode");
   JSCC_REQUIRE(sysmat_dtype == JSCC_DTYPE_F32 || sysmat_dtype == JSCC_DTYPE_BF16, "jscc_sparse_weight_grouped: dtype");
   if (n_events == 0 || n_groups == 0) return JSCC_OK;
-  JSCC_REQUIRE(order && group_offsets && group_rows && cta_group_begin && sysmat && img && weight,
+  JSCC_REQUIRE(order && group_offsets && group_rows && sysmat && img && weight,
                "jscc_sparse_weight_grouped: null pointer argument");
+  JSCC_REQUIRE(mode == JSCC_SPARSE_GROUPED || event_sums, "jscc_sparse_weight_grouped: event_sums needed");
   JSCC_REQUIRE(packed_rows || (row_id && t_coarse), "jscc_sparse_weight_grouped: rows missing");
   JSCC_REQUIRE(packed_rows || tc_dtype == JSCC_DTYPE_F32 || tc_dtype == JSCC_DTYPE_BF16,
                "jscc_sparse_weight_grouped: row dtype");
@@ -708,19 +791,13 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
   const int64_t vf = (int64_t)n_zf * n_lf;
   const int64_t vc = (int64_t)n_zc * n_lc;
   JSCC_REQUIRE(ld_sysmat >= vf, "jscc_sparse_weight_grouped: ld_sysmat < fine voxels");
-  const size_t smem = (align_up((size_t)vf, 4) + 2 * align_up((size_t)vc, 4)) * sizeof(float);
-  JSCC_REQUIRE(smem <= 227 * 1024, "jscc_sparse_weight_grouped: fine + 2 coarse grids (%zu bytes) exceed shared memory",
-               smem);
-  const size_t need = jscc_sparse_grouped_workspace_bytes(n_events, vf, n_ctas);
+  const size_t need = jscc_sparse_grouped_workspace_bytes(n_events, vf, vc, n_groups);
   JSCC_REQUIRE(workspace && workspace_bytes >= need, "jscc_sparse_weight_grouped: workspace too small (%zu < %zu)",
                workspace_bytes, need);
-  const int64_t ldp = (int64_t)align_up((size_t)vf, 8);
-  Carver cv(workspace, workspace_bytes);
-  float* xr = cv.take<float>((size_t)ldp);
-  float* coef = cv.take<float>((size_t)n_events);
-  float* part = cv.take<float>((size_t)n_ctas * ldp);
-  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace carve overflow");
   cudaStream_t st = as_stream(stream);
+  const int64_t ldp = (int64_t)align_up((size_t)vf, 8);
+  Carver cv0(workspace, workspace_bytes);
+  float* xr = cv0.take<float>((size_t)ldp);  // same first slot as grouped_launch's carve
   const float* x = img;
   if (rotmat) {
     int64_t blocks = (vf + 255) / 256;
@@ -731,52 +808,22 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
     x = xr;
   }
   MapCsr adj{adj_z_ptr, adj_z_idx, adj_z_w, adj_l_ptr, adj_l_idx, adj_l_w, n_lc, n_lf};
-  const bool mat = mode == JSCC_SPARSE_MATERIALIZE;
-  cudaError_t attr = cudaSuccess;
-#define JSCC_GRP_LAUNCH(MAT, TE, TC, ROWS)                                                                       \
-  do {                                                                                                           \
-    attr = cudaFuncSetAttribute(sparse_grouped_kernel<MAT, TE, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                (int)smem);                                                                      \
-    if (attr == cudaSuccess)                                                                                     \
-      JSCC_TIMED("sparse_grouped", st,                                                                           \
-                 (sparse_grouped_kernel<MAT, TE, TC><<<(unsigned)n_ctas, kGrpThreads, smem, st>>>(               \
-                     ROWS, order, group_offsets, group_rows, cta_group_begin, vf, vc, x,                         \
-                     static_cast<const TE*>(sysmat), ld_sysmat, t, adj, coef, part, ldp)));                      \
-  } while (0)
+#define JSCC_GROUPED(TE, TC, ROWS)                                                                             \
+  grouped_launch<TE, TC>(ROWS, n_events, order, group_offsets, group_rows, n_groups,                           \
+                         static_cast<const TE*>(sysmat), ld_sysmat, t, adj, vf, vc, mode, x, event_sums,         \
+                         rotmat_inv, ld_rot, scale, weight, workspace, workspace_bytes, st)
   if (packed_rows) {
     SpRows<float> r{packed_rows, nullptr, nullptr, ld_tc, n_det};
-    if (sysmat_dtype == JSCC_DTYPE_F32) {
-      if (mat) JSCC_GRP_LAUNCH(true, float, float, r); else JSCC_GRP_LAUNCH(false, float, float, r);
-    } else {
-      if (mat) JSCC_GRP_LAUNCH(true, __nv_bfloat16, float, r); else JSCC_GRP_LAUNCH(false, __nv_bfloat16, float, r);
-    }
-  } else if (tc_dtype == JSCC_DTYPE_F32) {
-    SpRows<float> r{nullptr, row_id, static_cast<const float*>(t_coarse), ld_tc, n_det};
-    if (sysmat_dtype == JSCC_DTYPE_F32) {
-      if (mat) JSCC_GRP_LAUNCH(true, float, float, r); else JSCC_GRP_LAUNCH(false, float, float, r);
-    } else {
-      if (mat) JSCC_GRP_LAUNCH(true, __nv_bfloat16, float, r); else JSCC_GRP_LAUNCH(false, __nv_bfloat16, float, r);
-    }
-  } else {
-    SpRows<__nv_bfloat16> r{nullptr, row_id, static_cast<const __nv_bfloat16*>(t_coarse), ld_tc, n_det};
-    if (sysmat_dtype == JSCC_DTYPE_F32) {
-      if (mat) JSCC_GRP_LAUNCH(true, float, __nv_bfloat16, r); else JSCC_GRP_LAUNCH(false, float, __nv_bfloat16, r);
-    } else {
-      if (mat) JSCC_GRP_LAUNCH(true, __nv_bfloat16, __nv_bfloat16, r);
-      else JSCC_GRP_LAUNCH(false, __nv_bfloat16, __nv_bfloat16, r);
-    }
+    return sysmat_dtype == JSCC_DTYPE_F32 ? JSCC_GROUPED(float, float, r) : JSCC_GROUPED(__nv_bfloat16, float, r);
   }
-#undef JSCC_GRP_LAUNCH
-  JSCC_CUDA_CHECK(attr);
-  JSCC_LAUNCH_CHECK();
-  int64_t blocks = (vf + 255) / 256;
-  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
-  const int has_scale = scale != 1.0f;
-  JSCC_TIMED("sparse_reduce", st,
-             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, n_ctas, rotmat_inv, ld_rot, vf,
-                                                                     has_scale, scale, weight)));
-  JSCC_LAUNCH_CHECK();
-  return JSCC_OK;
+  if (tc_dtype == JSCC_DTYPE_F32) {
+    SpRows<float> r{nullptr, row_id, static_cast<const float*>(t_coarse), ld_tc, n_det};
+    return sysmat_dtype == JSCC_DTYPE_F32 ? JSCC_GROUPED(float, float, r) : JSCC_GROUPED(__nv_bfloat16, float, r);
+  }
+  SpRows<__nv_bfloat16> r{nullptr, row_id, static_cast<const __nv_bfloat16*>(t_coarse), ld_tc, n_det};
+  return sysmat_dtype == JSCC_DTYPE_F32 ? JSCC_GROUPED(float, __nv_bfloat16, r)
+                                        : JSCC_GROUPED(__nv_bfloat16, __nv_bfloat16, r);
+#undef JSCC_GROUPED
 }
 
 }  // extern "C"

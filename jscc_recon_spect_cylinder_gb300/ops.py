@@ -493,47 +493,33 @@ def sparse_weight_split(row_id, t_coarse, sysmat, tables: SparseTables, img, gro
 # ============================================================================ grouped sparse weight
 class GroupPlan:
     """Grouping of a block of sparse events by first-hit row for jscc_sparse_weight_grouped:
-    stable order by row, group offsets / rows, and contiguous group ranges per CTA balanced
-    by cost (one fine-grid pass per group + coarse passes per event)."""
+    event order sorted (stably) by row, group offsets into that order and group rows."""
 
-    def __init__(self, row_ids: torch.Tensor, n_fine: int, n_coarse: int, n_ctas: int):
+    def __init__(self, row_ids: torch.Tensor):
         ids = row_ids.to(torch.int64)
         order = torch.argsort(ids, stable=True)
-        sorted_ids = ids[order]
-        rows, counts = torch.unique_consecutive(sorted_ids, return_counts=True)
+        rows, counts = torch.unique_consecutive(ids[order], return_counts=True)
         offsets = torch.zeros(rows.numel() + 1, dtype=torch.int64, device=ids.device)
         offsets[1:] = torch.cumsum(counts, 0)
-        cost = 3.0 * n_fine + counts.double() * (3.0 * n_coarse)
-        ccost = torch.cumsum(cost, 0)
-        targets = ccost[-1] * torch.arange(1, n_ctas, device=ids.device, dtype=torch.float64) / n_ctas
-        cuts = torch.searchsorted(ccost, targets)
-        begin = torch.zeros(n_ctas + 1, dtype=torch.int64, device=ids.device)
-        begin[1:-1] = cuts
-        begin[-1] = rows.numel()
-        begin = torch.cummax(begin, 0).values
         self.order = order.to(torch.int32).contiguous()
         self.offsets = offsets.to(torch.int32).contiguous()
         self.rows = rows.to(torch.int32).contiguous()
-        self.cta_begin = begin.to(torch.int32).contiguous()
         self.n_groups = int(rows.numel())
-        self.n_ctas = n_ctas
 
 
-def _group_plan(key_tensor, row_ids_fn, tables, n_ctas):
-    """GroupPlan cached on ``key_tensor`` (keyed by its version and the grid sizes)."""
+def _group_plan(key_tensor, row_ids_fn):
+    """GroupPlan cached on ``key_tensor`` (rebuilt when the tensor is modified in place)."""
     cache = getattr(key_tensor, "_jscc_group_plan", None)
-    key = (key_tensor._version, tables.n_zf * tables.n_lf, tables.n_zc * tables.n_lc, n_ctas)
-    if cache is not None and cache[0] == key:
+    if cache is not None and cache[0] == key_tensor._version:
         return cache[1]
-    plan = GroupPlan(row_ids_fn(), key[1], key[2], n_ctas)
-    key_tensor._jscc_group_plan = (key, plan)
+    plan = GroupPlan(row_ids_fn())
+    key_tensor._jscc_group_plan = (key_tensor._version, plan)
     return plan
 
 
 def grouped_fits(tables: SparseTables) -> bool:
-    vf = tables.n_zf * tables.n_lf
-    vc = tables.n_zc * tables.n_lc
-    return ((vf + 3) // 4 * 4 + 2 * ((vc + 3) // 4 * 4)) * 4 <= 227 * 1024
+    """The grouped kernels keep one coarse row per CTA in shared memory."""
+    return ((tables.n_zc * tables.n_lc + 3) // 4 * 4) * 4 <= 227 * 1024
 
 
 def _sms(dev):
@@ -548,26 +534,30 @@ def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=N
                             what="sparse_weight_grouped")
     A = _rows_contig(sysmat)
     vf = tables.n_zf * tables.n_lf
+    vc = tables.n_zc * tables.n_lc
     x = _f32_contig(img.reshape(-1))
     if x.numel() != vf:
         raise ValueError(f"img has {x.numel()} voxels, the projector has {vf}")
     if out is None:
         out = torch.zeros((vf, 1), dtype=torch.float32, device=dev)
-    n_ctas = _sms(dev)
     if rows is not None:
         r = _rows_contig(rows) if rows.dtype == torch.float32 else _f32_contig(rows)
         n = r.size(0)
+        if r.size(1) != vc + 1:
+            raise ValueError(f"packed rows must have 1 + {vc} columns (got {r.size(1)})")
         if n == 0:
             return out
-        plan = _group_plan(r, lambda: torch.clamp(sparse_unpack_ids(r) - 1, 0, A.size(0) - 1), tables, n_ctas)
+        plan = _group_plan(r, lambda: torch.clamp(sparse_unpack_ids(r) - 1, 0, A.size(0) - 1))
         packed, ids_p, tc_p, tc_dt, ld = r.data_ptr(), None, None, _lib.DTYPE_F32, r.stride(0)
     else:
         tc = _rows_contig(t_coarse)
         ids = row_id.to(torch.int32).contiguous()
         n = ids.numel()
+        if tc.size(1) < vc or tc.size(0) != n:
+            raise ValueError(f"coarse rows must be [{n}, >= {vc}] (got {tuple(tc.shape)})")
         if n == 0:
             return out
-        plan = _group_plan(ids, lambda: torch.clamp(ids.long(), 0, A.size(0) - 1), tables, n_ctas)
+        plan = _group_plan(ids, lambda: torch.clamp(ids.long(), 0, A.size(0) - 1))
         packed, ids_p, tc_p, tc_dt, ld = None, ids.data_ptr(), tc.data_ptr(), _dtype_code(tc), tc.stride(0)
     rotmat = _index_table(rotmat, vf, "rotmat")
     rotmat_inv = _index_table(rotmat_inv, vf, "rotmat_inv")
@@ -579,10 +569,11 @@ def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=N
         ld_rot = rotmat.stride(0)
     (azp, azi, azw), (alp, ali, alw) = tables.adj
     lib = _lib.load()
-    ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, n_ctas))
+    ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, vc, plan.n_groups))
+    sums = torch.empty(n, dtype=torch.float32, device=dev)
     rc = lib.jscc_sparse_weight_grouped(
         ids_p, tc_p, tc_dt, ld, packed, n, plan.order.data_ptr(), plan.offsets.data_ptr(), plan.rows.data_ptr(),
-        plan.n_groups, plan.cta_begin.data_ptr(), n_ctas, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
+        plan.n_groups, sums.data_ptr(), A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
         tables.z_taps.data_ptr(), tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(),
         tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, azp.data_ptr(), azi.data_ptr(), azw.data_ptr(),
         tables.n_zc, alp.data_ptr(), ali.data_ptr(), alw.data_ptr(),
