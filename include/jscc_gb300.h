@@ -307,24 +307,26 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  *   w_j += sum_g A[g, j] * up(q_g)[j]     (fine grid, one thread per voxel)
  * with c_i as in jscc_sparse_weight. Rows come packed (packed_rows, row stride ld_tc) or
  * split (row_id + t_coarse of tc_dtype, stride ld_tc). The host supplies the grouping:
- * order [n_events] (event indices sorted by row), group_offsets [n_groups + 1] into order and
- * group_rows [n_groups] (0-based sysmat rows); the adjoint as CSR tables of z_expand^T and
- * layer_expand^T. event_sums [n_events] receives S_i (MATERIALIZE mode). The coarse grid must
- * fit in shared memory (V_c floats <= 227 KB). Deterministic (fixed-order reductions).
+ * order [n_events] (event indices sorted by row), group_offsets [n_groups + 1] into order,
+ * group_rows [n_groups] (0-based sysmat rows), and the adjoint as a fixed-width tap table
+ * adj_idx / adj_w [adj_width, V_c] (fine index and weight of each tap of coarse voxel c;
+ * padding taps have weight 0). event_sums [n_events] holds S_i in MATERIALIZE mode: it is
+ * computed when have_sums == 0 and only read when have_sums != 0 (S_i depends on the rows
+ * and the sysmat only, so callers keep it across iterations). The coarse grid must fit in
+ * shared memory (V_c floats <= 227 KB). Deterministic (fixed-order reductions).
  */
 JSCC_API size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse,
-                   int32_t n_groups);
+                   int32_t n_groups, int32_t adj_width);
 JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype,
                    int64_t ld_tc, const float* packed_rows, int64_t n_events, const int32_t* order,
                    const int32_t* group_offsets, const int32_t* group_rows, int32_t n_groups,
-                   float* event_sums, const void* sysmat, int32_t sysmat_dtype, int64_t ld_sysmat,
-                   int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
-                   const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc,
-                   const int32_t* adj_z_ptr, const int32_t* adj_z_idx, const float* adj_z_w,
-                   int32_t n_zc, const int32_t* adj_l_ptr, const int32_t* adj_l_idx,
-                   const float* adj_l_w, int32_t mode, const float* img, const int64_t* rotmat,
-                   const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight,
-                   void* workspace, size_t workspace_bytes, void* stream);
+                   float* event_sums, int32_t have_sums, const void* sysmat, int32_t sysmat_dtype,
+                   int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw,
+                   int32_t n_zf, const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc,
+                   int32_t n_zc, const int32_t* adj_idx, const float* adj_w, int32_t adj_width,
+                   int32_t mode, const float* img, const int64_t* rotmat, const int64_t* rotmat_inv,
+                   int64_t ld_rot, float scale, float* weight, void* workspace, size_t workspace_bytes,
+                   void* stream);
 
 /* ------------------------------------------------------------ EM update */
 

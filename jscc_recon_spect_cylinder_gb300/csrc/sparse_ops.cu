@@ -415,55 +415,94 @@ static int sparse_weight_impl(const SpRows<TC>& rows, int64_t n_events, const vo
 //   group_scatter: one thread per fine voxel (its taps in registers) x a chunk of groups,
 //                  partial sums per chunk, reduced in chunk order by sparse_reduce.
 // Events are visited through `order` (event indices sorted by row).
-struct MapCsr {
-  const int32_t* zp;
-  const int32_t* zi;
-  const float* zw;
-  const int32_t* lp;
-  const int32_t* li;
-  const float* lw;
-  int n_lo;   // coarse layers (outputs of the adjoint)
-  int n_li;   // fine layers (inputs)
-};
 
 constexpr int kGcThreads = 256;
 
-// MODE 0: materialise semantics (needs S), 1: grouped semantics, 2: compute S (x = 1, no q)
+// xw[k][c] = w[k][c] * x[j[k][c]] : the adjoint taps with the image folded in (once per call)
+__global__ void sparse_fold_x_kernel(const int32_t* __restrict__ tj, const float* __restrict__ tw, int64_t n,
+                                     const float* __restrict__ x, float* __restrict__ xw) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    xw[t] = tw[t] * __ldg(x + tj[t]);
+}
+
+// Dot of a coarse row (global, TC) with a shared-memory vector, by one warp; 16-byte loads
+// with four independent accumulators when the row is 16-byte aligned.
+template <typename TC>
+__device__ __forceinline__ float warp_row_dot(const TC* __restrict__ tc, const float* b, int64_t vc, bool vec,
+                                              int lane) {
+  constexpr int NV = 16 / (int)sizeof(TC);
+  float f0 = 0.f, f1 = 0.f, f2 = 0.f, f3 = 0.f;
+  int64_t tail = 0;
+  if (vec) {
+    const int64_t nv = vc / NV;
+    tail = nv * NV;
+#pragma unroll 2
+    for (int64_t v = lane; v < nv; v += 32) {
+      const uint4 raw = __ldg(reinterpret_cast<const uint4*>(tc) + v);
+      const float* bb = b + v * NV;
+      if (sizeof(TC) == 2) {
+        f0 = fmaf(bf16_lo(raw.x), bb[0], f0);
+        f1 = fmaf(bf16_hi(raw.x), bb[1], f1);
+        f2 = fmaf(bf16_lo(raw.y), bb[2], f2);
+        f3 = fmaf(bf16_hi(raw.y), bb[3], f3);
+        f0 = fmaf(bf16_lo(raw.z), bb[4], f0);
+        f1 = fmaf(bf16_hi(raw.z), bb[5], f1);
+        f2 = fmaf(bf16_lo(raw.w), bb[6], f2);
+        f3 = fmaf(bf16_hi(raw.w), bb[7], f3);
+      } else {
+        f0 = fmaf(__uint_as_float(raw.x), bb[0], f0);
+        f1 = fmaf(__uint_as_float(raw.y), bb[1], f1);
+        f2 = fmaf(__uint_as_float(raw.z), bb[2], f2);
+        f3 = fmaf(__uint_as_float(raw.w), bb[3], f3);
+      }
+    }
+  }
+  for (int64_t c = tail + lane; c < vc; c += 32) f0 = fmaf(ld_any(tc, c), b[c], f0);
+  return warp_sum((f0 + f1) + (f2 + f3));
+}
+
+// MODE 0: materialise semantics (reads S), 1: grouped semantics, 2: compute S (adjoint of A_g
+// alone, no q). Adjoint taps: fixed width K, tj/tw(or xw) [K][vc] (padding has weight 0).
 template <int MODE, typename TE, typename TC>
 __global__ void __launch_bounds__(kGcThreads)
-sparse_group_coef_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
-                         const int32_t* __restrict__ grow, int n_groups, int64_t vc, const float* __restrict__ x,
-                         const TE* __restrict__ eff, int64_t ld_eff, MapCsr adj, float* __restrict__ s_ev,
-                         float* __restrict__ coef, float* __restrict__ q, int64_t ldq) {
+sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restrict__ order,
+                         const int32_t* __restrict__ goff, const int32_t* __restrict__ grow, int n_groups, int64_t vc,
+                         const int32_t* __restrict__ tj, const float* __restrict__ tw, int K,
+                         const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ s_ev, float* __restrict__ coef,
+                         float* __restrict__ q, int64_t ldq) {
   extern __shared__ float4 sm4[];
   float* b = reinterpret_cast<float*>(sm4);  // [vc]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NVq = 4;  // coarse values per thread-slot in the q pass
   for (int gi = blockIdx.x; gi < n_groups; gi += gridDim.x) {
     const TE* er = eff + (int64_t)grow[gi] * ld_eff;
     const int e0 = goff[gi], e1 = goff[gi + 1];
     __syncthreads();
-    for (int64_t c = tid; c < vc; c += kGcThreads) {
-      const int zo = (int)(c / adj.n_lo), lo = (int)(c % adj.n_lo);
-      float sb = 0.f;
-      for (int a = adj.zp[zo]; a < adj.zp[zo + 1]; ++a) {
-        const int64_t base = (int64_t)adj.zi[a] * adj.n_li;
-        float tb = 0.f;
-        for (int k = adj.lp[lo]; k < adj.lp[lo + 1]; ++k) {
-          const int64_t j = base + adj.li[k];
-          const float av = ld_any(er, j);
-          tb = fmaf(adj.lw[k], MODE == 2 ? av : av * __ldg(x + j), tb);
+    // b[c] = sum_k tw[k][c] * A_g[tj[k][c]]  (x already folded into tw except for MODE 2)
+    for (int64_t c0 = tid; c0 < vc; c0 += 4 * kGcThreads) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int k = 0; k < K; ++k) {
+        const int32_t* tjk = tj + (int64_t)k * vc;
+        const float* twk = tw + (int64_t)k * vc;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t c = c0 + (int64_t)u * kGcThreads;
+          if (c < vc) {
+            const float wv = __ldg(twk + c);
+            if (wv != 0.f) acc[u] = fmaf(wv, ld_any(er, __ldg(tjk + c)), acc[u]);
+          }
         }
-        sb = fmaf(adj.zw[a], tb, sb);
       }
-      b[c] = sb;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t c = c0 + (int64_t)u * kGcThreads;
+        if (c < vc) b[c] = acc[u];
+      }
     }
     __syncthreads();
     for (int e = e0 + warp; e < e1; e += kGcThreads / 32) {
       const int64_t i = order[e];
-      const TC* tc = rows.coarse(i);
-      float f = 0.f;
-      for (int64_t c = lane; c < vc; c += 32) f = fmaf(ld_any(tc, c), b[c], f);
-      f = warp_sum(f);
+      const float f = warp_row_dot<TC>(rows.coarse(i), b, vc, vec_rows, lane);
       if (lane == 0) {
         if (MODE == 2) {
           s_ev[i] = f;
@@ -477,15 +516,22 @@ sparse_group_coef_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, con
     }
     if (MODE == 2) continue;
     __syncthreads();
+    // q_g = sum_i c_i t_i : each thread owns NVq consecutive coarse values
     float* qg = q + (int64_t)gi * ldq;
-    for (int64_t c = tid; c < vc; c += kGcThreads) {
-      float acc = 0.f;
+    for (int64_t c0 = (int64_t)tid * NVq; c0 < vc; c0 += (int64_t)kGcThreads * NVq) {
+      float acc[NVq] = {0.f, 0.f, 0.f, 0.f};
       for (int e = e0; e < e1; ++e) {
         const int64_t i = order[e];
         const float ci = coef[i];
-        if (ci != 0.f) acc = fmaf(ci, ld_any(rows.coarse(i), c), acc);
+        if (ci == 0.f) continue;
+        const TC* tc = rows.coarse(i);
+#pragma unroll
+        for (int u = 0; u < NVq; ++u)
+          if (c0 + u < vc) acc[u] = fmaf(ci, ld_any(tc, c0 + u), acc[u]);
       }
-      qg[c] = acc;
+#pragma unroll
+      for (int u = 0; u < NVq; ++u)
+        if (c0 + u < vc) qg[c0 + u] = acc[u];
     }
   }
 }
@@ -534,42 +580,56 @@ static int64_t group_chunks(int64_t n_groups, int64_t vf) {
 
 
 template <typename TE, typename TC>
-static int grouped_launch(const SpRows<TC>& rows, int64_t n_events, const int32_t* order, const int32_t* goff,
-                          const int32_t* grow, int32_t n_groups, const TE* eff, int64_t ld_eff, const UpTaps& taps,
-                          const MapCsr& adj, int64_t vf, int64_t vc, int32_t mode, const float* x, float* s_ev,
-                          const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight, void* workspace,
-                          size_t workspace_bytes, cudaStream_t st) {
+static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_events, const int32_t* order,
+                          const int32_t* goff, const int32_t* grow, int32_t n_groups, const TE* eff, int64_t ld_eff,
+                          const UpTaps& taps, const int32_t* tj, const float* tw, int K, int64_t vf, int64_t vc,
+                          int32_t mode, const float* x, float* s_ev, int have_sums, const int64_t* rotmat_inv,
+                          int64_t ld_rot, float scale, float* weight, void* workspace, size_t workspace_bytes,
+                          cudaStream_t st) {
   const int64_t ldp = (int64_t)align_up((size_t)vf, 8);
   const int64_t ldq = (int64_t)align_up((size_t)vc, 8);
   Carver cv(workspace, workspace_bytes);
   cv.take<float>((size_t)ldp);  // rotated image slot (used by the caller)
   float* coef = cv.take<float>((size_t)n_events);
+  float* xw = cv.take<float>((size_t)K * vc);
   float* q = cv.take<float>((size_t)n_groups * ldq);
   const int64_t chunks = group_chunks(n_groups, vf);
   float* part = cv.take<float>((size_t)chunks * ldp);
   JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
   const size_t smem = align_up((size_t)vc, 4) * sizeof(float);
   JSCC_REQUIRE(smem <= 227 * 1024, "jscc_sparse_weight_grouped: coarse grid (%zu bytes) exceeds shared memory", smem);
-  int64_t grid = (int64_t)num_sms() * ((227 * 1024) / (smem + 1024) < 8 ? (227 * 1024) / (smem + 1024) : 8);
-  if (grid < 1) grid = 1;
+  int64_t per_sm = (227 * 1024) / (int64_t)(smem + 1024);
+  if (per_sm > 8) per_sm = 8;
+  if (per_sm < 1) per_sm = 1;
+  int64_t grid = (int64_t)num_sms() * per_sm;
   if (grid > n_groups) grid = n_groups;
+  {
+    const int64_t n = (int64_t)K * vc;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > (int64_t)num_sms() * 8) blocks = (int64_t)num_sms() * 8;
+    JSCC_TIMED("sparse_fold_x", st, (sparse_fold_x_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, n, x, xw)));
+    JSCC_LAUNCH_CHECK();
+  }
   cudaError_t attr = cudaSuccess;
-#define JSCC_GC(MODE)                                                                                            \
+#define JSCC_GC(MODE, TW)                                                                                        \
   do {                                                                                                           \
     attr = cudaFuncSetAttribute(sparse_group_coef_kernel<MODE, TE, TC>,                                          \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                         \
     if (attr == cudaSuccess)                                                                                     \
       JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
                  (sparse_group_coef_kernel<MODE, TE, TC><<<(unsigned)grid, kGcThreads, smem, st>>>(              \
-                     rows, order, goff, grow, n_groups, vc, x, eff, ld_eff, adj, s_ev, coef, q, ldq)));          \
+                     rows, vec_rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, coef, q,     \
+                     ldq)));                                                                                     \
   } while (0)
   if (mode == JSCC_SPARSE_MATERIALIZE) {
-    JSCC_GC(2);  // S_i = t_i . adj(A_g)
-    JSCC_CUDA_CHECK(attr);
-    JSCC_LAUNCH_CHECK();
-    JSCC_GC(0);
+    if (!have_sums) {
+      JSCC_GC(2, tw);  // S_i = t_i . adj(A_g), kept by the caller across calls
+      JSCC_CUDA_CHECK(attr);
+      JSCC_LAUNCH_CHECK();
+    }
+    JSCC_GC(0, xw);
   } else {
-    JSCC_GC(1);
+    JSCC_GC(1, xw);
   }
 #undef JSCC_GC
   JSCC_CUDA_CHECK(attr);
@@ -753,11 +813,13 @@ int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coarse, int32_
 }
 
 
-size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse, int32_t n_groups) {
+size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse, int32_t n_groups,
+                                           int32_t adj_width) {
   const int64_t ldp = (int64_t)align_up((size_t)(n_fine > 0 ? n_fine : 1), 8);
   const int64_t ldq = (int64_t)align_up((size_t)(n_coarse > 0 ? n_coarse : 1), 8);
   const int64_t chunks = group_chunks(n_groups, n_fine);
   return align_up((size_t)ldp * sizeof(float), 256) + align_up((size_t)(n_events > 0 ? n_events : 1) * 4, 256) +
+         align_up((size_t)(adj_width > 0 ? adj_width : 1) * (n_coarse > 0 ? n_coarse : 1) * 4, 256) +
          align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) +
          align_up((size_t)chunks * ldp * sizeof(float), 256) + 256;
 }
@@ -765,11 +827,10 @@ size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int
 int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,
                                const float* packed_rows, int64_t n_events, const int32_t* order,
                                const int32_t* group_offsets, const int32_t* group_rows, int32_t n_groups,
-                               float* event_sums, const void* sysmat, int32_t sysmat_dtype, int64_t ld_sysmat,
-                               int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
-                               const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc,
-                               const int32_t* adj_z_ptr, const int32_t* adj_z_idx, const float* adj_z_w, int32_t n_zc,
-                               const int32_t* adj_l_ptr, const int32_t* adj_l_idx, const float* adj_l_w, int32_t mode,
+                               float* event_sums, int32_t have_sums, const void* sysmat, int32_t sysmat_dtype,
+                               int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
+                               const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc, int32_t n_zc,
+                               const int32_t* adj_idx, const float* adj_w, int32_t adj_width, int32_t mode,
                                const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
                                float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
   JSCC_REQUIRE(n_events >= 0 && n_det > 0 && n_groups >= 0, "jscc_sparse_weight_grouped: bad sizes");
@@ -782,8 +843,8 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
   JSCC_REQUIRE(packed_rows || (row_id && t_coarse), "jscc_sparse_weight_grouped: rows missing");
   JSCC_REQUIRE(packed_rows || tc_dtype == JSCC_DTYPE_F32 || tc_dtype == JSCC_DTYPE_BF16,
                "jscc_sparse_weight_grouped: row dtype");
-  JSCC_REQUIRE(adj_z_ptr && adj_z_idx && adj_z_w && adj_l_ptr && adj_l_idx && adj_l_w,
-               "jscc_sparse_weight_grouped: adjoint tables missing");
+  JSCC_REQUIRE(adj_idx && adj_w && adj_width > 0 && adj_width <= 64,
+               "jscc_sparse_weight_grouped: adjoint tap table missing or wider than 64");
   JSCC_REQUIRE((rotmat == nullptr) == (rotmat_inv == nullptr), "jscc_sparse_weight_grouped: give both tables");
   UpTaps t;
   int rc = make_taps(z_taps, z_tw, l_taps, l_tw, n_lf, n_lc, &t);
@@ -791,7 +852,7 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
   const int64_t vf = (int64_t)n_zf * n_lf;
   const int64_t vc = (int64_t)n_zc * n_lc;
   JSCC_REQUIRE(ld_sysmat >= vf, "jscc_sparse_weight_grouped: ld_sysmat < fine voxels");
-  const size_t need = jscc_sparse_grouped_workspace_bytes(n_events, vf, vc, n_groups);
+  const size_t need = jscc_sparse_grouped_workspace_bytes(n_events, vf, vc, n_groups, adj_width);
   JSCC_REQUIRE(workspace && workspace_bytes >= need, "jscc_sparse_weight_grouped: workspace too small (%zu < %zu)",
                workspace_bytes, need);
   cudaStream_t st = as_stream(stream);
@@ -807,11 +868,14 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
     JSCC_LAUNCH_CHECK();
     x = xr;
   }
-  MapCsr adj{adj_z_ptr, adj_z_idx, adj_z_w, adj_l_ptr, adj_l_idx, adj_l_w, n_lc, n_lf};
+  const size_t tcsz = packed_rows ? 4 : (tc_dtype == JSCC_DTYPE_BF16 ? 2 : 4);
+  const bool vec_rows = !packed_rows && (ld_tc * (int64_t)tcsz) % 16 == 0 &&
+                        reinterpret_cast<uintptr_t>(t_coarse) % 16 == 0;
 #define JSCC_GROUPED(TE, TC, ROWS)                                                                             \
-  grouped_launch<TE, TC>(ROWS, n_events, order, group_offsets, group_rows, n_groups,                           \
-                         static_cast<const TE*>(sysmat), ld_sysmat, t, adj, vf, vc, mode, x, event_sums,         \
-                         rotmat_inv, ld_rot, scale, weight, workspace, workspace_bytes, st)
+  grouped_launch<TE, TC>(ROWS, vec_rows, n_events, order, group_offsets, group_rows, n_groups,                 \
+                         static_cast<const TE*>(sysmat), ld_sysmat, t, adj_idx, adj_w, adj_width, vf, vc, mode,  \
+                         x, event_sums, have_sums, rotmat_inv, ld_rot, scale, weight, workspace,                 \
+                         workspace_bytes, st)
   if (packed_rows) {
     SpRows<float> r{packed_rows, nullptr, nullptr, ld_tc, n_det};
     return sysmat_dtype == JSCC_DTYPE_F32 ? JSCC_GROUPED(float, float, r) : JSCC_GROUPED(__nv_bfloat16, float, r);

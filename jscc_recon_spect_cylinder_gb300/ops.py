@@ -290,6 +290,38 @@ def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None,
 
 
 # ============================================================================ sparse rows
+def _padded_rows(m):
+    """Non-zeros of each row of m as padded [rows, width] (index, weight); padding weight 0."""
+    nz = m != 0
+    counts = nz.sum(dim=1)
+    width = max(int(counts.max()), 1)
+    rows, cols = torch.nonzero(nz, as_tuple=True)
+    first = torch.zeros(m.size(0), dtype=torch.int64)
+    first[1:] = torch.cumsum(counts, 0)[:-1]
+    slot = torch.arange(rows.numel()) - first[rows]
+    idx = torch.zeros((m.size(0), width), dtype=torch.int64)
+    w = torch.zeros((m.size(0), width), dtype=torch.float32)
+    idx[rows, slot] = cols
+    w[rows, slot] = m[rows, cols]
+    return idx, w
+
+
+def _fixed_width_adjoint(z_expand, layer_expand, device):
+    """Adjoint of the upsample as taps of fixed width K per coarse voxel c = zc * n_lc + lc:
+    fine index zf * n_lf + lf and weight z_expand[zf, zc] * layer_expand[lf, lc]; returned
+    [K, V_c] (tap-major, so a warp reading one tap of consecutive c is coalesced)."""
+    ze = z_expand.detach().to("cpu", torch.float32)
+    le = layer_expand.detach().to("cpu", torch.float32)
+    zi, zw = _padded_rows(ze.t())
+    li, lw = _padded_rows(le.t())
+    n_lf = le.size(0)
+    idx = zi[:, None, :, None] * n_lf + li[None, :, None, :]
+    w = zw[:, None, :, None] * lw[None, :, None, :]
+    idx = idx.reshape(ze.size(1) * le.size(1), -1)
+    w = w.reshape(ze.size(1) * le.size(1), -1)
+    return (idx.t().contiguous().to(torch.int32).to(device), w.t().contiguous().to(device), int(idx.size(1)))
+
+
 class SparseTables:
     """Device tables of a ComptonSparseProjector: CSR forms of the four separable maps and
     the two-tap upsample arrays of the fused kernels, built from the projector's own
@@ -336,6 +368,7 @@ class SparseTables:
         self.red_t = (csr(z_reduce.t()), csr(layer_reduce.t()))      # coarse -> fine (weight image)
         self.z_taps, self.z_tw = two_taps(z_expand)
         self.l_taps, self.l_tw = two_taps(layer_expand)
+        self.adj_idx, self.adj_w, self.adj_width = _fixed_width_adjoint(z_expand, layer_expand, device)
 
 
 def sparse_map(rows_in, maps, n_zo, n_zi, n_lo, n_li, row_idx=None):
@@ -505,6 +538,7 @@ class GroupPlan:
         self.offsets = offsets.to(torch.int32).contiguous()
         self.rows = rows.to(torch.int32).contiguous()
         self.n_groups = int(rows.numel())
+        self.sums = {}  # per sysmat key: S_i of the materialise form
 
 
 def _group_plan(key_tensor, row_ids_fn):
@@ -567,17 +601,26 @@ def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=N
         rm = rotmat.data_ptr() + rot_col * 8
         ri = rotmat_inv.data_ptr() + rot_col * 8
         ld_rot = rotmat.stride(0)
-    (azp, azi, azw), (alp, ali, alw) = tables.adj
     lib = _lib.load()
-    ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, vc, plan.n_groups))
-    sums = torch.empty(n, dtype=torch.float32, device=dev)
+    ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, vc, plan.n_groups,
+                                                                         tables.adj_width))
+    # S_i = t_i . adj(A_g) depends on the rows and the sysmat only: kept on the plan per sysmat
+    skey = (A.data_ptr(), A._version, A.dtype, tuple(A.shape))
+    sums = plan.sums.get(skey)
+    have = sums is not None
+    if not have:
+        sums = torch.empty(n, dtype=torch.float32, device=dev)
     rc = lib.jscc_sparse_weight_grouped(
         ids_p, tc_p, tc_dt, ld, packed, n, plan.order.data_ptr(), plan.offsets.data_ptr(), plan.rows.data_ptr(),
-        plan.n_groups, sums.data_ptr(), A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
+        plan.n_groups, sums.data_ptr(), 1 if have else 0, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
         tables.z_taps.data_ptr(), tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(),
-        tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, azp.data_ptr(), azi.data_ptr(), azw.data_ptr(),
-        tables.n_zc, alp.data_ptr(), ali.data_ptr(), alw.data_ptr(),
-        _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE, x.data_ptr(), rm, ri, ld_rot, float(scale),
-        out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+        tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, tables.n_zc, tables.adj_idx.data_ptr(),
+        tables.adj_w.data_ptr(), tables.adj_width, _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE,
+        x.data_ptr(), rm, ri, ld_rot, float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(),
+        _lib.stream_handle(dev))
     _lib.check(rc, "jscc_sparse_weight_grouped")
+    if not have and not grouped:
+        if len(plan.sums) > 4:
+            plan.sums.clear()
+        plan.sums[skey] = sums
     return out

@@ -170,3 +170,19 @@ def test_product_path_refuses_cpu_tensors():
 
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         ops.sc_weight(torch.ones((2, 3)), torch.ones((2, 1)), torch.ones((3, 1)))
+
+
+def test_fixed_width_adjoint_equals_dense_adjoint(golden):
+    """The [K, V_c] adjoint tap table (grouped sparse kernel) reproduces the transpose of
+    the reference's upsample matrices, multi-plane grid with stride reduction included."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    g = golden("sparse_ops")
+    p = cso.build_compton_sparse_projector(torch.from_numpy(g["s_coor"]), theta_stride=4, z_stride=2, rotate_num=4)
+    tb = ops.SparseTables(p.layer_reduce, p.z_reduce, p.layer_expand, p.z_expand, torch.device("cpu"))
+    x = torch.rand(p.fine_pixel_num, dtype=torch.float64)
+    U = torch.kron(p.z_expand.double(), p.layer_expand.double())  # [V_f, V_c]
+    dense = U.t() @ x
+    fw = (tb.adj_w.double() * x[tb.adj_idx.long()]).sum(0)
+    assert torch.allclose(fw, dense, rtol=1e-6, atol=1e-9)
