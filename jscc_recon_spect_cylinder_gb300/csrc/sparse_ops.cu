@@ -436,7 +436,7 @@ __device__ __forceinline__ float warp_row_dot(const TC* __restrict__ tc, const f
   if (vec) {
     const int64_t nv = vc / NV;
     tail = nv * NV;
-#pragma unroll 2
+#pragma unroll 4
     for (int64_t v = lane; v < nv; v += 32) {
       const uint4 raw = __ldg(reinterpret_cast<const uint4*>(tc) + v);
       const float* bb = b + v * NV;
@@ -463,7 +463,81 @@ __device__ __forceinline__ float warp_row_dot(const TC* __restrict__ tc, const f
 
 // MODE 0: materialise semantics (reads S), 1: grouped semantics, 2: compute S (adjoint of A_g
 // alone, no q). Adjoint taps: fixed width K, tj/tw(or xw) [K][vc] (padding has weight 0).
-template <int MODE, typename TE, typename TC>
+// Adjoint of one group: b[c] = sum_k tw[k][c] * A_g[tj[k][c]], four coarse voxels per thread
+// at a time; with a compile-time width KT all index loads, then all gathers, are issued
+// before the first FMA (KT = 0: runtime width K).
+template <int KT, typename TE>
+__device__ __forceinline__ void group_adjoint(float* b, int64_t vc, const int32_t* __restrict__ tj,
+                                              const float* __restrict__ tw, int K, const TE* __restrict__ er,
+                                              int tid) {
+  for (int64_t c0 = tid; c0 < vc; c0 += 4 * kGcThreads) {
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (KT > 0) {
+      int idx[4][KT > 0 ? KT : 1];
+      float wv[4][KT > 0 ? KT : 1];
+#pragma unroll
+      for (int k = 0; k < KT; ++k)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t c = c0 + (int64_t)u * kGcThreads;
+          const bool in = c < vc;
+          idx[u][k] = in ? __ldg(tj + (int64_t)k * vc + c) : 0;
+          wv[u][k] = in ? __ldg(tw + (int64_t)k * vc + c) : 0.f;
+        }
+      float av[4][KT > 0 ? KT : 1];
+#pragma unroll
+      for (int k = 0; k < KT; ++k)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) av[u][k] = ld_any(er, idx[u][k]);
+#pragma unroll
+      for (int k = 0; k < KT; ++k)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc[u] = fmaf(wv[u][k], av[u][k], acc[u]);
+    } else {
+      for (int k = 0; k < K; ++k) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t c = c0 + (int64_t)u * kGcThreads;
+          if (c < vc) {
+            const float wvv = __ldg(tw + (int64_t)k * vc + c);
+            if (wvv != 0.f) acc[u] = fmaf(wvv, ld_any(er, __ldg(tj + (int64_t)k * vc + c)), acc[u]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t c = c0 + (int64_t)u * kGcThreads;
+      if (c < vc) b[c] = acc[u];
+    }
+  }
+}
+
+// four consecutive coarse values of a row (8-byte loads for bf16, 16-byte for float when aligned)
+template <typename TC>
+__device__ __forceinline__ void load4(const TC* p, int64_t c, bool vec, float (&v)[4]);
+template <>
+__device__ __forceinline__ void load4<__nv_bfloat16>(const __nv_bfloat16* p, int64_t c, bool vec, float (&v)[4]) {
+  if (vec) {
+    const uint2 u = __ldg(reinterpret_cast<const uint2*>(p + c));
+    v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x); v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __bfloat162float(p[c + k]);
+  }
+}
+template <>
+__device__ __forceinline__ void load4<float>(const float* p, int64_t c, bool vec, float (&v)[4]) {
+  if (vec) {
+    const float4 u = __ldg(reinterpret_cast<const float4*>(p + c));
+    v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __ldg(p + c + k);
+  }
+}
+
+template <int MODE, int KT, typename TE, typename TC>
 __global__ void __launch_bounds__(kGcThreads)
 sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restrict__ order,
                          const int32_t* __restrict__ goff, const int32_t* __restrict__ grow, int n_groups, int64_t vc,
@@ -479,26 +553,7 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
     const int e0 = goff[gi], e1 = goff[gi + 1];
     __syncthreads();
     // b[c] = sum_k tw[k][c] * A_g[tj[k][c]]  (x already folded into tw except for MODE 2)
-    for (int64_t c0 = tid; c0 < vc; c0 += 4 * kGcThreads) {
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      for (int k = 0; k < K; ++k) {
-        const int32_t* tjk = tj + (int64_t)k * vc;
-        const float* twk = tw + (int64_t)k * vc;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int64_t c = c0 + (int64_t)u * kGcThreads;
-          if (c < vc) {
-            const float wv = __ldg(twk + c);
-            if (wv != 0.f) acc[u] = fmaf(wv, ld_any(er, __ldg(tjk + c)), acc[u]);
-          }
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int64_t c = c0 + (int64_t)u * kGcThreads;
-        if (c < vc) b[c] = acc[u];
-      }
-    }
+    group_adjoint<KT, TE>(b, vc, tj, tw, K, er, tid);
     __syncthreads();
     for (int e = e0 + warp; e < e1; e += kGcThreads / 32) {
       const int64_t i = order[e];
@@ -516,18 +571,26 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
     }
     if (MODE == 2) continue;
     __syncthreads();
-    // q_g = sum_i c_i t_i : each thread owns NVq consecutive coarse values
+    // q_g = sum_i c_i t_i : each thread owns 4 consecutive coarse values; events in order
     float* qg = q + (int64_t)gi * ldq;
+    const bool vq = vec_rows && (vc % 4 == 0);
     for (int64_t c0 = (int64_t)tid * NVq; c0 < vc; c0 += (int64_t)kGcThreads * NVq) {
       float acc[NVq] = {0.f, 0.f, 0.f, 0.f};
+      const bool full = c0 + NVq <= vc;
       for (int e = e0; e < e1; ++e) {
         const int64_t i = order[e];
         const float ci = coef[i];
         if (ci == 0.f) continue;
         const TC* tc = rows.coarse(i);
+        if (full) {
+          float v[4];
+          load4<TC>(tc, c0, vq, v);
 #pragma unroll
-        for (int u = 0; u < NVq; ++u)
-          if (c0 + u < vc) acc[u] = fmaf(ci, ld_any(tc, c0 + u), acc[u]);
+          for (int u = 0; u < NVq; ++u) acc[u] = fmaf(ci, v[u], acc[u]);
+        } else {
+          for (int u = 0; u < NVq; ++u)
+            if (c0 + u < vc) acc[u] = fmaf(ci, ld_any(tc, c0 + u), acc[u]);
+        }
       }
 #pragma unroll
       for (int u = 0; u < NVq; ++u)
@@ -611,15 +674,21 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     JSCC_LAUNCH_CHECK();
   }
   cudaError_t attr = cudaSuccess;
-#define JSCC_GC(MODE, TW)                                                                                        \
+#define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
-    attr = cudaFuncSetAttribute(sparse_group_coef_kernel<MODE, TE, TC>,                                          \
+    attr = cudaFuncSetAttribute(sparse_group_coef_kernel<MODE, KT, TE, TC>,                                      \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                         \
     if (attr == cudaSuccess)                                                                                     \
       JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
-                 (sparse_group_coef_kernel<MODE, TE, TC><<<(unsigned)grid, kGcThreads, smem, st>>>(              \
+                 (sparse_group_coef_kernel<MODE, KT, TE, TC><<<(unsigned)grid, kGcThreads, smem, st>>>(          \
                      rows, vec_rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, coef, q,     \
                      ldq)));                                                                                     \
+  } while (0)
+#define JSCC_GC(MODE, TW)                                                                                        \
+  do {                                                                                                           \
+    if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                          \
+    else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
+    else JSCC_GC_K(MODE, 0, TW);                                                                                 \
   } while (0)
   if (mode == JSCC_SPARSE_MATERIALIZE) {
     if (!have_sums) {
@@ -632,6 +701,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     JSCC_GC(1, xw);
   }
 #undef JSCC_GC
+#undef JSCC_GC_K
   JSCC_CUDA_CHECK(attr);
   JSCC_LAUNCH_CHECK();
   const int gpc = (int)((n_groups + chunks - 1) / chunks);
