@@ -480,7 +480,7 @@ __device__ __forceinline__ void group_adjoint(float* b, int64_t vc, const int32_
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int64_t c = c0 + (int64_t)u * kGcThreads;
-          const bool in = c < vc;
+          const bool in = c < vc && k < K;  // the table has K rows; KT may exceed K
           idx[u][k] = in ? __ldg(tj + (int64_t)k * vc + c) : 0;
           wv[u][k] = in ? __ldg(tw + (int64_t)k * vc + c) : 0.f;
         }

@@ -380,3 +380,32 @@ def test_grouped_kernel_matches_event_kernel(cuda, golden, grouped, dtype):
     assert rel_l2(b.cpu(), a.cpu()) < TOL_W
     # deterministic
     assert torch.equal(ops.sparse_weight(rows, A, tb, x, grouped=grouped), w_gr)
+
+
+@pytest.mark.parametrize("theta_stride", [2, 4, 8])
+def test_grouped_kernel_tap_widths(cuda, theta_stride):
+    """One-plane grids whose adjoint tap width K = 2 * stride - 1 (3, 7, 15) takes each of
+    the kernel's compile-time widths (4, 8) and the runtime-width path."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import ops, synthetic
+
+    grid = synthetic.polar_grid(12, 72, 30.0)
+    p = cso.build_compton_sparse_projector(grid.coor, theta_stride, 1, rotate_num=1)
+    tb = cso.tables(p, cuda)
+    assert tb.adj_width == 2 * theta_stride - 1
+    g = torch.Generator().manual_seed(theta_stride)
+    n_det = 50
+    A = (torch.rand((n_det, grid.n_vox), generator=g) + 0.05).to(cuda)
+    n = 4000
+    tc = torch.rand((n, p.coarse_pixel_num), generator=g) ** 3
+    cp1 = torch.randint(1, n_det + 1, (n,), generator=g)
+    rows = torch.cat((cp1.float().unsqueeze(1), tc), dim=1).to(cuda)
+    x = (torch.rand((grid.n_vox, 1), generator=g) + 0.2).to(cuda)
+    for grouped in (False, True):
+        w_ev = ops.sparse_weight(rows, A, tb, x, grouped=grouped, method="event")
+        w_gr = ops.sparse_weight(rows, A, tb, x, grouped=grouped)
+        assert rel_l2(w_gr.cpu(), w_ev.cpu()) < TOL_W
+        ids, tcb = ops.split_sparse_rows(rows, torch.bfloat16)
+        a = ops.sparse_weight_split(ids, tcb, A.to(torch.bfloat16), tb, x, grouped=grouped, method="event")
+        b = ops.sparse_weight_split(ids, tcb, A.to(torch.bfloat16), tb, x, grouped=grouped)
+        assert rel_l2(b.cpu(), a.cpu()) < TOL_W
