@@ -314,7 +314,18 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * computed when have_sums == 0 and only read when have_sums != 0 (S_i depends on the rows
  * and the sysmat only, so callers keep it across iterations). The coarse grid must fit in
  * shared memory (V_c floats <= 227 KB). Deterministic (fixed-order reductions).
+ * With split rows whose starts and lengths are 16-byte aligned (and a 16-byte aligned
+ * sysmat row pitch) the per-group step streams the sysmat row and the coarse rows into
+ * shared memory with bulk copies; its waits are bounded and a wait that gives up is
+ * counted (jscc_take_wait_timeout_count), the weight of that call then being invalid.
  */
+/*
+ * Number of bounded device waits that gave up since the last call (then reset to 0).
+ * Nonzero means a bulk copy never completed and the weights computed meanwhile are
+ * invalid. No counterpart in the reference (diagnostic of this library's pipeline).
+ */
+JSCC_API int jscc_take_wait_timeout_count(unsigned int* out);
+
 JSCC_API size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse,
                    int32_t n_groups, int32_t adj_width);
 JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype,

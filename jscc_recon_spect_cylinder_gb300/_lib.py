@@ -78,6 +78,7 @@ _SIGNATURES: dict[str, tuple] = {
          c_void_p, c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
     "jscc_take_bad_detector_count": (c_int, [POINTER(c_uint)]),
+    "jscc_take_wait_timeout_count": (c_int, [POINTER(c_uint)]),
     "jscc_sparse_map": (
         c_int,
         [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int32,
@@ -168,6 +169,13 @@ def reset_launch_count() -> None:
 def take_bad_detector_count() -> int:
     out = c_uint(0)
     check(load().jscc_take_bad_detector_count(ctypes.byref(out)), "jscc_take_bad_detector_count")
+    return int(out.value)
+
+
+def take_wait_timeout_count() -> int:
+    """Bounded device waits (bulk-copy pipeline) that gave up since the last call."""
+    out = ctypes.c_uint(0)
+    check(load().jscc_take_wait_timeout_count(ctypes.byref(out)), "jscc_take_wait_timeout_count")
     return int(out.value)
 
 

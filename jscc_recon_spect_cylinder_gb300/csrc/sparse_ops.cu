@@ -20,6 +20,9 @@ template <typename TI>
 __device__ __forceinline__ float ld_any(const TI* p, int64_t i);
 template <>
 __device__ __forceinline__ float ld_any<float>(const float* p, int64_t i) { return __ldg(p + i); }
+// plain conversions (usable on shared-memory values)
+__device__ __forceinline__ float to_float(float v) { return v; }
+__device__ __forceinline__ float to_float(__nv_bfloat16 v) { return __bfloat162float(v); }
 template <>
 __device__ __forceinline__ float ld_any<__nv_bfloat16>(const __nv_bfloat16* p, int64_t i) {
   return __bfloat162float(p[i]);
@@ -141,6 +144,11 @@ __device__ __forceinline__ const __nv_bfloat16* SpRows<__nv_bfloat16>::coarse(in
 }
 
 __device__ __forceinline__ float finite_or_zero(float v) { return isfinite(v) ? v : 0.f; }
+
+// a sysmat row index clamped into [0, n_det)
+__device__ __forceinline__ int64_t clamp_row(int64_t g, int64_t n_det) {
+  return g < 0 ? 0 : (g >= n_det ? n_det - 1 : g);
+}
 
 // ------------------------------------------------------------------ materialise
 // fine[i][j] = nan_to_num(up(tc_i)[j] * sysmat[clamp(cp1_i - 1)][j]); rsum[i] = sum_j fine[i][j]
@@ -549,7 +557,7 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NVq = 4;  // coarse values per thread-slot in the q pass
   for (int gi = blockIdx.x; gi < n_groups; gi += gridDim.x) {
-    const TE* er = eff + (int64_t)grow[gi] * ld_eff;
+    const TE* er = eff + clamp_row(grow[gi], rows.n_det) * ld_eff;
     const int e0 = goff[gi], e1 = goff[gi + 1];
     __syncthreads();
     // b[c] = sum_k tw[k][c] * A_g[tj[k][c]]  (x already folded into tw except for MODE 2)
@@ -599,12 +607,242 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
   }
 }
 
+// ------------------------------------------------------------------ grouped coefficients, bulk-copy pipeline
+// The same per-group computation with every operand staged in shared memory by bulk copies
+// (cp.async.bulk completing on mbarriers), so each byte is read from HBM once and the adjoint
+// gather, the event dots and the q accumulation all read shared memory. One persistent CTA
+// per SM walks its groups gi = blockIdx.x, + gridDim.x, ...; shared memory holds
+//   erow  [vf] TE       the group's sysmat row; the next group's row is fetched as soon as
+//                       the adjoint of the current one is done
+//   b     [vc] float    adj(A_g * x) (MODE 2: adj(A_g))
+//   slots [2][batch][vc] TC   coarse rows of two batches of (up to `batch`) events of one
+//                       group: while one batch is used the next one, possibly of a later
+//                       group, is in flight
+// Dots: each thread owns four coarse values per 2048 and accumulates all the batch's events,
+// partial sums are reduced per warp and then over warps in warp order (deterministic). q is
+// accumulated over the group's events in event order, batch after batch, in the q row.
+// Every wait is bounded: on a timeout the CTA counts it (jscc_take_wait_timeout_count),
+// waits (bounded) for its copies still in flight and returns.
+constexpr int kBkThreads = 512;
+constexpr int kBkWarps = kBkThreads / 32;
+constexpr int kBkMaxBatch = 8;
+constexpr int kBkHeader = 1024;               // barriers, dot partials, coefficients, abort flag
+constexpr uint32_t kBkMaxPolls = 1u << 22;    // per wait
+
+__device__ unsigned int g_wait_timeout_count = 0;
+
+// Adjoint of one group from the shared-memory sysmat row (plain loads; see group_adjoint).
+template <int KT, typename TE>
+__device__ __forceinline__ void group_adjoint_smem(float* b, int64_t vc, const int32_t* __restrict__ tj,
+                                                   const float* __restrict__ tw, int K, const TE* er, int tid) {
+  for (int64_t c0 = tid; c0 < vc; c0 += 2 * kBkThreads) {
+    float acc[2] = {0.f, 0.f};
+    if (KT > 0) {
+      int idx[2][KT > 0 ? KT : 1];
+      float wv[2][KT > 0 ? KT : 1];
+#pragma unroll
+      for (int k = 0; k < KT; ++k)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int64_t c = c0 + (int64_t)u * kBkThreads;
+          const bool in = c < vc && k < K;  // the table has K rows; KT may exceed K
+          idx[u][k] = in ? __ldg(tj + (int64_t)k * vc + c) : 0;
+          wv[u][k] = in ? __ldg(tw + (int64_t)k * vc + c) : 0.f;
+        }
+#pragma unroll
+      for (int k = 0; k < KT; ++k)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) acc[u] = fmaf(wv[u][k], to_float(er[idx[u][k]]), acc[u]);
+    } else {
+      for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int64_t c = c0 + (int64_t)u * kBkThreads;
+          if (c < vc) {
+            const float wvv = __ldg(tw + (int64_t)k * vc + c);
+            if (wvv != 0.f) acc[u] = fmaf(wvv, to_float(er[__ldg(tj + (int64_t)k * vc + c)]), acc[u]);
+          }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t c = c0 + (int64_t)u * kBkThreads;
+      if (c < vc) b[c] = acc[u];
+    }
+  }
+}
+
+// four consecutive coarse values from shared memory (c a multiple of 4)
+__device__ __forceinline__ void smem4(const __nv_bfloat16* p, int64_t c, float (&v)[4]) {
+  const uint2 u = *reinterpret_cast<const uint2*>(p + c);
+  v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x); v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
+}
+__device__ __forceinline__ void smem4(const float* p, int64_t c, float (&v)[4]) {
+  const float4 u = *reinterpret_cast<const float4*>(p + c);
+  v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
+}
+
+template <int MODE, int KT, typename TE, typename TC>
+__global__ void __launch_bounds__(kBkThreads, 1)
+sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
+                              const int32_t* __restrict__ grow, int n_groups, int64_t vc,
+                              const int32_t* __restrict__ tj, const float* __restrict__ tw, int K,
+                              const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ s_ev,
+                              float* __restrict__ q, int64_t ldq, int batch, uint32_t erow_bytes, uint32_t row_bytes,
+                              uint32_t b_off, uint32_t slot_off, uint32_t slot_stride) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // [2][kBkMaxBatch] row slots, then the sysmat row
+  uint64_t* ebar = bar + 2 * kBkMaxBatch;
+  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkWarps][kBkMaxBatch]
+  float* cs = red + kBkWarps * kBkMaxBatch;           // [kBkMaxBatch]
+  int* abort_flag = reinterpret_cast<int*>(cs + kBkMaxBatch);
+  TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
+  float* b = reinterpret_cast<float*>(smem + b_off);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int G = gridDim.x;
+  auto slot = [&](int h, int k) { return reinterpret_cast<TC*>(smem + slot_off + (size_t)(h * batch + k) * slot_stride); };
+  if (tid == 0) {
+    for (int s = 0; s < 2 * kBkMaxBatch + 1; ++s) mbar_init(bar + s, 1);
+    *abort_flag = 0;
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // ---- producer state (thread 0): the last batch issued and the barriers with a copy in flight
+  uint32_t pending = 0;
+  int ig = blockIdx.x, ib = ig < n_groups ? goff[ig] : 0;
+  auto seek = [&]() -> bool {  // (ig, ib) -> the first batch at or after it, skipping empty groups
+    while (ig < n_groups) {
+      if (ib < goff[ig + 1]) return true;
+      ig += G;
+      if (ig < n_groups) ib = goff[ig];
+    }
+    return false;
+  };
+  auto issue_row = [&](int gi) {
+    mbar_arrive_expect_tx(ebar, erow_bytes);
+    bulk_copy_g2s(erow, eff + clamp_row(grow[gi], rows.n_det) * ld_eff, erow_bytes, ebar);
+    pending |= 1u << (2 * kBkMaxBatch);
+  };
+  auto issue_batch = [&](int h) {
+    const int n = min(batch, goff[ig + 1] - ib);
+    for (int k = 0; k < n; ++k) {
+      uint64_t* bk = bar + h * kBkMaxBatch + k;
+      mbar_arrive_expect_tx(bk, row_bytes);
+      bulk_copy_g2s(slot(h, k), rows.coarse(order[ib + k]), row_bytes, bk);
+      pending |= 1u << (h * kBkMaxBatch + k);
+    }
+  };
+  if (tid == 0 && blockIdx.x < n_groups) {
+    issue_row(blockIdx.x);
+    if (seek()) issue_batch(0);
+  }
+  uint32_t ph = 0;  // parity of every barrier's next phase (bit s: barrier s)
+  auto wait = [&](int s) {
+    if (!mbar_wait_bounded(bar + s, (ph >> s) & 1u, kBkMaxPolls)) *abort_flag = 1;
+    ph ^= 1u << s;
+    pending &= ~(1u << s);
+  };
+  int nb = 0;  // batches consumed (selects the half)
+  bool aborted = false;
+  for (int gi = blockIdx.x; gi < n_groups && !aborted; gi += G) {
+    wait(2 * kBkMaxBatch);
+    group_adjoint_smem<KT, TE>(b, vc, tj, tw, K, erow, tid);
+    __syncthreads();
+    if (*abort_flag) { aborted = true; break; }
+    if (tid == 0 && gi + G < n_groups) {
+      fence_proxy_async_smem();
+      issue_row(gi + G);
+    }
+    const int e0 = goff[gi], e1 = goff[gi + 1];
+    float* qg = q + (int64_t)gi * ldq;
+    if (MODE != 2 && e0 == e1)
+      for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4)
+        *reinterpret_cast<float4*>(qg + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int bs = e0; bs < e1; bs += batch, ++nb) {
+      const int n = min(batch, e1 - bs), h = nb & 1;
+      if (tid == 0) {  // the next batch into the other half (its last batch ended at the last barrier)
+        ib += batch;
+        if (seek()) {
+          fence_proxy_async_smem();
+          issue_batch(h ^ 1);
+        }
+      }
+      for (int k = 0; k < n; ++k) wait(h * kBkMaxBatch + k);
+      // ---- dots f_i = t_i . b
+      float acc[kBkMaxBatch];
+#pragma unroll
+      for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = 0.f;
+      for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4) {
+        const float4 bv = *reinterpret_cast<const float4*>(b + c);
+#pragma unroll
+        for (int k = 0; k < kBkMaxBatch; ++k)
+          if (k < n) {
+            float v[4];
+            smem4(slot(h, k), c, v);
+            acc[k] = fmaf(v[0], bv.x, acc[k]);
+            acc[k] = fmaf(v[1], bv.y, acc[k]);
+            acc[k] = fmaf(v[2], bv.z, acc[k]);
+            acc[k] = fmaf(v[3], bv.w, acc[k]);
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < kBkMaxBatch; ++k)
+        if (k < n) {
+          const float f = warp_sum(acc[k]);
+          if (lane == 0) red[warp * kBkMaxBatch + k] = f;
+        }
+      __syncthreads();
+      if (*abort_flag) { aborted = true; break; }
+      if (tid < n) {
+        float f = 0.f;
+        for (int w = 0; w < kBkWarps; ++w) f += red[w * kBkMaxBatch + tid];
+        const int64_t i = order[bs + tid];
+        if (MODE == 2) {
+          s_ev[i] = f;
+        } else if (MODE == 0) {
+          const float si = s_ev[i];
+          cs[tid] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
+        } else {
+          cs[tid] = 1.0f / fmaxf(f, 1e-12f);
+        }
+      }
+      if (MODE != 2) {
+        __syncthreads();
+        // ---- q_g += sum over the batch of c_i t_i, events in order
+        for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4) {
+          float4 a = bs == e0 ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(qg + c);
+#pragma unroll
+          for (int k = 0; k < kBkMaxBatch; ++k)
+            if (k < n) {
+              const float ck = cs[k];
+              if (ck != 0.f) {
+                float v[4];
+                smem4(slot(h, k), c, v);
+                a.x = fmaf(ck, v[0], a.x);
+                a.y = fmaf(ck, v[1], a.y);
+                a.z = fmaf(ck, v[2], a.z);
+                a.w = fmaf(ck, v[3], a.w);
+              }
+            }
+          *reinterpret_cast<float4*>(qg + c) = a;
+        }
+      }
+      __syncthreads();  // the batch's slots and coefficients are free
+    }
+  }
+  if (aborted && tid == 0) {
+    atomicAdd(&g_wait_timeout_count, 1u);
+    for (int s = 0; s <= 2 * kBkMaxBatch; ++s)  // copies still in flight write this CTA's memory
+      if (pending & (1u << s)) mbar_wait_bounded(bar + s, (ph >> s) & 1u, kBkMaxPolls);
+  }
+}
+
 // part[chunk][j] = sum_{groups in chunk} A[g, j] * up(q_g)[j]
 template <typename TE>
 __global__ void __launch_bounds__(256)
 sparse_group_scatter_kernel(const float* __restrict__ q, int64_t ldq, const int32_t* __restrict__ grow, int n_groups,
-                            int groups_per_chunk, int64_t vf, const TE* __restrict__ eff, int64_t ld_eff, UpTaps taps,
-                            float* __restrict__ part, int64_t ldp) {
+                            int groups_per_chunk, int64_t vf, const TE* __restrict__ eff, int64_t ld_eff,
+                            int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= vf) return;
   const int zf = (int)(j / taps.n_lf), lf = (int)(j % taps.n_lf);
@@ -628,7 +866,7 @@ sparse_group_scatter_kernel(const float* __restrict__ q, int64_t ldq, const int3
       bb = fmaf(w1, __ldg(qg + c11), bb);
       v = fmaf(u1, bb, v);
     }
-    if (v != 0.f) acc = fmaf(ld_any(eff + (int64_t)grow[gi] * ld_eff, j), v, acc);
+    if (v != 0.f) acc = fmaf(ld_any(eff + clamp_row(grow[gi], n_det) * ld_eff, j), v, acc);
   }
   part[(int64_t)blockIdx.y * ldp + j] = acc;
 }
@@ -674,6 +912,36 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     JSCC_LAUNCH_CHECK();
   }
   cudaError_t attr = cudaSuccess;
+  // bulk-copy pipeline when every row start and length is 16-byte aligned (split storage)
+  // and a sysmat row, b and two batches of coarse rows fit in shared memory
+  const uint32_t erow_bytes = (uint32_t)((size_t)vf * sizeof(TE)), row_bytes = (uint32_t)((size_t)vc * sizeof(TC));
+  const uint32_t b_off = (uint32_t)align_up(kBkHeader + align_up(erow_bytes, 128), 128);
+  const uint32_t slot_off = (uint32_t)(b_off + align_up((size_t)vc * 4, 128));
+  const uint32_t slot_stride = (uint32_t)align_up(row_bytes, 128);
+  const size_t bk_limit = 227 * 1024;
+  int batch = 0;
+  if (slot_off < bk_limit && slot_stride > 0) {
+    batch = (int)((bk_limit - slot_off) / (2 * (size_t)slot_stride));
+    if (batch > kBkMaxBatch) batch = kBkMaxBatch;
+  }
+  const bool bulk = rows.packed == nullptr && batch >= 1 && (size_t)vf * sizeof(TE) < (1u << 20) &&
+                    reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 && (rows.ld * sizeof(TC)) % 16 == 0 &&
+                    row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(eff) % 16 == 0 &&
+                    (ld_eff * sizeof(TE)) % 16 == 0 && erow_bytes % 16 == 0;
+  const size_t bk_smem = (size_t)slot_off + 2 * (size_t)batch * slot_stride;
+  int64_t bk_grid = num_sms();
+  if (bk_grid > n_groups) bk_grid = n_groups;
+#define JSCC_GC_BK(MODE, KT, TW)                                                                                 \
+  do {                                                                                                           \
+    attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, KT, TE, TC>,                                 \
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                      \
+    if (attr == cudaSuccess)                                                                                     \
+      JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
+                 (sparse_group_coef_bulk_kernel<MODE, KT, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,      \
+                                                                     st>>>(                                      \
+                     rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, q, ldq, batch,         \
+                     erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                                     \
+  } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
     attr = cudaFuncSetAttribute(sparse_group_coef_kernel<MODE, KT, TE, TC>,                                      \
@@ -686,7 +954,11 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   } while (0)
 #define JSCC_GC(MODE, TW)                                                                                        \
   do {                                                                                                           \
-    if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                          \
+    if (bulk) {                                                                                                  \
+      if (K <= 4) JSCC_GC_BK(MODE, 4, TW);                                                                       \
+      else if (K <= 8) JSCC_GC_BK(MODE, 8, TW);                                                                  \
+      else JSCC_GC_BK(MODE, 0, TW);                                                                              \
+    } else if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                   \
     else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
     else JSCC_GC_K(MODE, 0, TW);                                                                                 \
   } while (0)
@@ -702,13 +974,14 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   }
 #undef JSCC_GC
 #undef JSCC_GC_K
+#undef JSCC_GC_BK
   JSCC_CUDA_CHECK(attr);
   JSCC_LAUNCH_CHECK();
   const int gpc = (int)((n_groups + chunks - 1) / chunks);
   dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
   JSCC_TIMED("sparse_group_scatter", st,
-             (sparse_group_scatter_kernel<TE><<<sgrid, 256, 0, st>>>(q, ldq, grow, n_groups, gpc, vf, eff, ld_eff, taps,
-                                                                     part, ldp)));
+             (sparse_group_scatter_kernel<TE><<<sgrid, 256, 0, st>>>(q, ldq, grow, n_groups, gpc, vf, eff, ld_eff,
+                                                                     rows.n_det, taps, part, ldp)));
   JSCC_LAUNCH_CHECK();
   int64_t blocks = (vf + 255) / 256;
   if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
@@ -958,6 +1231,15 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
   return sysmat_dtype == JSCC_DTYPE_F32 ? JSCC_GROUPED(float, __nv_bfloat16, r)
                                         : JSCC_GROUPED(__nv_bfloat16, __nv_bfloat16, r);
 #undef JSCC_GROUPED
+}
+
+int jscc_take_wait_timeout_count(unsigned int* out) {
+  JSCC_REQUIRE(out, "jscc_take_wait_timeout_count: null pointer argument");
+  unsigned int h = 0, zero = 0;
+  JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_wait_timeout_count, sizeof(h)));
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_wait_timeout_count, &zero, sizeof(zero)));
+  *out = h;
+  return JSCC_OK;
 }
 
 }  // extern "C"

@@ -409,3 +409,35 @@ def test_grouped_kernel_tap_widths(cuda, theta_stride):
         a = ops.sparse_weight_split(ids, tcb, A.to(torch.bfloat16), tb, x, grouped=grouped, method="event")
         b = ops.sparse_weight_split(ids, tcb, A.to(torch.bfloat16), tb, x, grouped=grouped)
         assert rel_l2(b.cpu(), a.cpu()) < TOL_W
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
+@pytest.mark.parametrize("n_det,n_events", [(400, 3000), (30, 2000), (700, 700)])
+def test_grouped_bulk_pipeline(cuda, dtype, n_det, n_events):
+    """Split rows with 16-byte aligned starts and lengths take the bulk-copy pipeline: groups
+    larger than a batch (several batches per group), more groups than CTAs (batches
+    prefetched across group boundaries) and one-event groups all match the per-event
+    kernel, both semantics, and no device wait gives up."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    grid = synthetic.polar_grid(16, 96, 30.0)
+    p = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1)
+    tb = cso.tables(p, cuda)
+    vc = p.coarse_pixel_num
+    assert (vc * 2) % 16 == 0 and (grid.n_vox * 2) % 16 == 0
+    g = torch.Generator().manual_seed(n_det + n_events)
+    A = (torch.rand((n_det, grid.n_vox), generator=g) + 0.05).to(cuda).to(dtype)
+    tc = (torch.rand((n_events, vc), generator=g) ** 3).to(cuda)
+    ids = torch.randint(0, n_det, (n_events,), generator=g, dtype=torch.int32).to(cuda)
+    x = (torch.rand((grid.n_vox, 1), generator=g) + 0.2).to(cuda)
+    _lib.take_wait_timeout_count()
+    tcd = tc.to(dtype)
+    for grouped in (False, True):
+        a = ops.sparse_weight_split(ids, tcd, A, tb, x, grouped=grouped, method="event")
+        b = ops.sparse_weight_split(ids, tcd, A, tb, x, grouped=grouped)
+        b2 = ops.sparse_weight_split(ids, tcd, A, tb, x, grouped=grouped)
+        torch.cuda.synchronize()
+        assert rel_l2(b.cpu(), a.cpu()) < TOL_W
+        assert torch.equal(b, b2)
+    assert _lib.take_wait_timeout_count() == 0
