@@ -433,6 +433,29 @@ __global__ void sparse_fold_x_kernel(const int32_t* __restrict__ tj, const float
     xw[t] = tw[t] * __ldg(x + tj[t]);
 }
 
+// The adjoint taps packed in pairs for the bulk pipeline: tp[m][c] = (j[2m][c], w'[2m][c],
+// j[2m+1][c], w'[2m+1][c]) with w' = w * x[j] (x null: w' = w), m < ceil(K / 2); a tap
+// past K is (0, 0). One 16-byte load brings two taps.
+__global__ void sparse_fold_pack_kernel(const int32_t* __restrict__ tj, const float* __restrict__ tw, int K, int M,
+                                        int64_t vc, const float* __restrict__ x, int4* __restrict__ tp) {
+  const int64_t n = (int64_t)M * vc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int m = (int)(t / vc);
+    const int64_t c = t - (int64_t)m * vc;
+    int idx[2] = {0, 0};
+    float w[2] = {0.f, 0.f};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 2 * m + h;
+      if (k < K) {
+        idx[h] = tj[(int64_t)k * vc + c];
+        w[h] = x ? tw[(int64_t)k * vc + c] * __ldg(x + idx[h]) : tw[(int64_t)k * vc + c];
+      }
+    }
+    tp[t] = make_int4(idx[0], __float_as_int(w[0]), idx[1], __float_as_int(w[1]));
+  }
+}
+
 // Dot of a coarse row (global, TC) with a shared-memory vector, by one warp; 16-byte loads
 // with four independent accumulators when the row is 16-byte aligned.
 template <typename TC>
@@ -608,69 +631,130 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
 }
 
 // ------------------------------------------------------------------ grouped coefficients, bulk-copy pipeline
-// The same per-group computation with every operand staged in shared memory by bulk copies
-// (cp.async.bulk completing on mbarriers), so each byte is read from HBM once and the adjoint
-// gather, the event dots and the q accumulation all read shared memory. One persistent CTA
-// per SM walks its groups gi = blockIdx.x, + gridDim.x, ...; shared memory holds
-//   erow  [vf] TE       the group's sysmat row; the next group's row is fetched as soon as
-//                       the adjoint of the current one is done
-//   b     [vc] float    adj(A_g * x) (MODE 2: adj(A_g))
-//   slots [2][batch][vc] TC   coarse rows of two batches of (up to `batch`) events of one
-//                       group: while one batch is used the next one, possibly of a later
-//                       group, is in flight
-// Dots: each thread owns four coarse values per 2048 and accumulates all the batch's events,
-// partial sums are reduced per warp and then over warps in warp order (deterministic). q is
-// accumulated over the group's events in event order, batch after batch, in the q row.
-// Every wait is bounded: on a timeout the CTA counts it (jscc_take_wait_timeout_count),
-// waits (bounded) for its copies still in flight and returns.
+// The same per-group computation with its operands staged in shared memory by bulk copies
+// (cp.async.bulk completing on mbarriers): each byte is read from HBM once, and the adjoint
+// gather, the event dots and the q accumulation read shared memory. One persistent CTA per
+// SM walks its groups gi = blockIdx.x, + gridDim.x, ... with two warp roles:
+//   producer (the last warp): runs ahead of the consumers, copying each group's sysmat row
+//     into `erow` once the previous group's adjoint has released it, and every event's
+//     coarse row into a ring of `n_slots` slots, each once its previous row was consumed;
+//   consumers (the other 15 warps): per group b = adjoint of erow, then batches of up to
+//     `batch` events: dots f_i = t_i . b (each thread four coarse values per 1,920, reduced
+//     per warp and then over warps in warp order), coefficients, q += c_i t_i in registers
+//     (events in order); q_g is stored at the end of the group.
+// Shared memory: header (barriers, dot partials, coefficients), erow[vf] TE, b[vc] float,
+// slots[n_slots][vc] TC. Every wait is bounded: on a timeout the CTA counts it
+// (jscc_take_wait_timeout_count), waits (bounded) for the copies it still has in flight and
+// returns.
 constexpr int kBkThreads = 512;
-constexpr int kBkWarps = kBkThreads / 32;
-constexpr int kBkMaxBatch = 8;
-constexpr int kBkHeader = 1024;               // barriers, dot partials, coefficients, abort flag
-constexpr uint32_t kBkMaxPolls = 1u << 22;    // per wait
+constexpr int kBkConsumers = kBkThreads - 32;
+constexpr int kBkConsumerWarps = kBkConsumers / 32;
+constexpr int kBkMaxSlots = 8;
+constexpr int kBkMaxBatch = kBkMaxSlots / 2;
+constexpr int kBkQ = 6;  // q registers: chunks of four coarse values per consumer thread
+constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkConsumers;
+constexpr int kBkHeader = 1024;
+constexpr uint32_t kBkMaxPolls = 1u << 22;  // per wait
 
 __device__ unsigned int g_wait_timeout_count = 0;
 
-// Adjoint of one group from the shared-memory sysmat row (plain loads; see group_adjoint).
-template <int KT, typename TE>
-__device__ __forceinline__ void group_adjoint_smem(float* b, int64_t vc, const int32_t* __restrict__ tj,
-                                                   const float* __restrict__ tw, int K, const TE* er, int tid) {
-  for (int64_t c0 = tid; c0 < vc; c0 += 2 * kBkThreads) {
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// named barrier over the consumer warps only
+__device__ __forceinline__ void consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(kBkConsumers) : "memory");
+}
+
+// named barrier over the consumer warps returning the OR of every consumer's `v` (the same
+// value in all of them, so a decision taken on it is uniform)
+__device__ __forceinline__ bool consumer_sync_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(kBkConsumers)
+      : "memory");
+  return r != 0;
+}
+
+// bounded wait that also gives up once another thread has flagged an abort
+__device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kBkMaxPolls; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 31u) == 31u && *abort_flag) return false;
+  }
+  return false;
+}
+
+// Adjoint of one group from the shared-memory sysmat row by NT threads: b[c] = sum over the
+// packed taps of w' * erow[j] (plain shared loads), two coarse voxels per thread at a time;
+// with MT = KT / 2 > 0 all tap loads are issued before the first gather (MT = 0: runtime M).
+template <int KT, int NT, typename TE>
+__device__ __forceinline__ void group_adjoint_packed(float* b, int vc, const int4* __restrict__ tp, int M,
+                                                     const TE* er, int tid) {
+  constexpr int MT = KT / 2;
+  for (int c0 = tid; c0 < vc; c0 += 2 * NT) {
     float acc[2] = {0.f, 0.f};
-    if (KT > 0) {
-      int idx[2][KT > 0 ? KT : 1];
-      float wv[2][KT > 0 ? KT : 1];
+    if (MT > 0) {
+      int4 t[2][MT > 0 ? MT : 1];
 #pragma unroll
-      for (int k = 0; k < KT; ++k)
+      for (int m = 0; m < MT; ++m)
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const int64_t c = c0 + (int64_t)u * kBkThreads;
-          const bool in = c < vc && k < K;  // the table has K rows; KT may exceed K
-          idx[u][k] = in ? __ldg(tj + (int64_t)k * vc + c) : 0;
-          wv[u][k] = in ? __ldg(tw + (int64_t)k * vc + c) : 0.f;
+          const int c = c0 + u * NT;
+          t[u][m] = (c < vc && m < M) ? __ldg(tp + (size_t)m * vc + c) : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
-      for (int k = 0; k < KT; ++k)
-#pragma unroll
-        for (int u = 0; u < 2; ++u) acc[u] = fmaf(wv[u][k], to_float(er[idx[u][k]]), acc[u]);
-    } else {
-      for (int k = 0; k < K; ++k)
+      for (int m = 0; m < MT; ++m)
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const int64_t c = c0 + (int64_t)u * kBkThreads;
+          acc[u] = fmaf(__int_as_float(t[u][m].y), to_float(er[t[u][m].x]), acc[u]);
+          acc[u] = fmaf(__int_as_float(t[u][m].w), to_float(er[t[u][m].z]), acc[u]);
+        }
+    } else {
+      for (int m = 0; m < M; ++m)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int c = c0 + u * NT;
           if (c < vc) {
-            const float wvv = __ldg(tw + (int64_t)k * vc + c);
-            if (wvv != 0.f) acc[u] = fmaf(wvv, to_float(er[__ldg(tj + (int64_t)k * vc + c)]), acc[u]);
+            const int4 tt = __ldg(tp + (size_t)m * vc + c);
+            acc[u] = fmaf(__int_as_float(tt.y), to_float(er[tt.x]), acc[u]);
+            acc[u] = fmaf(__int_as_float(tt.w), to_float(er[tt.z]), acc[u]);
           }
         }
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-      const int64_t c = c0 + (int64_t)u * kBkThreads;
+      const int c = c0 + u * NT;
       if (c < vc) b[c] = acc[u];
     }
   }
 }
+
+// coarse rows of a batch held in registers between the dot and the q pass: four BF16 values
+// per chunk as a uint2 (float rows are re-read from shared memory instead)
+template <typename TC>
+struct RowChunk;
+template <>
+struct RowChunk<__nv_bfloat16> {
+  static constexpr bool kKeep = true;
+  uint2 v;
+  __device__ __forceinline__ void load(const __nv_bfloat16* p, int c) { v = *reinterpret_cast<const uint2*>(p + c); }
+  __device__ __forceinline__ void get(const __nv_bfloat16*, int, float (&f)[4]) const {
+    f[0] = bf16_lo(v.x); f[1] = bf16_hi(v.x); f[2] = bf16_lo(v.y); f[3] = bf16_hi(v.y);
+  }
+};
+template <>
+struct RowChunk<float> {
+  static constexpr bool kKeep = false;
+  __device__ __forceinline__ void load(const float*, int) {}
+  __device__ __forceinline__ void get(const float* p, int c, float (&f)[4]) const {
+    const float4 u = *reinterpret_cast<const float4*>(p + c);
+    f[0] = u.x; f[1] = u.y; f[2] = u.z; f[3] = u.w;
+  }
+};
 
 // four consecutive coarse values from shared memory (c a multiple of 4)
 __device__ __forceinline__ void smem4(const __nv_bfloat16* p, int64_t c, float (&v)[4]) {
@@ -685,155 +769,206 @@ __device__ __forceinline__ void smem4(const float* p, int64_t c, float (&v)[4]) 
 template <int MODE, int KT, typename TE, typename TC>
 __global__ void __launch_bounds__(kBkThreads, 1)
 sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
-                              const int32_t* __restrict__ grow, int n_groups, int64_t vc,
-                              const int32_t* __restrict__ tj, const float* __restrict__ tw, int K,
-                              const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ s_ev,
-                              float* __restrict__ q, int64_t ldq, int batch, uint32_t erow_bytes, uint32_t row_bytes,
-                              uint32_t b_off, uint32_t slot_off, uint32_t slot_stride) {
+                              const int32_t* __restrict__ grow, int n_groups, int vc,
+                              const int4* __restrict__ tp, int M, const TE* __restrict__ eff, int64_t ld_eff,
+                              float* __restrict__ s_ev, float* __restrict__ q, int64_t ldq, int n_slots, int batch,
+                              uint32_t erow_bytes,
+                              uint32_t row_bytes, uint32_t b_off, uint32_t slot_off, uint32_t slot_stride) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // [2][kBkMaxBatch] row slots, then the sysmat row
-  uint64_t* ebar = bar + 2 * kBkMaxBatch;
-  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkWarps][kBkMaxBatch]
-  float* cs = red + kBkWarps * kBkMaxBatch;           // [kBkMaxBatch]
-  int* abort_flag = reinterpret_cast<int*>(cs + kBkMaxBatch);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kBkMaxSlots]
+  uint64_t* empty = full + kBkMaxSlots;                // [kBkMaxSlots]
+  uint64_t* erow_full = empty + kBkMaxSlots;
+  uint64_t* erow_empty = erow_full + 1;
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 160);
+  int* rows_issued = reinterpret_cast<int*>(smem + 164);
+  int* erows_issued = reinterpret_cast<int*>(smem + 168);
+  int* rows_used = reinterpret_cast<int*>(smem + 172);
+  int* erows_used = reinterpret_cast<int*>(smem + 176);
+  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkConsumerWarps][kBkMaxBatch]
+  float* cs = reinterpret_cast<float*>(smem + 512);   // [kBkMaxBatch]
   TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
   float* b = reinterpret_cast<float*>(smem + b_off);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = gridDim.x;
-  auto slot = [&](int h, int k) { return reinterpret_cast<TC*>(smem + slot_off + (size_t)(h * batch + k) * slot_stride); };
+  auto slot = [&](int s) { return reinterpret_cast<const TC*>(smem + slot_off + (size_t)s * slot_stride); };
   if (tid == 0) {
-    for (int s = 0; s < 2 * kBkMaxBatch + 1; ++s) mbar_init(bar + s, 1);
+    for (int s = 0; s < kBkMaxSlots; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+    }
+    mbar_init(erow_full, 1);
+    mbar_init(erow_empty, 1);
     *abort_flag = 0;
+    *rows_issued = *erows_issued = *rows_used = *erows_used = 0;
     mbar_init_fence();
   }
   __syncthreads();
-  // ---- producer state (thread 0): the last batch issued and the barriers with a copy in flight
-  uint32_t pending = 0;
-  int ig = blockIdx.x, ib = ig < n_groups ? goff[ig] : 0;
-  auto seek = [&]() -> bool {  // (ig, ib) -> the first batch at or after it, skipping empty groups
-    while (ig < n_groups) {
-      if (ib < goff[ig + 1]) return true;
-      ig += G;
-      if (ig < n_groups) ib = goff[ig];
-    }
-    return false;
-  };
-  auto issue_row = [&](int gi) {
-    mbar_arrive_expect_tx(ebar, erow_bytes);
-    bulk_copy_g2s(erow, eff + clamp_row(grow[gi], rows.n_det) * ld_eff, erow_bytes, ebar);
-    pending |= 1u << (2 * kBkMaxBatch);
-  };
-  auto issue_batch = [&](int h) {
-    const int n = min(batch, goff[ig + 1] - ib);
-    for (int k = 0; k < n; ++k) {
-      uint64_t* bk = bar + h * kBkMaxBatch + k;
-      mbar_arrive_expect_tx(bk, row_bytes);
-      bulk_copy_g2s(slot(h, k), rows.coarse(order[ib + k]), row_bytes, bk);
-      pending |= 1u << (h * kBkMaxBatch + k);
-    }
-  };
-  if (tid == 0 && blockIdx.x < n_groups) {
-    issue_row(blockIdx.x);
-    if (seek()) issue_batch(0);
-  }
-  uint32_t ph = 0;  // parity of every barrier's next phase (bit s: barrier s)
-  auto wait = [&](int s) {
-    if (!mbar_wait_bounded(bar + s, (ph >> s) & 1u, kBkMaxPolls)) *abort_flag = 1;
-    ph ^= 1u << s;
-    pending &= ~(1u << s);
-  };
-  int nb = 0;  // batches consumed (selects the half)
-  bool aborted = false;
-  for (int gi = blockIdx.x; gi < n_groups && !aborted; gi += G) {
-    wait(2 * kBkMaxBatch);
-    group_adjoint_smem<KT, TE>(b, vc, tj, tw, K, erow, tid);
-    __syncthreads();
-    if (*abort_flag) { aborted = true; break; }
-    if (tid == 0 && gi + G < n_groups) {
-      fence_proxy_async_smem();
-      issue_row(gi + G);
-    }
-    const int e0 = goff[gi], e1 = goff[gi + 1];
-    float* qg = q + (int64_t)gi * ldq;
-    if (MODE != 2 && e0 == e1)
-      for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4)
-        *reinterpret_cast<float4*>(qg + c) = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int bs = e0; bs < e1; bs += batch, ++nb) {
-      const int n = min(batch, e1 - bs), h = nb & 1;
-      if (tid == 0) {  // the next batch into the other half (its last batch ended at the last barrier)
-        ib += batch;
-        if (seek()) {
-          fence_proxy_async_smem();
-          issue_batch(h ^ 1);
+  if (warp == kBkConsumerWarps) {
+    // ------------------------------------------------------------ producer warp
+    int pseq = 0, kg = 0;
+    bool ok = true;
+    for (int gi = blockIdx.x; gi < n_groups && ok; gi += G, ++kg) {
+      const int e0 = goff[gi], e1 = goff[gi + 1];
+      const TE* src = eff + clamp_row(grow[gi], rows.n_det) * ld_eff;
+      if (lane == 0) {
+        if (kg > 0) ok = bk_wait(erow_empty, (kg - 1) & 1, abort_flag);
+        if (ok) {
+          mbar_arrive_expect_tx(erow_full, erow_bytes);
+          bulk_copy_g2s(erow, src, erow_bytes, erow_full);
+          *erows_issued = kg + 1;
         }
       }
-      for (int k = 0; k < n; ++k) wait(h * kBkMaxBatch + k);
-      // ---- dots f_i = t_i . b
-      float acc[kBkMaxBatch];
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      for (int w0 = e0; w0 < e1 && ok; w0 += 32) {
+        const int iv = w0 + lane < e1 ? order[w0 + lane] : 0;  // 32 event indices per load
+        const int m = min(32, e1 - w0);
+        for (int k = 0; k < m && ok; ++k, ++pseq) {
+          const int i = __shfl_sync(0xffffffffu, iv, k);
+          if (lane == 0) {
+            const int s = pseq % n_slots;
+            if (pseq >= n_slots) ok = bk_wait(empty + s, (pseq / n_slots - 1) & 1, abort_flag);
+            if (ok) {
+              mbar_arrive_expect_tx(full + s, row_bytes);
+              bulk_copy_g2s(const_cast<TC*>(slot(s)), rows.coarse(i), row_bytes, full + s);
+              *rows_issued = pseq + 1;
+            }
+          }
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+        }
+      }
+    }
+    if (!ok && lane == 0) *abort_flag = 1;
+  } else {
+    // ------------------------------------------------------------ consumer warps
+    const int ct = tid;
+    int seq = 0, kg = 0;
+    bool aborted = false, bad = false;  // bad: one of this thread's waits gave up
+    int ne0 = blockIdx.x < n_groups ? goff[blockIdx.x] : 0;
+    int ne1 = blockIdx.x < n_groups ? goff[blockIdx.x + 1] : 0;
+    for (int gi = blockIdx.x; gi < n_groups && !aborted; gi += G, ++kg) {
+      const int e0 = ne0, e1 = ne1;
+      if (gi + G < n_groups) {  // the next group's range, fetched a group ahead
+        ne0 = goff[gi + G];
+        ne1 = goff[gi + G + 1];
+      }
+      if (!bk_wait(erow_full, kg & 1, abort_flag)) bad = true;
+      group_adjoint_packed<KT, kBkConsumers, TE>(b, vc, tp, M, erow, ct);
+      if (consumer_sync_or(bad)) {
+        aborted = true;
+        break;
+      }
+      if (ct == 0) {
+        mbar_arrive(erow_empty);  // the producer may refill erow
+        *erows_used = kg + 1;
+      }
+      float4 qa[kBkQ];
 #pragma unroll
-      for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = 0.f;
-      for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4) {
-        const float4 bv = *reinterpret_cast<const float4*>(b + c);
+      for (int u = 0; u < kBkQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int bs = e0; bs < e1; bs += batch) {
+        const int n = min(batch, e1 - bs);
+        int64_t my_i = 0;
+        float my_s = 0.f;
+        if (ct < n) {  // issued before the dots, used after them
+          my_i = order[bs + ct];
+          if (MODE == 0) my_s = s_ev[my_i];
+        }
+        for (int k = 0; k < n; ++k) {
+          const int sq = seq + k;
+          if (!bk_wait(full + sq % n_slots, (sq / n_slots) & 1, abort_flag)) bad = true;
+        }
+        // ---- dots f_i = t_i . b; BF16 rows stay in registers for the q pass
+        const TC* rp[kBkMaxBatch];
+#pragma unroll
+        for (int k = 0; k < kBkMaxBatch; ++k) rp[k] = slot((seq + k) % n_slots);
+        RowChunk<TC> rc[kBkMaxBatch][kBkQ];
+        float acc[kBkMaxBatch];
+#pragma unroll
+        for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = 0.f;
+#pragma unroll
+        for (int u = 0; u < kBkQ; ++u) {
+          const int c = ct * 4 + u * (kBkConsumers * 4);
+          if (c < vc) {
+            const float4 bv = *reinterpret_cast<const float4*>(b + c);
+#pragma unroll
+            for (int k = 0; k < kBkMaxBatch; ++k)
+              if (k < n) {
+                float v[4];
+                rc[k][u].load(rp[k], c);
+                if (RowChunk<TC>::kKeep) rc[k][u].get(rp[k], c, v);
+                else smem4(rp[k], c, v);
+                acc[k] = fmaf(v[0], bv.x, acc[k]);
+                acc[k] = fmaf(v[1], bv.y, acc[k]);
+                acc[k] = fmaf(v[2], bv.z, acc[k]);
+                acc[k] = fmaf(v[3], bv.w, acc[k]);
+              }
+          }
+        }
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k)
           if (k < n) {
-            float v[4];
-            smem4(slot(h, k), c, v);
-            acc[k] = fmaf(v[0], bv.x, acc[k]);
-            acc[k] = fmaf(v[1], bv.y, acc[k]);
-            acc[k] = fmaf(v[2], bv.z, acc[k]);
-            acc[k] = fmaf(v[3], bv.w, acc[k]);
+            const float f = warp_sum(acc[k]);
+            if (lane == 0) red[warp * kBkMaxBatch + k] = f;
           }
-      }
-#pragma unroll
-      for (int k = 0; k < kBkMaxBatch; ++k)
-        if (k < n) {
-          const float f = warp_sum(acc[k]);
-          if (lane == 0) red[warp * kBkMaxBatch + k] = f;
+        if (consumer_sync_or(bad)) {
+          aborted = true;
+          break;
         }
-      __syncthreads();
-      if (*abort_flag) { aborted = true; break; }
-      if (tid < n) {
-        float f = 0.f;
-        for (int w = 0; w < kBkWarps; ++w) f += red[w * kBkMaxBatch + tid];
-        const int64_t i = order[bs + tid];
-        if (MODE == 2) {
-          s_ev[i] = f;
-        } else if (MODE == 0) {
-          const float si = s_ev[i];
-          cs[tid] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
-        } else {
-          cs[tid] = 1.0f / fmaxf(f, 1e-12f);
+        if (ct < n) {
+          float f = 0.f;
+          for (int w = 0; w < kBkConsumerWarps; ++w) f += red[w * kBkMaxBatch + ct];
+          if (MODE == 2) s_ev[my_i] = f;
+          else if (MODE == 0) cs[ct] = (isfinite(my_s) && my_s > 0.f) ? (1.0f / fmaxf(f / my_s, 1e-12f)) / my_s : 0.f;
+          else cs[ct] = 1.0f / fmaxf(f, 1e-12f);
         }
-      }
-      if (MODE != 2) {
-        __syncthreads();
-        // ---- q_g += sum over the batch of c_i t_i, events in order
-        for (int64_t c = (int64_t)tid * 4; c < vc; c += kBkThreads * 4) {
-          float4 a = bs == e0 ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4*>(qg + c);
+        if (MODE != 2) {
+          consumer_sync();
+          // ---- q_g += c_i t_i over the batch, events in order
 #pragma unroll
           for (int k = 0; k < kBkMaxBatch; ++k)
             if (k < n) {
               const float ck = cs[k];
               if (ck != 0.f) {
-                float v[4];
-                smem4(slot(h, k), c, v);
-                a.x = fmaf(ck, v[0], a.x);
-                a.y = fmaf(ck, v[1], a.y);
-                a.z = fmaf(ck, v[2], a.z);
-                a.w = fmaf(ck, v[3], a.w);
+#pragma unroll
+                for (int u = 0; u < kBkQ; ++u) {
+                  const int c = ct * 4 + u * (kBkConsumers * 4);
+                  if (c < vc) {
+                    float v[4];
+                    rc[k][u].get(rp[k], c, v);
+                    qa[u].x = fmaf(ck, v[0], qa[u].x);
+                    qa[u].y = fmaf(ck, v[1], qa[u].y);
+                    qa[u].z = fmaf(ck, v[2], qa[u].z);
+                    qa[u].w = fmaf(ck, v[3], qa[u].w);
+                  }
+                }
               }
             }
-          *reinterpret_cast<float4*>(qg + c) = a;
+        }
+        consumer_sync();  // the batch's slots, partials and coefficients are free
+        if (ct == 0) {
+          for (int k = 0; k < n; ++k) mbar_arrive(empty + (seq + k) % n_slots);
+          *rows_used = seq + n;
+        }
+        seq += n;
+      }
+      if (aborted) break;
+      if (MODE != 2) {
+        float* qg = q + (int64_t)gi * ldq;
+#pragma unroll
+        for (int u = 0; u < kBkQ; ++u) {
+          const int c = ct * 4 + u * (kBkConsumers * 4);
+          if (c < vc) *reinterpret_cast<float4*>(qg + c) = qa[u];
         }
       }
-      __syncthreads();  // the batch's slots and coefficients are free
     }
+    if (aborted) *abort_flag = 1;  // stops the producer
   }
-  if (aborted && tid == 0) {
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
     atomicAdd(&g_wait_timeout_count, 1u);
-    for (int s = 0; s <= 2 * kBkMaxBatch; ++s)  // copies still in flight write this CTA's memory
-      if (pending & (1u << s)) mbar_wait_bounded(bar + s, (ph >> s) & 1u, kBkMaxPolls);
+    // copies still in flight write this CTA's shared memory: wait (bounded) for them
+    for (int sq = *rows_used; sq < *rows_issued; ++sq)
+      mbar_wait_bounded(full + sq % n_slots, (sq / n_slots) & 1, kBkMaxPolls);
+    if (*erows_issued > *erows_used) mbar_wait_bounded(erow_full, *erows_used & 1, kBkMaxPolls);
   }
 }
 
@@ -854,19 +989,37 @@ sparse_group_scatter_kernel(const float* __restrict__ q, int64_t ldq, const int3
   const int64_t c10 = (int64_t)z1 * taps.n_lc + l0, c11 = (int64_t)z1 * taps.n_lc + l1;
   const int g_begin = blockIdx.y * groups_per_chunk;
   const int g_end = (g_begin + groups_per_chunk) < n_groups ? g_begin + groups_per_chunk : n_groups;
+  const bool two_z = u1 != 0.f;
   float acc = 0.f;
-#pragma unroll 4
-  for (int gi = g_begin; gi < g_end; ++gi) {
-    const float* qg = q + (int64_t)gi * ldq;
-    float a = w0 * __ldg(qg + c00);
-    a = fmaf(w1, __ldg(qg + c01), a);
-    float v = u0 * a;
-    if (u1 != 0.f) {
-      float bb = w0 * __ldg(qg + c10);
-      bb = fmaf(w1, __ldg(qg + c11), bb);
-      v = fmaf(u1, bb, v);
+  // eight groups at a time: every load of the eight is issued before the first FMA
+  constexpr int U = 8;
+  for (int g0 = g_begin; g0 < g_end; g0 += U) {
+    int64_t off[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) off[u] = g0 + u < g_end ? clamp_row(__ldg(grow + g0 + u), n_det) * ld_eff : -1;
+    float a[U], p0[U], p1[U], r0[U], r1[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool in = off[u] >= 0;
+      const float* qg = q + (int64_t)(g0 + u) * ldq;
+      a[u] = in ? ld_any(eff + off[u], j) : 0.f;
+      p0[u] = in ? __ldg(qg + c00) : 0.f;
+      p1[u] = in ? __ldg(qg + c01) : 0.f;
+      r0[u] = in && two_z ? __ldg(qg + c10) : 0.f;
+      r1[u] = in && two_z ? __ldg(qg + c11) : 0.f;
     }
-    if (v != 0.f) acc = fmaf(ld_any(eff + clamp_row(grow[gi], n_det) * ld_eff, j), v, acc);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      float t = w0 * p0[u];
+      t = fmaf(w1, p1[u], t);
+      float v = u0 * t;
+      if (two_z) {
+        float bb = w0 * r0[u];
+        bb = fmaf(w1, r1[u], bb);
+        v = fmaf(u1, bb, v);
+      }
+      if (v != 0.f) acc = fmaf(a[u], v, acc);
+    }
   }
   part[(int64_t)blockIdx.y * ldp + j] = acc;
 }
@@ -904,34 +1057,52 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   if (per_sm < 1) per_sm = 1;
   int64_t grid = (int64_t)num_sms() * per_sm;
   if (grid > n_groups) grid = n_groups;
-  {
-    const int64_t n = (int64_t)K * vc;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > (int64_t)num_sms() * 8) blocks = (int64_t)num_sms() * 8;
-    JSCC_TIMED("sparse_fold_x", st, (sparse_fold_x_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, n, x, xw)));
-    JSCC_LAUNCH_CHECK();
-  }
-  cudaError_t attr = cudaSuccess;
-  // bulk-copy pipeline when every row start and length is 16-byte aligned (split storage)
-  // and a sysmat row, b and two batches of coarse rows fit in shared memory
+  // bulk-copy pipeline when every row start and length is 16-byte aligned (split storage),
+  // q fits the consumer registers and a sysmat row, b and at least two coarse rows fit in
+  // shared memory
   const uint32_t erow_bytes = (uint32_t)((size_t)vf * sizeof(TE)), row_bytes = (uint32_t)((size_t)vc * sizeof(TC));
   const uint32_t b_off = (uint32_t)align_up(kBkHeader + align_up(erow_bytes, 128), 128);
   const uint32_t slot_off = (uint32_t)(b_off + align_up((size_t)vc * 4, 128));
   const uint32_t slot_stride = (uint32_t)align_up(row_bytes, 128);
   const size_t bk_limit = 227 * 1024;
-  int batch = 0;
+  int n_slots = 0;
   if (slot_off < bk_limit && slot_stride > 0) {
-    batch = (int)((bk_limit - slot_off) / (2 * (size_t)slot_stride));
-    if (batch > kBkMaxBatch) batch = kBkMaxBatch;
+    n_slots = (int)((bk_limit - slot_off) / (size_t)slot_stride);
+    if (n_slots > kBkMaxSlots) n_slots = kBkMaxSlots;
   }
-  const bool bulk = rows.packed == nullptr && batch >= 1 && (size_t)vf * sizeof(TE) < (1u << 20) &&
-                    reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 && (rows.ld * sizeof(TC)) % 16 == 0 &&
-                    row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(eff) % 16 == 0 &&
-                    (ld_eff * sizeof(TE)) % 16 == 0 && erow_bytes % 16 == 0;
-  const size_t bk_smem = (size_t)slot_off + 2 * (size_t)batch * slot_stride;
+  const int batch = n_slots / 2;
+  const bool bulk = rows.packed == nullptr && n_slots >= 2 && vc <= kBkMaxCoarse &&
+                    (size_t)vf * sizeof(TE) < (1u << 20) && reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 &&
+                    (rows.ld * sizeof(TC)) % 16 == 0 && row_bytes % 16 == 0 &&
+                    reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
+                    erow_bytes % 16 == 0;
+  const size_t bk_smem = (size_t)slot_off + (size_t)n_slots * slot_stride;
   int64_t bk_grid = num_sms();
   if (bk_grid > n_groups) bk_grid = n_groups;
-#define JSCC_GC_BK(MODE, KT, TW)                                                                                 \
+  const int M = (K + 1) / 2;
+  int4* tpx = cv.take<int4>((size_t)M * vc);  // packed taps with x folded in
+  int4* tpw = cv.take<int4>((size_t)M * vc);  // packed taps, weights only (row sums)
+  JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
+  {
+    int64_t blocks = ((int64_t)K * vc + 255) / 256;
+    if (blocks > (int64_t)num_sms() * 8) blocks = (int64_t)num_sms() * 8;
+    if (bulk) {
+      JSCC_TIMED("sparse_fold_x", st,
+                 (sparse_fold_pack_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, K, M, vc, x, tpx)));
+      JSCC_LAUNCH_CHECK();
+      if (mode == JSCC_SPARSE_MATERIALIZE && !have_sums) {
+        JSCC_TIMED("sparse_fold_x", st,
+                   (sparse_fold_pack_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, K, M, vc, nullptr, tpw)));
+        JSCC_LAUNCH_CHECK();
+      }
+    } else {
+      JSCC_TIMED("sparse_fold_x", st,
+                 (sparse_fold_x_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, (int64_t)K * vc, x, xw)));
+      JSCC_LAUNCH_CHECK();
+    }
+  }
+  cudaError_t attr = cudaSuccess;
+#define JSCC_GC_BK(MODE, KT, TP)                                                                                 \
   do {                                                                                                           \
     attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, KT, TE, TC>,                                 \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                      \
@@ -939,8 +1110,8 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
       JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
                  (sparse_group_coef_bulk_kernel<MODE, KT, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,      \
                                                                      st>>>(                                      \
-                     rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, q, ldq, batch,         \
-                     erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                                     \
+                     rows, order, goff, grow, n_groups, (int)vc, TP, M, eff, ld_eff, s_ev, q, ldq, n_slots,      \
+                     batch, erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                              \
   } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
@@ -952,25 +1123,25 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
                      rows, vec_rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, coef, q,     \
                      ldq)));                                                                                     \
   } while (0)
-#define JSCC_GC(MODE, TW)                                                                                        \
+#define JSCC_GC(MODE, TW, TP)                                                                                    \
   do {                                                                                                           \
     if (bulk) {                                                                                                  \
-      if (K <= 4) JSCC_GC_BK(MODE, 4, TW);                                                                       \
-      else if (K <= 8) JSCC_GC_BK(MODE, 8, TW);                                                                  \
-      else JSCC_GC_BK(MODE, 0, TW);                                                                              \
+      if (K <= 4) JSCC_GC_BK(MODE, 4, TP);                                                                       \
+      else if (K <= 8) JSCC_GC_BK(MODE, 8, TP);                                                                  \
+      else JSCC_GC_BK(MODE, 0, TP);                                                                              \
     } else if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                   \
     else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
     else JSCC_GC_K(MODE, 0, TW);                                                                                 \
   } while (0)
   if (mode == JSCC_SPARSE_MATERIALIZE) {
     if (!have_sums) {
-      JSCC_GC(2, tw);  // S_i = t_i . adj(A_g), kept by the caller across calls
+      JSCC_GC(2, tw, tpw);  // S_i = t_i . adj(A_g), kept by the caller across calls
       JSCC_CUDA_CHECK(attr);
       JSCC_LAUNCH_CHECK();
     }
-    JSCC_GC(0, xw);
+    JSCC_GC(0, xw, tpx);
   } else {
-    JSCC_GC(1, xw);
+    JSCC_GC(1, xw, tpx);
   }
 #undef JSCC_GC
 #undef JSCC_GC_K
@@ -1164,7 +1335,9 @@ size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int
   return align_up((size_t)ldp * sizeof(float), 256) + align_up((size_t)(n_events > 0 ? n_events : 1) * 4, 256) +
          align_up((size_t)(adj_width > 0 ? adj_width : 1) * (n_coarse > 0 ? n_coarse : 1) * 4, 256) +
          align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) +
-         align_up((size_t)chunks * ldp * sizeof(float), 256) + 256;
+         align_up((size_t)chunks * ldp * sizeof(float), 256) +
+         2 * align_up((size_t)((adj_width > 0 ? adj_width : 1) + 1) / 2 * (n_coarse > 0 ? n_coarse : 1) * 16, 256) +
+         256;
 }
 
 int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,
