@@ -318,6 +318,11 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * sysmat row pitch) the per-group step streams the sysmat row and the coarse rows into
  * shared memory with bulk copies; its waits are bounded and a wait that gives up is
  * counted (jscc_take_wait_timeout_count), the weight of that call then being invalid.
+ * ring_len / ring_stride (0 / 0: no claim) state that the adjoint table is a stride-4 ring
+ * stencil: z the identity, each fine plane made of rings of ring_len theta voxels, coarse
+ * voxel lc = r * (ring_len / 4) + th with taps r * ring_len + (4 th + d) mod ring_len,
+ * d = -3..3, in each plane (the caller checks the table; the kernel then computes the tap
+ * indices instead of loading them).
  */
 /*
  * Number of bounded device waits that gave up since the last call (then reset to 0).
@@ -335,6 +340,7 @@ JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coa
                    int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw,
                    int32_t n_zf, const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc,
                    int32_t n_zc, const int32_t* adj_idx, const float* adj_w, int32_t adj_width,
+                   int32_t ring_len, int32_t ring_stride,
                    int32_t mode, const float* img, const int64_t* rotmat, const int64_t* rotmat_inv,
                    int64_t ld_rot, float scale, float* weight, void* workspace, size_t workspace_bytes,
                    void* stream);

@@ -109,8 +109,8 @@ _SIGNATURES: dict[str, tuple] = {
         c_int,
         [c_void_p, c_void_p, c_int32, c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int32, c_void_p,
          c_int32, c_void_p, c_int32, c_int64, c_int64, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_int32,
-         c_int32, c_int32, c_void_p, c_void_p, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64, c_float,
-         c_void_p, c_void_p, c_size_t, c_void_p],
+         c_int32, c_int32, c_void_p, c_void_p, c_int32, c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+         c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
     "jscc_em_update": (
         c_int,

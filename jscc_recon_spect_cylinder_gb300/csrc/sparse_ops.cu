@@ -11,6 +11,7 @@
 //
 // out[r][zo * n_lo + lo] = sum_{(zi, wz) in Z[zo]} wz * sum_{(li, wl) in L[lo]} wl * in[r][zi * n_li + li]
 // (layer sum first, then z, as the reference's two matmuls).
+#include <climits>
 #include "jscc_common.cuh"
 
 namespace jscc {
@@ -456,6 +457,32 @@ __global__ void sparse_fold_pack_kernel(const int32_t* __restrict__ tj, const fl
   }
 }
 
+// The adjoint of a ring stencil of stride 4 (lateral theta interpolation with stride 4 in
+// every ring, z the identity; the host checks the tap table has exactly this form): coarse
+// c = zc * n_lc + lc, lc = r * n_thc + th, centre jb = zc * n_lf + r * ring_len + 4 th, taps
+// jb + d for d = -3..3 (ring-periodic, which only th = 0 needs). xs[c] = the seven folded
+// weights w * x[j] (x null: w) in d order and, in the eighth float, jb | (th == 0) << 30.
+__global__ void sparse_fold_ring_kernel(const int32_t* __restrict__ tj, const float* __restrict__ tw, int K, int vc,
+                                        int n_lc, int n_lf, int ring_len, const float* __restrict__ x,
+                                        float4* __restrict__ xs) {
+  const int n_thc = ring_len / 4;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < vc; c += gridDim.x * blockDim.x) {
+    const int zc = c / n_lc, lc = c - zc * n_lc;
+    const int r = lc / n_thc, th = lc - r * n_thc;
+    const int jb = zc * n_lf + r * ring_len + 4 * th;
+    float w[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < K; ++k) {
+      const int j = tj[(int64_t)k * vc + c];
+      int d = j - jb;
+      if (d > 3) d -= ring_len;
+      if (d < -3) d += ring_len;
+      if (d >= -3 && d <= 3) w[d + 3] = x ? tw[(int64_t)k * vc + c] * __ldg(x + j) : tw[(int64_t)k * vc + c];
+    }
+    xs[2 * c] = make_float4(w[0], w[1], w[2], w[3]);
+    xs[2 * c + 1] = make_float4(w[4], w[5], w[6], __int_as_float(jb | (th == 0 ? 1 << 30 : 0)));
+  }
+}
+
 // Dot of a coarse row (global, TC) with a shared-memory vector, by one warp; 16-byte loads
 // with four independent accumulators when the row is 16-byte aligned.
 template <typename TC>
@@ -733,6 +760,56 @@ __device__ __forceinline__ void group_adjoint_packed(float* b, int vc, const int
   }
 }
 
+// eight consecutive sysmat-row values from shared memory starting at p (p 8-byte aligned for
+// BF16, 16-byte aligned for float)
+__device__ __forceinline__ void smem8(const __nv_bfloat16* p, float (&v)[8]) {
+  const uint2 a = *reinterpret_cast<const uint2*>(p), b = *reinterpret_cast<const uint2*>(p + 4);
+  v[0] = bf16_lo(a.x); v[1] = bf16_hi(a.x); v[2] = bf16_lo(a.y); v[3] = bf16_hi(a.y);
+  v[4] = bf16_lo(b.x); v[5] = bf16_hi(b.x); v[6] = bf16_lo(b.y); v[7] = bf16_hi(b.y);
+}
+__device__ __forceinline__ void smem8(const float* p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+// Adjoint of one group for the stride-4 ring stencil (sparse_fold_ring_kernel's table):
+// b[c] = sum_{d=-3..3} xs[c][d] * erow[jb + d]; a centre away from theta 0 reads
+// erow[jb - 4 .. jb + 3] with two vector loads (jb is a multiple of 4).
+template <int NT, typename TE>
+__device__ __forceinline__ void group_adjoint_ring4(float* b, int vc, const float4* __restrict__ xs, int ring_len,
+                                                    const TE* er, int tid) {
+  for (int c0 = tid; c0 < vc; c0 += 2 * NT) {
+    float4 wa[2], wb[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int c = c0 + u * NT;
+      wa[u] = c < vc ? __ldg(xs + 2 * c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wb[u] = c < vc ? __ldg(xs + 2 * c + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int c = c0 + u * NT;
+      if (c < vc) {
+        const int info = __float_as_int(wb[u].w);
+        const int jb = info & 0x3fffffff;
+        float v[8];
+        if ((info >> 30) == 0) {
+          smem8(er + jb - 4, v);
+        } else {
+          v[0] = 0.f;
+#pragma unroll
+          for (int k = 1; k < 8; ++k) v[k] = to_float(er[jb + k - 4 + (k < 4 ? ring_len : 0)]);
+        }
+        const float w[7] = {wa[u].x, wa[u].y, wa[u].z, wa[u].w, wb[u].x, wb[u].y, wb[u].z};
+        float acc = 0.f;
+#pragma unroll
+        for (int d = 0; d < 7; ++d) acc = fmaf(w[d], v[d + 1], acc);
+        b[c] = acc;
+      }
+    }
+  }
+}
+
 // coarse rows of a batch held in registers between the dot and the q pass: four BF16 values
 // per chunk as a uint2 (float rows are re-read from shared memory instead)
 template <typename TC>
@@ -766,11 +843,23 @@ __device__ __forceinline__ void smem4(const float* p, int64_t c, float (&v)[4]) 
   v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
 }
 
-template <int MODE, int KT, typename TE, typename TC>
+// eight consecutive values (16-byte aligned; shared or global memory, plain loads)
+__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x); v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
+  v[4] = bf16_lo(u.z); v[5] = bf16_hi(u.z); v[6] = bf16_lo(u.w); v[7] = bf16_hi(u.w);
+}
+__device__ __forceinline__ void load8(const float* p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+template <int MODE, int KT, int RS, typename TE, typename TC>
 __global__ void __launch_bounds__(kBkThreads, 1)
 sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
                               const int32_t* __restrict__ grow, int n_groups, int vc,
-                              const int4* __restrict__ tp, int M, const TE* __restrict__ eff, int64_t ld_eff,
+                              const int4* __restrict__ tp, int M, const float4* __restrict__ xs, int ring_len,
+                              const TE* __restrict__ eff, int64_t ld_eff,
                               float* __restrict__ s_ev, float* __restrict__ q, int64_t ldq, int n_slots, int batch,
                               uint32_t erow_bytes,
                               uint32_t row_bytes, uint32_t b_off, uint32_t slot_off, uint32_t slot_stride) {
@@ -852,7 +941,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         ne1 = goff[gi + G + 1];
       }
       if (!bk_wait(erow_full, kg & 1, abort_flag)) bad = true;
-      group_adjoint_packed<KT, kBkConsumers, TE>(b, vc, tp, M, erow, ct);
+      if (RS == 4) group_adjoint_ring4<kBkConsumers, TE>(b, vc, xs, ring_len, erow, ct);
+      else group_adjoint_packed<KT, kBkConsumers, TE>(b, vc, tp, M, erow, ct);
       if (consumer_sync_or(bad)) {
         aborted = true;
         break;
@@ -1024,6 +1114,184 @@ sparse_group_scatter_kernel(const float* __restrict__ q, int64_t ldq, const int3
   part[(int64_t)blockIdx.y * ldp + j] = acc;
 }
 
+// Bulk-copy form of the scatter (same arithmetic and group order, so the same result).
+// CTA = one tile of kScTile fine voxels of one z plane x one chunk of groups; a producer warp
+// streams, per group, the sysmat row's tile and the q segment(s) the tile's lateral taps
+// touch ([lmin, lmax] of the tile, one segment per z tap) into a ring of stages; eight
+// consumer warps hold their voxels' taps and sums in registers (eight voxels per thread)
+// and read only shared memory. A tile whose tap span exceeds a segment reads q and the
+// sysmat from global memory instead (no producer). Waits are bounded as in the
+// coefficient kernel.
+constexpr int kScConsumers = 256;
+constexpr int kScThreads = kScConsumers + 32;
+constexpr int kScVox = 8;
+constexpr int kScTile = kScConsumers * kScVox;
+constexpr int kScSeg = 1024;  // coarse values per staged q segment
+constexpr int kScMaxStages = 16;
+constexpr int kScHeader = 384;  // 2 x kScMaxStages barriers, flags, tap span
+static_assert(16 * kScMaxStages + 20 <= kScHeader, "scatter header");
+
+template <typename TE>
+__global__ void __launch_bounds__(kScThreads, 2)
+sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const int32_t* __restrict__ grow,
+                                 int n_groups, int groups_per_chunk, const TE* __restrict__ eff, int64_t ld_eff,
+                                 int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp, int n_stages,
+                                 uint32_t stage_bytes, uint32_t seg_off) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kScMaxStages]
+  uint64_t* empty = full + kScMaxStages;               // [kScMaxStages]
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 16 * kScMaxStages);
+  int* issued = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 4);
+  int* used = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 8);
+  int* span = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 12);  // [lmin, lmax]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n_lf = taps.n_lf, n_lc = taps.n_lc;
+  const int tiles_per_plane = (n_lf + kScTile - 1) / kScTile;
+  const int zf = blockIdx.x / tiles_per_plane;
+  const int l_begin = (blockIdx.x - zf * tiles_per_plane) * kScTile;
+  const int l_end = min(l_begin + kScTile, n_lf);
+  const int64_t j0 = (int64_t)zf * n_lf + l_begin;
+  const int z0 = taps.zt[2 * zf], z1 = taps.zt[2 * zf + 1];
+  const float u0 = taps.zwt[2 * zf], u1 = taps.zwt[2 * zf + 1];
+  const bool two_z = u1 != 0.f;
+  const int g_begin = blockIdx.y * groups_per_chunk;
+  const int g_end = min(g_begin + groups_per_chunk, n_groups);
+  if (tid == 0) {
+    for (int s = 0; s < kScMaxStages; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, kScConsumers / 32);
+    }
+    *abort_flag = 0;
+    *issued = *used = 0;
+    span[0] = INT_MAX;
+    span[1] = -1;
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // this thread's voxels and their lateral taps
+  const int lf0 = l_begin + tid * kScVox;
+  int l0[kScVox], l1[kScVox];
+  float w0[kScVox], w1[kScVox];
+  if (tid < kScConsumers) {
+    int mn = INT_MAX, mx = -1;
+#pragma unroll
+    for (int v = 0; v < kScVox; ++v) {
+      const int lf = lf0 + v;
+      const bool in = lf < l_end;
+      l0[v] = in ? taps.lt[2 * lf] : 0;
+      l1[v] = in ? taps.lt[2 * lf + 1] : 0;
+      w0[v] = in ? taps.lwt[2 * lf] : 0.f;
+      w1[v] = in ? taps.lwt[2 * lf + 1] : 0.f;
+      if (in) {
+        mn = min(mn, min(l0[v], l1[v]));
+        mx = max(mx, max(l0[v], l1[v]));
+      }
+    }
+    if (mx >= 0) {
+      atomicMin(span, mn);
+      atomicMax(span + 1, mx);
+    }
+  }
+  __syncthreads();
+  const int cs0 = span[0] & ~3;
+  const int seg_len = span[1] < 0 ? 4 : ((span[1] + 1 - cs0 + 3) & ~3);
+  const bool staged = seg_len <= kScSeg;
+  const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
+  const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
+  auto stage = [&](int s) { return smem + kScHeader + (size_t)s * stage_bytes; };
+  if (warp == kScConsumers / 32) {
+    // ------------------------------------------------------------ producer warp
+    if (staged) {
+      bool ok = true;
+      for (int w = g_begin; w < g_end && ok; w += 32) {
+        const int gv = w + lane < g_end ? grow[w + lane] : 0;  // 32 group rows per load
+        const int m = min(32, g_end - w);
+        for (int k = 0; k < m && ok; ++k) {
+          const int row = __shfl_sync(0xffffffffu, gv, k);
+          const int kk = w - g_begin + k;
+          if (lane == 0) {
+            const int s = kk % n_stages;
+            if (kk >= n_stages) ok = bk_wait(empty + s, (kk / n_stages - 1) & 1, abort_flag);
+            if (ok) {
+              unsigned char* st = stage(s);
+              const float* qg = q + (int64_t)(w + k) * ldq;
+              mbar_arrive_expect_tx(full + s, a_bytes + seg_bytes * (two_z ? 2u : 1u));
+              bulk_copy_g2s(st, eff + clamp_row(row, n_det) * ld_eff + j0, a_bytes, full + s);
+              bulk_copy_g2s(st + seg_off, qg + (int64_t)z0 * n_lc + cs0, seg_bytes, full + s);
+              if (two_z) bulk_copy_g2s(st + seg_off + kScSeg * 4, qg + (int64_t)z1 * n_lc + cs0, seg_bytes, full + s);
+              *issued = kk + 1;
+            }
+          }
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+        }
+      }
+      if (!ok && lane == 0) *abort_flag = 1;
+    }
+  } else {
+    // ------------------------------------------------------------ consumer warps
+    float acc[kScVox];
+#pragma unroll
+    for (int v = 0; v < kScVox; ++v) acc[v] = 0.f;
+    bool bad = false;
+    for (int g = g_begin; g < g_end; ++g) {
+      const int kk = g - g_begin;
+      const int s = kk % n_stages;
+      const TE* ap;
+      const float *q0, *q1;
+      if (staged) {
+        if (!bk_wait(full + s, (kk / n_stages) & 1, abort_flag)) {
+          bad = true;
+          break;
+        }
+        unsigned char* st = stage(s);
+        ap = reinterpret_cast<const TE*>(st) + tid * kScVox;
+        q0 = reinterpret_cast<const float*>(st + seg_off) - cs0;
+        q1 = reinterpret_cast<const float*>(st + seg_off + kScSeg * 4) - cs0;
+      } else {
+        ap = eff + clamp_row(grow[g], n_det) * ld_eff + j0 + tid * kScVox;
+        q0 = q + (int64_t)g * ldq + (int64_t)z0 * n_lc;
+        q1 = q + (int64_t)g * ldq + (int64_t)z1 * n_lc;
+      }
+      if (lf0 < l_end) {
+        float a[kScVox];
+        load8(ap, a);
+#pragma unroll
+        for (int v = 0; v < kScVox; ++v) {
+          float t = w0[v] * q0[l0[v]];
+          t = fmaf(w1[v], q0[l1[v]], t);
+          float val = u0 * t;
+          if (two_z) {
+            float bb = w0[v] * q1[l0[v]];
+            bb = fmaf(w1[v], q1[l1[v]], bb);
+            val = fmaf(u1, bb, val);
+          }
+          if (val != 0.f) acc[v] = fmaf(a[v], val, acc[v]);
+        }
+      }
+      if (staged) {
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(empty + s);
+          if (warp == 0) *used = kk + 1;
+        }
+      }
+    }
+    if (bad) *abort_flag = 1;
+    if (!bad && lf0 < l_end) {
+      float* out = part + (int64_t)blockIdx.y * ldp + j0 + tid * kScVox;
+#pragma unroll
+      for (int v = 0; v < kScVox; ++v)
+        if (lf0 + v < l_end) out[v] = acc[v];
+    }
+  }
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
+    atomicAdd(&g_wait_timeout_count, 1u);
+    for (int kk = *used; kk < *issued; ++kk)
+      mbar_wait_bounded(full + kk % n_stages, (kk / n_stages) & 1, kBkMaxPolls);
+  }
+}
+
 static int64_t group_chunks(int64_t n_groups, int64_t vf) {
   const int64_t tiles = (vf + 255) / 256;
   int64_t chunks = (2432 + tiles - 1) / (tiles > 0 ? tiles : 1);  // ~16 CTAs x 152 SMs
@@ -1036,8 +1304,9 @@ static int64_t group_chunks(int64_t n_groups, int64_t vf) {
 template <typename TE, typename TC>
 static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_events, const int32_t* order,
                           const int32_t* goff, const int32_t* grow, int32_t n_groups, const TE* eff, int64_t ld_eff,
-                          const UpTaps& taps, const int32_t* tj, const float* tw, int K, int64_t vf, int64_t vc,
-                          int32_t mode, const float* x, float* s_ev, int have_sums, const int64_t* rotmat_inv,
+                          const UpTaps& taps, const int32_t* tj, const float* tw, int K, int ring_len,
+                          int ring_stride, int64_t vf, int64_t vc, int32_t mode, const float* x, float* s_ev,
+                          int have_sums, const int64_t* rotmat_inv,
                           int64_t ld_rot, float scale, float* weight, void* workspace, size_t workspace_bytes,
                           cudaStream_t st) {
   const int64_t ldp = (int64_t)align_up((size_t)vf, 8);
@@ -1082,11 +1351,28 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   const int M = (K + 1) / 2;
   int4* tpx = cv.take<int4>((size_t)M * vc);  // packed taps with x folded in
   int4* tpw = cv.take<int4>((size_t)M * vc);  // packed taps, weights only (row sums)
+  float4* xsx = cv.take<float4>((size_t)2 * vc);  // ring stencil, x folded in
+  float4* xsw = cv.take<float4>((size_t)2 * vc);  // ring stencil, weights only
   JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
+  // stride-4 ring stencil (checked by the caller against the tap table): centres multiples of 4
+  const bool ring = bulk && ring_stride == 4 && K == 7 && ring_len >= 8 && ring_len % 4 == 0 &&
+                    taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf && vf / taps.n_lf == vc / taps.n_lc &&
+                    vf < (1 << 30);
   {
     int64_t blocks = ((int64_t)K * vc + 255) / 256;
     if (blocks > (int64_t)num_sms() * 8) blocks = (int64_t)num_sms() * 8;
-    if (bulk) {
+    if (ring) {
+      JSCC_TIMED("sparse_fold_x", st,
+                 (sparse_fold_ring_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, K, (int)vc, taps.n_lc, taps.n_lf,
+                                                                            ring_len, x, xsx)));
+      JSCC_LAUNCH_CHECK();
+      if (mode == JSCC_SPARSE_MATERIALIZE && !have_sums) {
+        JSCC_TIMED("sparse_fold_x", st,
+                   (sparse_fold_ring_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, K, (int)vc, taps.n_lc,
+                                                                              taps.n_lf, ring_len, nullptr, xsw)));
+        JSCC_LAUNCH_CHECK();
+      }
+    } else if (bulk) {
       JSCC_TIMED("sparse_fold_x", st,
                  (sparse_fold_pack_kernel<<<(unsigned)blocks, 256, 0, st>>>(tj, tw, K, M, vc, x, tpx)));
       JSCC_LAUNCH_CHECK();
@@ -1102,16 +1388,16 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     }
   }
   cudaError_t attr = cudaSuccess;
-#define JSCC_GC_BK(MODE, KT, TP)                                                                                 \
+#define JSCC_GC_BK(MODE, KT, RS, TP, XS)                                                                         \
   do {                                                                                                           \
-    attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, KT, TE, TC>,                                 \
+    attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, KT, RS, TE, TC>,                             \
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                      \
     if (attr == cudaSuccess)                                                                                     \
       JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
-                 (sparse_group_coef_bulk_kernel<MODE, KT, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,      \
-                                                                     st>>>(                                      \
-                     rows, order, goff, grow, n_groups, (int)vc, TP, M, eff, ld_eff, s_ev, q, ldq, n_slots,      \
-                     batch, erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                              \
+                 (sparse_group_coef_bulk_kernel<MODE, KT, RS, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,  \
+                                                                         st>>>(                                  \
+                     rows, order, goff, grow, n_groups, (int)vc, TP, M, XS, ring_len, eff, ld_eff, s_ev, q, ldq, \
+                     n_slots, batch, erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                     \
   } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
@@ -1123,25 +1409,27 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
                      rows, vec_rows, order, goff, grow, n_groups, vc, tj, TW, K, eff, ld_eff, s_ev, coef, q,     \
                      ldq)));                                                                                     \
   } while (0)
-#define JSCC_GC(MODE, TW, TP)                                                                                    \
+#define JSCC_GC(MODE, TW, TP, XS)                                                                                \
   do {                                                                                                           \
-    if (bulk) {                                                                                                  \
-      if (K <= 4) JSCC_GC_BK(MODE, 4, TP);                                                                       \
-      else if (K <= 8) JSCC_GC_BK(MODE, 8, TP);                                                                  \
-      else JSCC_GC_BK(MODE, 0, TP);                                                                              \
+    if (ring) {                                                                                                  \
+      JSCC_GC_BK(MODE, 0, 4, TP, XS);                                                                            \
+    } else if (bulk) {                                                                                           \
+      if (K <= 4) JSCC_GC_BK(MODE, 4, 0, TP, XS);                                                                \
+      else if (K <= 8) JSCC_GC_BK(MODE, 8, 0, TP, XS);                                                           \
+      else JSCC_GC_BK(MODE, 0, 0, TP, XS);                                                                       \
     } else if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                   \
     else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
     else JSCC_GC_K(MODE, 0, TW);                                                                                 \
   } while (0)
   if (mode == JSCC_SPARSE_MATERIALIZE) {
     if (!have_sums) {
-      JSCC_GC(2, tw, tpw);  // S_i = t_i . adj(A_g), kept by the caller across calls
+      JSCC_GC(2, tw, tpw, xsw);  // S_i = t_i . adj(A_g), kept by the caller across calls
       JSCC_CUDA_CHECK(attr);
       JSCC_LAUNCH_CHECK();
     }
-    JSCC_GC(0, xw, tpx);
+    JSCC_GC(0, xw, tpx, xsx);
   } else {
-    JSCC_GC(1, xw, tpx);
+    JSCC_GC(1, xw, tpx, xsx);
   }
 #undef JSCC_GC
 #undef JSCC_GC_K
@@ -1149,16 +1437,47 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   JSCC_CUDA_CHECK(attr);
   JSCC_LAUNCH_CHECK();
   const int gpc = (int)((n_groups + chunks - 1) / chunks);
-  dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
-  JSCC_TIMED("sparse_group_scatter", st,
-             (sparse_group_scatter_kernel<TE><<<sgrid, 256, 0, st>>>(q, ldq, grow, n_groups, gpc, vf, eff, ld_eff,
-                                                                     rows.n_det, taps, part, ldp)));
+  // bulk scatter when the sysmat tiles and the q segments start on 16-byte boundaries
+  // (one q segment per stage when the coarse grid has one z plane, else two; stages to
+  // ~98 KB so that two CTAs share an SM)
+  const int n_zc = (int)(vc / taps.n_lc);
+  const uint32_t sc_a = (uint32_t)align_up((size_t)kScTile * sizeof(TE), 128);
+  const uint32_t sc_stage = sc_a + (n_zc > 1 ? 2u : 1u) * kScSeg * 4u;
+  int sc_stages = (int)((98u * 1024u - kScHeader) / sc_stage);
+  if (sc_stages > kScMaxStages) sc_stages = kScMaxStages;
+  if (sc_stages < 2) sc_stages = 2;
+  const size_t sc_smem = kScHeader + (size_t)sc_stages * sc_stage;
+  const bool sc_bulk = reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
+                       ((size_t)taps.n_lf * sizeof(TE)) % 16 == 0 && taps.n_lf % kScVox == 0 && taps.n_lc % 4 == 0 &&
+                       reinterpret_cast<uintptr_t>(q) % 16 == 0 && ldq % 4 == 0;
+  int64_t n_part = chunks;
+  if (sc_bulk) {
+    const int tiles = (int)(vf / taps.n_lf) * ((taps.n_lf + kScTile - 1) / kScTile);
+    // one wave: tiles x chunks <= two CTAs per SM (fewer chunks than the workspace allows)
+    int64_t sc_chunks = 2 * (int64_t)num_sms() / tiles;
+    if (sc_chunks > chunks) sc_chunks = chunks;
+    if (sc_chunks < 1) sc_chunks = 1;
+    const int sc_gpc = (int)((n_groups + sc_chunks - 1) / sc_chunks);
+    JSCC_CUDA_CHECK(cudaFuncSetAttribute(sparse_group_scatter_bulk_kernel<TE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem));
+    JSCC_TIMED("sparse_group_scatter", st,
+               (sparse_group_scatter_bulk_kernel<TE><<<dim3((unsigned)tiles, (unsigned)sc_chunks), kScThreads,
+                                                       sc_smem, st>>>(q, ldq, grow, n_groups, sc_gpc, eff, ld_eff,
+                                                                      rows.n_det, taps, part, ldp, sc_stages, sc_stage,
+                                                                      sc_a)));
+    n_part = sc_chunks;
+  } else {
+    dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
+    JSCC_TIMED("sparse_group_scatter", st,
+               (sparse_group_scatter_kernel<TE><<<sgrid, 256, 0, st>>>(q, ldq, grow, n_groups, gpc, vf, eff, ld_eff,
+                                                                       rows.n_det, taps, part, ldp)));
+  }
   JSCC_LAUNCH_CHECK();
   int64_t blocks = (vf + 255) / 256;
   if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
   const int has_scale = scale != 1.0f;
   JSCC_TIMED("sparse_reduce", st,
-             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, (int)chunks, rotmat_inv, ld_rot, vf,
+             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, (int)n_part, rotmat_inv, ld_rot, vf,
                                                                      has_scale, scale, weight)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
@@ -1337,7 +1656,7 @@ size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int
          align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) +
          align_up((size_t)chunks * ldp * sizeof(float), 256) +
          2 * align_up((size_t)((adj_width > 0 ? adj_width : 1) + 1) / 2 * (n_coarse > 0 ? n_coarse : 1) * 16, 256) +
-         256;
+         2 * align_up((size_t)(n_coarse > 0 ? n_coarse : 1) * 32, 256) + 256;
 }
 
 int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,
@@ -1346,10 +1665,12 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
                                float* event_sums, int32_t have_sums, const void* sysmat, int32_t sysmat_dtype,
                                int64_t ld_sysmat, int64_t n_det, const int32_t* z_taps, const float* z_tw, int32_t n_zf,
                                const int32_t* l_taps, const float* l_tw, int32_t n_lf, int32_t n_lc, int32_t n_zc,
-                               const int32_t* adj_idx, const float* adj_w, int32_t adj_width, int32_t mode,
-                               const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
-                               float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+                               const int32_t* adj_idx, const float* adj_w, int32_t adj_width, int32_t ring_len,
+                               int32_t ring_stride, int32_t mode, const float* img, const int64_t* rotmat,
+                               const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight, void* workspace,
+                               size_t workspace_bytes, void* stream) {
   JSCC_REQUIRE(n_events >= 0 && n_det > 0 && n_groups >= 0, "jscc_sparse_weight_grouped: bad sizes");
+  JSCC_REQUIRE(ring_len >= 0 && ring_stride >= 0, "jscc_sparse_weight_grouped: negative ring description");
   JSCC_REQUIRE(mode == JSCC_SPARSE_MATERIALIZE || mode == JSCC_SPARSE_GROUPED, "jscc_sparse_weight_grouped: mode");
   JSCC_REQUIRE(sysmat_dtype == JSCC_DTYPE_F32 || sysmat_dtype == JSCC_DTYPE_BF16, "jscc_sparse_weight_grouped: dtype");
   if (n_events == 0 || n_groups == 0) return JSCC_OK;
@@ -1389,7 +1710,8 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
                         reinterpret_cast<uintptr_t>(t_coarse) % 16 == 0;
 #define JSCC_GROUPED(TE, TC, ROWS)                                                                             \
   grouped_launch<TE, TC>(ROWS, vec_rows, n_events, order, group_offsets, group_rows, n_groups,                 \
-                         static_cast<const TE*>(sysmat), ld_sysmat, t, adj_idx, adj_w, adj_width, vf, vc, mode,  \
+                         static_cast<const TE*>(sysmat), ld_sysmat, t, adj_idx, adj_w, adj_width, ring_len,      \
+                         ring_stride, vf, vc, mode,                                                              \
                          x, event_sums, have_sums, rotmat_inv, ld_rot, scale, weight, workspace,                 \
                          workspace_bytes, st)
   if (packed_rows) {

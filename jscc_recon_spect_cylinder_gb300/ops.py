@@ -322,6 +322,35 @@ def _fixed_width_adjoint(z_expand, layer_expand, device):
     return (idx.t().contiguous().to(torch.int32).to(device), w.t().contiguous().to(device), int(idx.size(1)))
 
 
+def _ring_stencil(z_expand, layer_expand):
+    """(ring_len, 4) when the upsample's adjoint is a stride-4 ring stencil: z the identity
+    and, within each fine plane, rings of ring_len theta voxels where coarse voxel
+    lc = r * (ring_len / 4) + th has exactly the taps r * ring_len + (4 th + d) mod ring_len,
+    d = -3..3 (linear theta interpolation with stride 4, as the polar projector builds it);
+    else (0, 0)."""
+    ze = z_expand.detach().to("cpu", torch.float32)
+    le = layer_expand.detach().to("cpu", torch.float32)
+    if ze.size(0) != ze.size(1) or not torch.equal(ze, torch.eye(ze.size(0))):
+        return 0, 0
+    n_lf, n_lc = le.shape
+    if n_lc == 0 or n_lf != 4 * n_lc:
+        return 0, 0
+    li, lw = _padded_rows(le.t())
+    if li.size(1) != 7 or not bool((lw != 0).all()):
+        return 0, 0
+    ring_len = int(li[0].max()) + 1
+    if ring_len < 8 or ring_len % 4 or n_lf % ring_len:
+        return 0, 0
+    n_thc = ring_len // 4
+    lc = torch.arange(n_lc)
+    r, th = lc // n_thc, lc % n_thc
+    d = torch.arange(-3, 4)
+    expect = r[:, None] * ring_len + (4 * th[:, None] + d[None, :]) % ring_len
+    if not torch.equal(torch.sort(expect, dim=1).values, torch.sort(li, dim=1).values):
+        return 0, 0
+    return ring_len, 4
+
+
 class SparseTables:
     """Device tables of a ComptonSparseProjector: CSR forms of the four separable maps and
     the two-tap upsample arrays of the fused kernels, built from the projector's own
@@ -369,6 +398,7 @@ class SparseTables:
         self.z_taps, self.z_tw = two_taps(z_expand)
         self.l_taps, self.l_tw = two_taps(layer_expand)
         self.adj_idx, self.adj_w, self.adj_width = _fixed_width_adjoint(z_expand, layer_expand, device)
+        self.ring_len, self.ring_stride = _ring_stencil(z_expand, layer_expand)
 
 
 def sparse_map(rows_in, maps, n_zo, n_zi, n_lo, n_li, row_idx=None):
@@ -615,7 +645,8 @@ def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=N
         plan.n_groups, sums.data_ptr(), 1 if have else 0, A.data_ptr(), _dtype_code(A), A.stride(0), A.size(0),
         tables.z_taps.data_ptr(), tables.z_tw.data_ptr(), tables.n_zf, tables.l_taps.data_ptr(),
         tables.l_tw.data_ptr(), tables.n_lf, tables.n_lc, tables.n_zc, tables.adj_idx.data_ptr(),
-        tables.adj_w.data_ptr(), tables.adj_width, _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE,
+        tables.adj_w.data_ptr(), tables.adj_width, tables.ring_len, tables.ring_stride,
+        _lib.SPARSE_GROUPED if grouped else _lib.SPARSE_MATERIALIZE,
         x.data_ptr(), rm, ri, ld_rot, float(scale), out.data_ptr(), ws.data_ptr(), ws.numel(),
         _lib.stream_handle(dev))
     _lib.check(rc, "jscc_sparse_weight_grouped")

@@ -441,3 +441,30 @@ def test_grouped_bulk_pipeline(cuda, dtype, n_det, n_events):
         assert rel_l2(b.cpu(), a.cpu()) < TOL_W
         assert torch.equal(b, b2)
     assert _lib.take_wait_timeout_count() == 0
+
+
+def test_grouped_bulk_scatter_wide_rings(cuda):
+    """Two 8,192-theta rings on a stride-4 grid: the fine tile at the end of each ring, whose
+    lateral taps wrap around to coarse theta 0, spans more coarse voxels than one staged q
+    segment and is scattered from global memory, the other tiles from shared memory; both
+    match the per-event kernel."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    grid = synthetic.polar_grid(2, 8192, 30.0)
+    p = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1)
+    tb = cso.tables(p, cuda)
+    vc = p.coarse_pixel_num
+    g = torch.Generator().manual_seed(7)
+    n_det, n = 300, 1500
+    A = (torch.rand((n_det, grid.n_vox), generator=g) + 0.05).to(cuda).to(torch.bfloat16)
+    tc = (torch.rand((n, vc), generator=g) ** 3).to(cuda).to(torch.bfloat16)
+    ids = torch.randint(0, n_det, (n,), generator=g, dtype=torch.int32).to(cuda)
+    x = (torch.rand((grid.n_vox, 1), generator=g) + 0.2).to(cuda)
+    _lib.take_wait_timeout_count()
+    for grouped in (False, True):
+        a = ops.sparse_weight_split(ids, tc, A, tb, x, grouped=grouped, method="event")
+        b = ops.sparse_weight_split(ids, tc, A, tb, x, grouped=grouped)
+        torch.cuda.synchronize()
+        assert rel_l2(b.cpu(), a.cpu()) < TOL_W
+    assert _lib.take_wait_timeout_count() == 0

@@ -186,3 +186,28 @@ def test_fixed_width_adjoint_equals_dense_adjoint(golden):
     dense = U.t() @ x
     fw = (tb.adj_w.double() * x[tb.adj_idx.long()]).sum(0)
     assert torch.allclose(fw, dense, rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("n_r,n_theta,stride,z_stride,expect", [
+    (100, 360, 4, 1, (360, 4)), (12, 72, 4, 1, (72, 4)), (12, 72, 2, 1, (0, 0)), (12, 72, 8, 1, (0, 0))])
+def test_ring_stencil_detection(n_r, n_theta, stride, z_stride, expect):
+    """The stride-4 ring-stencil claim passed to the grouped kernel holds exactly for the
+    polar projector's stride-4 theta interpolation and for nothing else; a re-ordered
+    table (rings not in voxel order) is refused."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import ops, synthetic
+
+    grid = synthetic.polar_grid(n_r, n_theta, 30.0)
+    p = cso.build_compton_sparse_projector(grid.coor, stride, z_stride, rotate_num=1)
+    assert ops._ring_stencil(p.z_expand, p.layer_expand) == expect
+    if expect != (0, 0):
+        # the claimed taps are exactly the table's
+        ring_len = expect[0]
+        le = p.layer_expand
+        lc = torch.arange(le.size(1))
+        th, r = lc % (ring_len // 4), lc // (ring_len // 4)
+        for d in range(-3, 4):
+            j = r * ring_len + (4 * th + d) % ring_len
+            assert bool((le[j, lc] != 0).all())
+        perm = torch.randperm(le.size(1), generator=torch.Generator().manual_seed(0))
+        assert ops._ring_stencil(p.z_expand, le[:, perm]) == (0, 0)
