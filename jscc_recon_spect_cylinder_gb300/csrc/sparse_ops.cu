@@ -849,6 +849,20 @@ __device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&v)[8]) {
   v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x); v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
   v[4] = bf16_lo(u.z); v[5] = bf16_hi(u.z); v[6] = bf16_lo(u.w); v[7] = bf16_hi(u.w);
 }
+// two runs of four consecutive values at p and p + 128 (plain loads; p 8-byte aligned for
+// BF16, 16-byte aligned for float)
+template <typename T>
+__device__ __forceinline__ void load4x2(const T* p, float (&v)[8]) {
+  float a[4], b[4];
+  smem4(p, 0, a);
+  smem4(p + 128, 0, b);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[i] = a[i];
+    v[4 + i] = b[i];
+  }
+}
+
 __device__ __forceinline__ void load8(const float* p, float (&v)[8]) {
   const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
@@ -1168,15 +1182,18 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     mbar_init_fence();
   }
   __syncthreads();
-  // this thread's voxels and their lateral taps
-  const int lf0 = l_begin + tid * kScVox;
+  // this thread's voxels and their lateral taps: two runs of four, voxels
+  // (warp * 256 + h * 128 + lane * 4 + i), so that one tap of the warp's voxels reads
+  // consecutive q words (no bank conflicts) and each run is one 8-byte sysmat load
+  const int lf0 = l_begin + warp * (32 * kScVox) + lane * 4;
+  auto vox = [&](int v) { return lf0 + (v >> 2) * 128 + (v & 3); };
   int l0[kScVox], l1[kScVox];
   float w0[kScVox], w1[kScVox];
   if (tid < kScConsumers) {
     int mn = INT_MAX, mx = -1;
 #pragma unroll
     for (int v = 0; v < kScVox; ++v) {
-      const int lf = lf0 + v;
+      const int lf = vox(v);
       const bool in = lf < l_end;
       l0[v] = in ? taps.lt[2 * lf] : 0;
       l1[v] = in ? taps.lt[2 * lf + 1] : 0;
@@ -1195,6 +1212,12 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   __syncthreads();
   const int cs0 = span[0] & ~3;
   const int seg_len = span[1] < 0 ? 4 : ((span[1] + 1 - cs0 + 3) & ~3);
+  const bool run1 = lf0 + 128 < l_end;  // the second run of four is in the tile
+  if (tid < kScConsumers) {
+#pragma unroll
+    for (int v = 0; v < kScVox; ++v)
+      if (vox(v) >= l_end) l0[v] = l1[v] = cs0;  // (weight 0) keeps every gather inside the segment
+  }
   const bool staged = seg_len <= kScSeg;
   const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
   const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
@@ -1233,55 +1256,68 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
 #pragma unroll
     for (int v = 0; v < kScVox; ++v) acc[v] = 0.f;
     bool bad = false;
-    for (int g = g_begin; g < g_end; ++g) {
-      const int kk = g - g_begin;
-      const int s = kk % n_stages;
-      const TE* ap;
-      const float *q0, *q1;
-      if (staged) {
+    // acc[v] += a[v] * (u0 * (w0 q0[l0] + w1 q0[l1]) + u1 * (w0 q1[l0] + w1 q1[l1]))
+    auto accumulate = [&](const float (&a)[kScVox], const float* q0, const float* q1) {
+#pragma unroll
+      for (int v = 0; v < kScVox; ++v) {
+        float t = w0[v] * q0[l0[v]];
+        t = fmaf(w1[v], q0[l1[v]], t);
+        float val = u0 * t;
+        if (two_z) {
+          float bb = w0[v] * q1[l0[v]];
+          bb = fmaf(w1[v], q1[l1[v]], bb);
+          val = fmaf(u1, bb, val);
+        }
+        if (val != 0.f) acc[v] = fmaf(a[v], val, acc[v]);
+      }
+    };
+    if (staged) {
+      // shared-memory operands only (the pointers below are derived from the shared array)
+      for (int g = g_begin; g < g_end; ++g) {
+        const int kk = g - g_begin;
+        const int s = kk % n_stages;
         if (!bk_wait(full + s, (kk / n_stages) & 1, abort_flag)) {
           bad = true;
           break;
         }
         unsigned char* st = stage(s);
-        ap = reinterpret_cast<const TE*>(st) + tid * kScVox;
-        q0 = reinterpret_cast<const float*>(st + seg_off) - cs0;
-        q1 = reinterpret_cast<const float*>(st + seg_off + kScSeg * 4) - cs0;
-      } else {
-        ap = eff + clamp_row(grow[g], n_det) * ld_eff + j0 + tid * kScVox;
-        q0 = q + (int64_t)g * ldq + (int64_t)z0 * n_lc;
-        q1 = q + (int64_t)g * ldq + (int64_t)z1 * n_lc;
-      }
-      if (lf0 < l_end) {
-        float a[kScVox];
-        load8(ap, a);
-#pragma unroll
-        for (int v = 0; v < kScVox; ++v) {
-          float t = w0[v] * q0[l0[v]];
-          t = fmaf(w1[v], q0[l1[v]], t);
-          float val = u0 * t;
-          if (two_z) {
-            float bb = w0[v] * q1[l0[v]];
-            bb = fmaf(w1[v], q1[l1[v]], bb);
-            val = fmaf(u1, bb, val);
-          }
-          if (val != 0.f) acc[v] = fmaf(a[v], val, acc[v]);
+        if (lf0 < l_end) {
+          const TE* at = reinterpret_cast<const TE*>(st) + (lf0 - l_begin);
+          float a[kScVox];
+          load4x2(at, a);
+          accumulate(a, reinterpret_cast<const float*>(st + seg_off) - cs0,
+                     reinterpret_cast<const float*>(st + seg_off + kScSeg * 4) - cs0);
         }
-      }
-      if (staged) {
         __syncwarp();
         if (lane == 0) {
           mbar_arrive(empty + s);
           if (warp == 0) *used = kk + 1;
         }
       }
+    } else if (lf0 < l_end) {
+      for (int g = g_begin; g < g_end; ++g) {
+        float a[kScVox];
+        const TE* ag = eff + clamp_row(grow[g], n_det) * ld_eff + j0 + (lf0 - l_begin);
+        if (run1) {
+          load4x2(ag, a);
+        } else {  // the second run would read past the tile (and possibly the row)
+          float h[4];
+          smem4(ag, 0, h);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            a[i] = h[i];
+            a[4 + i] = 0.f;
+          }
+        }
+        accumulate(a, q + (int64_t)g * ldq + (int64_t)z0 * n_lc, q + (int64_t)g * ldq + (int64_t)z1 * n_lc);
+      }
     }
     if (bad) *abort_flag = 1;
-    if (!bad && lf0 < l_end) {
-      float* out = part + (int64_t)blockIdx.y * ldp + j0 + tid * kScVox;
+    if (!bad) {
+      float* out = part + (int64_t)blockIdx.y * ldp + (int64_t)zf * n_lf;
 #pragma unroll
       for (int v = 0; v < kScVox; ++v)
-        if (lf0 + v < l_end) out[v] = acc[v];
+        if (vox(v) < l_end) out[vox(v)] = acc[v];
     }
   }
   __syncthreads();

@@ -444,14 +444,14 @@ def test_grouped_bulk_pipeline(cuda, dtype, n_det, n_events):
 
 
 def test_grouped_bulk_scatter_wide_rings(cuda):
-    """Two 8,192-theta rings on a stride-4 grid: the fine tile at the end of each ring, whose
-    lateral taps wrap around to coarse theta 0, spans more coarse voxels than one staged q
-    segment and is scattered from global memory, the other tiles from shared memory; both
-    match the per-event kernel."""
+    """Two 8,208-theta rings on a stride-4 grid: fine tiles at the end of a ring, whose
+    lateral taps wrap around to coarse theta 0, span more coarse voxels than one staged q
+    segment and are scattered from global memory (the last one only partly filled), the
+    other tiles from shared memory; all match the per-event kernel."""
     from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
     from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
 
-    grid = synthetic.polar_grid(2, 8192, 30.0)
+    grid = synthetic.polar_grid(2, 8208, 30.0)
     p = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1)
     tb = cso.tables(p, cuda)
     vc = p.coarse_pixel_num
