@@ -661,27 +661,35 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
 // The same per-group computation with its operands staged in shared memory by bulk copies
 // (cp.async.bulk completing on mbarriers): each byte is read from HBM once, and the adjoint
 // gather, the event dots and the q accumulation read shared memory. One persistent CTA per
-// SM walks its groups gi = blockIdx.x, + gridDim.x, ... with two warp roles:
-//   producer (the last warp): runs ahead of the consumers, copying each group's sysmat row
-//     into `erow` once the previous group's adjoint has released it, and every event's
-//     coarse row into a ring of `n_slots` slots, each once its previous row was consumed;
-//   consumers (the other 15 warps): per group b = adjoint of erow, then batches of up to
-//     `batch` events: dots f_i = t_i . b (each thread four coarse values per 1,920, reduced
-//     per warp and then over warps in warp order), coefficients, q += c_i t_i in registers
-//     (events in order); q_g is stored at the end of the group.
-// Shared memory: header (barriers, dot partials, coefficients), erow[vf] TE, b[vc] float,
-// slots[n_slots][vc] TC. Every wait is bounded: on a timeout the CTA counts it
-// (jscc_take_wait_timeout_count), waits (bounded) for the copies it still has in flight and
-// returns.
+// SM walks its groups gi = blockIdx.x, + gridDim.x, ... (group k of the CTA) with three
+// warp roles that overlap:
+//   producer (warp 15): two copy streams, each issued as soon as its buffer is free: the
+//     group's sysmat row into `erow` (after the adjoint of group k - 1 released it) and
+//     every event's coarse row, in order, into a ring of `n_slots` slots;
+//   adjoint warps (7-14): b[k & 1] = adjoint of erow for group k, once the event warps
+//     have released that buffer (group k - 2);
+//   event warps (0-7): per group, batches of up to `batch` events: dots f_i = t_i . b
+//     (each thread four coarse values per 1,024, reduced per warp and then over warps in
+//     warp order), coefficients, q += c_i t_i in registers (events in order); q_g stored at
+//     the end of the group, then b[k & 1] released.
+// So group k + 1's adjoint and the copies of later rows proceed while group k's events are
+// processed. Shared memory: header (barriers, flags, dot partials, coefficients),
+// erow[vf] TE, b[2][vc] float, slots[n_slots][vc] TC. Every wait is bounded: on a timeout
+// the CTA counts it (jscc_take_wait_timeout_count), waits (bounded) for the copies it still
+// has in flight and returns.
 constexpr int kBkThreads = 512;
-constexpr int kBkConsumers = kBkThreads - 32;
-constexpr int kBkConsumerWarps = kBkConsumers / 32;
+constexpr int kBkEventWarps = 8;
+constexpr int kBkEvents = kBkEventWarps * 32;
+constexpr int kBkAdjWarps = 7;
+constexpr int kBkAdj = kBkAdjWarps * 32;
+constexpr int kBkProducerWarp = kBkEventWarps + kBkAdjWarps;
 constexpr int kBkMaxSlots = 8;
-constexpr int kBkMaxBatch = kBkMaxSlots / 2;
-constexpr int kBkQ = 6;  // q registers: chunks of four coarse values per consumer thread
-constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkConsumers;
+constexpr int kBkMaxBatch = 2;
+constexpr int kBkQ = 10;  // q registers: chunks of four coarse values per event thread
+constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkEvents;
 constexpr int kBkHeader = 1024;
 constexpr uint32_t kBkMaxPolls = 1u << 22;  // per wait
+static_assert(kBkProducerWarp * 32 + 32 == kBkThreads, "warp roles");
 
 __device__ unsigned int g_wait_timeout_count = 0;
 
@@ -689,19 +697,19 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// named barrier over the consumer warps only
-__device__ __forceinline__ void consumer_sync() {
-  asm volatile("bar.sync 1, %0;" ::"r"(kBkConsumers) : "memory");
+// named barrier `id` over `count` threads (the warps of one role)
+__device__ __forceinline__ void role_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-// named barrier over the consumer warps returning the OR of every consumer's `v` (the same
-// value in all of them, so a decision taken on it is uniform)
-__device__ __forceinline__ bool consumer_sync_or(bool v) {
+// named barrier returning the OR of every participant's `v` (the same value in all of them,
+// so a decision taken on it is uniform within the role)
+__device__ __forceinline__ bool role_sync_or(int id, int count, bool v) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(r)
-      : "r"((uint32_t)v), "r"(kBkConsumers)
+      : "r"((uint32_t)v), "r"(id), "r"(count)
       : "memory");
   return r != 0;
 }
@@ -774,20 +782,21 @@ __device__ __forceinline__ void smem8(const float* p, float (&v)[8]) {
 
 // Adjoint of one group for the stride-4 ring stencil (sparse_fold_ring_kernel's table):
 // b[c] = sum_{d=-3..3} xs[c][d] * erow[jb + d]; a centre away from theta 0 reads
-// erow[jb - 4 .. jb + 3] with two vector loads (jb is a multiple of 4).
-template <int NT, typename TE>
+// erow[jb - 4 .. jb + 3] with two vector loads (jb is a multiple of 4). U coarse voxels per
+// thread at a time, all their table loads issued first.
+template <int NT, typename TE, int U = 4>
 __device__ __forceinline__ void group_adjoint_ring4(float* b, int vc, const float4* __restrict__ xs, int ring_len,
                                                     const TE* er, int tid) {
-  for (int c0 = tid; c0 < vc; c0 += 2 * NT) {
-    float4 wa[2], wb[2];
+  for (int c0 = tid; c0 < vc; c0 += U * NT) {
+    float4 wa[U], wb[U];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < U; ++u) {
       const int c = c0 + u * NT;
       wa[u] = c < vc ? __ldg(xs + 2 * c) : make_float4(0.f, 0.f, 0.f, 0.f);
       wb[u] = c < vc ? __ldg(xs + 2 * c + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < U; ++u) {
       const int c = c0 + u * NT;
       if (c < vc) {
         const int info = __float_as_int(wb[u].w);
@@ -875,24 +884,26 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
                               const int4* __restrict__ tp, int M, const float4* __restrict__ xs, int ring_len,
                               const TE* __restrict__ eff, int64_t ld_eff,
                               float* __restrict__ s_ev, float* __restrict__ q, int64_t ldq, int n_slots, int batch,
-                              uint32_t erow_bytes,
-                              uint32_t row_bytes, uint32_t b_off, uint32_t slot_off, uint32_t slot_stride) {
+                              uint32_t erow_bytes, uint32_t row_bytes, uint32_t b_off, uint32_t b_stride,
+                              uint32_t slot_off, uint32_t slot_stride) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kBkMaxSlots]
   uint64_t* empty = full + kBkMaxSlots;                // [kBkMaxSlots]
   uint64_t* erow_full = empty + kBkMaxSlots;
   uint64_t* erow_empty = erow_full + 1;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 160);
-  int* rows_issued = reinterpret_cast<int*>(smem + 164);
-  int* erows_issued = reinterpret_cast<int*>(smem + 168);
-  int* rows_used = reinterpret_cast<int*>(smem + 172);
-  int* erows_used = reinterpret_cast<int*>(smem + 176);
-  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkConsumerWarps][kBkMaxBatch]
+  uint64_t* b_full = erow_empty + 1;  // [2]
+  uint64_t* b_empty = b_full + 2;     // [2]
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 192);
+  int* rows_issued = reinterpret_cast<int*>(smem + 196);
+  int* erows_issued = reinterpret_cast<int*>(smem + 200);
+  int* rows_used = reinterpret_cast<int*>(smem + 204);
+  int* erows_used = reinterpret_cast<int*>(smem + 208);
+  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkEventWarps][kBkMaxBatch]
   float* cs = reinterpret_cast<float*>(smem + 512);   // [kBkMaxBatch]
   TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
-  float* b = reinterpret_cast<float*>(smem + b_off);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = gridDim.x;
+  auto bbuf = [&](int k) { return reinterpret_cast<float*>(smem + b_off + (size_t)(k & 1) * b_stride); };
   auto slot = [&](int s) { return reinterpret_cast<const TC*>(smem + slot_off + (size_t)s * slot_stride); };
   if (tid == 0) {
     for (int s = 0; s < kBkMaxSlots; ++s) {
@@ -901,49 +912,107 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     }
     mbar_init(erow_full, 1);
     mbar_init(erow_empty, 1);
+    for (int h = 0; h < 2; ++h) {
+      mbar_init(b_full + h, 1);
+      mbar_init(b_empty + h, 1);
+    }
     *abort_flag = 0;
     *rows_issued = *erows_issued = *rows_used = *erows_used = 0;
     mbar_init_fence();
   }
   __syncthreads();
-  if (warp == kBkConsumerWarps) {
+  if (warp == kBkProducerWarp) {
     // ------------------------------------------------------------ producer warp
-    int pseq = 0, kg = 0;
+    // erow stream: group eg (k-th of the CTA: ek); row stream: event re of group rg
+    int eg = blockIdx.x, ek = 0;
+    int rg = blockIdx.x, re = 0, re_end = 0, pseq = 0;
+    if (rg < n_groups) {
+      re = goff[rg];
+      re_end = goff[rg + 1];
+    }
+    int win_base = INT_MIN, win_val = 0;  // 32 order values, one per lane
+    uint32_t idle = 0;
     bool ok = true;
-    for (int gi = blockIdx.x; gi < n_groups && ok; gi += G, ++kg) {
-      const int e0 = goff[gi], e1 = goff[gi + 1];
-      const TE* src = eff + clamp_row(grow[gi], rows.n_det) * ld_eff;
-      if (lane == 0) {
-        if (kg > 0) ok = bk_wait(erow_empty, (kg - 1) & 1, abort_flag);
-        if (ok) {
-          mbar_arrive_expect_tx(erow_full, erow_bytes);
-          bulk_copy_g2s(erow, src, erow_bytes, erow_full);
-          *erows_issued = kg + 1;
+    while (ok) {
+      while (rg < n_groups && re >= re_end) {  // next group with events
+        rg += G;
+        if (rg < n_groups) {
+          re = goff[rg];
+          re_end = goff[rg + 1];
+          win_base = INT_MIN;  // the window holds one group's events only
         }
       }
-      ok = __shfl_sync(0xffffffffu, ok, 0);
-      for (int w0 = e0; w0 < e1 && ok; w0 += 32) {
-        const int iv = w0 + lane < e1 ? order[w0 + lane] : 0;  // 32 event indices per load
-        const int m = min(32, e1 - w0);
-        for (int k = 0; k < m && ok; ++k, ++pseq) {
-          const int i = __shfl_sync(0xffffffffu, iv, k);
+      const bool rows_left = rg < n_groups, erows_left = eg < n_groups;
+      if (!rows_left && !erows_left) break;
+      bool progress = false;
+      if (erows_left) {
+        bool ready = ek == 0 || mbar_test_wait(erow_empty, (ek - 1) & 1);
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (ready) {
           if (lane == 0) {
-            const int s = pseq % n_slots;
-            if (pseq >= n_slots) ok = bk_wait(empty + s, (pseq / n_slots - 1) & 1, abort_flag);
-            if (ok) {
-              mbar_arrive_expect_tx(full + s, row_bytes);
-              bulk_copy_g2s(const_cast<TC*>(slot(s)), rows.coarse(i), row_bytes, full + s);
-              *rows_issued = pseq + 1;
-            }
+            mbar_arrive_expect_tx(erow_full, erow_bytes);
+            bulk_copy_g2s(erow, eff + clamp_row(grow[eg], rows.n_det) * ld_eff, erow_bytes, erow_full);
+            *erows_issued = ek + 1;
           }
-          ok = __shfl_sync(0xffffffffu, ok, 0);
+          eg += G;
+          ++ek;
+          progress = true;
         }
+      }
+      if (rows_left) {
+        const int s = pseq % n_slots;
+        bool ready = pseq < n_slots || mbar_test_wait(empty + s, (pseq / n_slots - 1) & 1);
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (ready) {
+          if (re < win_base || re >= win_base + 32) {  // refill the window of event indices
+            win_base = re;
+            win_val = re + lane < re_end ? order[re + lane] : 0;
+          }
+          const int i = __shfl_sync(0xffffffffu, win_val, re - win_base);
+          if (lane == 0) {
+            mbar_arrive_expect_tx(full + s, row_bytes);
+            bulk_copy_g2s(const_cast<TC*>(slot(s)), rows.coarse(i), row_bytes, full + s);
+            *rows_issued = pseq + 1;
+          }
+          ++pseq;
+          ++re;
+          progress = true;
+        }
+      }
+      if (progress) {
+        idle = 0;
+      } else if (++idle > kBkMaxPolls || *abort_flag) {
+        ok = false;
+      } else {
+        __nanosleep(64);  // neither buffer is free yet: leave the issue slots to the other warps
       }
     }
     if (!ok && lane == 0) *abort_flag = 1;
+  } else if (warp >= kBkEventWarps) {
+    // ------------------------------------------------------------ adjoint warps
+    const int at = tid - kBkEvents;
+    bool bad = false, aborted = false;
+    int kg = 0;
+    for (int gi = blockIdx.x; gi < n_groups; gi += G, ++kg) {
+      if (!bk_wait(erow_full, kg & 1, abort_flag)) bad = true;
+      if (kg >= 2 && !bk_wait(b_empty + (kg & 1), ((kg >> 1) - 1) & 1, abort_flag)) bad = true;
+      float* b = bbuf(kg);
+      if (RS == 4) group_adjoint_ring4<kBkAdj, TE>(b, vc, xs, ring_len, erow, at);
+      else group_adjoint_packed<KT, kBkAdj, TE>(b, vc, tp, M, erow, at);
+      if (role_sync_or(2, kBkAdj, bad)) {
+        aborted = true;
+        break;
+      }
+      if (at == 0) {
+        *erows_used = kg + 1;
+        mbar_arrive(erow_empty);  // the producer may refill erow
+        mbar_arrive(b_full + (kg & 1));
+      }
+    }
+    if (aborted) *abort_flag = 1;
   } else {
-    // ------------------------------------------------------------ consumer warps
-    const int ct = tid;
+    // ------------------------------------------------------------ event warps
+    const int et = tid;
     int seq = 0, kg = 0;
     bool aborted = false, bad = false;  // bad: one of this thread's waits gave up
     int ne0 = blockIdx.x < n_groups ? goff[blockIdx.x] : 0;
@@ -954,17 +1023,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         ne0 = goff[gi + G];
         ne1 = goff[gi + G + 1];
       }
-      if (!bk_wait(erow_full, kg & 1, abort_flag)) bad = true;
-      if (RS == 4) group_adjoint_ring4<kBkConsumers, TE>(b, vc, xs, ring_len, erow, ct);
-      else group_adjoint_packed<KT, kBkConsumers, TE>(b, vc, tp, M, erow, ct);
-      if (consumer_sync_or(bad)) {
-        aborted = true;
-        break;
-      }
-      if (ct == 0) {
-        mbar_arrive(erow_empty);  // the producer may refill erow
-        *erows_used = kg + 1;
-      }
+      const float* b = bbuf(kg);
+      if (!bk_wait(b_full + (kg & 1), (kg >> 1) & 1, abort_flag)) bad = true;
       float4 qa[kBkQ];
 #pragma unroll
       for (int u = 0; u < kBkQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -972,8 +1032,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         const int n = min(batch, e1 - bs);
         int64_t my_i = 0;
         float my_s = 0.f;
-        if (ct < n) {  // issued before the dots, used after them
-          my_i = order[bs + ct];
+        if (et < n) {  // issued before the dots, used after them
+          my_i = order[bs + et];
           if (MODE == 0) my_s = s_ev[my_i];
         }
         for (int k = 0; k < n; ++k) {
@@ -985,47 +1045,55 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k) rp[k] = slot((seq + k) % n_slots);
         RowChunk<TC> rc[kBkMaxBatch][kBkQ];
-        float acc[kBkMaxBatch];
+        float4 acc[kBkMaxBatch];  // four independent partial sums per event
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = 0.f;
+        for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < kBkQ; ++u) {
-          const int c = ct * 4 + u * (kBkConsumers * 4);
+          const int c = et * 4 + u * (kBkEvents * 4);
+          if (c < vc) {
+#pragma unroll
+            for (int k = 0; k < kBkMaxBatch; ++k)
+              if (k < n) rc[k][u].load(rp[k], c);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kBkQ; ++u) {
+          const int c = et * 4 + u * (kBkEvents * 4);
           if (c < vc) {
             const float4 bv = *reinterpret_cast<const float4*>(b + c);
 #pragma unroll
             for (int k = 0; k < kBkMaxBatch; ++k)
               if (k < n) {
                 float v[4];
-                rc[k][u].load(rp[k], c);
                 if (RowChunk<TC>::kKeep) rc[k][u].get(rp[k], c, v);
                 else smem4(rp[k], c, v);
-                acc[k] = fmaf(v[0], bv.x, acc[k]);
-                acc[k] = fmaf(v[1], bv.y, acc[k]);
-                acc[k] = fmaf(v[2], bv.z, acc[k]);
-                acc[k] = fmaf(v[3], bv.w, acc[k]);
+                acc[k].x = fmaf(v[0], bv.x, acc[k].x);
+                acc[k].y = fmaf(v[1], bv.y, acc[k].y);
+                acc[k].z = fmaf(v[2], bv.z, acc[k].z);
+                acc[k].w = fmaf(v[3], bv.w, acc[k].w);
               }
           }
         }
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k)
           if (k < n) {
-            const float f = warp_sum(acc[k]);
+            const float f = warp_sum((acc[k].x + acc[k].y) + (acc[k].z + acc[k].w));
             if (lane == 0) red[warp * kBkMaxBatch + k] = f;
           }
-        if (consumer_sync_or(bad)) {
+        if (role_sync_or(1, kBkEvents, bad)) {
           aborted = true;
           break;
         }
-        if (ct < n) {
+        if (et < n) {
           float f = 0.f;
-          for (int w = 0; w < kBkConsumerWarps; ++w) f += red[w * kBkMaxBatch + ct];
+          for (int w = 0; w < kBkEventWarps; ++w) f += red[w * kBkMaxBatch + et];
           if (MODE == 2) s_ev[my_i] = f;
-          else if (MODE == 0) cs[ct] = (isfinite(my_s) && my_s > 0.f) ? (1.0f / fmaxf(f / my_s, 1e-12f)) / my_s : 0.f;
-          else cs[ct] = 1.0f / fmaxf(f, 1e-12f);
+          else if (MODE == 0) cs[et] = (isfinite(my_s) && my_s > 0.f) ? (1.0f / fmaxf(f / my_s, 1e-12f)) / my_s : 0.f;
+          else cs[et] = 1.0f / fmaxf(f, 1e-12f);
         }
         if (MODE != 2) {
-          consumer_sync();
+          role_sync(1, kBkEvents);
           // ---- q_g += c_i t_i over the batch, events in order
 #pragma unroll
           for (int k = 0; k < kBkMaxBatch; ++k)
@@ -1034,7 +1102,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
               if (ck != 0.f) {
 #pragma unroll
                 for (int u = 0; u < kBkQ; ++u) {
-                  const int c = ct * 4 + u * (kBkConsumers * 4);
+                  const int c = et * 4 + u * (kBkEvents * 4);
                   if (c < vc) {
                     float v[4];
                     rc[k][u].get(rp[k], c, v);
@@ -1047,24 +1115,30 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
               }
             }
         }
-        consumer_sync();  // the batch's slots, partials and coefficients are free
-        if (ct == 0) {
+        role_sync(1, kBkEvents);  // the batch's slots, partials and coefficients are free
+        if (et == 0) {
           for (int k = 0; k < n; ++k) mbar_arrive(empty + (seq + k) % n_slots);
           *rows_used = seq + n;
         }
         seq += n;
       }
       if (aborted) break;
+      if (e0 == e1 && role_sync_or(1, kBkEvents, bad)) {  // no batch consumed the b wait's status
+        aborted = true;
+        break;
+      }
+      // every event thread is past its last read of b (the last batch's barrier)
+      if (et == 0) mbar_arrive(b_empty + (kg & 1));
       if (MODE != 2) {
         float* qg = q + (int64_t)gi * ldq;
 #pragma unroll
         for (int u = 0; u < kBkQ; ++u) {
-          const int c = ct * 4 + u * (kBkConsumers * 4);
+          const int c = et * 4 + u * (kBkEvents * 4);
           if (c < vc) *reinterpret_cast<float4*>(qg + c) = qa[u];
         }
       }
     }
-    if (aborted) *abort_flag = 1;  // stops the producer
+    if (aborted) *abort_flag = 1;  // stops the other roles
   }
   __syncthreads();
   if (*abort_flag && tid == 0) {
@@ -1151,7 +1225,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
                                  int n_groups, int groups_per_chunk, const TE* __restrict__ eff, int64_t ld_eff,
                                  int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp, int n_stages,
                                  uint32_t stage_bytes, uint32_t seg_off) {
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kScMaxStages]
   uint64_t* empty = full + kScMaxStages;               // [kScMaxStages]
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 16 * kScMaxStages);
@@ -1367,7 +1441,8 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   // shared memory
   const uint32_t erow_bytes = (uint32_t)((size_t)vf * sizeof(TE)), row_bytes = (uint32_t)((size_t)vc * sizeof(TC));
   const uint32_t b_off = (uint32_t)align_up(kBkHeader + align_up(erow_bytes, 128), 128);
-  const uint32_t slot_off = (uint32_t)(b_off + align_up((size_t)vc * 4, 128));
+  const uint32_t b_stride = (uint32_t)align_up((size_t)vc * 4, 128);
+  const uint32_t slot_off = b_off + 2 * b_stride;
   const uint32_t slot_stride = (uint32_t)align_up(row_bytes, 128);
   const size_t bk_limit = 227 * 1024;
   int n_slots = 0;
@@ -1375,7 +1450,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     n_slots = (int)((bk_limit - slot_off) / (size_t)slot_stride);
     if (n_slots > kBkMaxSlots) n_slots = kBkMaxSlots;
   }
-  const int batch = n_slots / 2;
+  const int batch = n_slots / 2 < kBkMaxBatch ? n_slots / 2 : kBkMaxBatch;
   const bool bulk = rows.packed == nullptr && n_slots >= 2 && vc <= kBkMaxCoarse &&
                     (size_t)vf * sizeof(TE) < (1u << 20) && reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 &&
                     (rows.ld * sizeof(TC)) % 16 == 0 && row_bytes % 16 == 0 &&
@@ -1433,7 +1508,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
                  (sparse_group_coef_bulk_kernel<MODE, KT, RS, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,  \
                                                                          st>>>(                                  \
                      rows, order, goff, grow, n_groups, (int)vc, TP, M, XS, ring_len, eff, ld_eff, s_ev, q, ldq, \
-                     n_slots, batch, erow_bytes, row_bytes, b_off, slot_off, slot_stride)));                     \
+                     n_slots, batch, erow_bytes, row_bytes, b_off, b_stride, slot_off, slot_stride)));           \
   } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
