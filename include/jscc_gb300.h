@@ -310,9 +310,10 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * order [n_events] (event indices sorted by row), group_offsets [n_groups + 1] into order,
  * group_rows [n_groups] (0-based sysmat rows), and the adjoint as a fixed-width tap table
  * adj_idx / adj_w [adj_width, V_c] (fine index and weight of each tap of coarse voxel c;
- * padding taps have weight 0). event_sums [n_events] holds S_i in MATERIALIZE mode: it is
- * computed when have_sums == 0 and only read when have_sums != 0 (S_i depends on the rows
- * and the sysmat only, so callers keep it across iterations). The coarse grid must fit in
+ * padding taps have weight 0). event_sums [n_events] holds S_i in MATERIALIZE mode, stored
+ * by position in `order` (event_sums[p] = S_order[p]): it is computed when have_sums == 0
+ * and only read when have_sums != 0 (S_i depends on the rows, the sysmat and the grouping
+ * only, so callers keep it across iterations with the same `order`). The coarse grid must fit in
  * shared memory (V_c floats <= 227 KB). Deterministic (fixed-order reductions).
  * With split rows whose starts and lengths are 16-byte aligned (and a 16-byte aligned
  * sysmat row pitch) the per-group step streams the sysmat row and the coarse rows into

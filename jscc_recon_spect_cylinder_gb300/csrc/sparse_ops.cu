@@ -618,9 +618,9 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
       const float f = warp_row_dot<TC>(rows.coarse(i), b, vc, vec_rows, lane);
       if (lane == 0) {
         if (MODE == 2) {
-          s_ev[i] = f;
+          s_ev[e] = f;  // event sums are kept by position in `order`
         } else if (MODE == 0) {
-          const float si = s_ev[i];
+          const float si = s_ev[e];
           coef[i] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
         } else {
           coef[i] = 1.0f / fmaxf(f, 1e-12f);
@@ -687,7 +687,7 @@ constexpr int kBkMaxSlots = 8;
 constexpr int kBkMaxBatch = 2;
 constexpr int kBkQ = 10;  // q registers: chunks of four coarse values per event thread
 constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkEvents;
-constexpr int kBkHeader = 1024;
+constexpr int kBkHeader = 2048;  // barriers, flags, dot partials, coefficients, group event sums
 constexpr uint32_t kBkMaxPolls = 1u << 22;  // per wait
 static_assert(kBkProducerWarp * 32 + 32 == kBkThreads, "warp roles");
 
@@ -900,6 +900,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
   int* erows_used = reinterpret_cast<int*>(smem + 208);
   float* red = reinterpret_cast<float*>(smem + 256);  // [kBkEventWarps][kBkMaxBatch]
   float* cs = reinterpret_cast<float*>(smem + 512);   // [kBkMaxBatch]
+  float* s_grp = reinterpret_cast<float*>(smem + 1024);  // [kBkEvents] event sums of the group
   TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = gridDim.x;
@@ -1015,14 +1016,24 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     const int et = tid;
     int seq = 0, kg = 0;
     bool aborted = false, bad = false;  // bad: one of this thread's waits gave up
-    int ne0 = blockIdx.x < n_groups ? goff[blockIdx.x] : 0;
-    int ne1 = blockIdx.x < n_groups ? goff[blockIdx.x + 1] : 0;
+    // software pipeline over groups: the event range of group k + 2 and the event sums of
+    // group k + 1 (this thread's event of it) are loaded while group k is processed
+    auto range = [&](int g, int& a, int& e) {
+      a = g < n_groups ? goff[g] : 0;
+      e = g < n_groups ? goff[g + 1] : 0;
+    };
+    int r0a, r0e, r1a, r1e;
+    range(blockIdx.x, r0a, r0e);
+    range(blockIdx.x + G, r1a, r1e);
+    float s_next = (MODE == 0 && r0a + et < r0e) ? s_ev[r0a + et] : 0.f;
     for (int gi = blockIdx.x; gi < n_groups && !aborted; gi += G, ++kg) {
-      const int e0 = ne0, e1 = ne1;
-      if (gi + G < n_groups) {  // the next group's range, fetched a group ahead
-        ne0 = goff[gi + G];
-        ne1 = goff[gi + G + 1];
-      }
+      const int e0 = r0a, e1 = r0e;
+      const float s_mine = s_next;
+      r0a = r1a;
+      r0e = r1e;
+      range(gi + 2 * G, r1a, r1e);
+      s_next = (MODE == 0 && r0a + et < r0e) ? s_ev[r0a + et] : 0.f;
+      if (MODE == 0) s_grp[et] = s_mine;  // read after the first batch barrier
       const float* b = bbuf(kg);
       if (!bk_wait(b_full + (kg & 1), (kg >> 1) & 1, abort_flag)) bad = true;
       float4 qa[kBkQ];
@@ -1030,12 +1041,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       for (int u = 0; u < kBkQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
       for (int bs = e0; bs < e1; bs += batch) {
         const int n = min(batch, e1 - bs);
-        int64_t my_i = 0;
-        float my_s = 0.f;
-        if (et < n) {  // issued before the dots, used after them
-          my_i = order[bs + et];
-          if (MODE == 0) my_s = s_ev[my_i];
-        }
+        // event sums beyond the first kBkEvents of a group are read here (issued before the dots)
+        const float s_far = (MODE == 0 && et < n && bs + et - e0 >= kBkEvents) ? s_ev[bs + et] : 0.f;
         for (int k = 0; k < n; ++k) {
           const int sq = seq + k;
           if (!bk_wait(full + sq % n_slots, (sq / n_slots) & 1, abort_flag)) bad = true;
@@ -1088,9 +1095,15 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         if (et < n) {
           float f = 0.f;
           for (int w = 0; w < kBkEventWarps; ++w) f += red[w * kBkMaxBatch + et];
-          if (MODE == 2) s_ev[my_i] = f;
-          else if (MODE == 0) cs[et] = (isfinite(my_s) && my_s > 0.f) ? (1.0f / fmaxf(f / my_s, 1e-12f)) / my_s : 0.f;
-          else cs[et] = 1.0f / fmaxf(f, 1e-12f);
+          if (MODE == 2) {
+            s_ev[bs + et] = f;  // event sums are kept by position in `order`
+          } else if (MODE == 0) {
+            const int p = bs + et - e0;
+            const float si = p < kBkEvents ? s_grp[p] : s_far;
+            cs[et] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
+          } else {
+            cs[et] = 1.0f / fmaxf(f, 1e-12f);
+          }
         }
         if (MODE != 2) {
           role_sync(1, kBkEvents);

@@ -568,7 +568,7 @@ class GroupPlan:
         self.offsets = offsets.to(torch.int32).contiguous()
         self.rows = rows.to(torch.int32).contiguous()
         self.n_groups = int(rows.numel())
-        self.sums = {}  # per sysmat key: S_i of the materialise form
+        self.sums = {}  # per sysmat key: S of the materialise form, by position in `order`
 
 
 def _group_plan(key_tensor, row_ids_fn):
