@@ -263,6 +263,7 @@ class JointBench:
         w = self.w
         return {"workload": self.name, "sc_bins": w.B, "voxels": w.V, "coarse_voxels": w.Vc,
                 "compton_events_listed": w.n_list, "compton_events_kept": w.n_events, "subsets": w.subsets,
+                "groups_per_subset": round(w.group_count(), 1),
                 "alpha": w.alpha, "views": w.views,
                 "storage": "bf16 system matrix + bf16 sparse rows (int32 ids split out)",
                 "l2": "inputs larger than L2 (no flush)"}

@@ -113,6 +113,23 @@ JSCC_API int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const i
                    size_t workspace_bytes, void* stream);
 
 /*
+ * SC sensitivity (column sums of the system matrix through the inverse rotations):
+ *
+ *   weight[j] += (sum_{r < n_rot} colsum(A)[rotmat_inv[j * ld_rot + r] - 1]) / n_rot,
+ *   colsum(A)[c] = sum_b A[rb, c]   (rb = row_idx ? row_idx[b] : b)
+ *
+ * Replaces main_local_cntstat.py:140-146 (compute_sensitivity_local) and the s_map_s loop of
+ * main_plane_sparse.py:440-444 (one call per energy; the caller sums energies). rotmat_inv
+ * NULL means the identity (n_rot must then be 1). Workspace:
+ * jscc_sc_weight_workspace_bytes(n_bins, n_vox, 1). The sum over rows runs in a fixed
+ * chunk order (deterministic).
+ */
+JSCC_API int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, int32_t n_rot, const int64_t* rotmat_inv,
+                   int64_t ld_rot, float* weight, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/*
  * jscc_sc_weight without a workspace: the same computation and arguments minus
  * (workspace, workspace_bytes). No counterpart in the reference (its PyTorch code
  * allocates freely); it exists for callers that cannot allocate device memory — a

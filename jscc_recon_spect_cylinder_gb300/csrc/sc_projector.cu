@@ -434,6 +434,37 @@ __global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t
   }
 }
 
+// SC sensitivity: s[j] += (sum_r colsum[rotinv[j, r] - 1]) / n_rot, colsum[c] = the chunk
+// partials of column c summed in chunk order (rotations summed first, then divided, as
+// main_local_cntstat.py:140-146 does).
+__global__ void sc_fill_kernel(float* __restrict__ p, int64_t n, float v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void sc_sensitivity_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
+                                      const int64_t* __restrict__ rotinv, int64_t ld_rot, int n_rot, int64_t V,
+                                      float* __restrict__ weight) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int r = 0; r < n_rot; ++r) {
+      int64_t src = j;
+      if (rotinv != nullptr) {
+        src = rotinv[j * ld_rot + r] - 1;
+        if (src < 0 || src >= V) {
+          atomicAdd(&g_bad_index_count, 1u);
+          continue;
+        }
+      }
+      float s = 0.f;
+      for (int c = 0; c < chunks; ++c) s += part[(int64_t)c * ldp + src];
+      acc = __fadd_rn(acc, s);
+    }
+    weight[j] = __fadd_rn(weight[j], __fdiv_rn(acc, (float)n_rot));
+  }
+}
+
 // ------------------------------------------------------------------ host planning
 struct ScPlan {
   int rb;                  // rotation block (1, 2, 4, 8)
@@ -620,11 +651,73 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
   return JSCC_OK;
 }
 
+template <typename T>
+static int sc_sensitivity_typed(const T* A, int64_t lda, const int64_t* row_idx, int64_t n_bins, int64_t V,
+                                int n_rot, const int64_t* rotinv, int64_t ld_rot, float* weight, const ScPlan& p,
+                                float* ratio, float* part, cudaStream_t st) {
+  constexpr int NV = VecTraits<T>::kVec;
+  const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) && (reinterpret_cast<uintptr_t>(A) % 16 == 0);
+  const int sms = num_sms();
+  int64_t blocks = (n_bins + 255) / 256;
+  if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+  if (blocks < 1) blocks = 1;
+  JSCC_TIMED("sc_fill", st, sc_fill_kernel<<<(unsigned)blocks, 256, 0, st>>>(ratio, n_bins, 1.0f));
+  JSCC_LAUNCH_CHECK();
+  dim3 grid((unsigned)p.col_tiles, (unsigned)p.chunks);
+  const int threads = kColTile / NV;
+  JSCC_TIMED("sc_back_partial", st, {
+    if (vec_ok)
+      sc_back_partial_kernel<T, 1, true><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, ratio, 1,
+                                                                   p.rows_per_chunk, part, p.ldx);
+    else
+      sc_back_partial_kernel<T, 1, false><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, ratio, 1,
+                                                                    p.rows_per_chunk, part, p.ldx);
+  });
+  JSCC_LAUNCH_CHECK();
+  blocks = (V + 255) / 256;
+  if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+  if (blocks < 1) blocks = 1;
+  JSCC_TIMED("sc_sensitivity", st,
+             sc_sensitivity_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldx, (int)p.chunks, rotinv, ld_rot,
+                                                                     n_rot, V, weight));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
 }  // namespace jscc
 
 using namespace jscc;
 
 extern "C" {
+
+int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx, int64_t n_bins,
+                        int64_t n_vox, int32_t n_rot, const int64_t* rotmat_inv, int64_t ld_rot, float* weight,
+                        void* workspace, size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0, "jscc_sc_sensitivity: negative size");
+  JSCC_REQUIRE(n_rot >= 1, "jscc_sc_sensitivity: n_rot must be >= 1 (got %d)", n_rot);
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16, "jscc_sc_sensitivity: unsupported a_dtype %d",
+               a_dtype);
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(A && weight, "jscc_sc_sensitivity: null pointer argument");
+  JSCC_REQUIRE(lda >= n_vox, "jscc_sc_sensitivity: lda (%lld) < n_vox (%lld)", (long long)lda, (long long)n_vox);
+  JSCC_REQUIRE(rotmat_inv != nullptr || n_rot == 1, "jscc_sc_sensitivity: n_rot > 1 needs rotmat_inv");
+  JSCC_REQUIRE(rotmat_inv == nullptr || ld_rot >= n_rot, "jscc_sc_sensitivity: ld_rot (%lld) < n_rot (%d)",
+               (long long)ld_rot, n_rot);
+  const ScPlan p = plan_sc(n_bins, n_vox, 1);
+  JSCC_REQUIRE(workspace != nullptr && workspace_bytes >= p.ws_bytes,
+               "jscc_sc_sensitivity: workspace too small (%zu < %zu bytes)", workspace_bytes, p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  cv.take<float>((size_t)p.rb * p.ldx);
+  float* ratio = cv.take<float>((size_t)n_bins * p.rb);
+  float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  JSCC_REQUIRE(cv.ok(), "jscc_sc_sensitivity: workspace carve overflow");
+  cudaStream_t st = as_stream(stream);
+  if (a_dtype == JSCC_DTYPE_F32)
+    return sc_sensitivity_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, n_rot, rotmat_inv,
+                                       ld_rot, weight, p, ratio, part, st);
+  return sc_sensitivity_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox,
+                                             n_rot, rotmat_inv, ld_rot, weight, p, ratio, part, st);
+}
 
 size_t jscc_sc_weight_workspace_bytes(int64_t n_bins, int64_t n_vox, int32_t n_rot) {
   return plan_sc(n_bins, n_vox, n_rot).ws_bytes;

@@ -153,6 +153,39 @@ def sc_weight(
     return out
 
 
+def sc_sensitivity(sysmat: torch.Tensor, rotmat_inv: torch.Tensor | None = None, n_rot: int | None = None,
+                   out: torch.Tensor | None = None, row_idx: torch.Tensor | None = None) -> torch.Tensor:
+    """``out += (sum_r colsum(A)[rotmat_inv[:, r] - 1]) / n_rot`` over the first ``n_rot``
+    columns of ``rotmat_inv`` (identity when None): the SC sensitivity of
+    main_local_cntstat.py:140-146 / main_plane_sparse.py:440-444, on the device."""
+    dev = _lib.require_cuda(sysmat, rotmat_inv, out, row_idx, what="sc_sensitivity")
+    if sysmat.dim() != 2:
+        raise ValueError("sysmat must be 2-D [bins, voxels]")
+    A = _rows_contig(sysmat)
+    n_rows, n_vox = A.shape
+    if row_idx is not None:
+        row_idx = row_idx.to(torch.int64).contiguous()
+    n_bins = n_rows if row_idx is None else row_idx.numel()
+    ri = _index_table(rotmat_inv, n_vox, "rotmat_inv")
+    if ri is None:
+        n_rot = 1
+    elif n_rot is None:
+        n_rot = ri.size(1)
+    if n_rot < 1 or (ri is not None and n_rot > ri.size(1)):
+        raise ValueError(f"n_rot={n_rot} out of range")
+    if out is None:
+        out = torch.zeros((n_vox, 1), dtype=torch.float32, device=dev)
+    if out.dtype != torch.float32 or not out.is_contiguous() or out.numel() != n_vox:
+        raise ValueError("out must be a contiguous float32 tensor with one entry per voxel")
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sc_weight_workspace_bytes(n_bins, n_vox, 1))
+    rc = lib.jscc_sc_sensitivity(A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins, n_vox,
+                                 n_rot, _lib.ptr(ri), 0 if ri is None else ri.stride(0), out.data_ptr(),
+                                 ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sc_sensitivity")
+    return out
+
+
 def em_update(
     img: torch.Tensor,
     weight: torch.Tensor,
@@ -579,6 +612,18 @@ def _group_plan(key_tensor, row_ids_fn):
     plan = GroupPlan(row_ids_fn())
     key_tensor._jscc_group_plan = (key_tensor._version, plan)
     return plan
+
+
+def sparse_sensitivity(sysmat, tables: SparseTables, rows=None, row_id=None, t_coarse=None, out=None):
+    """``out += sum_i t_norm,i``: the sum over events of the normalised fine rows of
+    materialize_sparse_event_rows_to_fine (compton_sparse_ops.py:380-400), i.e. the Compton
+    sensitivity of main_local_sparse_jsccsd_only.py:95-108. It is the materialise-form
+    weight at x = 1: there f_i = S_i, so every valid event gets c_i = 1 / S_i."""
+    vf = tables.n_zf * tables.n_lf
+    ones = torch.ones((vf, 1), dtype=torch.float32, device=sysmat.device)
+    if rows is not None:
+        return sparse_weight(rows, sysmat, tables, ones, grouped=False, out=out)
+    return sparse_weight_split(row_id, t_coarse, sysmat, tables, ones, grouped=False, out=out)
 
 
 def grouped_fits(tables: SparseTables) -> bool:

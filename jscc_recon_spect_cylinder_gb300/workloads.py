@@ -70,7 +70,7 @@ class JointWorkload:
         # the same rows in the same order as the copied subsets)
         self.A = {"f32": A}
         self.A["bf16"] = A.to(torch.bfloat16)
-        s_sc = A.sum(dim=0, keepdim=True).transpose(0, 1).contiguous()
+        s_sc = ops.sc_sensitivity(A)  # column sums (views are rows of the flat matrix)
         # ---------------- Compton channel
         abs_views = [synthetic.cylinder_pixels(ABS_R, N_PHI, N_AXIAL, AXIAL_PITCH, 2 * math.pi * v / views, device)
                      for v in range(views)]
@@ -115,11 +115,11 @@ class JointWorkload:
         # ---------------- sensitivities: s (SC column sums), d (Compton, build_sparse_sensi_d
         # rescaling: sum(d) = sum(s) * E_C / E_S), joint s_j = alpha s + (2 - alpha) d
         d = torch.zeros((self.V, 1), dtype=torch.float32, device=device)
-        for p in (self.rows_f32 or []):
-            for a in range(0, p.size(0), 8192):
-                fine, rsum = ops.sparse_materialize(p[a:a + 8192], A, self.tables)
-                ok = torch.isfinite(rsum) & (rsum > 0)
-                d += (fine[ok] / rsum[ok].unsqueeze(1)).sum(dim=0).unsqueeze(1)
+        for k in range(subsets):
+            if self.rows_f32 is not None:
+                ops.sparse_sensitivity(A, self.tables, rows=self.rows_f32[k], out=d)
+            else:
+                ops.sparse_sensitivity(A, self.tables, row_id=self.ids[k], t_coarse=self.tc_bf16[k], out=d)
         if d.sum() > 0:
             d = d * s_sc.sum() / d.sum() * (self.n_events / max(float(self.proj.sum()), 1.0))
         else:
@@ -191,11 +191,18 @@ class JointWorkload:
         return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4}
 
     def sparse_kernel_bytes(self, dtype):
-        """Algorithmic bytes of one sparse forward / back launch: every coarse row of the
-        subset once plus one efficiency row per distinct first-hit row."""
+        """Algorithmic bytes of one launch of the grouped sparse kernels (one subset, the
+        subset's mean event and group counts): sparse_group_coef reads every coarse row and
+        its event sum once and one sysmat row per group (distinct first-hit row), and writes
+        q (float32 [groups, V_c]); sparse_group_scatter reads one sysmat row and one q row per
+        group and writes one float32 partial image per group chunk (16 chunks)."""
         b = 2 if dtype == "bf16" else 4
         ev = self.n_events / self.subsets
-        distinct = float(sum(torch.unique(i).numel() for i in self.ids)) / self.subsets
-        coarse = ev * (self.Vc * b + 4)
-        eff = distinct * self.V * b
-        return {"sparse_forward": coarse + eff + self.V * 4, "sparse_back": coarse + eff}
+        groups = float(sum(torch.unique(i).numel() for i in self.ids)) / self.subsets
+        coef = ev * (self.Vc * b + 4) + groups * (self.V * b + self.Vc * 4)
+        scatter = groups * (self.V * b + self.Vc * 4) + 16 * self.V * 4
+        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter}
+
+    def group_count(self):
+        """Mean number of groups (distinct first-hit rows) per subset."""
+        return float(sum(torch.unique(i).numel() for i in self.ids)) / self.subsets

@@ -117,3 +117,14 @@ def safe_em_update(img, weight, s_map, eps=1e-12, dtype=np.float64):
     out = np.zeros_like(img)
     out[valid] = img[valid] * np.maximum(w[valid], 0.0) / s[valid]
     return out
+
+
+def sc_sensitivity(A, rotinv, rotate_num, dtype=np.float64):
+    """main_local_cntstat.py:140-146 (compute_sensitivity_local; the same formula as
+    main_plane_sparse.py:440-444): s = (1/R) sum_r colsum(A)[rotinv[:, r] - 1]."""
+    A = np.asarray(A, dtype=dtype)
+    col = A.sum(axis=0)
+    s = np.zeros(A.shape[1], dtype=dtype)
+    for r in range(rotate_num):
+        s = s + col[np.asarray(rotinv)[:, r].astype(np.int64) - 1]
+    return (s / rotate_num)[:, None]

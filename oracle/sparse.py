@@ -346,3 +346,20 @@ def weight_materialize_csr(rows, sysmat, x, U, dtype=np.float64):
     with np.errstate(divide="ignore"):
         w = t.T @ (dtype(1.0) / np.maximum(t @ x, dtype(1e-12)))
     return np.nan_to_num(w, nan=0.0, posinf=0.0, neginf=0.0)
+
+
+def sensitivity_d(rows, sysmat, p, dtype=np.float64):
+    """main_local_sparse_jsccsd_only.py:95-108 (build_sparse_sensi_d_local) and the summing
+    half of main_plane_sparse.py:214-226 (build_sparse_sensi_d): the sum over events of the
+    normalised fine rows of materialize_sparse_event_rows_to_fine."""
+    t, _ = materialize(rows, sysmat, p, dtype)
+    return t.sum(axis=0)[:, None] if t.size else np.zeros((p.fine_pixel_num, 1), dtype=dtype)
+
+
+def sensitivity_d_rescale(d, s_map_s, single_event_count_total, compton_event_count_total):
+    """main_plane_sparse.py:228-230: d scaled to sum(s) * E_C / max(E_S, 1) when sum(d) > 0."""
+    d = np.asarray(d, dtype=np.float64)
+    if d.sum() > 0:
+        d = d * np.sum(s_map_s) / d.sum()
+        d = d * compton_event_count_total / max(single_event_count_total, 1)
+    return d

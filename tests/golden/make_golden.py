@@ -289,11 +289,45 @@ def golden_sparse(ref):
     save("sparse_ops", **out)
 
 
+def golden_sensitivity(ref):
+    """Sensitivity builders: the Compton d of build_sparse_sensi_d_local
+    (main_local_sparse_jsccsd_only.py:95-108; build_sparse_sensi_d, main_plane_sparse.py:214-231,
+    is the same sum followed by a rescale, and pins "cuda:0") on the sparse_ops fixture's rows
+    split into two rotation blocks, and the SC sensitivity of compute_sensitivity_local
+    (main_local_cntstat.py:140-146, the same formula as main_plane_sparse.py:440-444) on the
+    shipped 10-view rotation tables."""
+    import importlib
+
+    cso = ref["compton_sparse_ops"]
+    msp = importlib.import_module("main_local_sparse_jsccsd_only")
+    mcs = importlib.import_module("main_local_cntstat")
+    sp = np.load(Path(__file__).parent / "sparse_ops.npz")
+    coor = torch.from_numpy(sp["s_coor"])
+    p = cso.build_compton_sparse_projector(coor, theta_stride=4, z_stride=2, rotate_num=4)
+    rows = torch.from_numpy(sp["s_event_rows"])
+    sysmat = torch.from_numpy(sp["s_sysmat"])
+    half = rows.size(0) // 2
+    with torch.no_grad():
+        d = msp.build_sparse_sensi_d_local([[rows[:half], rows[half:]]], [sysmat], [p], coor.size(0),
+                                           torch.device("cpu"), block_size=16)
+    rotinv = torch.from_numpy(np.genfromtxt(REF_DIR / "Factors" / "511keV_RotateNum10" / "RotMatInv_full.csv",
+                                            delimiter=",", dtype=np.int64))
+    g = torch.Generator().manual_seed(17)
+    # an SC matrix of exact float32 values k * 2^-18 (k < 256) stored as its uint8 codes
+    codes = torch.randint(0, 256, (32, rotinv.size(0)), generator=g, dtype=torch.uint8)
+    sc_sysmat = codes.to(torch.float32) * 2.0 ** -18
+    with torch.no_grad():
+        s = mcs.compute_sensitivity_local(sc_sysmat, rotinv, 10)
+    save("sensitivity", d_rows=rows.numpy(), d_half=np.array(half), d_local=d.numpy(),
+         sc_codes=codes.numpy(), sc_s=s.numpy())  # rotation tables: sparse_ops r10_rotmat_inv
+
+
 GENERATORS = {
     "sc_osem": golden_sc,
     "dense_compton": golden_dense_compton,
     "compton_builders": golden_compton,
     "sparse_ops": golden_sparse,
+    "sensitivity": golden_sensitivity,
 }
 
 

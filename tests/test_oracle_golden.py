@@ -215,3 +215,23 @@ def test_sparse_restatement_matches_dense_operators(golden):
                                rtol=1e-12, atol=1e-15)
     w = osp.weight_materialize_csr(rows, g["s_sysmat"], g["s_x"], U)
     assert rel_l2(w, g["s_w_mat"]) < 1e-5
+
+
+def test_sensitivity_builders_match_reference(golden):
+    """Compton d (build_sparse_sensi_d_local, summed over two rotation blocks) and the SC
+    sensitivity (compute_sensitivity_local over the shipped 10-view tables) against the
+    reference's own outputs; the rescale of build_sparse_sensi_d on top of d."""
+    from oracle import osem_sc
+
+    g = golden("sensitivity")
+    sp = golden("sparse_ops")
+    p = osp.build_projector(sp["s_coor"], theta_stride=4, z_stride=2, rotate_num=4)
+    rows, half = g["d_rows"], int(g["d_half"])
+    d = osp.sensitivity_d(rows[:half], sp["s_sysmat"], p) + osp.sensitivity_d(rows[half:], sp["s_sysmat"], p)
+    assert rel_l2(d, g["d_local"]) < 1e-6
+    A = g["sc_codes"].astype(np.float32) * np.float32(2.0 ** -18)
+    s = osem_sc.sc_sensitivity(A, sp["r10_rotmat_inv"], 10)
+    assert rel_l2(s, g["sc_s"]) < 1e-6
+    r = osp.sensitivity_d_rescale(d, s, 1000, 250)
+    np.testing.assert_allclose(r.sum(), s.sum() * 250 / 1000, rtol=1e-12)
+    assert np.array_equal(osp.sensitivity_d_rescale(np.zeros_like(d), s, 1, 1), np.zeros_like(d))
