@@ -232,6 +232,61 @@ class Sc3Workload:
                 "seconds": el}
 
 
+class SparseLaunchBench:
+    """Profiling case: one grouped sparse Compton weight launch with a config-3 subset's sizes
+    (99,850 BF16 coarse rows of 9,000 voxels, 12,239 groups, 100 x 360 fine grid, theta-stride-4
+    ring stencil, materialise semantics) on a random 16,384-row BF16 sysmat, so that a full
+    ncu capture holds ~3 GB on the device. One step = one weight call (the image is not
+    updated); the fp32 pass repeats the same BF16 launch."""
+
+    def __init__(self, dev, n_det=16384, n_events=99850, n_groups=12239, seed=1):
+        from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+        from jscc_recon_spect_cylinder_gb300 import synthetic
+
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        grid = synthetic.polar_grid(100, 360, 100.0)
+        self.projector = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1)
+        self.tables = cso.tables(self.projector, dev)
+        self.V, self.Vc = grid.n_vox, self.projector.coarse_pixel_num
+        self.A = torch.rand((n_det, self.V), generator=g, device=dev).to(torch.bfloat16)
+        used = torch.randperm(n_det, generator=g, device=dev)[:n_groups].to(torch.int32)
+        ids = used[torch.randint(0, n_groups, (n_events,), generator=g, device=dev)]
+        self.ids = ids[torch.argsort(ids)].contiguous()
+        self.tc = torch.rand((n_events, self.Vc), generator=g, device=dev).to(torch.bfloat16)
+        self.n_events, self.n_groups = n_events, int(torch.unique(self.ids).numel())
+        self.name = "sparse-launch"
+        self.metric = "grouped sparse weight launches/s (one config-3 subset, synthetic rows), 1xGB300"
+        self.traffic_file = "traffic_jsccsd3.json"
+        self.dev = dev
+        self.subsets = 1
+        self.w = torch.zeros((self.V, 1), device=dev)
+        torch.cuda.synchronize(dev)
+
+    def step(self, img, dtype):
+        from jscc_recon_spect_cylinder_gb300 import ops
+
+        self.w.zero_()
+        ops.sparse_weight_split(self.ids, self.tc, self.A, self.tables, img, grouped=False, out=self.w)
+        return img
+
+    def units_per_step(self):
+        return 1
+
+    def kernel_bytes(self, dtype):
+        coef = self.n_events * (self.Vc * 2 + 4) + self.n_groups * (self.V * 2 + self.Vc * 4)
+        scatter = self.n_groups * (self.V * 2 + self.Vc * 4) + 16 * self.V * 4
+        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter}
+
+    def config(self):
+        return {"workload": self.name, "events": self.n_events, "groups": self.n_groups, "voxels": self.V,
+                "coarse_voxels": self.Vc, "sysmat_rows": self.A.size(0), "storage": "bf16",
+                "l2": "inputs larger than L2 (no flush)"}
+
+    def extra(self, ms_per_step):
+        return {}
+
+
 class JointBench:
     """workloads.JointWorkload behind the bench interface."""
 
@@ -366,6 +421,8 @@ def make_workload(name, dev):
         return JointBench(dev)
     if name == "jsccsd-small":
         return JointBench(dev, small=True)
+    if name == "sparse-launch":
+        return SparseLaunchBench(dev)
     if name == "sc3":
         return Sc3Workload(dev)
     if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
@@ -531,7 +588,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small"], default="jsccsd3")
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch"],
+                    default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
