@@ -932,6 +932,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       re_end = goff[rg + 1];
     }
     int win_base = INT_MIN, win_val = 0;  // 32 order values, one per lane
+    int ps = 0;            // slot of row pseq (pseq mod n_slots, kept incrementally)
+    uint32_t uses = 0;     // bit s: parity of the number of rows issued into slot s
     uint32_t idle = 0;
     bool ok = true;
     while (ok) {
@@ -961,8 +963,9 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         }
       }
       if (rows_left) {
-        const int s = pseq % n_slots;
-        bool ready = pseq < n_slots || mbar_test_wait(empty + s, (pseq / n_slots - 1) & 1);
+        const int s = ps;
+        // the slot's previous row (use u - 1) must have been released: phase u - 1 of empty[s]
+        bool ready = pseq < n_slots || mbar_test_wait(empty + s, ((uses >> s) & 1u) ^ 1u);
         ready = __shfl_sync(0xffffffffu, ready, 0);
         if (ready) {
           if (re < win_base || re >= win_base + 32) {  // refill the window of event indices
@@ -975,6 +978,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
             bulk_copy_g2s(const_cast<TC*>(slot(s)), rows.coarse(i), row_bytes, full + s);
             *rows_issued = pseq + 1;
           }
+          uses ^= 1u << s;
+          ps = ps + 1 == n_slots ? 0 : ps + 1;
           ++pseq;
           ++re;
           progress = true;
@@ -1015,6 +1020,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     // ------------------------------------------------------------ event warps
     const int et = tid;
     int seq = 0, kg = 0;
+    int cs_slot = 0;         // slot of event seq (seq mod n_slots, kept incrementally)
+    uint32_t cphase = 0;     // bit s: parity of the next phase of full[s]
     bool aborted = false, bad = false;  // bad: one of this thread's waits gave up
     // software pipeline over groups: the event range of group k + 2 and the event sums of
     // group k + 1 (this thread's event of it) are loaded while group k is processed
@@ -1043,14 +1050,22 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         const int n = min(batch, e1 - bs);
         // event sums beyond the first kBkEvents of a group are read here (issued before the dots)
         const float s_far = (MODE == 0 && et < n && bs + et - e0 >= kBkEvents) ? s_ev[bs + et] : 0.f;
-        for (int k = 0; k < n; ++k) {
-          const int sq = seq + k;
-          if (!bk_wait(full + sq % n_slots, (sq / n_slots) & 1, abort_flag)) bad = true;
+        int sl[kBkMaxBatch];
+#pragma unroll
+        for (int k = 0; k < kBkMaxBatch; ++k) {
+          sl[k] = cs_slot;
+          if (k < n) cs_slot = cs_slot + 1 == n_slots ? 0 : cs_slot + 1;
         }
+#pragma unroll
+        for (int k = 0; k < kBkMaxBatch; ++k)
+          if (k < n) {
+            if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag)) bad = true;
+            cphase ^= 1u << sl[k];
+          }
         // ---- dots f_i = t_i . b; BF16 rows stay in registers for the q pass
         const TC* rp[kBkMaxBatch];
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k) rp[k] = slot((seq + k) % n_slots);
+        for (int k = 0; k < kBkMaxBatch; ++k) rp[k] = slot(sl[k]);
         RowChunk<TC> rc[kBkMaxBatch][kBkQ];
         float4 acc[kBkMaxBatch];  // four independent partial sums per event
 #pragma unroll
@@ -1130,7 +1145,9 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         }
         role_sync(1, kBkEvents);  // the batch's slots, partials and coefficients are free
         if (et == 0) {
-          for (int k = 0; k < n; ++k) mbar_arrive(empty + (seq + k) % n_slots);
+#pragma unroll
+          for (int k = 0; k < kBkMaxBatch; ++k)
+            if (k < n) mbar_arrive(empty + sl[k]);
           *rows_used = seq + n;
         }
         seq += n;
@@ -1305,6 +1322,38 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     for (int v = 0; v < kScVox; ++v)
       if (vox(v) >= l_end) l0[v] = l1[v] = cs0;  // (weight 0) keeps every gather inside the segment
   }
+  // Two-value runs: when every tap of a run of four voxels is one of two coarse voxels (the
+  // polar projector's theta interpolation), the run needs two q loads and each voxel two
+  // folded weights, val = ra * q[pc0] + rb * q[pc1]; otherwise the thread gathers each tap.
+  int pc0[2], pc1[2];
+  float ra[kScVox], rb[kScVox];
+  bool pair = true;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int a = l0[4 * r];
+    int b = a;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int v = 4 * r + i;
+      if (vox(v) >= l_end) continue;
+      const int ls[2] = {l0[v], l1[v]};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (ls[h] == a) continue;
+        if (b == a) b = ls[h];
+        else if (ls[h] != b) pair = false;
+      }
+    }
+    pc0[r] = a;
+    pc1[r] = b;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int v = 4 * r + i;
+      const bool in = vox(v) < l_end;
+      ra[v] = in ? (l0[v] == a ? w0[v] : 0.f) + (l1[v] == a ? w1[v] : 0.f) : 0.f;
+      rb[v] = in && b != a ? (l0[v] == b ? w0[v] : 0.f) + (l1[v] == b ? w1[v] : 0.f) : 0.f;
+    }
+  }
   const bool staged = seg_len <= kScSeg;
   const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
   const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
@@ -1313,6 +1362,8 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     // ------------------------------------------------------------ producer warp
     if (staged) {
       bool ok = true;
+      int s = 0;              // stage of group kk (kk mod n_stages, kept incrementally)
+      uint32_t eph = 0;       // bit s: parity of the next phase of empty[s] to wait for
       for (int w = g_begin; w < g_end && ok; w += 32) {
         const int gv = w + lane < g_end ? grow[w + lane] : 0;  // 32 group rows per load
         const int m = min(32, g_end - w);
@@ -1320,8 +1371,10 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
           const int row = __shfl_sync(0xffffffffu, gv, k);
           const int kk = w - g_begin + k;
           if (lane == 0) {
-            const int s = kk % n_stages;
-            if (kk >= n_stages) ok = bk_wait(empty + s, (kk / n_stages - 1) & 1, abort_flag);
+            if (kk >= n_stages) {
+              ok = bk_wait(empty + s, (eph >> s) & 1u, abort_flag);
+              eph ^= 1u << s;
+            }
             if (ok) {
               unsigned char* st = stage(s);
               const float* qg = q + (int64_t)(w + k) * ldq;
@@ -1332,6 +1385,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
               *issued = kk + 1;
             }
           }
+          s = s + 1 == n_stages ? 0 : s + 1;
           ok = __shfl_sync(0xffffffffu, ok, 0);
         }
       }
@@ -1345,6 +1399,27 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     bool bad = false;
     // acc[v] += a[v] * (u0 * (w0 q0[l0] + w1 q0[l1]) + u1 * (w0 q1[l0] + w1 q1[l1]))
     auto accumulate = [&](const float (&a)[kScVox], const float* q0, const float* q1) {
+      if (pair) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const float qa = q0[pc0[r]], qb = q0[pc1[r]];
+          const float qa1 = two_z ? q1[pc0[r]] : 0.f, qb1 = two_z ? q1[pc1[r]] : 0.f;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int v = 4 * r + i;
+            float t = ra[v] * qa;
+            t = fmaf(rb[v], qb, t);
+            float val = u0 * t;
+            if (two_z) {
+              float bb = ra[v] * qa1;
+              bb = fmaf(rb[v], qb1, bb);
+              val = fmaf(u1, bb, val);
+            }
+            if (val != 0.f) acc[v] = fmaf(a[v], val, acc[v]);
+          }
+        }
+        return;
+      }
 #pragma unroll
       for (int v = 0; v < kScVox; ++v) {
         float t = w0[v] * q0[l0[v]];
@@ -1360,13 +1435,15 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     };
     if (staged) {
       // shared-memory operands only (the pointers below are derived from the shared array)
-      for (int g = g_begin; g < g_end; ++g) {
+      int s = 0;              // stage of group kk (kk mod n_stages, kept incrementally)
+      uint32_t fph = 0;       // bit s: parity of the next phase of full[s]
+      for (int g = g_begin; g < g_end; ++g, s = s + 1 == n_stages ? 0 : s + 1) {
         const int kk = g - g_begin;
-        const int s = kk % n_stages;
-        if (!bk_wait(full + s, (kk / n_stages) & 1, abort_flag)) {
+        if (!bk_wait(full + s, (fph >> s) & 1u, abort_flag)) {
           bad = true;
           break;
         }
+        fph ^= 1u << s;
         unsigned char* st = stage(s);
         if (lf0 < l_end) {
           const TE* at = reinterpret_cast<const TE*>(st) + (lf0 - l_begin);
