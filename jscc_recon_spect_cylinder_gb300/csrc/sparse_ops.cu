@@ -1115,7 +1115,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
           } else if (MODE == 0) {
             const int p = bs + et - e0;
             const float si = p < kBkEvents ? s_grp[p] : s_far;
-            cs[et] = (isfinite(si) && si > 0.f) ? (1.0f / fmaxf(f / si, 1e-12f)) / si : 0.f;
+            // (1 / max(f / S, 1e-12)) / S = 1 / max(f, 1e-12 S) for S > 0: one division
+            cs[et] = (isfinite(si) && si > 0.f) ? 1.0f / fmaxf(f, 1e-12f * si) : 0.f;
           } else {
             cs[et] = 1.0f / fmaxf(f, 1e-12f);
           }
