@@ -431,6 +431,15 @@ def make_workload(name, dev):
 
 
 # ----------------------------------------------------------------------------- timing
+def max_over_ranks(ms, world, device):
+    """The slowest rank's time (every rank gets it): the whole-job time of a replicated run."""
+    if world <= 1:
+        return ms
+    t = torch.tensor([float(ms)], device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def timed_steps(work, dtype, steps, warmup, world):
     img = torch.ones((work.V, 1), device=work.dev)
     for _ in range(warmup):
@@ -452,11 +461,7 @@ def timed_steps(work, dtype, steps, warmup, world):
     launches = _lib.launch_count() - n0
     if world > 1:
         torch.distributed.barrier()
-    ms = t0.elapsed_time(t1)
-    if world > 1:
-        t = torch.tensor([ms], device=work.dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(t0.elapsed_time(t1), world, work.dev)
     return ms, launches, img
 
 
