@@ -626,6 +626,18 @@ def sparse_sensitivity(sysmat, tables: SparseTables, rows=None, row_id=None, t_c
     return sparse_weight_split(row_id, t_coarse, sysmat, tables, ones, grouped=False, out=out)
 
 
+def plan_groups(row_id: torch.Tensor, n_det: int) -> GroupPlan:
+    """Build (and cache on ``row_id``) the first-hit-row grouping that the grouped sparse
+    weight uses for split storage, so that a caller staging data can do it ahead of the first
+    weight call. ``n_det`` is the sysmat's row count (ids are clamped to it, as the weight
+    call does). ``row_id`` must already be a contiguous int32 tensor for the cache to be
+    found again by the weight call."""
+    _lib.require_cuda(row_id, what="plan_groups")
+    if row_id.dtype != torch.int32 or not row_id.is_contiguous():
+        raise ValueError("plan_groups: row_id must be a contiguous int32 tensor")
+    return _group_plan(row_id, lambda: torch.clamp(row_id.long(), 0, n_det - 1))
+
+
 def grouped_fits(tables: SparseTables) -> bool:
     """The grouped kernels keep one coarse row per CTA in shared memory."""
     return ((tables.n_zc * tables.n_lc + 3) // 4 * 4) * 4 <= 227 * 1024

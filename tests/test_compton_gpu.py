@@ -468,3 +468,27 @@ def test_grouped_bulk_scatter_wide_rings(cuda):
         torch.cuda.synchronize()
         assert rel_l2(b.cpu(), a.cpu()) < TOL_W
     assert _lib.take_wait_timeout_count() == 0
+
+
+def test_plan_groups_ahead_of_the_weight_call(cuda):
+    """A grouping built ahead (ops.plan_groups) is the one the weight call then uses, and the
+    weight equals the one computed with a fresh id tensor."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+    from jscc_recon_spect_cylinder_gb300 import ops, synthetic
+
+    grid = synthetic.polar_grid(16, 96, 30.0)
+    p = cso.build_compton_sparse_projector(grid.coor, 4, 1, rotate_num=1)
+    tb = cso.tables(p, cuda)
+    g = torch.Generator().manual_seed(5)
+    n_det, n = 64, 900
+    A = (torch.rand((n_det, grid.n_vox), generator=g) + 0.05).to(cuda).to(torch.bfloat16)
+    tc = (torch.rand((n, p.coarse_pixel_num), generator=g) ** 3).to(cuda).to(torch.bfloat16)
+    ids = torch.randint(0, n_det, (n,), generator=g, dtype=torch.int32).to(cuda)
+    x = (torch.rand((grid.n_vox, 1), generator=g) + 0.2).to(cuda)
+    plan = ops.plan_groups(ids, n_det)
+    w = ops.sparse_weight_split(ids, tc, A, tb, x)
+    assert ids._jscc_group_plan[1] is plan
+    w_fresh = ops.sparse_weight_split(ids.clone(), tc, A, tb, x)
+    assert torch.equal(w, w_fresh)
+    with pytest.raises(ValueError):
+        ops.plan_groups(ids.long(), n_det)
