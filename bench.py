@@ -232,6 +232,104 @@ class Sc3Workload:
                 "seconds": el}
 
 
+class Cone2Bench:
+    """Config 2 (JSCCD list mode, FP32): the fused strict cone weight w = T^T (1 / T x) with
+    T recomputed on the fly from 64-byte event records. 100 x 360 polar grid (36,000 voxels);
+    scatter cylinder r = 120 mm and absorber r = 150 mm, 32 x 128 pixels each (8,192 detector
+    pixels); 200,000 two-interaction events at 511 keV forward-simulated from the hot-rod
+    phantom, energies blurred with the reference's convention (8 % FWHM at 662 keV scaled by
+    sqrt(0.662 / E)), selected by the strict builder's filters and row statistics. One step =
+    one weight pass (forward and back over every kept event), cos-beta window at 9 sigma."""
+
+    K_CONE = 100  # FP32 operations per fully evaluated event-voxel pair (strict formula, see flops())
+
+    def __init__(self, dev, n_events=200000, seed=None):
+        from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+        from jscc_recon_spect_cylinder_gb300 import synthetic
+
+        seed = synthetic.SEED if seed is None else seed
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        grid = synthetic.polar_grid(100, 360, 100.0, device=dev)
+        pitch = 2.0 * math.pi * 120.0 / 128
+        scat = synthetic.cylinder_pixels(120.0, 128, 32, 2.0, 0.0, dev)
+        absb = synthetic.cylinder_pixels(150.0, 128, 32, 2.0, 0.0, dev)
+        self.A = synthetic.sc_system_matrix(grid.coor, scat, pitch * 2.0, 100.0, generator=gen)
+        det = torch.cat((scat, absb), dim=0).to(torch.float32)
+        x_true = synthetic.hot_rod_phantom(grid.coor.cpu(), 100.0).to(dev)
+        e0 = 0.511
+        lst = synthetic.compton_list(grid.coor, x_true, scat, 150.0, 128, 32, 2.0, e0, int(n_events * 2.3) + 64, gen,
+                                     cp1_offset=0, cp2_offset=scat.size(0))[:n_events]
+        res = 0.08 * (0.662 / e0) ** 0.5
+        noise = torch.randn((lst.size(0), 2), generator=gen, device=dev)
+        for k, col in ((0, 1), (1, 3)):
+            e = lst[:, col]
+            lst[:, col] = e + (e * res / 2.355 * (e0 / e) ** 0.5) * noise[:, k]
+        thr_max = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
+        self.coor = grid.coor.to(torch.float32)
+        self.ev = pls.get_compton_event_params(self.A, det, self.coor, lst, 1.0, 1.0, e0, res, thr_max, 0.05,
+                                               e0 - 0.06, window_sigmas=9.0)
+        self.n_list = lst.size(0)
+        self.V = grid.n_vox
+        self.dev = dev
+        self.subsets = 1
+        self.name = "jsccd-config2"
+        self.metric = "event-voxel pairs/s: fused strict cone weight (T recomputed on the fly), config 2, 1xGB300"
+        self.unit = "event-voxel pairs/s"
+        self.dtypes = ("f32",)
+        self.traffic_file = "traffic_cone2.json"
+        self.w = torch.zeros((self.V, 1), device=dev)
+        torch.cuda.synchronize(dev)
+
+    def step(self, img, dtype, use_window=True):
+        from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+        self.w.zero_()
+        rop.get_weight_compton_fused(self.ev, self.coor, self.A, img, out=self.w, use_window=use_window)
+        return img
+
+    def units_per_step(self):
+        return 2 * len(self.ev) * self.V  # forward and back pairs
+
+    def kernel_bytes(self, dtype):
+        return {}
+
+    def flops(self):
+        """K_CONE per pair: v = x_j - r1 (3), |v|^2 (5), v . u12 (5), cos beta (2), window
+        test (2), acos (~12 incl. the SFU), beta - theta (1), sigma_pos^2 Jacobian of beta in
+        r1 and r2 with per-axis variances (~45), sigma^2 and the Gaussian exponent (~6), exp
+        (~4), Klein-Nishina - sin^2 beta (3), x efficiency (1), forward or back FMA (2); ~90,
+        rounded to 100. Pairs outside the window stop after the test (~20)."""
+        return self.K_CONE
+
+    def config(self):
+        return {"workload": self.name, "voxels": self.V, "events_listed": self.n_list, "events_kept": len(self.ev),
+                "detector_pixels": 8192, "e0_mev": 0.511, "window_sigmas": 9.0, "model": "strict",
+                "l2": "records 13 MB, sysmat rows 590 MB; compute-bound"}
+
+    def extra(self, ms_per_step):
+        """The same pass with every pair evaluated (no window): the FP32 roofline figure."""
+        img = torch.ones((self.V, 1), device=self.dev)
+        for _ in range(2):
+            self.step(img, "f32", use_window=False)
+        torch.cuda.synchronize(self.dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        n = 3
+        for _ in range(n):
+            self.step(img, "f32", use_window=False)
+        t1.record()
+        torch.cuda.synchronize(self.dev)
+        ms = t0.elapsed_time(t1) / n
+        pairs = self.units_per_step() / (ms / 1e3)
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 FMA peak, TFLOP/s (no measured figure)
+        achieved = pairs * self.K_CONE / 1e12
+        return {"no_window": {"pairs_per_s": pairs, "ms_per_step": ms},
+                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                                  "flop_per_pair": self.K_CONE}}
+
+
 class SparseLaunchBench:
     """Profiling case: one grouped sparse Compton weight launch with a config-3 subset's sizes
     (99,850 BF16 coarse rows of 9,000 voxels, 12,239 groups, 100 x 360 fine grid, theta-stride-4
@@ -423,6 +521,8 @@ def make_workload(name, dev):
         return JointBench(dev, small=True)
     if name == "sparse-launch":
         return SparseLaunchBench(dev)
+    if name == "cone2":
+        return Cone2Bench(dev)
     if name == "sc3":
         return Sc3Workload(dev)
     if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
@@ -524,20 +624,24 @@ def ours_arm(args):
 
     _lib.load()
     work = make_workload(args.workload, dev)
+    dtypes = getattr(work, "dtypes", ("bf16", "f32"))  # primary arm first
+    unit = getattr(work, "unit", "subset-iters/s")
     sampler = ClockSampler(local)
     sampler.start()
-    ms_bf16, launches, img_bf16 = timed_steps(work, "bf16", args.steps, args.warmup, world)
+    ms_main, launches, _ = timed_steps(work, dtypes[0], args.steps, args.warmup, world)
     clocks = sampler.stop()
-    ms_f32, _, img_f32 = timed_steps(work, "f32", args.steps, args.warmup, world)
     units = world * args.steps * work.units_per_step()
-    value = units / (ms_bf16 / 1e3)
-    value_f32 = units / (ms_f32 / 1e3)
+    value = units / (ms_main / 1e3)
+    second = None
+    if len(dtypes) > 1:
+        ms_2, _, _ = timed_steps(work, dtypes[1], args.steps, args.warmup, world)
+        second = {"value": units / (ms_2 / 1e3), "ms_per_step": ms_2 / args.steps}
 
     line = None
     if rank == 0:
         peaks = measured_peaks()
-        kt = kernel_times(work, "bf16", max(3, min(args.steps, 10)))
-        kbytes = work.kernel_bytes("bf16")
+        kt = kernel_times(work, dtypes[0], max(3, min(args.steps, 10)))
+        kbytes = work.kernel_bytes(dtypes[0])
         kernels = {}
         total_ms = sum(tot for _, tot in kt.values())
         for name, (n, tot) in kt.items():
@@ -547,39 +651,45 @@ def ours_arm(args):
                 entry["algorithmic_bytes"] = kbytes[name]
                 entry["achieved_gbs"] = kbytes[name] / (avg / 1e3) / 1e9
             kernels[name] = entry
-        top = max((k for k in kernels if "achieved_gbs" in kernels[k]),
-                  key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
-        traffic = None
-        tf = REPO / "profiles" / work.traffic_file
-        if tf.exists():
-            traffic = json.loads(tf.read_text()).get(top)
-        achieved = kernels[top]["achieved_gbs"]
-        roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                    "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"]}
+        roofline = None
+        with_bytes = [k for k in kernels if "achieved_gbs" in kernels[k]]
+        if with_bytes:
+            top = max(with_bytes, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"])
+            traffic = None
+            tf = REPO / "profiles" / work.traffic_file
+            if tf.exists():
+                traffic = json.loads(tf.read_text()).get(top)
+            achieved = kernels[top]["achieved_gbs"]
+            roofline = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peaks["source"]}
         errors = None
         err_iters = args.error_iters
-        if not args.no_errors:
+        if not args.no_errors and hasattr(work, "fp64_reference"):
             imgs = {}
-            for dt in ("bf16", "f32"):
+            for dt in dtypes:
                 x = torch.ones((work.V, 1), device=dev)
                 for _ in range(err_iters):
                     x = work.step(x, dt)
                 imgs[dt] = x
             errors = image_errors(work.fp64_reference(err_iters), imgs)
-        e2e = work.e2e(30) if not args.no_e2e else None
-        cpu = work.cpu_rate() if (world == 1 and not args.no_cpu_baseline) else None
+        e2e = work.e2e(30) if not args.no_e2e and hasattr(work, "e2e") else None
+        cpu = work.cpu_rate() if (world == 1 and not args.no_cpu_baseline and hasattr(work, "cpu_rate")) else None
         line = {
-            "metric": work.metric, "value": value, "unit": "subset-iters/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_bf16 / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "metric": work.metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_main / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtypes[0], "data": "synthetic",
             "config": dict(work.config(), parallelism="replicas" if world > 1 else "single"),
-            "fp32": {"value": value_f32, "ms_per_step": ms_f32 / args.steps},
-            "speedup_bf16_vs_fp32": value / value_f32,
-            "errors_vs_fp64": errors, "errors_after_iterations": err_iters,
-            "gpu_launches": launches, "clocks": clocks, "roofline": roofline, "kernels": kernels,
-            "e2e": e2e, "cpu_baseline": cpu,
         }
-        line.update(work.extra(ms_bf16 / args.steps))
+        if second is not None:
+            line[dtypes[1] if dtypes[1] != "f32" else "fp32"] = second
+            line["speedup_bf16_vs_fp32"] = value / second["value"]
+        line.update({"errors_vs_fp64": errors, "errors_after_iterations": err_iters, "gpu_launches": launches,
+                     "clocks": clocks, "roofline": roofline, "kernels": kernels, "e2e": e2e, "cpu_baseline": cpu})
+        extra = work.extra(ms_main / args.steps)
+        if roofline is None and "fp32_roofline" in extra:
+            top = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"]) if kernels else None
+            line["roofline"] = dict(extra.pop("fp32_roofline"), kernel=top, traffic=None)
+        line.update(extra)
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
@@ -593,7 +703,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch"],
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2"],
                     default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
