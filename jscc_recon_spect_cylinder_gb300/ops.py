@@ -290,6 +290,20 @@ def compton_row_stats(records, row_id, coor, model=_lib.CONE_STRICT, eff=None, u
     return s1, s2, nan.bool()
 
 
+def _row_sorted_events(records, row_id):
+    """(records, row_id) stably sorted by row id, cached on the records tensor (rebuilt when
+    either tensor is modified in place)."""
+    key = (id(row_id), records._version, row_id._version)
+    cache = getattr(records, "_jscc_row_sorted", None)
+    if cache is not None and cache[0] == key:
+        return cache[1], cache[2]
+    perm = torch.argsort(row_id.to(torch.int64), stable=True)
+    rec_s = records.index_select(0, perm).contiguous()
+    rid_s = row_id.index_select(0, perm).contiguous()
+    records._jscc_row_sorted = (key, rec_s, rid_s)
+    return rec_s, rid_s
+
+
 def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
                    rotmat_inv=None, rot_col=0, scale=1.0, out=None):
     """``out += scale * rotinv( T^T (1 / T rot(img)) )`` with T recomputed on the fly."""
@@ -312,6 +326,10 @@ def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None,
             ld_rot = rotmat.stride(0)
     e, edt, ld = _eff_args(eff)
     n = records.size(0)
+    if e is not None and n > 1:
+        # the weight is a sum over events: visiting them sorted by efficiency row lets the
+        # events a CTA handles share those rows in L1/L2 (only float32 rounding changes)
+        records, row_id = _row_sorted_events(records, row_id)
     lib = _lib.load()
     ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
     rc = lib.jscc_compton_weight(
