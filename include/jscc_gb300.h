@@ -113,6 +113,29 @@ JSCC_API int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const i
                    size_t workspace_bytes, void* stream);
 
 /*
+ * The two halves of jscc_sc_weight on their own — the forward and the adjoint of the SC
+ * projector, for a differentiable projector (no counterpart in the reference, whose autograd
+ * would go through torch.matmul; its backprojection is the transpose used in
+ * recon_osem_plane.py:28-30):
+ *
+ *   jscc_sc_project:     out[b * ld_out + r] = sum_j A[rb, j] * img[rotmat[j * ld_rot + r] - 1]
+ *   jscc_sc_backproject: weight[j] += scale * sum_r u_r[rotmat_inv[j * ld_rot + r] - 1],
+ *                        u_r = A^T g[:, r]   (g [n_bins, ld_g], column r)
+ *
+ * for r < n_rot (rotation tables NULL: identity, n_rot = 1). Workspace:
+ * jscc_sc_weight_workspace_bytes(n_bins, n_vox, n_rot). Same kernels and reduction orders as
+ * jscc_sc_weight.
+ */
+JSCC_API int jscc_sc_project(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, int32_t n_rot, const float* img,
+                   const int64_t* rotmat, int64_t ld_rot, float* out, int64_t ld_out,
+                   void* workspace, size_t workspace_bytes, void* stream);
+JSCC_API int jscc_sc_backproject(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, int32_t n_rot, const float* g, int64_t ld_g,
+                   const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/*
  * SC sensitivity (column sums of the system matrix through the inverse rotations):
  *
  *   weight[j] += (sum_{r < n_rot} colsum(A)[rotmat_inv[j * ld_rot + r] - 1]) / n_rot,
@@ -234,6 +257,25 @@ JSCC_API int jscc_compton_weight(const float* records, const int32_t* row_id, in
 /* Detector ids outside the table seen by jscc_compton_event_prep since the last call
  * (synchronous device read; resets the count). */
 JSCC_API int jscc_take_bad_detector_count(unsigned int* out);
+
+/*
+ * The two halves of jscc_compton_weight on their own (T recomputed in both, never stored):
+ *   jscc_compton_project:     f_out[i] = sum_j t_ij * rot(img)_j
+ *   jscc_compton_backproject: weight[j] += scale * rotinv(sum_i t_ij * g_i)
+ * with the same records, row ids, efficiency rows, model and window as jscc_compton_weight
+ * (whose workspace size they use). No counterpart in the reference (a differentiable fused
+ * projector: the forward and its adjoint).
+ */
+JSCC_API int jscc_compton_project(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t n_vox, int32_t model, int32_t use_window,
+                   const void* eff, int32_t eff_dtype, int64_t ld_eff, const float* img,
+                   const int64_t* rotmat, int64_t ld_rot, float* f_out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+JSCC_API int jscc_compton_backproject(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t n_vox, int32_t model, int32_t use_window,
+                   const void* eff, int32_t eff_dtype, int64_t ld_eff, const float* g,
+                   const int64_t* rotmat_inv, int64_t ld_rot, float scale, float* weight,
+                   void* workspace, size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------ sparse coarse<->fine Compton rows (kernel c) */
 

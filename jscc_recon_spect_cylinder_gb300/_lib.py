@@ -45,6 +45,26 @@ _SIGNATURES: dict[str, tuple] = {
     "jscc_kernel_timing_enable": (None, [c_int]),
     "jscc_kernel_timing_collect": (c_int, [ctypes.c_char_p, c_size_t]),
     "jscc_sc_weight_workspace_bytes": (c_size_t, [c_int64, c_int64, c_int32]),
+    "jscc_sc_project": (
+        c_int,
+        [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64, c_void_p,
+         c_int64, c_void_p, c_size_t, c_void_p],
+    ),
+    "jscc_sc_backproject": (
+        c_int,
+        [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_int64, c_void_p, c_int64,
+         c_float, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "jscc_compton_project": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+         c_void_p, c_int64, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "jscc_compton_backproject": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+         c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
     "jscc_sc_sensitivity": (
         c_int,
         [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_int64, c_void_p, c_void_p,

@@ -405,17 +405,21 @@ static ConePlan plan_cone(int64_t n_ev, int64_t V) {
 template <int MODEL, bool WINDOW, typename TE>
 static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t n_ev, const float* coor, int64_t V,
                               const float* x, const TE* eff, int64_t ld_eff, float* f, float* q, float* part,
-                              const ConePlan& p, cudaStream_t st) {
+                              const ConePlan& p, cudaStream_t st, int stage = 0) {
+  // stage 0: forward, ratio, back (the weight); 1: forward only (f); 2: back-project q
   constexpr int EB = 16;
-  const unsigned fgrid = (unsigned)((n_ev + EB - 1) / EB);
-  JSCC_TIMED("cone_forward", st,
-             (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
-                 rec, rid, n_ev, coor, V, x, eff, ld_eff, f, nullptr, nullptr, nullptr)));
-  JSCC_LAUNCH_CHECK();
-  int64_t rb = (n_ev + 255) / 256;
-  if (rb > 4096) rb = 4096;
-  JSCC_TIMED("cone_ratio", st, (cone_ratio_kernel<<<(unsigned)rb, 256, 0, st>>>(f, n_ev, q)));
-  JSCC_LAUNCH_CHECK();
+  if (stage != 2) {
+    const unsigned fgrid = (unsigned)((n_ev + EB - 1) / EB);
+    JSCC_TIMED("cone_forward", st,
+               (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
+                   rec, rid, n_ev, coor, V, x, eff, ld_eff, f, nullptr, nullptr, nullptr)));
+    JSCC_LAUNCH_CHECK();
+    if (stage == 1) return JSCC_OK;
+    int64_t rb = (n_ev + 255) / 256;
+    if (rb > 4096) rb = 4096;
+    JSCC_TIMED("cone_ratio", st, (cone_ratio_kernel<<<(unsigned)rb, 256, 0, st>>>(f, n_ev, q)));
+    JSCC_LAUNCH_CHECK();
+  }
   dim3 bgrid((unsigned)((V + kConeThreads - 1) / kConeThreads), (unsigned)p.chunks);
   JSCC_TIMED("cone_back", st,
              (cone_back_kernel<MODEL, WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
@@ -526,30 +530,41 @@ int jscc_compton_row_stats(const float* records, const int32_t* row_id, int64_t 
 
 size_t jscc_compton_weight_workspace_bytes(int64_t n_ev, int64_t n_vox) { return plan_cone(n_ev, n_vox).ws_bytes; }
 
-int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t n_vox,
-                        int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
-                        const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
-                        float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
-  JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0, "jscc_compton_weight: negative size");
-  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_weight: bad model");
-  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_weight: bad dtype");
+// The weight and its two halves (the differentiable projector's forward and backward):
+// stage 0: weight += scale * rotinv(T^T (1 / T rot(img))); 1: f_out[i] = sum_j t_ij rot(img)_j;
+// 2: weight += scale * rotinv(T^T g).
+static int compton_stage_entry(const char* what, int stage, const float* records, const int32_t* row_id,
+                               int64_t n_ev, const float* coor, int64_t n_vox, int32_t model, int32_t use_window,
+                               const void* eff, int32_t eff_dtype, int64_t ld_eff, const float* img,
+                               const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, const float* g,
+                               float* f_out, float scale, float* weight, void* workspace, size_t workspace_bytes,
+                               void* stream) {
+  JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0, "%s: negative size", what);
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "%s: bad model", what);
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "%s: bad dtype", what);
   if (n_ev == 0 || n_vox == 0) return JSCC_OK;
-  JSCC_REQUIRE(records && coor && img && weight, "jscc_compton_weight: null pointer argument");
-  JSCC_REQUIRE(!eff || (row_id && ld_eff >= n_vox), "jscc_compton_weight: efficiency rows need row ids, ld >= V");
-  JSCC_REQUIRE((rotmat == nullptr) == (rotmat_inv == nullptr), "jscc_compton_weight: give both rotation tables");
+  JSCC_REQUIRE(records && coor, "%s: null pointer argument", what);
+  JSCC_REQUIRE(stage == 2 || img, "%s: null image", what);
+  JSCC_REQUIRE(stage != 1 || f_out, "%s: null output", what);
+  JSCC_REQUIRE(stage == 1 || weight, "%s: null weight", what);
+  JSCC_REQUIRE(stage != 2 || g, "%s: null input", what);
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= n_vox), "%s: efficiency rows need row ids, ld >= V", what);
+  JSCC_REQUIRE(stage != 0 || (rotmat == nullptr) == (rotmat_inv == nullptr), "%s: give both rotation tables", what);
   const ConePlan p = plan_cone(n_ev, n_vox);
-  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "jscc_compton_weight: workspace too small (%zu < %zu)",
+  JSCC_REQUIRE(workspace && workspace_bytes >= p.ws_bytes, "%s: workspace too small (%zu < %zu)", what,
                workspace_bytes, p.ws_bytes);
   Carver cv(workspace, workspace_bytes);
   float* xr = cv.take<float>((size_t)p.ldx);
   float* f = cv.take<float>((size_t)n_ev);
   float* q = cv.take<float>((size_t)n_ev);
   float* part = cv.take<float>((size_t)p.chunks * p.ldp);
-  JSCC_REQUIRE(cv.ok(), "jscc_compton_weight: workspace carve overflow");
+  JSCC_REQUIRE(cv.ok(), "%s: workspace carve overflow", what);
+  if (stage == 1) f = f_out;
+  if (stage == 2) q = const_cast<float*>(g);  // read only by the back kernel
   cudaStream_t st = as_stream(stream);
   const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
   const float* x = img;
-  if (rotmat) {
+  if (rotmat && stage != 2) {
     int64_t blocks = (n_vox + 255) / 256;
     if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
     JSCC_TIMED("sc_gather_rot", st,
@@ -562,24 +577,24 @@ int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_e
   if (eff_dtype == JSCC_DTYPE_F32) {
     const float* e = static_cast<const float*>(eff);
     if (model == JSCC_CONE_LEGACY)
-      rc = launch_cone_weight<1, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+      rc = launch_cone_weight<1, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
     else if (win)
-      rc = launch_cone_weight<0, true, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+      rc = launch_cone_weight<0, true, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
     else
-      rc = launch_cone_weight<0, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st);
+      rc = launch_cone_weight<0, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
   } else {
     const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
     if (model == JSCC_CONE_LEGACY)
       rc = launch_cone_weight<1, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
-                                                       st);
+                                                       st, stage);
     else if (win)
       rc = launch_cone_weight<0, true, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
-                                                      st);
+                                                      st, stage);
     else
       rc = launch_cone_weight<0, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
-                                                       st);
+                                                       st, stage);
   }
-  if (rc != JSCC_OK) return rc;
+  if (rc != JSCC_OK || stage == 1) return rc;
   int64_t blocks = (n_vox + 255) / 256;
   if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
   const int has_scale = scale != 1.0f;
@@ -589,6 +604,33 @@ int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_e
                                                                           weight)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
+}
+
+int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t n_vox,
+                        int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                        const float* img, const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot,
+                        float scale, float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  return compton_stage_entry("jscc_compton_weight", 0, records, row_id, n_ev, coor, n_vox, model, use_window, eff,
+                             eff_dtype, ld_eff, img, rotmat, rotmat_inv, ld_rot, nullptr, nullptr, scale, weight,
+                             workspace, workspace_bytes, stream);
+}
+
+int jscc_compton_project(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t n_vox,
+                         int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                         const float* img, const int64_t* rotmat, int64_t ld_rot, float* f_out, void* workspace,
+                         size_t workspace_bytes, void* stream) {
+  return compton_stage_entry("jscc_compton_project", 1, records, row_id, n_ev, coor, n_vox, model, use_window, eff,
+                             eff_dtype, ld_eff, img, rotmat, nullptr, ld_rot, nullptr, f_out, 1.f, nullptr, workspace,
+                             workspace_bytes, stream);
+}
+
+int jscc_compton_backproject(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor,
+                             int64_t n_vox, int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype,
+                             int64_t ld_eff, const float* g, const int64_t* rotmat_inv, int64_t ld_rot, float scale,
+                             float* weight, void* workspace, size_t workspace_bytes, void* stream) {
+  return compton_stage_entry("jscc_compton_backproject", 2, records, row_id, n_ev, coor, n_vox, model, use_window, eff,
+                             eff_dtype, ld_eff, nullptr, nullptr, rotmat_inv, ld_rot, g, nullptr, scale, weight,
+                             workspace, workspace_bytes, stream);
 }
 
 int jscc_take_bad_detector_count(unsigned int* out) {

@@ -328,6 +328,38 @@ __global__ void sc_finish_ratio_kernel(const float* __restrict__ part, int64_t n
   }
 }
 
+// out[b][r0 + r] = f(b, r) (the forward projection itself, no ratio)
+template <int RB>
+__global__ void sc_finish_raw_kernel(const float* __restrict__ part, int64_t n_bins, int64_t nvr, int64_t L,
+                                     int maxp, int r0, int nr, float* __restrict__ out, int64_t ld_out) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_bins * RB;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / RB;
+    const int r = (int)(t % RB);
+    if (r >= nr) continue;
+    const int64_t g0 = (b * nvr) / L;
+    const int64_t g1 = ((b + 1) * nvr - 1) / L;
+    float f = 0.f;
+    for (int64_t g = g0; g <= g1; ++g) {
+      const int64_t first_row = (g * L) / nvr;
+      f += part[((g * maxp) + (b - first_row)) * RB + r];
+    }
+    out[b * ld_out + r0 + r] = f;
+  }
+}
+
+// ratio[b][r] = g[b][r0 + r] (a caller-given vector to back-project)
+template <int RB>
+__global__ void sc_load_ratio_kernel(const float* __restrict__ g, int64_t ld_g, int64_t n_bins, int r0, int nr,
+                                     float* __restrict__ ratio) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_bins * RB;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / RB;
+    const int r = (int)(t % RB);
+    ratio[t] = r < nr ? g[b * ld_g + r0 + r] : 0.f;
+  }
+}
+
 // ------------------------------------------------------------------ back (partials)
 // part[chunk][r][col] = sum_{b in chunk} A[b, col] * ratio[b][r]
 template <typename T, int RB, bool VEC>
@@ -515,13 +547,23 @@ static int launch_sc_block(const T* A, int64_t lda, const int64_t* row_idx, int6
                            int64_t ld_proj, int64_t ld_rot, int r0, int nr, const int64_t* rotinv,
                            int use_floor, float floor_v, int has_scale, float scale,
                            float* weight, const ScPlan& p, float* xr, float* ratio, float* part,
-                           float* fpart, const float* xsrc_direct, cudaStream_t st) {
+                           float* fpart, const float* xsrc_direct, cudaStream_t st, int stage = 0,
+                           float* fout = nullptr, int64_t ld_fout = 0, const float* gin = nullptr,
+                           int64_t ld_gin = 0) {
+  // stage 0: forward, ratio, back (the weight); 1: forward only into fout; 2: back-project gin
   constexpr int NV = VecTraits<T>::kVec;
   const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) &&
                       (reinterpret_cast<uintptr_t>(A) % 16 == 0);
   const int sms = num_sms();
   // forward: balanced contiguous split over warps, then fixed-order row finish
-  {
+  if (stage == 2) {
+    int64_t blocks = (n_bins * RB + 255) / 256;
+    if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
+    if (blocks < 1) blocks = 1;
+    JSCC_TIMED("sc_load_ratio", st,
+               sc_load_ratio_kernel<RB><<<(unsigned)blocks, 256, 0, st>>>(gin, ld_gin, n_bins, r0, nr, ratio));
+    JSCC_LAUNCH_CHECK();
+  } else {
     constexpr int NVv = VecTraits<T>::kVec;
     const int64_t nvr = vec_ok ? (V + NVv - 1) / NVv : V;
     const int64_t U = n_bins * nvr;
@@ -568,6 +610,13 @@ static int launch_sc_block(const T* A, int64_t lda, const int64_t* row_idx, int6
     int64_t blocks = (n_bins * RB + 255) / 256;
     if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
     if (blocks < 1) blocks = 1;
+    if (stage == 1) {
+      JSCC_TIMED("sc_finish_raw", st,
+                 sc_finish_raw_kernel<RB><<<(unsigned)blocks, 256, 0, st>>>(fpart, n_bins, nvr, L, p.fwd_maxp, r0, nr,
+                                                                            fout, ld_fout));
+      JSCC_LAUNCH_CHECK();
+      return JSCC_OK;
+    }
     JSCC_TIMED("sc_finish_ratio", st,
                sc_finish_ratio_kernel<RB><<<(unsigned)blocks, 256, 0, st>>>(
                    fpart, n_bins, nvr, L, p.fwd_maxp, row_idx, proj, ld_proj, r0, nr, use_floor,
@@ -606,12 +655,15 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
                            int64_t ld_proj, int n_rot, const float* img, const int64_t* rotmat,
                            const int64_t* rotinv, int64_t ld_rot, int use_floor, float floor_v, int has_scale,
                            float scale, float* weight, const ScPlan& p, float* xr, float* ratio,
-                           float* part, float* fpart, cudaStream_t st) {
+                           float* part, float* fpart, cudaStream_t st, int stage = 0, float* fout = nullptr,
+                           int64_t ld_fout = 0, const float* gin = nullptr, int64_t ld_gin = 0) {
   const int sms = num_sms();
   for (int r0 = 0; r0 < n_rot; r0 += p.rb) {
     const int nr = (n_rot - r0) < p.rb ? (n_rot - r0) : p.rb;
     const float* direct = nullptr;
-    if (rotmat == nullptr && nr == 1 && (reinterpret_cast<uintptr_t>(img) % 16 == 0)) {
+    if (stage == 2) {
+      // back-projection only: no image
+    } else if (rotmat == nullptr && nr == 1 && (reinterpret_cast<uintptr_t>(img) % 16 == 0)) {
       direct = img;
     } else {
       int64_t total = (int64_t)nr * V;
@@ -628,22 +680,22 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
       case 1:
         rc = launch_sc_block<T, 1>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   fpart, direct, st);
+                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin);
         break;
       case 2:
         rc = launch_sc_block<T, 2>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   fpart, direct, st);
+                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin);
         break;
       case 4:
         rc = launch_sc_block<T, 4>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   fpart, direct, st);
+                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin);
         break;
       default:
         rc = launch_sc_block<T, 8>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   fpart, direct, st);
+                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin);
         break;
     }
     if (rc != JSCC_OK) return rc;
@@ -762,6 +814,63 @@ int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* r
                                         n_vox,
                                         proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
                                         floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st);
+}
+
+// The two halves of jscc_sc_weight on their own (the differentiable projector's forward and
+// backward): out[b * ld_out + r] = A[rb] . rot_r(img), and weight += scale * sum_r
+// rotinv_r(A^T g[:, r]). Same workspace as jscc_sc_weight for the same sizes.
+static int sc_stage_entry(const char* what, int stage, const void* A, int32_t a_dtype, int64_t lda,
+                          const int64_t* row_idx, int64_t n_bins, int64_t n_vox, int32_t n_rot, const float* img,
+                          const int64_t* rotmat, const int64_t* rotmat_inv, int64_t ld_rot, float* out,
+                          int64_t ld_out, const float* g, int64_t ld_g, float scale, float* weight, void* workspace,
+                          size_t workspace_bytes, void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0, "%s: negative size", what);
+  JSCC_REQUIRE(n_rot >= 1, "%s: n_rot must be >= 1 (got %d)", what, n_rot);
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16, "%s: unsupported a_dtype %d", what, a_dtype);
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(A, "%s: null matrix", what);
+  JSCC_REQUIRE(lda >= n_vox, "%s: lda (%lld) < n_vox (%lld)", what, (long long)lda, (long long)n_vox);
+  if (stage == 1) {
+    JSCC_REQUIRE(img && out && ld_out >= n_rot, "%s: null image/output or ld_out < n_rot", what);
+    JSCC_REQUIRE(rotmat != nullptr || n_rot == 1, "%s: n_rot > 1 needs rotmat", what);
+  } else {
+    JSCC_REQUIRE(g && weight && ld_g >= n_rot, "%s: null input/weight or ld_g < n_rot", what);
+    JSCC_REQUIRE(rotmat_inv != nullptr || n_rot == 1, "%s: n_rot > 1 needs rotmat_inv", what);
+  }
+  JSCC_REQUIRE(ld_rot >= n_rot || (rotmat == nullptr && rotmat_inv == nullptr), "%s: ld_rot < n_rot", what);
+  const ScPlan p = plan_sc(n_bins, n_vox, n_rot);
+  JSCC_REQUIRE(workspace != nullptr && workspace_bytes >= p.ws_bytes, "%s: workspace too small (%zu < %zu bytes)",
+               what, workspace_bytes, p.ws_bytes);
+  Carver cv(workspace, workspace_bytes);
+  float* xr = cv.take<float>((size_t)p.rb * p.ldx);
+  float* ratio = cv.take<float>((size_t)n_bins * p.rb);
+  float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  float* fpart = cv.take<float>((size_t)p.fwd_warps * p.fwd_maxp * p.rb);
+  JSCC_REQUIRE(cv.ok(), "%s: workspace carve overflow", what);
+  const int has_scale = scale != 1.0f;
+  cudaStream_t st = as_stream(stream);
+  if (a_dtype == JSCC_DTYPE_F32)
+    return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, nullptr, 0, n_rot, img,
+                                  rotmat, rotmat_inv, ld_rot, 0, 0.f, has_scale, scale, weight, p, xr, ratio, part,
+                                  fpart, st, stage, out, ld_out, g, ld_g);
+  return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox, nullptr,
+                                        0, n_rot, img, rotmat, rotmat_inv, ld_rot, 0, 0.f, has_scale, scale, weight, p,
+                                        xr, ratio, part, fpart, st, stage, out, ld_out, g, ld_g);
+}
+
+int jscc_sc_project(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx, int64_t n_bins,
+                    int64_t n_vox, int32_t n_rot, const float* img, const int64_t* rotmat, int64_t ld_rot, float* out,
+                    int64_t ld_out, void* workspace, size_t workspace_bytes, void* stream) {
+  return sc_stage_entry("jscc_sc_project", 1, A, a_dtype, lda, row_idx, n_bins, n_vox, n_rot, img, rotmat, nullptr,
+                        ld_rot, out, ld_out, nullptr, 0, 1.f, nullptr, workspace, workspace_bytes, stream);
+}
+
+int jscc_sc_backproject(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx, int64_t n_bins,
+                        int64_t n_vox, int32_t n_rot, const float* g, int64_t ld_g, const int64_t* rotmat_inv,
+                        int64_t ld_rot, float scale, float* weight, void* workspace, size_t workspace_bytes,
+                        void* stream) {
+  return sc_stage_entry("jscc_sc_backproject", 2, A, a_dtype, lda, row_idx, n_bins, n_vox, n_rot, nullptr, nullptr,
+                        rotmat_inv, ld_rot, nullptr, 0, g, ld_g, scale, weight, workspace, workspace_bytes, stream);
 }
 
 int jscc_take_bad_index_count(unsigned int* out) {

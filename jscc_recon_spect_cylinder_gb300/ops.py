@@ -153,6 +153,109 @@ def sc_weight(
     return out
 
 
+def _rot_tables(rot, n_vox, n_rot, name):
+    t = _index_table(rot, n_vox, name)
+    if t is None:
+        return None, 1, 0
+    n = t.size(1) if n_rot is None else n_rot
+    if n < 1 or n > t.size(1):
+        raise ValueError(f"n_rot={n} out of range")
+    return t, n, t.stride(0)
+
+
+def sc_project(sysmat, img, rotmat=None, n_rot=None, row_idx=None):
+    """Forward SC projection ``f[b, r] = A[b] . rot_r(img)`` -> ``[n_bins, n_rot]``
+    (jscc_sc_project)."""
+    dev = _lib.require_cuda(sysmat, img, rotmat, row_idx, what="sc_project")
+    A = _rows_contig(sysmat)
+    n_rows, n_vox = A.shape
+    if row_idx is not None:
+        row_idx = row_idx.to(torch.int64).contiguous()
+    n_bins = n_rows if row_idx is None else row_idx.numel()
+    rm, n_rot, ld_rot = _rot_tables(rotmat, n_vox, n_rot, "rotmat")
+    x = _f32_contig(img.reshape(-1))
+    if x.numel() != n_vox:
+        raise ValueError(f"img has {x.numel()} voxels, sysmat has {n_vox}")
+    out = torch.empty((n_bins, n_rot), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sc_weight_workspace_bytes(n_bins, n_vox, n_rot))
+    rc = lib.jscc_sc_project(A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins, n_vox, n_rot,
+                             x.data_ptr(), _lib.ptr(rm), ld_rot, out.data_ptr(), out.stride(0), ws.data_ptr(),
+                             ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sc_project")
+    return out
+
+
+def sc_backproject(sysmat, g, rotmat_inv=None, n_rot=None, row_idx=None, scale=1.0, out=None):
+    """Adjoint of sc_project: ``out += scale * sum_r rotinv_r(A^T g[:, r])`` (jscc_sc_backproject)."""
+    dev = _lib.require_cuda(sysmat, g, rotmat_inv, row_idx, out, what="sc_backproject")
+    A = _rows_contig(sysmat)
+    n_rows, n_vox = A.shape
+    if row_idx is not None:
+        row_idx = row_idx.to(torch.int64).contiguous()
+    n_bins = n_rows if row_idx is None else row_idx.numel()
+    ri, n_rot, ld_rot = _rot_tables(rotmat_inv, n_vox, n_rot, "rotmat_inv")
+    gg = _f32_contig(g.reshape(n_bins, -1))
+    if gg.size(1) < n_rot:
+        raise ValueError(f"g has {gg.size(1)} columns, {n_rot} rotations requested")
+    if out is None:
+        out = torch.zeros((n_vox, 1), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_sc_weight_workspace_bytes(n_bins, n_vox, n_rot))
+    rc = lib.jscc_sc_backproject(A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins, n_vox, n_rot,
+                                 gg.data_ptr(), gg.stride(0), _lib.ptr(ri), ld_rot, float(scale), out.data_ptr(),
+                                 ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_sc_backproject")
+    return out
+
+
+def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
+                    rot_col=0):
+    """Forward list-mode projection ``f[i] = sum_j t_ij rot(img)_j`` with T recomputed
+    (jscc_compton_project) -> ``[E]``."""
+    dev = _lib.require_cuda(records, row_id, coor, img, eff, rotmat, what="compton_project")
+    c = _f32_contig(coor)
+    V = c.size(0)
+    x = _f32_contig(img.reshape(-1))
+    rm = _index_table(rotmat, V, "rotmat")
+    e, edt, ld = _eff_args(eff)
+    n = records.size(0)
+    f = torch.empty(n, dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
+    rc = lib.jscc_compton_project(records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), V, int(model),
+                                  1 if use_window else 0, _lib.ptr(e), edt, ld, x.data_ptr(),
+                                  None if rm is None else rm.data_ptr() + rot_col * 8, 0 if rm is None else rm.stride(0),
+                                  f.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_compton_project")
+    return f
+
+
+def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat_inv=None,
+                        rot_col=0, scale=1.0, out=None):
+    """Adjoint of compton_project: ``out += scale * rotinv(T^T g)`` (jscc_compton_backproject)."""
+    dev = _lib.require_cuda(records, row_id, coor, g, eff, rotmat_inv, out, what="compton_backproject")
+    c = _f32_contig(coor)
+    V = c.size(0)
+    ri = _index_table(rotmat_inv, V, "rotmat_inv")
+    e, edt, ld = _eff_args(eff)
+    n = records.size(0)
+    gg = _f32_contig(g.reshape(-1))
+    if gg.numel() != n:
+        raise ValueError(f"g has {gg.numel()} entries for {n} events")
+    if out is None:
+        out = torch.zeros((V, 1), dtype=torch.float32, device=dev)
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
+    rc = lib.jscc_compton_backproject(records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), V, int(model),
+                                      1 if use_window else 0, _lib.ptr(e), edt, ld, gg.data_ptr(),
+                                      None if ri is None else ri.data_ptr() + rot_col * 8,
+                                      0 if ri is None else ri.stride(0), float(scale), out.data_ptr(), ws.data_ptr(),
+                                      ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_compton_backproject")
+    return out
+
+
 def sc_sensitivity(sysmat: torch.Tensor, rotmat_inv: torch.Tensor | None = None, n_rot: int | None = None,
                    out: torch.Tensor | None = None, row_idx: torch.Tensor | None = None) -> torch.Tensor:
     """``out += (sum_r colsum(A)[rotmat_inv[:, r] - 1]) / n_rot`` over the first ``n_rot``
