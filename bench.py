@@ -1,7 +1,8 @@
 """Benchmark of the GB300 OSEM hot path; prints ONE JSON line (rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload jsccsd3|sc3|sc3-small] [--no-cpu-baseline] [--no-e2e]
+                    [--workload jsccsd3|jsccsd-small|sc3|sc3-small|sparse-launch|cone2|map5]
+                    [--no-cpu-baseline] [--no-e2e]
 
 Workload "jsccsd3" (default): JSCCSD joint OSEM at the joint configuration's size —
 SC channel 20 views x 4,096 pixels = 81,920 bins x 36,000 voxels (100 x 360 polar grid,
@@ -13,7 +14,11 @@ system matrix and the sparse rows stored in BF16 (FP32 accumulation), the plain 
 storage run beside it, plus Compton event-voxel pairs/s. Inputs are synthetic (seeded)
 and far larger than L2, so no L2 flush is needed between timed iterations.
 
-Workload "sc3": the SC channel alone; "sc3-small": an 8,192-row SC case for profiling.
+Workload "sc3": the SC channel alone; "sc3-small": an 8,192-row SC case for profiling;
+"sparse-launch": one grouped sparse Compton weight launch (profiling case); "cone2": the
+fused strict cone weight of the list-mode configuration (200k events, event-voxel pairs/s);
+"map5": one Adam step of the differentiable MAP objective (SC + 2M Compton events + RDP
+prior, MAP steps/s).
 
 Multi-GPU: the path is run as independent replicas (one per rank, no collective on
 the data path); `value` sums the replicas' subset-iterations over the slowest rank's
@@ -302,6 +307,40 @@ class Cone2Bench:
         rounded to 100. Pairs outside the window stop after the test (~20)."""
         return self.K_CONE
 
+    def stored_t(self, img):
+        """The same weight from a stored dense T (FP32 [E, V], materialised once by the cone
+        kernel): build time, the streamed weight's time (T read twice: forward and back),
+        its HBM rate against the measured peak, and its agreement with the fused weight."""
+        from jscc_recon_spect_cylinder_gb300 import ops
+        from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+        ev, dev = self.ev, self.dev
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        _, T = ops.compton_cone_rows(ev.records, ev.row_id, self.coor, model=ev.model, eff=self.A, want_tc=False)
+        t1.record()
+        torch.cuda.synchronize(dev)
+        build_ms = t0.elapsed_time(t1)
+        w = rop.get_weight_compton(T, img)
+        torch.cuda.synchronize(dev)
+        n = 3
+        t0.record()
+        for _ in range(n):
+            w = rop.get_weight_compton(T, img)
+        t1.record()
+        torch.cuda.synchronize(dev)
+        ms = t0.elapsed_time(t1) / n
+        self.step(img, "f32", use_window=False)
+        rel = float((w - self.w).norm() / self.w.norm())
+        nbytes = 2 * T.numel() * 4
+        del T, w
+        torch.cuda.empty_cache()
+        gbs = nbytes / (ms / 1e3) / 1e9
+        hbm = measured_peaks()["hbm_gbs"]
+        return {"t_bytes": nbytes // 2, "build_ms": build_ms, "weight_ms": ms,
+                "pairs_per_s": self.units_per_step() / (ms / 1e3), "hbm_gbs": gbs, "hbm_frac": gbs / hbm,
+                "rel_l2_vs_fused_no_window": rel}
+
     def config(self):
         return {"workload": self.name, "voxels": self.V, "events_listed": self.n_list, "events_kept": len(self.ev),
                 "detector_pixels": 8192, "e0_mev": 0.511, "window_sigmas": 9.0, "model": "strict",
@@ -324,7 +363,128 @@ class Cone2Bench:
         pairs = self.units_per_step() / (ms / 1e3)
         peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 FMA peak, TFLOP/s (no measured figure)
         achieved = pairs * self.K_CONE / 1e12
-        return {"no_window": {"pairs_per_s": pairs, "ms_per_step": ms},
+        stored = self.stored_t(img)
+        return {"no_window": {"pairs_per_s": pairs, "ms_per_step": ms}, "stored_t": stored,
+                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                                  "flop_per_pair": self.K_CONE}}
+
+
+class Map5Bench:
+    """Config 5 (differentiable MAP): one Adam step of Phi(z) = -L(e^z) + beta R(e^z) on a
+    log-parameterised 100 x 360 image. SC channel: 20 views x 4,096 pixels = 81,920 bins x
+    36,000 voxels, FP32, flat (11.8 GB), Poisson data at 1e7 counts from the hot-rod phantom.
+    Compton channel: 2,000,000 two-interaction events at 662 keV (scatter cylinder of view 0,
+    absorber r = 150 mm), energies blurred as in config 2, strict model, T recomputed in the
+    forward and in the adjoint pass (cos-beta window at 9 sigma). Prior: relative difference,
+    beta = 0.01, gamma = 2, 8-neighbourhood. A step = SC forward + adjoint, Compton forward +
+    adjoint, prior value + gradient, the exp / log-chain and the Adam update."""
+
+    K_CONE = Cone2Bench.K_CONE
+
+    def __init__(self, dev, n_events=2_000_000, views=20, seed=None):
+        from jscc_recon_spect_cylinder_gb300 import ops, prior
+        from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+        from jscc_recon_spect_cylinder_gb300 import synthetic
+
+        seed = synthetic.SEED if seed is None else seed
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        grid = synthetic.polar_grid(100, 360, 100.0, device=dev)
+        pitch = 2.0 * math.pi * 120.0 / 128
+        scat_views = [synthetic.cylinder_pixels(120.0, 128, 32, 2.0, 2 * math.pi * v / views, dev) for v in range(views)]
+        A = torch.cat([synthetic.sc_system_matrix(grid.coor, p, pitch * 2.0, 100.0, generator=gen)
+                       for p in scat_views], dim=0)
+        x_true = synthetic.hot_rod_phantom(grid.coor.cpu(), 100.0).to(dev)
+        self.y = synthetic.poisson_projection(A, x_true, 1e7, generator=gen)
+        self.A = A
+        scat = scat_views[0]
+        absb = synthetic.cylinder_pixels(150.0, 128, 32, 2.0, 0.0, dev)
+        det = torch.cat((scat, absb), dim=0).to(torch.float32)
+        e0 = 0.662
+        lst = synthetic.compton_list(grid.coor, x_true, scat, 150.0, 128, 32, 2.0, e0, int(n_events * 2.3) + 64, gen,
+                                     cp1_offset=0, cp2_offset=scat.size(0))[:n_events]
+        res = 0.08 * (0.662 / e0) ** 0.5
+        noise = torch.randn((lst.size(0), 2), generator=gen, device=dev)
+        for k, col in ((0, 1), (1, 3)):
+            e = lst[:, col]
+            lst[:, col] = e + (e * res / 2.355 * (e0 / e) ** 0.5) * noise[:, k]
+        thr_max = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
+        self.coor = grid.coor.to(torch.float32)
+        self.eff = A[:scat.size(0)]  # efficiency rows of the scatter pixels (view 0 of the SC matrix)
+        self.ev = pls.get_compton_event_params(self.eff, det, self.coor, lst, 1.0, 1.0, e0, res, thr_max, 0.05,
+                                               e0 - 0.06, window_sigmas=9.0)
+        self.n_list = lst.size(0)
+        del lst, noise
+        self.V = grid.n_vox
+        self.s_c = ops.compton_backproject(self.ev.records, self.ev.row_id, self.coor,
+                                           torch.ones(len(self.ev), device=dev), model=self.ev.model, eff=self.eff)
+        self.table = prior.polar_neighbours(grid.coor.cpu()).to(dev)
+        self.beta, self.gamma, self.lr = 0.01, 2.0, 0.05
+        self.z = torch.zeros((self.V, 1), device=dev, requires_grad=True)
+        self.opt = torch.optim.Adam([self.z], lr=self.lr)
+        self.dev = dev
+        self.subsets = 1
+        self.name = "map-config5"
+        self.metric = "MAP steps/s: SC + Compton log-likelihood + RDP prior, forward + adjoint + Adam, config 5, 1xGB300"
+        self.unit = "MAP steps/s"
+        self.dtypes = ("f32",)
+        self.traffic_file = "traffic_map5.json"
+        torch.cuda.synchronize(dev)
+
+    def objective(self, z):
+        from jscc_recon_spect_cylinder_gb300 import autograd as ag
+
+        x = torch.exp(z)
+        return (-ag.poisson_log_likelihood(x, sc=(self.A, self.y, None, None),
+                                           compton=(self.ev, self.coor, self.eff, self.s_c))
+                + ag.rdp_prior(x, self.table, beta=self.beta, gamma=self.gamma))
+
+    def step(self, img, dtype):
+        self.opt.zero_grad(set_to_none=False)
+        self.objective(self.z).backward()
+        self.opt.step()
+        return img
+
+    def units_per_step(self):
+        return 1
+
+    def kernel_bytes(self, dtype):
+        return {}
+
+    def config(self):
+        return {"workload": self.name, "voxels": self.V, "sc_bins": self.A.size(0), "sc_dtype": "f32",
+                "events_listed": self.n_list, "events_kept": len(self.ev), "e0_mev": 0.662, "window_sigmas": 9.0,
+                "beta": self.beta, "gamma": self.gamma, "optimizer": f"Adam lr {self.lr} (log-intensity)",
+                "l2": "SC matrix 11.8 GB > L2 (streamed twice per step); records 90 MB"}
+
+    def extra(self, ms_per_step):
+        """Compton share of the step and the FP32 roofline of its cone passes without the
+        window (every pair evaluated), as for config 2."""
+        from jscc_recon_spect_cylinder_gb300 import ops
+
+        x = torch.ones((self.V, 1), device=self.dev)
+        g = torch.ones(len(self.ev), device=self.dev)
+
+        def cone_pass():
+            f = ops.compton_project(self.ev.records, self.ev.row_id, self.coor, x, model=self.ev.model, eff=self.eff,
+                                    use_window=False)
+            ops.compton_backproject(self.ev.records, self.ev.row_id, self.coor, g, model=self.ev.model, eff=self.eff,
+                                    use_window=False)
+            return f
+
+        cone_pass()
+        torch.cuda.synchronize(self.dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        cone_pass()
+        t1.record()
+        torch.cuda.synchronize(self.dev)
+        ms = t0.elapsed_time(t1)
+        pairs = 2 * len(self.ev) * self.V
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        achieved = pairs / (ms / 1e3) * self.K_CONE / 1e12
+        return {"no_window_cone_pass": {"pairs_per_s": pairs / (ms / 1e3), "ms": ms},
                 "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                                   "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
                                   "flop_per_pair": self.K_CONE}}
@@ -523,6 +683,8 @@ def make_workload(name, dev):
         return SparseLaunchBench(dev)
     if name == "cone2":
         return Cone2Bench(dev)
+    if name == "map5":
+        return Map5Bench(dev)
     if name == "sc3":
         return Sc3Workload(dev)
     if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
@@ -685,7 +847,7 @@ def ours_arm(args):
             line["speedup_bf16_vs_fp32"] = value / second["value"]
         line.update({"errors_vs_fp64": errors, "errors_after_iterations": err_iters, "gpu_launches": launches,
                      "clocks": clocks, "roofline": roofline, "kernels": kernels, "e2e": e2e, "cpu_baseline": cpu})
-        extra = work.extra(ms_main / args.steps)
+        extra = {} if args.no_extra else work.extra(ms_main / args.steps)
         if roofline is None and "fp32_roofline" in extra:
             top = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"]) if kernels else None
             line["roofline"] = dict(extra.pop("fp32_roofline"), kernel=top, traffic=None)
@@ -703,11 +865,13 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2"],
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2", "map5"],
                     default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-errors", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the workload's extra figures (e.g. cone2's stored-T arm): small profiling runs")
     ap.add_argument("--error-iters", type=int, default=10,
                     help="iterations (from a uniform image) at which BF16 / FP32 images are compared with FP64")
     args = ap.parse_args()

@@ -144,8 +144,9 @@ JSCC_API int jscc_sc_backproject(const void* A, int32_t a_dtype, int64_t lda, co
  * Replaces main_local_cntstat.py:140-146 (compute_sensitivity_local) and the s_map_s loop of
  * main_plane_sparse.py:440-444 (one call per energy; the caller sums energies). rotmat_inv
  * NULL means the identity (n_rot must then be 1). Workspace:
- * jscc_sc_weight_workspace_bytes(n_bins, n_vox, 1). The sum over rows runs in a fixed
- * chunk order (deterministic).
+ * jscc_sc_weight_workspace_bytes(n_bins, n_vox, 1). The sum over rows is Kahan-compensated
+ * (within row chunks, then over the chunk sums and their carried errors, in a fixed order:
+ * deterministic, and within a few ulp of the exact column sum for any row count).
  */
 JSCC_API int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
                    int64_t n_bins, int64_t n_vox, int32_t n_rot, const int64_t* rotmat_inv,
@@ -423,6 +424,23 @@ JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coa
 JSCC_API int jscc_em_update(float* img_out, const float* img, const float* w_a, int32_t has_coef_a,
                    float coef_a, const float* w_b, float coef_b, const float* s_map, int64_t n_vox,
                    int32_t mode, float eps, void* stream);
+
+/* ------------------------------------------------------------ MAP prior */
+
+/*
+ * Relative-difference prior (Nuyts et al. 2002) of img over a symmetric neighbour table,
+ * value and gradient in one pass (the reference has no MAP path; this serves gradient-driven
+ * reconstruction through the forward/adjoint projectors above):
+ *   R(x) = 1/2 sum_j sum_{k in N(j)} w_jk (x_j - x_k)^2 / (x_j + x_k + gamma |x_j - x_k| + eps)
+ * nbr / weight are neighbour-major [n_nbr, n_vox] (entry k * n_vox + j is the k-th neighbour
+ * of voxel j, -1 = none); every edge must appear in both directions with the same weight.
+ * value (may be NULL): *value += beta * R(x) (double, device memory; the caller zeroes it).
+ * grad  (may be NULL): grad[j] = (accumulate ? grad[j] : 0) + beta * dR/dx_j.
+ * Out-of-range neighbour indices are skipped and counted (jscc_take_bad_index_count).
+ */
+JSCC_API int jscc_rdp_prior(const float* img, const int32_t* nbr, const float* weight, int64_t n_vox,
+                   int32_t n_nbr, float gamma, float eps, float beta, double* value, float* grad,
+                   int32_t accumulate, void* stream);
 
 #ifdef __cplusplus
 }

@@ -65,6 +65,11 @@ _SIGNATURES: dict[str, tuple] = {
         [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
          c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
+    "jscc_rdp_prior": (
+        c_int,
+        [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_float, c_float, c_float, c_void_p, c_void_p, c_int32,
+         c_void_p],
+    ),
     "jscc_sc_sensitivity": (
         c_int,
         [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_int64, c_void_p, c_void_p,

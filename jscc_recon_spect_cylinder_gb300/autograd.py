@@ -9,6 +9,10 @@ as the OSEM weights). The Poisson log-likelihood of the joint data,
 
 has the gradient A^T(y / f) - A^T 1 + T^T(1 / g) - s_C, i.e. the OSEM weights minus the
 sensitivities (recon_osem_plane.py:28-42), which tests/test_autograd_gpu.py checks.
+
+RDPPrior is the relative-difference prior (jscc_rdp_prior: value and gradient in one pass,
+the gradient kept for backward), and map_reconstruct minimises
+-L(exp z) + beta R(exp z) over the log-parameterised image z.
 """
 from __future__ import annotations
 
@@ -81,3 +85,48 @@ def poisson_log_likelihood(x, sc=None, compton=None, eps=float(torch.finfo(torch
         g = compton_project(x, events, coor, sysmat).double()
         total = total + torch.log(g.clamp_min(eps)).sum() - (s_c.reshape(-1).double() * x.reshape(-1).double()).sum()
     return total
+
+
+class RDPPrior(torch.autograd.Function):
+    """beta R(x) over a NeighbourTable; the forward pass computes the gradient too."""
+
+    @staticmethod
+    def forward(ctx, x, table, beta, gamma, eps):
+        value, grad = ops.rdp_prior(x.detach(), table.nbr, table.weight, gamma=gamma, beta=beta, eps=eps)
+        ctx.save_for_backward(grad)
+        ctx.shape = x.shape
+        return value
+
+    @staticmethod
+    def backward(ctx, gv):
+        (grad,) = ctx.saved_tensors
+        return (grad * gv.to(grad.dtype)).reshape(ctx.shape), None, None, None, None
+
+
+def rdp_prior(x, table, beta=0.01, gamma=2.0, eps=1e-9):
+    """beta R(x) (float64 0-d tensor), differentiable in x."""
+    return RDPPrior.apply(x, table, beta, gamma, eps)
+
+
+def map_reconstruct(x0, sc=None, compton=None, table=None, beta=0.01, gamma=2.0, n_steps=200, lr=0.05,
+                    eps=1e-9, callback=None):
+    """MAP estimate on a log-parameterised image: minimise
+    Phi(z) = -L(exp z) + beta R(exp z) with Adam (``lr`` is a step in log-intensity, so it is
+    scale-free). ``sc`` / ``compton`` as in poisson_log_likelihood; ``table`` a NeighbourTable
+    on the device (None: no prior). Returns (x, objective history [n_steps] float64 on the
+    host); ``callback(step, x, objective)`` is called after each step with device tensors."""
+    z = torch.log(x0.detach().float().clamp_min(torch.finfo(torch.float32).tiny)).requires_grad_(True)
+    opt = torch.optim.Adam([z], lr=lr)
+    hist = []
+    for it in range(n_steps):
+        opt.zero_grad(set_to_none=False)
+        x = torch.exp(z)
+        obj = -poisson_log_likelihood(x, sc=sc, compton=compton)
+        if table is not None and beta != 0:
+            obj = obj + rdp_prior(x, table, beta=beta, gamma=gamma, eps=eps)
+        obj.backward()
+        opt.step()
+        hist.append(obj.detach())
+        if callback is not None:
+            callback(it, torch.exp(z.detach()), obj.detach())
+    return torch.exp(z.detach()), torch.stack(hist).cpu() if hist else torch.zeros(0, dtype=torch.float64)

@@ -211,6 +211,89 @@ __device__ __forceinline__ float cone_value(const ConeEvent& e, float cx, float 
   }
 }
 
+// ------------------------------------------------------------------ fast strict evaluation
+// The fused forward / back passes evaluate the strict kernel from a staged copy of the record
+// whose per-event factors are computed once: the unit second-leg direction w = v12 / d12,
+// 1 / d12, and the per-axis position variances divided by d12^2 (the Jacobian of beta in the
+// hit positions carries 1 / d12). Per pair: one refined reciprocal square root gives 1 / d01
+// and the unit first leg, cos(beta) = (a . w) / d01 serves as both the window test and the
+// sigma_pos cosine, sigma_pos^2 is used directly (the formula squares it again), the Gaussian
+// exponent takes one quotient, and the quotient and the exponential use the fast hardware forms. The materialised rows and the row
+// statistics (event selection) keep the reference-ordered arithmetic of cone_value.
+struct alignas(16) ConeFast {
+  float p1x, p1y, p1z;
+  float wx, wy, wz;       // v12 / max(d12, 1e-7)
+  float theta;
+  float sig_plus, sig_minus;
+  float kn;
+  float q0, q1, q2;       // s_k / max(d12, 1e-7)^2
+  float cos_lo, cos_hi;
+  float pad;
+};
+static_assert(sizeof(ConeFast) == 64, "staged record layout");
+
+__device__ __forceinline__ ConeFast stage_fast(const ConeEvent& r) {
+  ConeFast f;
+  const float i12 = 1.0f / fmaxf(r.d12, 1e-7f);
+  f.p1x = r.p1x; f.p1y = r.p1y; f.p1z = r.p1z;
+  f.wx = r.vx * i12; f.wy = r.vy * i12; f.wz = r.vz * i12;
+  f.theta = r.theta;
+  f.sig_plus = r.sig_plus;
+  f.sig_minus = r.sig_minus;
+  f.kn = r.kn;
+  f.q0 = r.s0 * i12 * i12; f.q1 = r.s1 * i12 * i12; f.q2 = r.s2 * i12 * i12;
+  f.cos_lo = r.cos_lo;
+  f.cos_hi = r.cos_hi;
+  f.pad = 0.f;
+  return f;
+}
+
+template <bool WINDOW>
+__device__ __forceinline__ float cone_value_fast(const ConeFast& e, float cx, float cy, float cz) {
+  const float ax = e.p1x - cx, ay = e.p1y - cy, az = e.p1z - cz;
+  const float d2 = fmaxf(fmaf(ax, ax, fmaf(ay, ay, az * az)), 1e-14f);
+  // 1 / d01: hardware estimate plus one Newton-Raphson step, r (3 - d2 r^2) / 2
+  const float r0 = rsqrtf(d2);
+  const float i01 = r0 * fmaf(-0.5f * d2 * r0, r0, 1.5f);
+  const float bcos = fmaf(ax, e.wx, fmaf(ay, e.wy, az * e.wz)) * i01;
+  if (WINDOW && (bcos < e.cos_lo || bcos > e.cos_hi)) return 0.f;
+  const float c = fminf(fmaxf(bcos, -1.0f + 1e-7f), 1.0f - 1e-7f);
+  const float delta = acosf(c) - e.theta;
+  const float sig_e = delta >= 0.f ? e.sig_plus : e.sig_minus;
+  // grad beta: (u01 - cos(beta) w) / d12 per axis, u01 = a / d01
+  const float jx = fmaf(-bcos, e.wx, ax * i01);
+  const float jy = fmaf(-bcos, e.wy, ay * i01);
+  const float jz = fmaf(-bcos, e.wz, az * i01);
+  const float sb2 = fmaxf(fmaf(-bcos, bcos, 1.0f), 1e-12f);
+  // sigma^2 = max(sigma_E^2 + max(num / sb2, 1e-12), 1e-12) with num / sb2 = sigma_pos^2, carried
+  // as sb2 * sigma^2 so the Gaussian exponent needs one quotient
+  const float num = fmaf(jx * jx, e.q0, fmaf(jy * jy, e.q1, jz * jz * e.q2));
+  const float sig2sb = fmaxf(fmaf(sig_e * sig_e, sb2, fmaxf(num, 1e-12f * sb2)), 1e-12f * sb2);
+  const float sinb2 = (1.0f - c) * (1.0f + c);
+  return __expf(__fdividef(-(delta * delta) * sb2, 2.0f * sig2sb)) * (e.kn - sinb2);
+}
+
+// Record type staged in shared memory and its evaluation: the fast form for the strict model
+// in the fused passes, the reference-ordered form otherwise.
+template <int MODEL, bool FAST>
+struct ConeStage {
+  using type = ConeEvent;
+  __device__ static ConeEvent stage(const ConeEvent& r) { return r; }
+  template <bool WINDOW>
+  __device__ static float eval(const ConeEvent& e, float cx, float cy, float cz) {
+    return cone_value<MODEL, WINDOW>(e, cx, cy, cz);
+  }
+};
+template <>
+struct ConeStage<0, true> {
+  using type = ConeFast;
+  __device__ static ConeFast stage(const ConeEvent& r) { return stage_fast(r); }
+  template <bool WINDOW>
+  __device__ static float eval(const ConeFast& e, float cx, float cy, float cz) {
+    return cone_value_fast<WINDOW>(e, cx, cy, cz);
+  }
+};
+
 template <typename TE>
 __device__ __forceinline__ float eff_load(const TE* p, int64_t i);
 template <>
@@ -247,14 +330,15 @@ cone_forward_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict
                     const float* __restrict__ coor, int64_t V, const float* __restrict__ x,
                     const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ f_out,
                     float* __restrict__ s1_out, float* __restrict__ s2_out, int32_t* __restrict__ nan_out) {
-  __shared__ ConeEvent sev[EB];
+  using Stage = ConeStage<MODEL, !STATS>;
+  __shared__ typename Stage::type sev[EB];
   __shared__ int64_t srow[EB];
   __shared__ float red[kConeThreads / 32][EB * (STATS ? 4 : 1)];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i0 = (int64_t)blockIdx.x * EB;
   if (tid < EB) {
     const int64_t i = i0 + tid < n_ev ? i0 + tid : n_ev - 1;
-    sev[tid] = rec[i];
+    sev[tid] = Stage::stage(rec[i]);
     srow[tid] = (int64_t)row_id[i] * ld_eff;
   }
   __syncthreads();
@@ -268,7 +352,7 @@ cone_forward_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict
 #pragma unroll
     for (int e = 0; e < EB; ++e) {
       if (e < ne) {
-        float t = cone_value<MODEL, WINDOW>(sev[e], cx, cy, cz);
+        float t = Stage::template eval<WINDOW>(sev[e], cx, cy, cz);
         if (t != 0.f) {
           t = eff ? t * eff_load(eff + srow[e], j) : t;
           af[e] = fmaf(t, xj, af[e]);
@@ -334,7 +418,8 @@ __global__ void __launch_bounds__(kConeThreads)
 cone_back_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
                  int64_t ev_per_chunk, const float* __restrict__ q, const float* __restrict__ coor, int64_t V,
                  const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp) {
-  __shared__ ConeEvent sev[kBackStage];
+  using Stage = ConeStage<MODEL, true>;
+  __shared__ typename Stage::type sev[kBackStage];
   __shared__ int64_t srow[kBackStage];
   __shared__ float sq[kBackStage];
   const int tid = threadIdx.x;
@@ -353,14 +438,14 @@ cone_back_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ 
     const int n = (e_end - s) < kBackStage ? (int)(e_end - s) : kBackStage;
     __syncthreads();
     if (tid < n) {
-      sev[tid] = rec[s + tid];
+      sev[tid] = Stage::stage(rec[s + tid]);
       srow[tid] = (int64_t)row_id[s + tid] * ld_eff;
       sq[tid] = q[s + tid];
     }
     __syncthreads();
     if (j < V) {
       for (int e = 0; e < n; ++e) {
-        float t = cone_value<MODEL, WINDOW>(sev[e], cx, cy, cz);
+        float t = Stage::template eval<WINDOW>(sev[e], cx, cy, cz);
         if (t != 0.f) {
           t = eff ? t * eff_load(eff + srow[e], j) : t;
           acc = fmaf(t, sq[e], acc);

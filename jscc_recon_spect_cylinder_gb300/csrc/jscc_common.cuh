@@ -65,6 +65,8 @@ void timing_end(const char* name, cudaStream_t st);
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 int num_sms();
+// Read and clear the neighbour-table index counter of the prior kernel (prior.cu).
+unsigned int take_prior_bad_index_count();
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 

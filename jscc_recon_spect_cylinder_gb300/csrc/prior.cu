@@ -1,0 +1,95 @@
+// Relative-difference prior (Nuyts et al., IEEE Trans. Nucl. Sci. 49(1):56-60, 2002) over a
+// symmetric neighbour table, value and gradient in one pass:
+//
+//   R(x)      = 1/2 sum_j sum_{k in N(j)} w_jk phi(x_j, x_k)
+//   phi(a, b) = d^2 / D,   d = a - b,   D = a + b + gamma |d| + eps
+//   dR/dx_j   = sum_{k in N(j)} w_jk dphi/da(x_j, x_k)
+//   dphi/da   = d (2 D - d (1 + gamma sgn d)) / D^2 = d (a + 3 b + gamma |d| + 2 eps) / D^2
+//
+// phi is symmetric in (a, b) and the table holds every edge in both directions with the same
+// weight, so the gradient is a gather over the voxel's own neighbours (no atomics). The table
+// is neighbour-major ([K, V]: nbr[k * V + j]) so a warp's loads of one neighbour slot are
+// coalesced; slot entries of -1 are padding. The image is only gathered from (36,000 voxels
+// at the 100 x 360 grid: 144 KB, L1/L2 resident), so the pass streams the 8 bytes per slot
+// of the table and writes 4 bytes per voxel.
+#include "jscc_common.cuh"
+
+namespace jscc {
+
+constexpr int kPriorThreads = 256;
+
+__device__ unsigned int g_prior_bad_index_count = 0;  // out-of-range neighbour indices seen
+
+// Read and clear this unit's counter (jscc_take_bad_index_count adds it to its own).
+unsigned int take_prior_bad_index_count() {
+  unsigned int h = 0, zero = 0;
+  if (cudaMemcpyFromSymbol(&h, g_prior_bad_index_count, sizeof(h)) != cudaSuccess) return 0;
+  cudaMemcpyToSymbol(g_prior_bad_index_count, &zero, sizeof(zero));
+  return h;
+}
+
+__global__ void __launch_bounds__(kPriorThreads)
+rdp_prior_kernel(const float* __restrict__ x, const int32_t* __restrict__ nbr, const float* __restrict__ wt,
+                 int64_t n_vox, int n_nbr, float gamma, float eps, float beta, double* __restrict__ value,
+                 float* __restrict__ grad, int accumulate) {
+  __shared__ float red[kPriorThreads / 32];
+  float part = 0.f;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n_vox;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const float a = x[j];
+    float g = 0.f;
+    for (int k = 0; k < n_nbr; ++k) {
+      const int32_t i = nbr[(int64_t)k * n_vox + j];
+      if (i < 0) continue;
+      if ((int64_t)i >= n_vox) {  // corrupt table: counted for the host, access skipped
+        atomicAdd(&g_prior_bad_index_count, 1u);
+        continue;
+      }
+      const float b = x[i];
+      const float w = wt[(int64_t)k * n_vox + j];
+      const float d = a - b;
+      if (d == 0.f) continue;  // phi and its derivative vanish (and D may be 0)
+      const float ad = fabsf(d);
+      const float D = a + b + gamma * ad + eps;
+      const float inv = 1.0f / D;
+      part += w * d * d * inv;
+      g += w * d * (a + 3.0f * b + gamma * ad + 2.0f * eps) * inv * inv;
+    }
+    if (grad != nullptr) grad[j] = (accumulate ? grad[j] : 0.f) + beta * g;
+  }
+  if (value == nullptr) return;
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = part;
+  __syncthreads();
+  if (warp == 0) {
+    part = lane < kPriorThreads / 32 ? red[lane] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) atomicAdd(value, 0.5 * (double)beta * (double)part);
+  }
+}
+
+}  // namespace jscc
+
+using namespace jscc;
+
+extern "C" int jscc_rdp_prior(const float* img, const int32_t* nbr, const float* weight, int64_t n_vox,
+                              int32_t n_nbr, float gamma, float eps, float beta, double* value, float* grad,
+                              int32_t accumulate, void* stream) {
+  JSCC_REQUIRE(n_vox >= 0 && n_vox <= INT32_MAX, "jscc_rdp_prior: n_vox %lld out of range", (long long)n_vox);
+  JSCC_REQUIRE(n_nbr >= 0 && n_nbr <= 64, "jscc_rdp_prior: n_nbr %d out of range [0, 64]", n_nbr);
+  JSCC_REQUIRE(gamma >= 0.f && eps >= 0.f, "jscc_rdp_prior: gamma and eps must be >= 0");
+  JSCC_REQUIRE(value != nullptr || grad != nullptr, "jscc_rdp_prior: neither value nor grad requested");
+  if (n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(img != nullptr && (n_nbr == 0 || (nbr != nullptr && weight != nullptr)),
+               "jscc_rdp_prior: null pointer argument");
+  int64_t blocks = (n_vox + kPriorThreads - 1) / kPriorThreads;
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  cudaStream_t st = as_stream(stream);
+  JSCC_TIMED("rdp_prior", st,
+             rdp_prior_kernel<<<(unsigned)blocks, kPriorThreads, 0, st>>>(img, nbr, weight, n_vox, n_nbr, gamma,
+                                                                        eps, beta, value, grad, accumulate));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}

@@ -441,6 +441,57 @@ sc_back_partial_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __re
   }
 }
 
+// ------------------------------------------------------------------ compensated column sums
+// Kahan summation (Kahan 1965): s accumulates, c carries the rounding error of each add with
+// the opposite sign; every add is an explicit round-to-nearest op so nothing is contracted.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = __fsub_rn(v, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+
+// sum[chunk][col] / comp[chunk][col]: compensated column sums of the chunk's rows of A.
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kColTile / VecTraits<T>::kVec)
+sc_colsum_kahan_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx, int64_t n_bins,
+                       int64_t V, int64_t rows_per_chunk, float* __restrict__ sum, float* __restrict__ comp,
+                       int64_t ldp) {
+  constexpr int NV = VecTraits<T>::kVec;
+  const int64_t col = (int64_t)blockIdx.x * kColTile + (int64_t)threadIdx.x * NV;
+  const int64_t b_begin = (int64_t)blockIdx.y * rows_per_chunk;
+  int64_t b_end = b_begin + rows_per_chunk;
+  if (b_end > n_bins) b_end = n_bins;
+  if (col >= V) return;
+  const int ncol = (int)((V - col) < NV ? (V - col) : NV);
+  float sa[NV], ca[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) sa[k] = ca[k] = 0.f;
+  if (VEC && ncol == NV) {
+    for (int64_t b = b_begin; b < b_end; ++b) {
+      float a[NV];
+      load_vec<T>(A + (row_idx ? row_idx[b] : b) * lda + col, a);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) kahan_add(sa[k], ca[k], a[k]);
+    }
+  } else {
+    for (int64_t b = b_begin; b < b_end; ++b) {
+      const T* rowb = A + (row_idx ? row_idx[b] : b) * lda;
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        if (k < ncol) kahan_add(sa[k], ca[k], load_elem(rowb, col + k));
+    }
+  }
+  float* ds = sum + (int64_t)blockIdx.y * ldp + col;
+  float* dc = comp + (int64_t)blockIdx.y * ldp + col;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+    if (k < ncol) {
+      ds[k] = sa[k];
+      dc[k] = ca[k];
+    }
+}
+
 // ------------------------------------------------------------------ reduce + inverse rotation
 __global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
                                          int nr, int rb_stride, const int64_t* __restrict__ rotinv,
@@ -467,19 +518,15 @@ __global__ void sc_reduce_scatter_kernel(const float* __restrict__ part, int64_t
 }
 
 // SC sensitivity: s[j] += (sum_r colsum[rotinv[j, r] - 1]) / n_rot, colsum[c] = the chunk
-// partials of column c summed in chunk order (rotations summed first, then divided, as
-// main_local_cntstat.py:140-146 does).
-__global__ void sc_fill_kernel(float* __restrict__ p, int64_t n, float v) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = v;
-}
+// partials of column c and their carried errors summed in chunk order with compensation
+// (rotations summed first, then divided, as main_local_cntstat.py:140-146 does).
 
-__global__ void sc_sensitivity_kernel(const float* __restrict__ part, int64_t ldp, int chunks,
-                                      const int64_t* __restrict__ rotinv, int64_t ld_rot, int n_rot, int64_t V,
-                                      float* __restrict__ weight) {
+__global__ void sc_sensitivity_kernel(const float* __restrict__ sum, const float* __restrict__ comp, int64_t ldp,
+                                      int chunks, const int64_t* __restrict__ rotinv, int64_t ld_rot, int n_rot,
+                                      int64_t V, float* __restrict__ weight) {
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V;
        j += (int64_t)gridDim.x * blockDim.x) {
-    float acc = 0.f;
+    float acc = 0.f, acc_c = 0.f;
     for (int r = 0; r < n_rot; ++r) {
       int64_t src = j;
       if (rotinv != nullptr) {
@@ -489,11 +536,15 @@ __global__ void sc_sensitivity_kernel(const float* __restrict__ part, int64_t ld
           continue;
         }
       }
-      float s = 0.f;
-      for (int c = 0; c < chunks; ++c) s += part[(int64_t)c * ldp + src];
-      acc = __fadd_rn(acc, s);
+      // the chunk sums and their carried errors, compensated in chunk order
+      float s = 0.f, c = 0.f;
+      for (int k = 0; k < chunks; ++k) {
+        kahan_add(s, c, sum[(int64_t)k * ldp + src]);
+        kahan_add(s, c, -comp[(int64_t)k * ldp + src]);
+      }
+      kahan_add(acc, acc_c, __fsub_rn(s, c));
     }
-    weight[j] = __fadd_rn(weight[j], __fdiv_rn(acc, (float)n_rot));
+    weight[j] = __fadd_rn(weight[j], __fdiv_rn(__fsub_rn(acc, acc_c), (float)n_rot));
   }
 }
 
@@ -705,32 +756,28 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
 
 template <typename T>
 static int sc_sensitivity_typed(const T* A, int64_t lda, const int64_t* row_idx, int64_t n_bins, int64_t V,
-                                int n_rot, const int64_t* rotinv, int64_t ld_rot, float* weight, const ScPlan& p,
-                                float* ratio, float* part, cudaStream_t st) {
+                                int n_rot, const int64_t* rotinv, int64_t ld_rot, float* weight, int64_t col_tiles,
+                                int64_t chunks, int64_t rows_per_chunk, int64_t ldp, float* sum, float* comp,
+                                cudaStream_t st) {
   constexpr int NV = VecTraits<T>::kVec;
   const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) && (reinterpret_cast<uintptr_t>(A) % 16 == 0);
   const int sms = num_sms();
-  int64_t blocks = (n_bins + 255) / 256;
-  if (blocks > (int64_t)sms * 8) blocks = (int64_t)sms * 8;
-  if (blocks < 1) blocks = 1;
-  JSCC_TIMED("sc_fill", st, sc_fill_kernel<<<(unsigned)blocks, 256, 0, st>>>(ratio, n_bins, 1.0f));
-  JSCC_LAUNCH_CHECK();
-  dim3 grid((unsigned)p.col_tiles, (unsigned)p.chunks);
+  dim3 grid((unsigned)col_tiles, (unsigned)chunks);
   const int threads = kColTile / NV;
-  JSCC_TIMED("sc_back_partial", st, {
+  JSCC_TIMED("sc_colsum_kahan", st, {
     if (vec_ok)
-      sc_back_partial_kernel<T, 1, true><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, ratio, 1,
-                                                                   p.rows_per_chunk, part, p.ldx);
+      sc_colsum_kahan_kernel<T, true><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, rows_per_chunk, sum,
+                                                                comp, ldp);
     else
-      sc_back_partial_kernel<T, 1, false><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, ratio, 1,
-                                                                    p.rows_per_chunk, part, p.ldx);
+      sc_colsum_kahan_kernel<T, false><<<grid, threads, 0, st>>>(A, lda, row_idx, n_bins, V, rows_per_chunk, sum,
+                                                                 comp, ldp);
   });
   JSCC_LAUNCH_CHECK();
-  blocks = (V + 255) / 256;
+  int64_t blocks = (V + 255) / 256;
   if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
   if (blocks < 1) blocks = 1;
   JSCC_TIMED("sc_sensitivity", st,
-             sc_sensitivity_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, p.ldx, (int)p.chunks, rotinv, ld_rot,
+             sc_sensitivity_kernel<<<(unsigned)blocks, 256, 0, st>>>(sum, comp, ldp, (int)chunks, rotinv, ld_rot,
                                                                      n_rot, V, weight));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
@@ -758,17 +805,23 @@ int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, const int64
   const ScPlan p = plan_sc(n_bins, n_vox, 1);
   JSCC_REQUIRE(workspace != nullptr && workspace_bytes >= p.ws_bytes,
                "jscc_sc_sensitivity: workspace too small (%zu < %zu bytes)", workspace_bytes, p.ws_bytes);
+  // compensated sums: half as many row chunks as the back pass, so the sums and their carried
+  // errors (2 x chunks x ldx floats) fit in the same workspace (>= (chunks + 1) x ldx floats)
+  int64_t chunks = (p.chunks + 1) / 2;
+  if (chunks < 1) chunks = 1;
+  const int64_t rows_per_chunk = (n_bins + chunks - 1) / chunks;
+  chunks = (n_bins + rows_per_chunk - 1) / rows_per_chunk;
   Carver cv(workspace, workspace_bytes);
-  cv.take<float>((size_t)p.rb * p.ldx);
-  float* ratio = cv.take<float>((size_t)n_bins * p.rb);
-  float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
+  float* sum = cv.take<float>((size_t)chunks * p.ldx);
+  float* comp = cv.take<float>((size_t)chunks * p.ldx);
   JSCC_REQUIRE(cv.ok(), "jscc_sc_sensitivity: workspace carve overflow");
   cudaStream_t st = as_stream(stream);
   if (a_dtype == JSCC_DTYPE_F32)
     return sc_sensitivity_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, n_rot, rotmat_inv,
-                                       ld_rot, weight, p, ratio, part, st);
+                                       ld_rot, weight, p.col_tiles, chunks, rows_per_chunk, p.ldx, sum, comp, st);
   return sc_sensitivity_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox,
-                                             n_rot, rotmat_inv, ld_rot, weight, p, ratio, part, st);
+                                             n_rot, rotmat_inv, ld_rot, weight, p.col_tiles, chunks, rows_per_chunk,
+                                             p.ldx, sum, comp, st);
 }
 
 size_t jscc_sc_weight_workspace_bytes(int64_t n_bins, int64_t n_vox, int32_t n_rot) {
@@ -877,6 +930,7 @@ int jscc_take_bad_index_count(unsigned int* out) {
   unsigned int h = 0, zero = 0;
   JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_bad_index_count, sizeof(h)));
   JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_bad_index_count, &zero, sizeof(zero)));
+  h += jscc::take_prior_bad_index_count();
   if (out) *out = h;
   return JSCC_OK;
 }

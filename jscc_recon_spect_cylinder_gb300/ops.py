@@ -220,6 +220,11 @@ def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None
     rm = _index_table(rotmat, V, "rotmat")
     e, edt, ld = _eff_args(eff)
     n = records.size(0)
+    perm = None
+    if e is not None and n > 1:
+        # events visited sorted by efficiency row (shared rows in L1/L2, as in compton_weight);
+        # f is returned in the caller's event order
+        records, row_id, perm = _row_sorted_events(records, row_id)
     f = torch.empty(n, dtype=torch.float32, device=dev)
     lib = _lib.load()
     ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
@@ -228,6 +233,8 @@ def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None
                                   None if rm is None else rm.data_ptr() + rot_col * 8, 0 if rm is None else rm.stride(0),
                                   f.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
     _lib.check(rc, "jscc_compton_project")
+    if perm is not None:
+        f = torch.empty_like(f).index_copy_(0, perm, f)
     return f
 
 
@@ -243,6 +250,10 @@ def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=No
     gg = _f32_contig(g.reshape(-1))
     if gg.numel() != n:
         raise ValueError(f"g has {gg.numel()} entries for {n} events")
+    if e is not None and n > 1:
+        # the adjoint is a sum over events: visit them sorted by efficiency row
+        records, row_id, perm = _row_sorted_events(records, row_id)
+        gg = gg.index_select(0, perm)
     if out is None:
         out = torch.zeros((V, 1), dtype=torch.float32, device=dev)
     lib = _lib.load()
@@ -254,6 +265,33 @@ def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=No
                                       ws.numel(), _lib.stream_handle(dev))
     _lib.check(rc, "jscc_compton_backproject")
     return out
+
+
+def rdp_prior(img, nbr, weight, gamma=2.0, beta=1.0, eps=1e-9, want_value=True, want_grad=True, grad_out=None,
+              accumulate=False):
+    """Relative-difference prior ``beta R(img)`` and its gradient (jscc_rdp_prior) over a
+    neighbour-major table ``nbr`` [K, V] int32 / ``weight`` [K, V] float32. Returns
+    ``(value, grad)``: value a float64 0-d device tensor (or None), grad [V, 1] float32
+    (``grad_out`` += when ``accumulate``) or None."""
+    dev = _lib.require_cuda(img, nbr, weight, grad_out, what="rdp_prior")
+    x = _f32_contig(img.reshape(-1))
+    V = x.numel()
+    if nbr.dim() != 2 or nbr.size(1) != V or weight.shape != nbr.shape:
+        raise ValueError(f"neighbour table {tuple(nbr.shape)} / {tuple(weight.shape)} does not match {V} voxels")
+    nb = nbr.to(torch.int32).contiguous()
+    wt = _f32_contig(weight)
+    value = torch.zeros((), dtype=torch.float64, device=dev) if want_value else None
+    grad = None
+    if want_grad:
+        grad = grad_out if grad_out is not None else torch.empty((V, 1), dtype=torch.float32, device=dev)
+        if grad.numel() != V or grad.dtype != torch.float32 or not grad.is_contiguous():
+            raise ValueError("grad_out must be a contiguous float32 tensor of V elements")
+    lib = _lib.load()
+    rc = lib.jscc_rdp_prior(x.data_ptr(), nb.data_ptr(), wt.data_ptr(), V, nb.size(0), float(gamma), float(eps),
+                            float(beta), _lib.ptr(value), _lib.ptr(grad), 1 if (accumulate and grad_out is not None)
+                            else 0, _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_rdp_prior")
+    return value, grad
 
 
 def sc_sensitivity(sysmat: torch.Tensor, rotmat_inv: torch.Tensor | None = None, n_rot: int | None = None,
@@ -394,17 +432,17 @@ def compton_row_stats(records, row_id, coor, model=_lib.CONE_STRICT, eff=None, u
 
 
 def _row_sorted_events(records, row_id):
-    """(records, row_id) stably sorted by row id, cached on the records tensor (rebuilt when
-    either tensor is modified in place)."""
+    """(records, row_id, perm): the events stably sorted by row id (``records[perm]``),
+    cached on the records tensor (rebuilt when either tensor is modified in place)."""
     key = (id(row_id), records._version, row_id._version)
     cache = getattr(records, "_jscc_row_sorted", None)
     if cache is not None and cache[0] == key:
-        return cache[1], cache[2]
+        return cache[1], cache[2], cache[3]
     perm = torch.argsort(row_id.to(torch.int64), stable=True)
     rec_s = records.index_select(0, perm).contiguous()
     rid_s = row_id.index_select(0, perm).contiguous()
-    records._jscc_row_sorted = (key, rec_s, rid_s)
-    return rec_s, rid_s
+    records._jscc_row_sorted = (key, rec_s, rid_s, perm)
+    return rec_s, rid_s, perm
 
 
 def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
@@ -432,7 +470,7 @@ def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None,
     if e is not None and n > 1:
         # the weight is a sum over events: visiting them sorted by efficiency row lets the
         # events a CTA handles share those rows in L1/L2 (only float32 rounding changes)
-        records, row_id = _row_sorted_events(records, row_id)
+        records, row_id, _ = _row_sorted_events(records, row_id)
     lib = _lib.load()
     ws = _lib.workspace.get(dev, lib.jscc_compton_weight_workspace_bytes(n, V))
     rc = lib.jscc_compton_weight(
