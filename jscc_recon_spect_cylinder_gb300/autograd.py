@@ -41,7 +41,7 @@ class ComptonProject(torch.autograd.Function):
     """g[i] = sum_j t_ij x_j over ComptonEvents (T recomputed); backward: T^T grad."""
 
     @staticmethod
-    def forward(ctx, x, events, coor, sysmat, use_window=True):
+    def forward(ctx, x, events, coor, sysmat, use_window=False):
         ctx.args = (events, coor, sysmat, use_window)
         ctx.shape = x.shape
         return ops.compton_project(events.records, events.row_id, coor, x.detach(), model=events.model, eff=sysmat,
@@ -59,7 +59,7 @@ def sc_project(x, sysmat, rotmat=None, rotmat_inv=None, n_rot=None, row_idx=None
     return SCProject.apply(x, sysmat, rotmat, rotmat_inv, n_rot, row_idx)
 
 
-def compton_project(x, events, coor, sysmat, use_window=True):
+def compton_project(x, events, coor, sysmat, use_window=False):
     return ComptonProject.apply(x, events, coor, sysmat, use_window)
 
 

@@ -456,6 +456,203 @@ cone_back_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ 
   if (j < V) part[(int64_t)blockIdx.y * ldp + j] = acc;
 }
 
+// ------------------------------------------------------------------ strict pairs (f32x2)
+// The strict fused passes evaluate two events per voxel at once: the events' staged fields
+// are stored as (event 2k, event 2k + 1) float pairs, and the geometry, the position-variance
+// Jacobian, the variance and exponent arithmetic and the Klein-Nishina factor run as packed
+// FP32 operations (one f32x2 instruction per two pairs); the reciprocal square root, acos,
+// the reciprocal and the exponential stay per lane. Same formulas as cone_value_fast, with
+// kn - sin^2(beta) written as (kn - 1) + cos^2(beta).
+struct alignas(16) ConePair {
+  float2 p1x, p1y, p1z;
+  float2 wx, wy, wz;
+  float2 ntheta;           // -theta
+  float2 knm1;             // kn - 1
+  float2 q0, q1, q2;
+  float2 sig_plus, sig_minus;
+  float2 cos_lo, cos_hi;
+  float2 pad;
+};
+static_assert(sizeof(ConePair) == 128, "pair record layout");
+
+// Writes event r into half h (0: .x, 1: .y) of a staged pair.
+__device__ __forceinline__ void stage_pair_half(ConePair* pr, int h, const ConeEvent& r) {
+  const ConeFast f = stage_fast(r);
+  float* d = reinterpret_cast<float*>(pr) + h;
+  const float v[16] = {f.p1x, f.p1y, f.p1z, f.wx, f.wy, f.wz, -f.theta, f.kn - 1.0f,
+                       f.q0, f.q1, f.q2, f.sig_plus, f.sig_minus, f.cos_lo, f.cos_hi, 0.f};
+#pragma unroll
+  for (int k = 0; k < 16; ++k) d[2 * k] = v[k];
+}
+
+__device__ __forceinline__ float ex2_approx(float z) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(z));
+  return r;
+}
+
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+
+// t for the two events of a staged pair at one voxel (ncx.. = minus the voxel centre).
+template <bool WINDOW>
+__device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, float2 ncy, float2 ncz) {
+  const float2 ax = __fadd2_rn(e.p1x, ncx), ay = __fadd2_rn(e.p1y, ncy), az = __fadd2_rn(e.p1z, ncz);
+  float2 d2 = __ffma2_rn(ax, ax, __ffma2_rn(ay, ay, __fmul2_rn(az, az)));
+  d2.x = fmaxf(d2.x, 1e-14f);
+  d2.y = fmaxf(d2.y, 1e-14f);
+  const float2 r0 = make_float2(rsqrtf(d2.x), rsqrtf(d2.y));
+  // 1 / d01: one Newton-Raphson step, r (3 - d2 r^2) / 2
+  const float2 h = __fmul2_rn(__fmul2_rn(d2, f2(-0.5f)), r0);
+  const float2 i01 = __fmul2_rn(r0, __ffma2_rn(h, r0, f2(1.5f)));
+  const float2 bcos = __fmul2_rn(__ffma2_rn(ax, e.wx, __ffma2_rn(ay, e.wy, __fmul2_rn(az, e.wz))), i01);
+  bool in0 = true, in1 = true;
+  if (WINDOW) {
+    in0 = !(bcos.x < e.cos_lo.x || bcos.x > e.cos_hi.x);
+    in1 = !(bcos.y < e.cos_lo.y || bcos.y > e.cos_hi.y);
+    if (!(in0 || in1)) return make_float2(0.f, 0.f);
+  }
+  const float2 c = make_float2(fminf(fmaxf(bcos.x, -1.0f + 1e-7f), 1.0f - 1e-7f),
+                               fminf(fmaxf(bcos.y, -1.0f + 1e-7f), 1.0f - 1e-7f));
+  const float2 delta = __fadd2_rn(make_float2(acosf(c.x), acosf(c.y)), e.ntheta);
+  const float2 sig_e = make_float2(delta.x >= 0.f ? e.sig_plus.x : e.sig_minus.x,
+                                   delta.y >= 0.f ? e.sig_plus.y : e.sig_minus.y);
+  const float2 nb = __fmul2_rn(bcos, f2(-1.0f));
+  const float2 jx = __ffma2_rn(nb, e.wx, __fmul2_rn(ax, i01));
+  const float2 jy = __ffma2_rn(nb, e.wy, __fmul2_rn(ay, i01));
+  const float2 jz = __ffma2_rn(nb, e.wz, __fmul2_rn(az, i01));
+  float2 sb2 = __ffma2_rn(nb, bcos, f2(1.0f));
+  sb2.x = fmaxf(sb2.x, 1e-12f);
+  sb2.y = fmaxf(sb2.y, 1e-12f);
+  const float2 num = __ffma2_rn(__fmul2_rn(jx, jx), e.q0,
+                                __ffma2_rn(__fmul2_rn(jy, jy), e.q1, __fmul2_rn(__fmul2_rn(jz, jz), e.q2)));
+  // sb2 * sigma^2 = max(sigma_E^2 sb2 + max(num, 1e-12 sb2), 1e-12 sb2)
+  // (the outer max is implied: sigma_E^2 sb2 >= 0 and the addend is >= 1e-12 sb2, and a
+  // rounded sum of the two cannot fall below the addend)
+  const float2 tiny = __fmul2_rn(sb2, f2(1e-12f));
+  const float2 s2 =
+      __ffma2_rn(__fmul2_rn(sig_e, sig_e), sb2, make_float2(fmaxf(num.x, tiny.x), fmaxf(num.y, tiny.y)));
+  // exp(-delta^2 / (2 sigma^2)) = 2^(-log2(e) / 2 * delta^2 sb2 / (sb2 sigma^2))
+  const float2 nd = __fmul2_rn(__fmul2_rn(delta, delta), sb2);
+  const float2 z = __fmul2_rn(__fmul2_rn(nd, make_float2(__fdividef(1.0f, s2.x), __fdividef(1.0f, s2.y))),
+                              f2(-0.72134752044448170f));
+  float2 t = __fmul2_rn(make_float2(ex2_approx(z.x), ex2_approx(z.y)), __ffma2_rn(c, c, e.knm1));
+  if (WINDOW) {
+    if (!in0) t.x = 0.f;
+    if (!in1) t.y = 0.f;
+  }
+  return t;
+}
+
+// f[i] = sum_j t_ij eff_ij x_j for the strict model, 16 events (8 pairs) per CTA.
+template <bool WINDOW, typename TE>
+__global__ void __launch_bounds__(kConeThreads, 5)
+cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                         const float* __restrict__ coor, int64_t V, const float* __restrict__ x,
+                         const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ f_out) {
+  constexpr int EB = 16, NP = EB / 2;
+  __shared__ ConePair sev[NP];
+  __shared__ int64_t srow[EB];
+  __shared__ float red[kConeThreads / 32][EB];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t i0 = (int64_t)blockIdx.x * EB;
+  if (tid < EB) {
+    const int64_t i = i0 + tid < n_ev ? i0 + tid : n_ev - 1;  // padding repeats a valid event
+    stage_pair_half(&sev[tid >> 1], tid & 1, rec[i]);
+    srow[tid] = (int64_t)row_id[i] * ld_eff;
+  }
+  __syncthreads();
+  const int ne = (n_ev - i0) < EB ? (int)(n_ev - i0) : EB;
+  const int np = (ne + 1) >> 1;
+  float2 af[NP];
+#pragma unroll
+  for (int k = 0; k < NP; ++k) af[k] = make_float2(0.f, 0.f);
+  for (int64_t j = tid; j < V; j += kConeThreads) {
+    const float2 ncx = f2(-coor[3 * j]), ncy = f2(-coor[3 * j + 1]), ncz = f2(-coor[3 * j + 2]);
+    const float2 xj = f2(x ? __ldg(x + j) : 0.f);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+      if (k < np) {
+        float2 t = cone_pair_fast<WINDOW>(sev[k], ncx, ncy, ncz);
+        if (t.x != 0.f || t.y != 0.f) {
+          if (eff) {
+            t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
+            t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+          }
+          af[k] = __ffma2_rn(t, xj, af[k]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < NP; ++k) {
+    const float v0 = warp_sum(af[k].x);
+    const float v1 = warp_sum(af[k].y);
+    if (lane == 0) {
+      red[warp][2 * k] = v0;
+      red[warp][2 * k + 1] = v1;
+    }
+  }
+  __syncthreads();
+  if (tid < ne) {
+    float f = 0.f;
+#pragma unroll
+    for (int w = 0; w < kConeThreads / 32; ++w) f += red[w][tid];
+    if (f_out) f_out[i0 + tid] = f;
+  }
+}
+
+// part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i for the strict model, events in pairs.
+template <bool WINDOW, typename TE>
+__global__ void __launch_bounds__(kConeThreads)
+cone_back_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                      int64_t ev_per_chunk, const float* __restrict__ q, const float* __restrict__ coor, int64_t V,
+                      const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp) {
+  __shared__ ConePair sev[kBackStage / 2];
+  __shared__ int64_t srow[kBackStage];
+  __shared__ float sq[kBackStage];
+  const int tid = threadIdx.x;
+  const int64_t j = (int64_t)blockIdx.x * kConeThreads + tid;
+  const int64_t e_begin = (int64_t)blockIdx.y * ev_per_chunk;
+  int64_t e_end = e_begin + ev_per_chunk;
+  if (e_end > n_ev) e_end = n_ev;
+  float2 ncx = f2(0.f), ncy = f2(0.f), ncz = f2(0.f);
+  if (j < V) {
+    ncx = f2(-coor[3 * j]);
+    ncy = f2(-coor[3 * j + 1]);
+    ncz = f2(-coor[3 * j + 2]);
+  }
+  float2 acc = make_float2(0.f, 0.f);
+  for (int64_t s = e_begin; s < e_end; s += kBackStage) {
+    const int n = (e_end - s) < kBackStage ? (int)(e_end - s) : kBackStage;
+    __syncthreads();
+    if (tid < n) {
+      stage_pair_half(&sev[tid >> 1], tid & 1, rec[s + tid]);
+      srow[tid] = (int64_t)row_id[s + tid] * ld_eff;
+      sq[tid] = q[s + tid];
+    } else if (tid == n && (n & 1)) {
+      // odd count: the pair's second half repeats event s with a zero ratio
+      stage_pair_half(&sev[tid >> 1], 1, rec[s]);
+      srow[tid] = (int64_t)row_id[s] * ld_eff;
+      sq[tid] = 0.f;
+    }
+    __syncthreads();
+    if (j < V) {
+      const int np = (n + 1) >> 1;
+      for (int k = 0; k < np; ++k) {
+        float2 t = cone_pair_fast<WINDOW>(sev[k], ncx, ncy, ncz);
+        if (t.x != 0.f || t.y != 0.f) {
+          if (eff) {
+            t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
+            t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+          }
+          acc = __ffma2_rn(t, make_float2(sq[2 * k], sq[2 * k + 1]), acc);
+        }
+      }
+    }
+  }
+  if (j < V) part[(int64_t)blockIdx.y * ldp + j] = acc.x + acc.y;
+}
+
 // ------------------------------------------------------------------ host planning
 struct ConePlan {
   int64_t chunks;
@@ -495,9 +692,14 @@ static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t 
   constexpr int EB = 16;
   if (stage != 2) {
     const unsigned fgrid = (unsigned)((n_ev + EB - 1) / EB);
-    JSCC_TIMED("cone_forward", st,
-               (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
-                   rec, rid, n_ev, coor, V, x, eff, ld_eff, f, nullptr, nullptr, nullptr)));
+    if (MODEL == 0)
+      JSCC_TIMED("cone_forward", st,
+                 (cone_forward_pair_kernel<WINDOW, TE><<<fgrid, kConeThreads, 0, st>>>(rec, rid, n_ev, coor, V, x,
+                                                                                       eff, ld_eff, f)));
+    else
+      JSCC_TIMED("cone_forward", st,
+                 (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
+                     rec, rid, n_ev, coor, V, x, eff, ld_eff, f, nullptr, nullptr, nullptr)));
     JSCC_LAUNCH_CHECK();
     if (stage == 1) return JSCC_OK;
     int64_t rb = (n_ev + 255) / 256;
@@ -506,9 +708,14 @@ static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t 
     JSCC_LAUNCH_CHECK();
   }
   dim3 bgrid((unsigned)((V + kConeThreads - 1) / kConeThreads), (unsigned)p.chunks);
-  JSCC_TIMED("cone_back", st,
-             (cone_back_kernel<MODEL, WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
-                 rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp)));
+  if (MODEL == 0)
+    JSCC_TIMED("cone_back", st,
+               (cone_back_pair_kernel<WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
+                   rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp)));
+  else
+    JSCC_TIMED("cone_back", st,
+               (cone_back_kernel<MODEL, WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
+                   rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
 }

@@ -209,7 +209,7 @@ def sc_backproject(sysmat, g, rotmat_inv=None, n_rot=None, row_idx=None, scale=1
     return out
 
 
-def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
+def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=False, rotmat=None,
                     rot_col=0):
     """Forward list-mode projection ``f[i] = sum_j t_ij rot(img)_j`` with T recomputed
     (jscc_compton_project) -> ``[E]``."""
@@ -238,7 +238,7 @@ def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None
     return f
 
 
-def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat_inv=None,
+def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=None, use_window=False, rotmat_inv=None,
                         rot_col=0, scale=1.0, out=None):
     """Adjoint of compton_project: ``out += scale * rotinv(T^T g)`` (jscc_compton_backproject)."""
     dev = _lib.require_cuda(records, row_id, coor, g, eff, rotmat_inv, out, what="compton_backproject")
@@ -445,7 +445,7 @@ def _row_sorted_events(records, row_id):
     return rec_s, rid_s, perm
 
 
-def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=True, rotmat=None,
+def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=False, rotmat=None,
                    rotmat_inv=None, rot_col=0, scale=1.0, out=None):
     """``out += scale * rotinv( T^T (1 / T rot(img)) )`` with T recomputed on the fly."""
     dev = _lib.require_cuda(records, row_id, coor, img, eff, rotmat, rotmat_inv, out, what="compton_weight")

@@ -4,13 +4,14 @@ The grid is z-major, and within a z layer ring after ring of possibly different 
 (the layout compton_sparse_ops.py:59-92 infers from ``coor_polar_full``). Edges of a voxel:
 
 * its two angular neighbours in the same ring (periodic);
-* in each adjacent ring, the voxel nearest in angle, and with ``diagonal`` also that
-  voxel's two angular neighbours (both directions are added, so rings of different lengths
-  still give a symmetric table);
+* in each adjacent ring, the voxel nearest in angle (both directions are added, so rings of
+  different lengths still give a symmetric table); with ``diagonal`` also that voxel's two
+  angular neighbours (the 8-neighbourhood on a uniform grid);
 * the voxel at the same (ring, angle) slot in the adjacent z layers.
 
-Weights: ``"index"`` gives face edges 1 and diagonal edges 1/sqrt(2) (the usual
-8-neighbourhood weights in index space, independent of the polar voxel sizes);
+The default (no diagonals) is the polar 4-neighbourhood: ring +-1 angular step plus the
+nearest angle in the adjacent rings. Weights: ``"index"`` gives face edges 1 and diagonal
+edges 1/sqrt(2) (index space, independent of the polar voxel sizes);
 ``"distance"`` gives 1 / |c_j - c_k| in 1/mm. The table is neighbour-major
 ``[K, V]`` (jscc_rdp_prior's layout), -1 / 0 padded.
 """
@@ -41,7 +42,7 @@ class NeighbourTable:
         return NeighbourTable(self.nbr.to(device).contiguous(), self.weight.to(device).contiguous())
 
 
-def polar_neighbour_edges(coor_full, diagonal=True):
+def polar_neighbour_edges(coor_full, diagonal=False):
     """Undirected edges ``(j, k, diagonal_flag)`` of the polar grid, j < k, no duplicates."""
     c = np.asarray(torch.as_tensor(coor_full, dtype=torch.float32).cpu().numpy(), dtype=np.float64)
     layout = cso._infer_polar_layout(torch.as_tensor(coor_full, dtype=torch.float32).cpu())
@@ -93,7 +94,7 @@ def polar_neighbour_edges(coor_full, diagonal=True):
     return out
 
 
-def polar_neighbours(coor_full, diagonal=True, weights="index", device="cpu") -> NeighbourTable:
+def polar_neighbours(coor_full, diagonal=False, weights="index", device="cpu") -> NeighbourTable:
     """The symmetric neighbour table of ``coor_full`` ([V, 3]) for jscc_rdp_prior."""
     if weights not in ("index", "distance"):
         raise ValueError(f"weights must be 'index' or 'distance', got {weights!r}")

@@ -363,8 +363,11 @@ def _run_multi_gpu_compton(t_list_all, sysmat_list_all, proj_list_all, rotmat_al
 # builder's row normalisation).
 
 def get_weight_compton_fused(events, coor, sysmat, img, rotmat=None, rotmat_inv=None, rot_col=0, scale=1.0, out=None,
-                             use_window=True):
-    """``T^T (1 / (T x))`` for a block of ComptonEvents; accumulated into ``out``."""
+                             use_window=False):
+    """``T^T (1 / (T x))`` for a block of ComptonEvents; accumulated into ``out``. Every
+    event-voxel pair is evaluated, as the reference's stored rows hold them; ``use_window``
+    skips pairs outside each record's cos(beta) window (t < exp(-K^2 / 2)), which pays only
+    when the windows exclude most of the grid."""
     if len(events) == 0:
         return torch.zeros_like(img) if out is None else out
     return ops.compton_weight(events.records, events.row_id, coor, img, model=events.model, eff=sysmat,
@@ -384,7 +387,7 @@ def _accumulate_compton_fused(weight, ev_list, coor_all, sysmat_all, rotmat_all,
 
 
 def osem_list_mode_fused(ev_list_all, coor_all, sysmat_all, rotmat_all, rotmat_inv_all, img, s_map, rotate_num,
-                         use_window=True):
+                         use_window=False):
     """osem_list_mode (recon_osem_plane.py:63-80) with T recomputed on the fly;
     ``ev_list_all[subset][rotation][divide][energy]`` holds ComptonEvents blocks."""
     for ev_list in ev_list_all:
@@ -396,7 +399,7 @@ def osem_list_mode_fused(ev_list_all, coor_all, sysmat_all, rotmat_all, rotmat_i
 
 
 def osem_joint_mode_fused(sysmat_list_all, proj_list_all, ev_list_all, coor_all, sysmat_all, rotmat_all,
-                          rotmat_inv_all, img, s_map, alpha, rotate_num, use_window=True):
+                          rotmat_inv_all, img, s_map, alpha, rotate_num, use_window=False):
     """osem_joint_mode (recon_osem_plane.py:100-125) with the Compton half on the fly."""
     for sysmat_list, proj_list, ev_list in zip(sysmat_list_all, proj_list_all, ev_list_all):
         w_c = torch.zeros_like(img)

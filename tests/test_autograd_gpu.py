@@ -91,8 +91,7 @@ def test_compton_adjoint_and_gradient(cuda):
     rhs = float((x.double() * xg.grad.double()).sum())
     assert abs(lhs - rhs) / abs(lhs) < 1e-6
     # list-mode likelihood gradient = T^T (1 / T x) - s_C (the fused OSEM weight)
-    s_c = ops.compton_backproject(ev.records, ev.row_id, coor, torch.ones_like(f), model=ev.model, eff=sysmat,
-                                  use_window=True)
+    s_c = ops.compton_backproject(ev.records, ev.row_id, coor, torch.ones_like(f), model=ev.model, eff=sysmat)
     assert float(f.min()) > 0  # every event sees the image: 1/f is finite for all of them
     xg = x.clone().requires_grad_(True)
     ag.poisson_log_likelihood(xg, compton=(ev, coor, sysmat, s_c)).backward()

@@ -111,8 +111,9 @@ def _cone_problem(cuda, n_events=3000, n_r=20, n_theta=72, seed=4):
 
 def test_fused_cone_weight_matches_stored_t(cuda):
     """The fused on-the-fly weight equals T^T(1/(Tx)) over the builder's stored rows
-    (row normalisation does not change the list-mode weight); window pruning changes it
-    by far less than float32 rounding."""
+    (row normalisation does not change the list-mode weight), with every pair evaluated
+    (the default) and with the 9-sigma window, which changes it by far less than float32
+    rounding."""
     from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
     from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
 
@@ -125,8 +126,9 @@ def test_fused_cone_weight_matches_stored_t(cuda):
     assert torch.equal(ev.list_index, kept)  # identical event selection incl. row filters
     x = torch.rand((grid.n_vox, 1), generator=torch.Generator().manual_seed(1)).to(cuda) + 0.5
     w_stored = rop.get_weight_compton(t, x)
-    w_fused = rop.get_weight_compton_fused(ev, coor, A, x)
-    w_exact = rop.get_weight_compton_fused(ev, coor, A, x, use_window=False)
+    w_fused = rop.get_weight_compton_fused(ev, coor, A, x, use_window=True)
+    w_exact = rop.get_weight_compton_fused(ev, coor, A, x)  # every pair (the default)
+    assert rel_l2(w_exact.cpu(), w_stored.cpu()) < TOL_W
     assert rel_l2(w_fused.cpu(), w_stored.cpu()) < TOL_W
     assert rel_l2(w_fused.cpu(), w_exact.cpu()) < 1e-6
     # against the float32 oracle (the reference's arithmetic, pinned by the golden tests)
@@ -144,6 +146,7 @@ def test_fused_cone_weight_matches_stored_t(cuda):
                                dtype=np.float32)
     w32 = osem_sc.get_weight_compton(tc32 * sysmat.numpy()[cp1 - 1], x.cpu().numpy(), dtype=np.float32)
     assert rel_l2(w_fused.cpu(), w32) < TOL_W
+    assert rel_l2(w_exact.cpu(), w32) < TOL_W
 
 
 def test_fused_list_mode_osem_with_rotations(cuda):

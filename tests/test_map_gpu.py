@@ -35,7 +35,8 @@ def test_rdp_kernel_matches_oracle(cuda, grid, gamma):
     from jscc_recon_spect_cylinder_gb300 import _lib, ops, prior, synthetic
 
     coor = synthetic.polar_grid(N_R, N_T, 50.0).coor if grid == "uniform" else _variable_rings()
-    tb = prior.polar_neighbours(coor, weights="index" if grid == "uniform" else "distance")
+    tb = prior.polar_neighbours(coor, weights="index" if grid == "uniform" else "distance",
+                                diagonal=grid != "uniform")
     V = coor.size(0)
     rng = np.random.default_rng(5)
     x = rng.uniform(0.1, 3.0, V).astype(np.float32)

@@ -1,12 +1,13 @@
 """MAP objective oracle and neighbour tables (CPU): the float64 gradients of the prior and of
 the joint log-posterior agree with float64 central differences, and the polar neighbour
-tables are the 8-neighbourhood on uniform grids and symmetric on rings of different lengths
-and on several z layers."""
+tables are the 4- (default) or 8-neighbourhood on uniform grids and symmetric on rings of
+different lengths and on several z layers."""
 from __future__ import annotations
 
 import math
 
 import numpy as np
+import pytest
 import torch
 
 from oracle import map as om
@@ -47,14 +48,20 @@ def _directed(tb):
     return out
 
 
-def test_uniform_grid_is_the_8_neighbourhood():
+@pytest.mark.parametrize("diagonal", [False, True])
+def test_uniform_grid_neighbourhoods(diagonal):
+    """Default: ring +-1 angle and the same angle in the adjacent rings (4-neighbourhood);
+    with diagonals, the 8-neighbourhood with weights 1 and 1/sqrt(2)."""
     n_r, n_t = 5, 8
-    e = _directed(_table(_grid(n_r, n_t)))
+    e = _directed(_table(_grid(n_r, n_t), diagonal=diagonal))
+    steps = ((0, 1), (0, -1), (1, 0), (-1, 0))
+    if diagonal:
+        steps += ((1, 1), (1, -1), (-1, 1), (-1, -1))
     want = {}
     for r in range(n_r):
         for t in range(n_t):
             j = r * n_t + t
-            for dr, dt in ((0, 1), (0, -1), (1, 0), (-1, 0), (1, 1), (1, -1), (-1, 1), (-1, -1)):
+            for dr, dt in steps:
                 if 0 <= r + dr < n_r:
                     want[(j, (r + dr) * n_t + (t + dt) % n_t)] = 1.0 if dr == 0 or dt == 0 else 1 / math.sqrt(2)
     assert set(e) == set(want)
@@ -64,8 +71,8 @@ def test_uniform_grid_is_the_8_neighbourhood():
 
 def test_variable_rings_and_layers_are_symmetric():
     coor = _variable_rings()
-    for w in ("index", "distance"):
-        e = _directed(_table(coor, weights=w))
+    for w, diag in (("index", False), ("index", True), ("distance", True)):
+        e = _directed(_table(coor, weights=w, diagonal=diag))
         for (j, k), wt in e.items():
             assert j != k
             assert e.get((k, j)) == wt
@@ -74,7 +81,8 @@ def test_variable_rings_and_layers_are_symmetric():
     # z faces: every voxel of layer 0 sees the same slot of layer 1
     for j in range(n_layer):
         assert e[(j, j + n_layer)] == 1.0
-    # every voxel has at least its two in-ring neighbours and one neighbour in each adjacent ring
+    # every voxel has its two in-ring neighbours, the nearest slot of each adjacent ring and
+    # its z face: at least 4 (innermost / outermost ring: one adjacent ring)
     for j in range(n_layer):
         assert sum(1 for (a, _) in e if a == j) >= 4
 
