@@ -1,7 +1,7 @@
 """Benchmark of the GB300 OSEM hot path; prints ONE JSON line (rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload jsccsd3|jsccsd-small|sc3|sc3-small|sparse-launch|cone2|map5]
+                    [--workload jsccsd3|jsccsd-small|sc3|sc3-small|sparse-launch|cone2|map5|batch4]
                     [--no-cpu-baseline] [--no-e2e]
 
 Workload "jsccsd3" (default): JSCCSD joint OSEM at the joint configuration's size —
@@ -18,7 +18,8 @@ Workload "sc3": the SC channel alone; "sc3-small": an 8,192-row SC case for prof
 "sparse-launch": one grouped sparse Compton weight launch (profiling case); "cone2": the
 fused strict cone weight of the list-mode configuration (200k events, event-voxel pairs/s);
 "map5": one Adam step of the differentiable MAP objective (SC + 2M Compton events + RDP
-prior, MAP steps/s).
+prior, MAP steps/s); "batch4": one OSEM iteration of 64 SC instances through the batched
+tensor-core GEMM path (subset-iterations/s summed over the instances).
 
 Multi-GPU: the path is run as independent replicas (one per rank, no collective on
 the data path); `value` sums the replicas' subset-iterations over the slowest rank's
@@ -493,6 +494,183 @@ class Map5Bench:
                                   "flop_per_pair": self.K_CONE}}
 
 
+class Batch4Bench:
+    """Config 4 (batched): 64 independent SC reconstructions sharing the joint configuration's
+    SC geometry (20 views x 4,096 pixels = 81,920 bins x 36,000 voxels, flat), Poisson
+    realisations of the hot-rod phantom at contrasts 2-8 with totals log-uniform in 1e5-1e7
+    counts, 8 subsets. One step = one OSEM iteration of every instance (8 subset updates x 64
+    instances) through the batched tensor-core path (BF16 matrix and its transpose, images and
+    ratios as BF16 hi / lo pairs, FP32 accumulation in tensor memory), replayed as one captured
+    CUDA graph. Metric: subset-iterations/s summed over the instances."""
+
+    def __init__(self, dev, n_inst=64, views=20, subsets=8, seed=None):
+        from jscc_recon_spect_cylinder_gb300 import batched, synthetic
+        from jscc_recon_spect_cylinder_gb300.recon_osem_plane import split_tensor_even
+
+        seed = synthetic.SEED if seed is None else seed
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(seed)
+        grid = synthetic.polar_grid(100, 360, 100.0, device=dev)
+        pitch = 2.0 * math.pi * 120.0 / 128
+        A = torch.cat([synthetic.sc_system_matrix(grid.coor, synthetic.cylinder_pixels(
+            120.0, 128, 32, 2.0, phi0=2 * math.pi * v / views, device=dev), pitch * 2.0, 100.0, generator=gen)
+            for v in range(views)], dim=0)
+        self.B, self.V = A.shape
+        gc = torch.Generator().manual_seed(seed)
+        counts = 10 ** (5 + 2 * torch.rand(n_inst, generator=gc, dtype=torch.float64))
+        contrasts = 2 + 6 * torch.rand(n_inst, generator=gc, dtype=torch.float64)
+        coor = grid.coor.cpu()
+        X_true = torch.stack([synthetic.hot_rod_phantom(coor, 100.0, contrast=float(c)).reshape(-1)
+                              for c in contrasts]).to(dev)
+        mean = X_true @ A.T
+        mean = mean * (counts.to(dev).float() / mean.sum(1))[:, None]
+        self.Y = torch.poisson(mean, generator=gen)
+        del mean
+        self.ids = split_tensor_even(torch.randperm(self.B, generator=gc), subsets)
+        self.s = A.sum(0)
+        self.A32 = A
+        self.n_inst, self.subsets, self.dev = n_inst, subsets, dev
+        self.bat = batched.BatchedScOsem(A, self.ids, self.s, n_inst, device=dev)
+        self.bat.set_projections(self.Y)
+        self.bat.set_images(torch.ones((n_inst, self.V)))
+        self.splits = self.bat.autotune()
+        self.bat.capture()
+        self.bat.set_images(torch.ones((n_inst, self.V)))
+        self.name = "batched-config4" if (views, subsets) == (20, 8) else f"batched-{views}views-{subsets}subsets"
+        self.metric = ("OSEM subset-iters/s summed over 64 instances: batched BF16 tensor-core GEMM path, "
+                       "config 4, 1xGB300")
+        self.unit = "subset-iters/s"
+        self.dtypes = ("bf16",)
+        self.traffic_file = "traffic_batch4.json"
+        torch.cuda.synchronize(dev)
+
+    def step(self, img, dtype):
+        self.bat.iterate(1)
+        return img
+
+    def step_eager(self, img, dtype):
+        """The same iteration launched kernel by kernel (for per-kernel timing)."""
+        g, self.bat.graph = self.bat.graph, None
+        try:
+            self.bat.iterate(1)
+        finally:
+            self.bat.graph = g
+        return img
+
+    def units_per_step(self):
+        return self.n_inst * self.subsets
+
+    def _launch_bytes(self):
+        """Algorithmic bytes of one forward and one back GEMM launch of a subset (matrix block
+        once, BF16 instance operand, FP32 result once)."""
+        nbp = max(b[2] for b in self.bat.blocks)
+        nr, V = self.bat.nr, self.V
+        fwd = nbp * V * 2 + nr * V * 2 + nbp * nr * 4
+        back = V * nbp * 2 + nr * nbp * 2 + V * nr * 4
+        return fwd, back, 2 * nbp * V * nr
+
+    def kernel_bytes(self, dtype):
+        fwd, back, _ = self._launch_bytes()
+        return {"bf16_gemm_nt": (fwd + back) / 2}
+
+    def config(self):
+        return {"workload": self.name, "instances": self.n_inst, "bins": self.B, "voxels": self.V,
+                "subsets": self.subsets, "counts": "log-uniform 1e5-1e7 per instance", "k_splits": {
+                    f"{k[0]}{k[1]}": v for k, v in self.splits.items()}, "graph": True,
+                "l2": "BF16 matrix 5.9 GB and its transpose, both > L2 (no flush)"}
+
+    def _sequential_fp32(self, iters=2):
+        """The plain FP32 single-instance path (jscc_sc_weight on the FP32 matrix with
+        row-index subsets + EM update) for one instance: subset-iterations/s."""
+        from jscc_recon_spect_cylinder_gb300 import ops
+
+        y = self.Y[0].reshape(-1, 1).contiguous()
+        x = torch.ones((self.V, 1), device=self.dev)
+        s = self.s.reshape(-1, 1)
+        ids = [i.to(self.dev) for i in self.ids]
+
+        def one():
+            nonlocal x
+            for r in ids:
+                w = ops.sc_weight(self.A32, y, x, row_idx=r)
+                x = x * w / s
+
+        one()
+        torch.cuda.synchronize(self.dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(iters):
+            one()
+        t1.record()
+        torch.cuda.synchronize(self.dev)
+        return self.subsets / (t0.elapsed_time(t1) / iters / 1e3)
+
+    def _errors(self, iters=5):
+        """Per-instance relative L2 / max-voxel error after `iters` iterations from x = 1,
+        against the float64 OSEM on the FP32 matrix (float64 GEMMs on the GPU)."""
+        self.bat.set_images(torch.ones((self.n_inst, self.V)))
+        X = self.bat.iterate(iters).double().clone()
+        self.bat.set_images(torch.ones((self.n_inst, self.V)))
+        X64 = torch.ones((self.n_inst, self.V), dtype=torch.float64, device=self.dev)
+        Y = self.Y.double()
+        s = self.s.double()
+        for _ in range(iters):
+            for r in self.ids:
+                r = r.to(self.dev)
+                As = self.A32[r].double()
+                W = (Y[:, r] / (X64 @ As.T)) @ As
+                X64 = X64 * W / s
+                del As, W
+        rel = ((X - X64).norm(dim=1) / X64.norm(dim=1)).cpu()
+        mx = ((X - X64).abs().max(dim=1).values / X64.abs().max(dim=1).values).cpu()
+        return {"iterations": iters, "rel_l2_median": float(rel.median()), "rel_l2_max": float(rel.max()),
+                "max_voxel_rel_max": float(mx.max())}
+
+    def extra(self, ms_per_step):
+        fwd, back, flops = self._launch_bytes()
+        seq = self._sequential_fp32()
+        value = self.units_per_step() / (ms_per_step / 1e3)
+        tens = None
+        kt = kernel_times(self, "bf16", 2)
+        if "bf16_gemm_nt" in kt:
+            n, tot = kt["bf16_gemm_nt"]
+            tf = flops / (tot / n / 1e3) / 1e12
+            pk = json.loads((REPO / "MEASURED_PEAKS.json").read_text()) if (REPO / "MEASURED_PEAKS.json").exists() else {}
+            peak = float(pk.get("bf16_tflops", 1900.0))
+            tens = {"achieved_tflops": tf, "peak_tflops": peak, "frac": tf / peak,
+                    "peak_source": "measured" if "bf16_tflops" in pk else "fallback",
+                    "flops_per_launch": flops, "note": "two BF16 rows (hi, lo) per instance"}
+        return {"sequential_fp32_single_instance": {"subset_iters_per_s": seq, "x64_instances_subset_iters_per_s": seq,
+                                                    "batched_speedup_vs_64_sequential": value / seq},
+                "tensor_pipe": tens, "errors_vs_fp64": self._errors()}
+
+    def e2e(self, iters):
+        """One job through the public batched API with host inputs: the 64 instances'
+        projections and initial images copied from pinned host memory, `iters` iterations
+        (the captured graph), the images read back. The matrix is the resident geometry."""
+        y_h = self.Y.cpu().pin_memory()
+        x_h = torch.ones((self.n_inst, self.V)).pin_memory()
+        out_h = torch.empty((self.n_inst, self.V)).pin_memory()
+        for _ in range(2):
+            self.bat.set_projections(y_h.to(self.dev, non_blocking=True))
+            self.bat.set_images(x_h.to(self.dev, non_blocking=True))
+            self.bat.iterate(iters)
+            out_h.copy_(self.bat.X, non_blocking=True)
+        torch.cuda.synchronize(self.dev)
+        t = time.perf_counter()
+        self.bat.set_projections(y_h.to(self.dev, non_blocking=True))
+        self.bat.set_images(x_h.to(self.dev, non_blocking=True))
+        self.bat.iterate(iters)
+        out_h.copy_(self.bat.X, non_blocking=True)
+        torch.cuda.synchronize(self.dev)
+        sec = time.perf_counter() - t
+        self.bat.set_images(torch.ones((self.n_inst, self.V)))
+        return {"value": iters * self.units_per_step() / sec, "unit": "subset-iters/s",
+                "h2d_bytes_per_step": (y_h.numel() + x_h.numel()) * 4 // iters,
+                "d2h_bytes_per_step": out_h.numel() * 4 // iters,
+                "step": f"one job: stage projections + images, {iters} iterations, read images", "seconds": sec}
+
+
 class SparseLaunchBench:
     """Profiling case: one grouped sparse Compton weight launch with a config-3 subset's sizes
     (99,850 BF16 coarse rows of 9,000 voxels, 12,239 groups, 100 x 360 fine grid, theta-stride-4
@@ -688,6 +866,10 @@ def make_workload(name, dev):
         return Cone2Bench(dev)
     if name == "map5":
         return Map5Bench(dev)
+    if name == "batch4":
+        return Batch4Bench(dev)
+    if name == "batch4-small":  # profiling case: 4 views (16,384 x 36,000), one subset, 64 instances; > L2
+        return Batch4Bench(dev, views=4, subsets=1)
     if name == "sc3":
         return Sc3Workload(dev)
     if name == "sc3-small":  # profiling case: 2 views (8,192 x 36,000), one subset; > L2
@@ -734,13 +916,14 @@ def kernel_times(work, dtype, steps):
     """Per-kernel CUDA-event durations on the launch stream (separate instrumented pass)."""
     from jscc_recon_spect_cylinder_gb300 import _lib
 
+    step = getattr(work, "step_eager", work.step)  # a captured graph records no per-kernel events
     img = torch.ones((work.V, 1), device=work.dev)
-    img = work.step(img, dtype)
+    img = step(img, dtype)
     torch.cuda.synchronize(work.dev)
     _lib.kernel_timing_collect()
     _lib.kernel_timing_enable(True)
     for _ in range(steps):
-        img = work.step(img, dtype)
+        img = step(img, dtype)
     torch.cuda.synchronize(work.dev)
     _lib.kernel_timing_enable(False)
     return _lib.kernel_timing_collect()
@@ -868,7 +1051,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2", "map5"],
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2", "map5", "batch4",
+                             "batch4-small"],
                     default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

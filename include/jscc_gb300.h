@@ -52,6 +52,9 @@ JSCC_API int jscc_abi_version(void);
 /* Number of kernels this library has launched since load / last reset. */
 JSCC_API unsigned long long jscc_launch_count(void);
 JSCC_API void jscc_reset_launch_count(void);
+/* Adds n to the launch count: the kernels of this library that one replay of a captured
+ * CUDA graph launches (the replay itself does not pass through the library). */
+JSCC_API void jscc_count_graph_launches(unsigned long long n);
 
 /*
  * Kernels never read or write out of bounds on a bad 1-based rotation index
@@ -424,6 +427,51 @@ JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coa
 JSCC_API int jscc_em_update(float* img_out, const float* img, const float* w_a, int32_t has_coef_a,
                    float coef_a, const float* w_b, float coef_b, const float* s_map, int64_t n_vox,
                    int32_t mode, float eps, void* stream);
+
+/* ------------------------------------------------ batched (multi-instance) SC path */
+
+/*
+ * BF16 GEMM on the tensor cores (tcgen05.mma, FP32 accumulation in tensor memory):
+ *   out[m * ldo + n] = sum_{k < K} P[m * ldp + k] * R[n * ldr + k]     (m < M, n < nr <= 256)
+ * P and R are BF16, both K-major (the K index contiguous); K, ldp and ldr multiples of 8;
+ * P and R 16-byte aligned. k_splits > 1 splits K over CTAs (partials summed in a fixed order,
+ * workspace jscc_bf16_gemm_workspace_bytes). For N instances sharing one SC matrix this is
+ * the forward projection F = A_s X (P = subset rows of A, R = images) and the back projection
+ * W = A_s^T Q (P = rows of a stored A^T restricted to the subset's bins, R = ratios): one pass
+ * over A serves every instance (the per-instance passes of recon_osem_plane.py:28-30).
+ */
+JSCC_API size_t jscc_bf16_gemm_workspace_bytes(int64_t M, int32_t nr, int64_t K, int32_t k_splits);
+JSCC_API int jscc_bf16_gemm_nt(const void* P, int64_t ldp, const void* R, int64_t ldr, int64_t M, int32_t nr,
+                   int64_t K, int32_t k_splits, float* out, int64_t ldo, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/*
+ * Helpers of the batched OSEM step (instances n < n_inst, padded to np rows):
+ *   jscc_batch_split:  xs[n][v] = bf16(x[n][v]), xs[np + n][v] = bf16(x[n][v] - xs[n][v])
+ *                      (BF16 hi / lo pairs of FP32 images; rows n_inst..np-1 zero)
+ *   jscc_batch_ratio:  f = F[b][n] + F[b][np + n]; q = y[n][b0 + b] / f; qs = hi / lo of q as
+ *                      above, [2 np x nb]; f_out[n][b] = f when non-NULL
+ *   jscc_batch_weight: w_out[n][v] (+)= scale * (W[v][n] + W[v][np + n])
+ */
+JSCC_API int jscc_batch_split(const float* x, int64_t ldx, int32_t n_inst, int32_t np, int64_t V, void* xs,
+                   int64_t ldxs, void* stream);
+JSCC_API int jscc_batch_ratio(const float* F, int64_t ldf, const float* y, int64_t ldy, int64_t b0, int64_t nb,
+                   int32_t n_inst, int32_t np, void* qs, int64_t ldqs, float* f_out, int64_t ldfo,
+                   void* stream);
+JSCC_API int jscc_batch_weight(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np, float scale,
+                   float* w_out, int64_t ldwo, int32_t accumulate, void* stream);
+
+/*
+ * Batched plain EM update (recon_osem_plane.py:54 per instance) from the back-projection GEMM:
+ *   x[n][v] = x[n][v] * (W[v][n] + W[v][np + n]) / s_map[v]      (in place)
+ * and, when xs is non-NULL, the updated images' BF16 hi / lo pairs as jscc_batch_split writes
+ * them (rows n_inst..np-1 of xs are left as they are).
+ */
+JSCC_API int jscc_batch_em(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np, float* x,
+                   int64_t ldx, const float* s_map, void* xs, int64_t ldxs, void* stream);
+
+/* Tensor-core GEMM waits that gave up since the last call (synchronous device read). */
+JSCC_API int jscc_take_gemm_timeout_count(unsigned int* out);
 
 /* ------------------------------------------------------------ MAP prior */
 

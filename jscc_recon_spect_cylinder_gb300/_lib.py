@@ -41,6 +41,7 @@ _SIGNATURES: dict[str, tuple] = {
     "jscc_abi_version": (c_int, []),
     "jscc_launch_count": (c_ulonglong, []),
     "jscc_reset_launch_count": (None, []),
+    "jscc_count_graph_launches": (None, [c_ulonglong]),
     "jscc_take_bad_index_count": (c_int, [POINTER(c_uint)]),
     "jscc_kernel_timing_enable": (None, [c_int]),
     "jscc_kernel_timing_collect": (c_int, [ctypes.c_char_p, c_size_t]),
@@ -65,6 +66,24 @@ _SIGNATURES: dict[str, tuple] = {
         [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
          c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
+    "jscc_bf16_gemm_workspace_bytes": (c_size_t, [c_int64, c_int32, c_int64, c_int32]),
+    "jscc_bf16_gemm_nt": (
+        c_int,
+        [c_void_p, c_int64, c_void_p, c_int64, c_int64, c_int32, c_int64, c_int32, c_void_p, c_int64, c_void_p,
+         c_size_t, c_void_p],
+    ),
+    "jscc_batch_split": (c_int, [c_void_p, c_int64, c_int32, c_int32, c_int64, c_void_p, c_int64, c_void_p]),
+    "jscc_batch_ratio": (
+        c_int,
+        [c_void_p, c_int64, c_void_p, c_int64, c_int64, c_int64, c_int32, c_int32, c_void_p, c_int64, c_void_p,
+         c_int64, c_void_p],
+    ),
+    "jscc_batch_weight": (
+        c_int, [c_void_p, c_int64, c_int64, c_int32, c_int32, c_float, c_void_p, c_int64, c_int32, c_void_p]),
+    "jscc_batch_em": (
+        c_int, [c_void_p, c_int64, c_int64, c_int32, c_int32, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
+                c_void_p]),
+    "jscc_take_gemm_timeout_count": (c_int, [POINTER(c_uint)]),
     "jscc_rdp_prior": (
         c_int,
         [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_float, c_float, c_float, c_void_p, c_void_p, c_int32,
@@ -206,6 +225,13 @@ def take_wait_timeout_count() -> int:
     """Bounded device waits (bulk-copy pipeline) that gave up since the last call."""
     out = ctypes.c_uint(0)
     check(load().jscc_take_wait_timeout_count(ctypes.byref(out)), "jscc_take_wait_timeout_count")
+    return int(out.value)
+
+
+def take_gemm_timeout_count() -> int:
+    """Tensor-core GEMM waits that gave up since the last call."""
+    out = c_uint(0)
+    check(load().jscc_take_gemm_timeout_count(ctypes.byref(out)), "jscc_take_gemm_timeout_count")
     return int(out.value)
 
 

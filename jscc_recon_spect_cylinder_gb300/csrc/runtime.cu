@@ -122,10 +122,12 @@ int jscc_kernel_timing_collect(char* buf, size_t buf_bytes) {
 
 const char* jscc_last_error(void) { return jscc::g_err; }
 
-int jscc_abi_version(void) { return 4; }
+int jscc_abi_version(void) { return 5; }
 
 unsigned long long jscc_launch_count(void) { return jscc::launch_counter().load(); }
 
 void jscc_reset_launch_count(void) { jscc::launch_counter().store(0); }
+
+void jscc_count_graph_launches(unsigned long long n) { jscc::launch_counter().fetch_add(n); }
 
 }  // extern "C"

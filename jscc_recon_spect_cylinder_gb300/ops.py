@@ -267,6 +267,31 @@ def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=No
     return out
 
 
+def bf16_gemm_nt(P, R, out=None, k_splits=1):
+    """``out[m, n] = sum_k P[m, k] R[n, k]`` on the tensor cores (jscc_bf16_gemm_nt): P [M, K]
+    and R [nr, K] BF16 with unit stride along K (row strides multiples of 8), nr <= 256;
+    FP32 result [M, nr]."""
+    dev = _lib.require_cuda(P, R, out, what="bf16_gemm_nt")
+    if P.dtype != torch.bfloat16 or R.dtype != torch.bfloat16:
+        raise ValueError("bf16_gemm_nt: P and R must be bfloat16")
+    if P.dim() != 2 or R.dim() != 2 or P.size(1) != R.size(1):
+        raise ValueError(f"bf16_gemm_nt: P {tuple(P.shape)} and R {tuple(R.shape)} do not share K")
+    if P.stride(1) != 1 or R.stride(1) != 1:
+        raise ValueError("bf16_gemm_nt: P and R need unit stride along K")
+    M, K = P.shape
+    nr = R.size(0)
+    if out is None:
+        out = torch.empty((M, nr), dtype=torch.float32, device=dev)
+    if out.dtype != torch.float32 or out.stride(1) != 1 or out.size(0) != M or out.size(1) < nr:
+        raise ValueError("bf16_gemm_nt: out must be float32 [M, >= nr] with unit column stride")
+    lib = _lib.load()
+    ws = _lib.workspace.get(dev, lib.jscc_bf16_gemm_workspace_bytes(M, nr, K, int(k_splits)))
+    rc = lib.jscc_bf16_gemm_nt(P.data_ptr(), P.stride(0), R.data_ptr(), R.stride(0), M, nr, K, int(k_splits),
+                               out.data_ptr(), out.stride(0), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+    _lib.check(rc, "jscc_bf16_gemm_nt")
+    return out
+
+
 def rdp_prior(img, nbr, weight, gamma=2.0, beta=1.0, eps=1e-9, want_value=True, want_grad=True, grad_out=None,
               accumulate=False):
     """Relative-difference prior ``beta R(img)`` and its gradient (jscc_rdp_prior) over a

@@ -1,0 +1,86 @@
+"""Batched (multi-instance) SC path on the tensor cores: the tcgen05 BF16 GEMM against an
+FP64 product of the same BF16 operands (every product of two BF16 values is exact in FP32,
+so only the FP32 accumulation order differs: 1e-5 relative)."""
+from __future__ import annotations
+
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,nr,K,splits", [(300, 128, 200, 1), (128, 64, 64, 1), (257, 100, 1032, 3), (40, 20, 8, 1),
+                                           (1000, 256, 4096, 4), (129, 32, 0, 1)])
+def test_bf16_gemm_matches_fp64(cuda, M, nr, K, splits):
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops
+
+    g = torch.Generator().manual_seed(M + nr + K)
+    P = (torch.rand((M, K), generator=g) - 0.3).to(torch.bfloat16)
+    R = (torch.rand((nr, K), generator=g) * 2 - 0.5).to(torch.bfloat16)
+    out = ops.bf16_gemm_nt(P.to(cuda), R.to(cuda), k_splits=splits)
+    torch.cuda.synchronize()
+    assert _lib.take_gemm_timeout_count() == 0
+    ref = P.double() @ R.double().T
+    if K == 0:
+        assert torch.count_nonzero(out.cpu()) == 0
+    else:
+        assert rel_l2(out.cpu(), ref) < 1e-5
+
+
+def test_bf16_gemm_strided_operands(cuda):
+    """Row strides larger than K (a column slice of a wider matrix, as the back projection
+    reads A^T restricted to a subset's bins)."""
+    from jscc_recon_spect_cylinder_gb300 import ops
+
+    g = torch.Generator().manual_seed(3)
+    big = (torch.rand((200, 512), generator=g)).to(torch.bfloat16).to(cuda)
+    P = big[:, 64:64 + 256]
+    R = (torch.rand((48, 256), generator=g)).to(torch.bfloat16).to(cuda)
+    out = ops.bf16_gemm_nt(P, R)
+    ref = P.double().cpu() @ R.double().cpu().T
+    assert rel_l2(out.cpu(), ref) < 1e-5
+
+
+def _fp64_osem(A, y, x0, s, subsets, iters):
+    """osem_bin_mode (one identity view) per instance in float64 (recon_osem_plane.py:45-61)."""
+    X = x0.double().clone()
+    for _ in range(iters):
+        for ids in subsets:
+            As = A[ids]
+            F = X @ As.T                      # [N, bins_s]
+            W = (y[:, ids] / F) @ As          # [N, V]
+            X = X * W / s
+    return X
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batched_osem_matches_fp64(cuda, graph):
+    """Five instances (different count levels of one geometry), three subsets of 85-86 bins
+    (padded to multiples of 8), three iterations: every instance within 1e-4 relative L2 of
+    the float64 OSEM on the same BF16 matrix (the instance vectors carry ~16 bits)."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, batched, synthetic
+    from jscc_recon_spect_cylinder_gb300.recon_osem_plane import split_tensor_even
+
+    prob = synthetic.sc_problem(n_r=8, n_theta=24, n_phi=64, views=4, flat=True, total_counts=1e5)
+    A = prob.sysmat.to(torch.bfloat16)
+    B, V = A.shape
+    g = torch.Generator().manual_seed(5)
+    mean = A.float() @ prob.phantom.reshape(-1)
+    y = torch.stack([torch.poisson(mean * (c / mean.sum()), generator=g) for c in (1e4, 3e4, 1e5, 3e5, 1e6)])
+    subsets = split_tensor_even(torch.randperm(B, generator=g), 3)
+    s = A.double().sum(0)
+    x0 = torch.ones((5, V))
+    b = batched.BatchedScOsem(A, subsets, s.float(), 5, device=cuda)
+    b.set_projections(y)
+    b.set_images(x0)
+    b.autotune()
+    if graph:
+        b.capture()
+    X = b.iterate(3).cpu()
+    torch.cuda.synchronize()
+    assert _lib.take_gemm_timeout_count() == 0
+    ref = _fp64_osem(A.double(), y.double(), x0, s, subsets, 3)
+    for n in range(5):
+        assert rel_l2(X[n], ref[n]) < 1e-4, n
