@@ -11,44 +11,41 @@
 // bits), stacked as 2 Np rows of R, so the tensor-core product keeps FP32-level accuracy in
 // the instance vectors while A is streamed from HBM once per pass for all instances.
 //
-// GEMM kernel (one 128-thread CTA per 128-row tile and K split):
-//   * operands staged into shared memory by cp.async in the no-swizzle K-major core-matrix
-//     layout (8 rows x 16 bytes per core matrix, core matrices K-fastest), zero-filled past
-//     the matrix edges, 4-stage ring;
-//   * one elected thread issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32, M = 128,
-//     N = Nr) into a TMEM accumulator of Nr columns and commits each stage to an mbarrier,
-//     which releases the stage for the next cp.async round;
-//   * epilogue: each warp reads its 32 TMEM lanes with tcgen05.ld and writes FP32 rows.
-//   Every wait is bounded; a wait that gives up is counted (jscc_take_wait_timeout_count
-//   does not see it: jscc_take_gemm_timeout_count does) and the CTA still frees its TMEM.
+// GEMM kernel (one 128-thread CTA per 128-row tile and K split, two CTAs per SM,
+// warp-specialised):
+//   * producer (warp 0, one thread): TMA tiled loads (cp.async.bulk.tensor, 128-byte swizzle)
+//     of the P and R tiles of each 64-wide K step into a ring of shared-memory stages, each
+//     completing on the stage's "full" mbarrier (expect-tx bytes);
+//   * MMA issuer (warp 1, one thread): waits "full", issues tcgen05.mma (kind::f16, BF16 x
+//     BF16 -> FP32, M = 128, N = Nr, K = 16 per instruction) into a TMEM accumulator of Nr
+//     columns, and commits to the stage's "empty" mbarrier, which the producer waits for
+//     before refilling it; a last commit signals the epilogue;
+//   * epilogue (all four warps): each warp reads its 32 TMEM lanes with tcgen05.ld and writes
+//     FP32 rows.
+//   Every wait is bounded and polls a CTA abort flag; a CTA that gives up is counted
+//   (jscc_take_gemm_timeout_count) and still frees its TMEM.
 #include "jscc_common.cuh"
+
+#include <cuda.h>
+#include <cstring>
 
 namespace jscc {
 
 constexpr int kGM = 128;          // tile rows = MMA M
 constexpr int kGK = 64;           // K per stage (128 bytes of BF16 per row)
-constexpr int kGStages = 4;
 constexpr int kGThreads = 128;
 constexpr uint32_t kGemmPolls = 1u << 22;
 
 __device__ unsigned int g_gemm_timeout_count = 0;
 
-// Byte offset of element (r, k) of a [rows x 64] K-major tile: core matrix (r / 8, k / 8) of
-// 8 rows x 16 bytes at ((r / 8) * 8 + k / 8) * 128, row r % 8 at 16-byte steps inside it.
-// Adjacent core matrices along K are 128 bytes apart (leading byte offset), adjacent 8-row
-// groups 1024 bytes (stride byte offset).
-__device__ __forceinline__ uint32_t tile_off(int r, int k) {
-  return (uint32_t)(((((r >> 3) << 3) + (k >> 3))) << 7) + (uint32_t)((r & 7) << 4) + (uint32_t)((k & 7) << 1);
-}
-constexpr uint32_t kLBO = 128;
-constexpr uint32_t kSBO = 1024;
-
-// tcgen05 shared-memory matrix descriptor: start address >> 4 (bits 0-13), leading byte
-// offset >> 4 (16-29), stride byte offset >> 4 (32-45), descriptor version 1 (46-47), base
-// offset 0, no swizzle (61-63 = 0).
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(kLBO >> 4) << 16) | ((uint64_t)(kSBO >> 4) << 32) |
-         (1ull << 46);
+// tcgen05 shared-memory matrix descriptor for a K-major tile written by TMA with 128-byte
+// swizzle (rows of 64 BF16 = 128 bytes, 8-row atoms of 1024 bytes): start address >> 4
+// (bits 0-13), leading byte offset 16 >> 4 (unused inside one swizzle row), stride byte
+// offset 1024 >> 4 (32-45), descriptor version 1 (46-47), layout SWIZZLE_128B = 2 (61-63).
+// A K = 16 slice starts 32 bytes further along the row.
+__device__ __forceinline__ uint64_t umma_desc_sw128(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
 }
 
 // Instruction descriptor for kind::f16: D FP32 (bits 4-5 = 1), A and B BF16 (bits 7-9 and
@@ -57,13 +54,12 @@ __host__ __device__ constexpr uint32_t umma_idesc(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -100,27 +96,45 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Bounded wait that also gives up when another role of the CTA raised the abort flag.
+__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kGemmPolls; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 255) == 255 && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
 template <int NR>
 struct GemmCfg {
   static_assert(NR % 16 == 0 && NR >= 16 && NR <= 256, "MMA N for M = 128");
-  static constexpr uint32_t kA = kGM * kGK * 2;
+  static constexpr uint32_t kA = kGM * kGK * 2;  // 16 KB
   static constexpr uint32_t kB = NR * kGK * 2;
   static constexpr uint32_t kStage = kA + kB;
+  // ~100 KB of stages: two CTAs per SM (their TMA rings interleave, so both grids of a
+  // config-4 subset fit one wave of 2 x 152 CTAs)
+  static constexpr int kStages = (100u * 1024u / kStage) < 8u ? (int)(100u * 1024u / kStage) : 8;
   static constexpr uint32_t kTmemCols = NR <= 32 ? 32 : NR <= 64 ? 64 : NR <= 128 ? 128 : 256;
-  static constexpr size_t kSmem = (size_t)kGStages * kStage + 64 + 1024;  // + barriers, TMEM slot, alignment
+  static constexpr size_t kSmem = (size_t)kStages * kStage + 256 + 1024;  // + barriers, flags, alignment
+  static_assert(kStages >= 2, "two stages at least");
 };
 
 // out[split][m][n] = sum_{k in split} P[m, k] R[n, k]   (rows m < M, n < nr; FP32)
 template <int NR>
-__global__ void __launch_bounds__(kGThreads, 1)
-bf16_gemm_nt_kernel(const __nv_bfloat16* __restrict__ P, int64_t ldp, const __nv_bfloat16* __restrict__ R,
-                    int64_t ldr, int64_t M, int nr, int64_t K, int64_t k_per_split, float* __restrict__ out,
-                    int64_t ldo, int64_t split_stride) {
+__global__ void __launch_bounds__(kGThreads, 2)
+bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_constant__ CUtensorMap tmR, int64_t M,
+                    int nr, int64_t K, int64_t k_per_split, float* __restrict__ out, int64_t ldo,
+                    int64_t split_stride) {
   using C = GemmCfg<NR>;
+  constexpr int S = C::kStages;
   extern __shared__ uint8_t gsm_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(gsm_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kGStages * C::kStage);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kGStages);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * C::kStage);
+  uint64_t* empty = full + S;
+  uint64_t* done = empty + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t m0 = (int64_t)blockIdx.x * kGM;
@@ -129,7 +143,12 @@ bf16_gemm_nt_kernel(const __nv_bfloat16* __restrict__ P, int64_t ldp, const __nv
   const int nk = ke > kb ? (int)((ke - kb + kGK - 1) / kGK) : 0;
 
   if (tid == 0) {
-    for (int s = 0; s < kGStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
     mbar_init_fence();
   }
   if (warp == 0) {
@@ -144,66 +163,35 @@ bf16_gemm_nt_kernel(const __nv_bfloat16* __restrict__ P, int64_t ldp, const __nv
   const uint32_t tmem = *tmem_slot;
   const uint32_t sbase = smem_u32(smem);
 
-  auto load_tile = [&](int t) {
-    const int s = t % kGStages;
-    const uint32_t a_base = sbase + s * C::kStage, b_base = a_base + C::kA;
-    const int64_t k0 = kb + (int64_t)t * kGK;
-    for (int c = tid; c < kGM * 8; c += kGThreads) {
-      const int r = c >> 3, kc = (c & 7) << 3;
-      const int64_t gr = m0 + r, gk = k0 + kc;
-      const bool ok = gr < M && gk < ke;  // K and the split boundaries are multiples of 8
-      cp_async16(a_base + tile_off(r, kc), ok ? (const void*)(P + gr * ldp + gk) : (const void*)P, ok ? 16u : 0u);
+  if (nk > 0 && warp == 0 && lane == 0) {
+    // producer
+    for (int t = 0; t < nk; ++t) {
+      const int s = t % S;
+      if (t >= S && !role_wait(&empty[s], (uint32_t)(((t / S) - 1) & 1), abort_flag)) break;
+      mbar_arrive_expect_tx(&full[s], C::kStage);
+      const int x = (int)(kb + (int64_t)t * kGK);
+      tma_load_2d(sbase + s * C::kStage, &tmP, x, (int)m0, &full[s]);
+      tma_load_2d(sbase + s * C::kStage + C::kA, &tmR, x, 0, &full[s]);
     }
-    for (int c = tid; c < NR * 8; c += kGThreads) {
-      const int r = c >> 3, kc = (c & 7) << 3;
-      const int64_t gk = k0 + kc;
-      const bool ok = r < nr && gk < ke;
-      cp_async16(b_base + tile_off(r, kc), ok ? (const void*)(R + (int64_t)r * ldr + gk) : (const void*)R,
-                 ok ? 16u : 0u);
-    }
-  };
-
-  constexpr uint32_t idesc = umma_idesc(kGM, NR);
-  bool failed = false;
-#pragma unroll 1
-  for (int t = 0; t < kGStages - 1; ++t) {
-    if (t < nk) load_tile(t);
-    cp_async_commit();
-  }
-#pragma unroll 1
-  for (int t = 0; t < nk; ++t) {
-    const int tn = t + kGStages - 1;
-    bool bad = false;
-    if (tn < nk) {
-      if (t >= 1) {
-        // stage (t - 1) % S is refilled: the MMAs of tile t - 1 must have read it
-        const int sp = (t - 1) % kGStages;
-        bad = !mbar_wait_bounded(&bars[sp], (uint32_t)(((t - 1) / kGStages) & 1), kGemmPolls);
-      }
-      if (!bad) load_tile(tn);
-    }
-    cp_async_commit();
-    cp_async_wait<kGStages - 1>();
-    fence_proxy_async_smem();
-    if (__syncthreads_or(bad)) {
-      failed = true;
-      break;
-    }
-    if (tid == 0) {
+  } else if (nk > 0 && warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = umma_idesc(kGM, NR);
+    int t = 0;
+    for (; t < nk; ++t) {
+      const int s = t % S;
+      if (!role_wait(&full[s], (uint32_t)((t / S) & 1), abort_flag)) break;
       tc_fence_after();
-      const uint32_t a_base = sbase + (t % kGStages) * C::kStage, b_base = a_base + C::kA;
+      const uint32_t a = sbase + s * C::kStage, b = a + C::kA;
 #pragma unroll
-      for (int kk = 0; kk < kGK / 16; ++kk)  // K = 16 per MMA: two core matrices = 256 bytes
-        tc_mma(tmem, umma_desc(a_base + kk * 256), umma_desc(b_base + kk * 256), idesc, (t > 0 || kk > 0) ? 1u : 0u);
-      tc_commit(&bars[t % kGStages]);
+      for (int kk = 0; kk < kGK / 16; ++kk)
+        tc_mma(tmem, umma_desc_sw128(a + kk * 32), umma_desc_sw128(b + kk * 32), idesc, (t > 0 || kk > 0) ? 1u : 0u);
+      tc_commit(&empty[s]);
     }
+    tc_commit(done);  // arrives when every MMA issued above has completed
   }
-  cp_async_wait<0>();
-  // the last commit covers every MMA issued before it
-  bool done = true;
-  if (nk > 0 && !failed) done = mbar_wait_bounded(&bars[(nk - 1) % kGStages], (uint32_t)(((nk - 1) / kGStages) & 1),
-                                                  kGemmPolls);
-  const bool ok = __syncthreads_and(done && !failed);
+  bool ok = true;
+  if (nk > 0) ok = role_wait(done, 0u, abort_flag) && !*abort_flag;
+  ok = __syncthreads_and(ok);
   tc_fence_after();
   const int64_t row = m0 + warp * 32 + lane;
   float* orow = out + (int64_t)blockIdx.y * split_stride + row * ldo;
@@ -328,6 +316,36 @@ using namespace jscc;
 
 namespace {
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// Tensor map of a row-major [rows x K] BF16 matrix (row stride ld elements), box = 64 K
+// elements (128 bytes) x box_rows rows, 128-byte swizzle, zero fill outside the matrix.
+bool make_map(CUtensorMap* map, const void* base, int64_t K, int64_t rows, int64_t ld, uint32_t box_rows) {
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)(K > 0 ? K : 8), (cuuint64_t)(rows > 0 ? rows : 1)};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kGK, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 template <int NR>
 int launch_gemm(const __nv_bfloat16* P, int64_t ldp, const __nv_bfloat16* R, int64_t ldr, int64_t M, int nr, int64_t K,
                 int splits, float* out, int64_t ldo, float* part, cudaStream_t st) {
@@ -343,13 +361,20 @@ int launch_gemm(const __nv_bfloat16* P, int64_t ldp, const __nv_bfloat16* R, int
   if (kps < kGK) kps = kGK;  // K = 0: one split whose tiles write zeros
   int64_t used = (K + kps - 1) / kps;
   if (used < 1) used = 1;
+  CUtensorMap mp, mr;
+  if (K > 0) {
+    JSCC_REQUIRE(make_map(&mp, P, K, M, ldp, kGM) && make_map(&mr, R, K, nr, ldr, NR),
+                 "jscc_bf16_gemm_nt: tensor map encoding failed");
+  } else {
+    memset(&mp, 0, sizeof(mp));
+    memset(&mr, 0, sizeof(mr));
+  }
   dim3 grid((unsigned)((M + kGM - 1) / kGM), (unsigned)used);
   float* dst = used > 1 ? part : out;
   const int64_t ldd = used > 1 ? nr : ldo;
   const int64_t sstride = used > 1 ? M * nr : 0;
   JSCC_TIMED("bf16_gemm_nt", st,
-             (bf16_gemm_nt_kernel<NR><<<grid, kGThreads, C::kSmem, st>>>(P, ldp, R, ldr, M, nr, K, kps, dst, ldd,
-                                                                        sstride)));
+             (bf16_gemm_nt_kernel<NR><<<grid, kGThreads, C::kSmem, st>>>(mp, mr, M, nr, K, kps, dst, ldd, sstride)));
   JSCC_LAUNCH_CHECK();
   if (used > 1) {
     int64_t blocks = (M * nr + 255) / 256;
