@@ -573,11 +573,17 @@ cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __res
     for (int k = 0; k < NP; ++k) {
       if (k < np) {
         float2 t = cone_pair_fast<WINDOW>(sev[k], ncx, ncy, ncz);
-        if (t.x != 0.f || t.y != 0.f) {
-          if (eff) {
-            t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
-            t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+        if constexpr (WINDOW) {
+          // pairs outside the window skip their efficiency load
+          if (t.x != 0.f || t.y != 0.f) {
+            if (eff) {
+              t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
+              t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+            }
+            af[k] = __ffma2_rn(t, xj, af[k]);
           }
+        } else {
+          if (eff) t = __fmul2_rn(t, make_float2(eff_load(eff + srow[2 * k], j), eff_load(eff + srow[2 * k + 1], j)));
           af[k] = __ffma2_rn(t, xj, af[k]);
         }
       }
@@ -640,11 +646,16 @@ cone_back_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restri
       const int np = (n + 1) >> 1;
       for (int k = 0; k < np; ++k) {
         float2 t = cone_pair_fast<WINDOW>(sev[k], ncx, ncy, ncz);
-        if (t.x != 0.f || t.y != 0.f) {
-          if (eff) {
-            t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
-            t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+        if constexpr (WINDOW) {
+          if (t.x != 0.f || t.y != 0.f) {
+            if (eff) {
+              t.x = t.x != 0.f ? t.x * eff_load(eff + srow[2 * k], j) : 0.f;
+              t.y = t.y != 0.f ? t.y * eff_load(eff + srow[2 * k + 1], j) : 0.f;
+            }
+            acc = __ffma2_rn(t, make_float2(sq[2 * k], sq[2 * k + 1]), acc);
           }
+        } else {
+          if (eff) t = __fmul2_rn(t, make_float2(eff_load(eff + srow[2 * k], j), eff_load(eff + srow[2 * k + 1], j)));
           acc = __ffma2_rn(t, make_float2(sq[2 * k], sq[2 * k + 1]), acc);
         }
       }
