@@ -428,6 +428,35 @@ JSCC_API int jscc_em_update(float* img_out, const float* img, const float* w_a, 
                    float coef_a, const float* w_b, float coef_b, const float* s_map, int64_t n_vox,
                    int32_t mode, float eps, void* stream);
 
+/* ------------------------------------------------ FP64 projector halves and prior */
+
+/*
+ * Reference-grade double-precision forms of jscc_sc_project / jscc_sc_backproject,
+ * jscc_compton_project / jscc_compton_backproject (strict model, every pair, no rotation
+ * tables on the Compton side) and jscc_rdp_prior: the same definitions with double images,
+ * projections, adjoint inputs and outputs, every sum in double (the matrix, efficiency rows and
+ * event records are read as stored and promoted exactly). For gradient checks of penalised-
+ * likelihood objectives against FP64 finite differences; simple kernels, not a hot path.
+ * Workspace of jscc_sc_backproject_f64: jscc_sc_f64_workspace_bytes(n_vox, n_rot).
+ */
+JSCC_API size_t jscc_sc_f64_workspace_bytes(int64_t n_vox, int32_t n_rot);
+JSCC_API int jscc_sc_project_f64(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, int32_t n_rot, const double* img, const int64_t* rotmat,
+                   int64_t ld_rot, double* out, int64_t ld_out, void* stream);
+JSCC_API int jscc_sc_backproject_f64(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
+                   int64_t n_bins, int64_t n_vox, int32_t n_rot, const double* g, int64_t ld_g,
+                   const int64_t* rotmat_inv, int64_t ld_rot, double scale, double* weight, void* workspace,
+                   size_t workspace_bytes, void* stream);
+JSCC_API int jscc_compton_project_f64(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor,
+                   int64_t n_vox, int32_t model, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                   const double* img, double* f_out, void* stream);
+JSCC_API int jscc_compton_backproject_f64(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const float* coor, int64_t n_vox, int32_t model, const void* eff, int32_t eff_dtype,
+                   int64_t ld_eff, const double* g, double scale, double* weight, void* stream);
+JSCC_API int jscc_rdp_prior_f64(const double* img, const int32_t* nbr, const float* weight, int64_t n_vox,
+                   int32_t n_nbr, double gamma, double eps, double beta, double* value, double* grad,
+                   int32_t accumulate, void* stream);
+
 /* ------------------------------------------------ batched (multi-instance) SC path */
 
 /*

@@ -66,6 +66,32 @@ _SIGNATURES: dict[str, tuple] = {
         [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int32, c_int64, c_void_p,
          c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
+    "jscc_sc_f64_workspace_bytes": (c_size_t, [c_int64, c_int32]),
+    "jscc_sc_project_f64": (
+        c_int,
+        [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_void_p, c_int64, c_void_p,
+         c_int64, c_void_p],
+    ),
+    "jscc_sc_backproject_f64": (
+        c_int,
+        [c_void_p, c_int32, c_int64, c_void_p, c_int64, c_int64, c_int32, c_void_p, c_int64, c_void_p, c_int64,
+         ctypes.c_double, c_void_p, c_void_p, c_size_t, c_void_p],
+    ),
+    "jscc_compton_project_f64": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p, c_int32, c_int64, c_void_p, c_void_p,
+         c_void_p],
+    ),
+    "jscc_compton_backproject_f64": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+         ctypes.c_double, c_void_p, c_void_p],
+    ),
+    "jscc_rdp_prior_f64": (
+        c_int,
+        [c_void_p, c_void_p, c_void_p, c_int64, c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+         c_void_p, c_void_p, c_int32, c_void_p],
+    ),
     "jscc_bf16_gemm_workspace_bytes": (c_size_t, [c_int64, c_int32, c_int64, c_int32]),
     "jscc_bf16_gemm_nt": (
         c_int,

@@ -664,6 +664,83 @@ cone_back_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restri
   if (j < V) part[(int64_t)blockIdx.y * ldp + j] = acc.x + acc.y;
 }
 
+// ------------------------------------------------------------------ FP64 evaluation
+// Reference-grade projector halves for gradient checks: the strict kernel of
+// process_list_plane_strict.py:201-228 evaluated in double from the same records (no window,
+// no staged factors), sums in double. Not a hot path: one CTA per event forward, one thread
+// per voxel back.
+__device__ __forceinline__ double cone_strict_f64(const ConeEvent& e, double cx, double cy, double cz) {
+  const double ax = (double)e.p1x - cx, ay = (double)e.p1y - cy, az = (double)e.p1z - cz;
+  const double vx = e.vx, vy = e.vy, vz = e.vz, d12 = e.d12;
+  const double dot = ax * vx + ay * vy + az * vz;
+  const double d01 = sqrt(ax * ax + ay * ay + az * az);
+  const double bcos = dot / fmax(d01 * d12, 1e-7);
+  const double c = fmin(fmax(bcos, -1.0 + 1e-7), 1.0 - 1e-7);
+  const double delta = acos(c) - (double)e.theta;
+  const double sig_e = delta >= 0.0 ? (double)e.sig_plus : (double)e.sig_minus;
+  const double i01 = 1.0 / fmax(d01, 1e-7), i12 = 1.0 / fmax(d12, 1e-7);
+  const double ux = ax * i01, uy = ay * i01, uz = az * i01;
+  const double wx = vx * i12, wy = vy * i12, wz = vz * i12;
+  const double cb = ux * wx + uy * wy + uz * wz;
+  const double sb2 = fmax(1.0 - cb * cb, 1e-12);
+  const double jx = (ux - cb * wx) * i12, jy = (uy - cb * wy) * i12, jz = (uz - cb * wz) * i12;
+  const double sp2 = (jx * jx * e.s0 + jy * jy * e.s1 + jz * jz * e.s2) / sb2;
+  const double sig_pos = sqrt(fmax(sp2, 1e-12));
+  const double sig2 = fmax(sig_pos * sig_pos + sig_e * sig_e, 1e-12);
+  return exp(-(delta * delta) / (2.0 * sig2)) * ((double)e.kn - (1.0 - c) * (1.0 + c));
+}
+
+template <typename TE>
+__device__ __forceinline__ double eff_f64(const TE* p, int64_t i) {
+  return (double)eff_load(p, i);
+}
+
+// f[i] = sum_j t_ij eff_ij x_j
+template <typename TE>
+__global__ void __launch_bounds__(256)
+cone_forward_f64_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                        const float* __restrict__ coor, int64_t V, const double* __restrict__ x,
+                        const TE* __restrict__ eff, int64_t ld_eff, double* __restrict__ f_out) {
+  __shared__ double red[8];
+  for (int64_t i = blockIdx.x; i < n_ev; i += gridDim.x) {
+    const ConeEvent e = rec[i];
+    const TE* er = eff ? eff + (int64_t)row_id[i] * ld_eff : nullptr;
+    double acc = 0.0;
+    for (int64_t j = threadIdx.x; j < V; j += blockDim.x) {
+      double t = cone_strict_f64(e, coor[3 * j], coor[3 * j + 1], coor[3 * j + 2]);
+      if (er) t *= eff_f64(er, j);
+      acc += t * x[j];
+    }
+    acc = warp_sum_d(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double f = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) f += red[w];
+      f_out[i] = f;
+    }
+    __syncthreads();
+  }
+}
+
+// weight[j] += scale * sum_i t_ij eff_ij g_i
+template <typename TE>
+__global__ void __launch_bounds__(256)
+cone_back_f64_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
+                     const float* __restrict__ coor, int64_t V, const double* __restrict__ g,
+                     const TE* __restrict__ eff, int64_t ld_eff, double scale, double* __restrict__ weight) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V; j += (int64_t)gridDim.x * blockDim.x) {
+    const double cx = coor[3 * j], cy = coor[3 * j + 1], cz = coor[3 * j + 2];
+    double acc = 0.0;
+    for (int64_t i = 0; i < n_ev; ++i) {
+      double t = cone_strict_f64(rec[i], cx, cy, cz);
+      if (eff) t *= eff_f64(eff + (int64_t)row_id[i] * ld_eff, j);
+      acc += t * g[i];
+    }
+    weight[j] += scale * acc;
+  }
+}
+
 // ------------------------------------------------------------------ host planning
 struct ConePlan {
   int64_t chunks;
@@ -934,6 +1011,58 @@ int jscc_compton_backproject(const float* records, const int32_t* row_id, int64_
   return compton_stage_entry("jscc_compton_backproject", 2, records, row_id, n_ev, coor, n_vox, model, use_window, eff,
                              eff_dtype, ld_eff, nullptr, nullptr, rotmat_inv, ld_rot, g, nullptr, scale, weight,
                              workspace, workspace_bytes, stream);
+}
+
+static int compton_f64_entry(const char* what, int stage, const float* records, const int32_t* row_id, int64_t n_ev,
+                             const float* coor, int64_t n_vox, int32_t model, const void* eff, int32_t eff_dtype,
+                             int64_t ld_eff, const double* in, double scale, double* out, void* stream) {
+  JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0, "%s: negative size", what);
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT, "%s: the FP64 evaluation implements the strict model only", what);
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "%s: bad dtype", what);
+  if (n_ev == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(records && coor && in && out, "%s: null pointer argument", what);
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= n_vox), "%s: efficiency rows need row ids, ld >= V", what);
+  cudaStream_t st = as_stream(stream);
+  const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
+  const int64_t cap = (int64_t)num_sms() * 8;
+  if (stage == 1) {
+    const unsigned grid = (unsigned)(n_ev < cap ? n_ev : cap);
+    if (eff_dtype == JSCC_DTYPE_BF16)
+      JSCC_TIMED("cone_forward_f64", st,
+                 (cone_forward_f64_kernel<__nv_bfloat16><<<grid, 256, 0, st>>>(
+                     rec, row_id, n_ev, coor, n_vox, in, static_cast<const __nv_bfloat16*>(eff), ld_eff, out)));
+    else
+      JSCC_TIMED("cone_forward_f64", st,
+                 (cone_forward_f64_kernel<float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, n_vox, in,
+                                                                      static_cast<const float*>(eff), ld_eff, out)));
+  } else {
+    int64_t blocks = (n_vox + 255) / 256;
+    if (blocks > cap) blocks = cap;
+    if (eff_dtype == JSCC_DTYPE_BF16)
+      JSCC_TIMED("cone_back_f64", st,
+                 (cone_back_f64_kernel<__nv_bfloat16><<<(unsigned)blocks, 256, 0, st>>>(
+                     rec, row_id, n_ev, coor, n_vox, in, static_cast<const __nv_bfloat16*>(eff), ld_eff, scale, out)));
+    else
+      JSCC_TIMED("cone_back_f64", st,
+                 (cone_back_f64_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
+                     rec, row_id, n_ev, coor, n_vox, in, static_cast<const float*>(eff), ld_eff, scale, out)));
+  }
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_compton_project_f64(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor,
+                             int64_t n_vox, int32_t model, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                             const double* img, double* f_out, void* stream) {
+  return compton_f64_entry("jscc_compton_project_f64", 1, records, row_id, n_ev, coor, n_vox, model, eff, eff_dtype,
+                           ld_eff, img, 1.0, f_out, stream);
+}
+
+int jscc_compton_backproject_f64(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor,
+                                 int64_t n_vox, int32_t model, const void* eff, int32_t eff_dtype, int64_t ld_eff,
+                                 const double* g, double scale, double* weight, void* stream) {
+  return compton_f64_entry("jscc_compton_backproject_f64", 2, records, row_id, n_ev, coor, n_vox, model, eff,
+                           eff_dtype, ld_eff, g, scale, weight, stream);
 }
 
 int jscc_take_bad_detector_count(unsigned int* out) {

@@ -28,16 +28,17 @@ unsigned int take_prior_bad_index_count() {
   return h;
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kPriorThreads)
-rdp_prior_kernel(const float* __restrict__ x, const int32_t* __restrict__ nbr, const float* __restrict__ wt,
-                 int64_t n_vox, int n_nbr, float gamma, float eps, float beta, double* __restrict__ value,
-                 float* __restrict__ grad, int accumulate) {
-  __shared__ float red[kPriorThreads / 32];
-  float part = 0.f;
+rdp_prior_kernel(const R* __restrict__ x, const int32_t* __restrict__ nbr, const float* __restrict__ wt,
+                 int64_t n_vox, int n_nbr, R gamma, R eps, R beta, double* __restrict__ value, R* __restrict__ grad,
+                 int accumulate) {
+  __shared__ R red[kPriorThreads / 32];
+  R part = 0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n_vox;
        j += (int64_t)gridDim.x * blockDim.x) {
-    const float a = x[j];
-    float g = 0.f;
+    const R a = x[j];
+    R g = 0;
     for (int k = 0; k < n_nbr; ++k) {
       const int32_t i = nbr[(int64_t)k * n_vox + j];
       if (i < 0) continue;
@@ -45,17 +46,17 @@ rdp_prior_kernel(const float* __restrict__ x, const int32_t* __restrict__ nbr, c
         atomicAdd(&g_prior_bad_index_count, 1u);
         continue;
       }
-      const float b = x[i];
-      const float w = wt[(int64_t)k * n_vox + j];
-      const float d = a - b;
-      if (d == 0.f) continue;  // phi and its derivative vanish (and D may be 0)
-      const float ad = fabsf(d);
-      const float D = a + b + gamma * ad + eps;
-      const float inv = 1.0f / D;
+      const R b = x[i];
+      const R w = (R)wt[(int64_t)k * n_vox + j];
+      const R d = a - b;
+      if (d == (R)0) continue;  // phi and its derivative vanish (and D may be 0)
+      const R ad = fabs(d);
+      const R D = a + b + gamma * ad + eps;
+      const R inv = (R)1 / D;
       part += w * d * d * inv;
-      g += w * d * (a + 3.0f * b + gamma * ad + 2.0f * eps) * inv * inv;
+      g += w * d * (a + (R)3 * b + gamma * ad + (R)2 * eps) * inv * inv;
     }
-    if (grad != nullptr) grad[j] = (accumulate ? grad[j] : 0.f) + beta * g;
+    if (grad != nullptr) grad[j] = (accumulate ? grad[j] : (R)0) + beta * g;
   }
   if (value == nullptr) return;
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -63,7 +64,7 @@ rdp_prior_kernel(const float* __restrict__ x, const int32_t* __restrict__ nbr, c
   if (lane == 0) red[warp] = part;
   __syncthreads();
   if (warp == 0) {
-    part = lane < kPriorThreads / 32 ? red[lane] : 0.f;
+    part = lane < kPriorThreads / 32 ? red[lane] : (R)0;
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if (lane == 0) atomicAdd(value, 0.5 * (double)beta * (double)part);
   }
@@ -73,12 +74,12 @@ rdp_prior_kernel(const float* __restrict__ x, const int32_t* __restrict__ nbr, c
 
 using namespace jscc;
 
-extern "C" int jscc_rdp_prior(const float* img, const int32_t* nbr, const float* weight, int64_t n_vox,
-                              int32_t n_nbr, float gamma, float eps, float beta, double* value, float* grad,
-                              int32_t accumulate, void* stream) {
+template <typename R>
+static int rdp_entry(const R* img, const int32_t* nbr, const float* weight, int64_t n_vox, int32_t n_nbr, R gamma,
+                     R eps, R beta, double* value, R* grad, int32_t accumulate, void* stream) {
   JSCC_REQUIRE(n_vox >= 0 && n_vox <= INT32_MAX, "jscc_rdp_prior: n_vox %lld out of range", (long long)n_vox);
   JSCC_REQUIRE(n_nbr >= 0 && n_nbr <= 64, "jscc_rdp_prior: n_nbr %d out of range [0, 64]", n_nbr);
-  JSCC_REQUIRE(gamma >= 0.f && eps >= 0.f, "jscc_rdp_prior: gamma and eps must be >= 0");
+  JSCC_REQUIRE(gamma >= 0 && eps >= 0, "jscc_rdp_prior: gamma and eps must be >= 0");
   JSCC_REQUIRE(value != nullptr || grad != nullptr, "jscc_rdp_prior: neither value nor grad requested");
   if (n_vox == 0) return JSCC_OK;
   JSCC_REQUIRE(img != nullptr && (n_nbr == 0 || (nbr != nullptr && weight != nullptr)),
@@ -88,8 +89,20 @@ extern "C" int jscc_rdp_prior(const float* img, const int32_t* nbr, const float*
   if (blocks > cap) blocks = cap;
   cudaStream_t st = as_stream(stream);
   JSCC_TIMED("rdp_prior", st,
-             rdp_prior_kernel<<<(unsigned)blocks, kPriorThreads, 0, st>>>(img, nbr, weight, n_vox, n_nbr, gamma,
-                                                                        eps, beta, value, grad, accumulate));
+             rdp_prior_kernel<R><<<(unsigned)blocks, kPriorThreads, 0, st>>>(img, nbr, weight, n_vox, n_nbr, gamma,
+                                                                           eps, beta, value, grad, accumulate));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
+}
+
+extern "C" int jscc_rdp_prior(const float* img, const int32_t* nbr, const float* weight, int64_t n_vox,
+                              int32_t n_nbr, float gamma, float eps, float beta, double* value, float* grad,
+                              int32_t accumulate, void* stream) {
+  return rdp_entry<float>(img, nbr, weight, n_vox, n_nbr, gamma, eps, beta, value, grad, accumulate, stream);
+}
+
+extern "C" int jscc_rdp_prior_f64(const double* img, const int32_t* nbr, const float* weight, int64_t n_vox,
+                                  int32_t n_nbr, double gamma, double eps, double beta, double* value, double* grad,
+                                  int32_t accumulate, void* stream) {
+  return rdp_entry<double>(img, nbr, weight, n_vox, n_nbr, gamma, eps, beta, value, grad, accumulate, stream);
 }

@@ -122,7 +122,7 @@ int jscc_kernel_timing_collect(char* buf, size_t buf_bytes) {
 
 const char* jscc_last_error(void) { return jscc::g_err; }
 
-int jscc_abi_version(void) { return 5; }
+int jscc_abi_version(void) { return 6; }
 
 unsigned long long jscc_launch_count(void) { return jscc::launch_counter().load(); }
 

@@ -783,6 +783,73 @@ static int sc_sensitivity_typed(const T* A, int64_t lda, const int64_t* row_idx,
   return JSCC_OK;
 }
 
+// ------------------------------------------------------------------ FP64 evaluation
+// Reference-grade projector halves for gradient checks (sums in double; not a hot path).
+// f[b, r] = sum_j A[rb, j] x[rot[j, r] - 1]: one warp per (b, r).
+template <typename T>
+__global__ void sc_project_f64_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx,
+                                      int64_t n_bins, int64_t V, int n_rot, const double* __restrict__ x,
+                                      const int64_t* __restrict__ rotmat, int64_t ld_rot, double* __restrict__ out,
+                                      int64_t ld_out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < n_bins * n_rot; w += warps) {
+    const int64_t b = w / n_rot;
+    const int r = (int)(w % n_rot);
+    const T* row = A + (row_idx ? row_idx[b] : b) * lda;
+    double acc = 0.0;
+    for (int64_t j = lane; j < V; j += 32) {
+      int64_t src = j;
+      if (rotmat) {
+        src = rotmat[j * ld_rot + r] - 1;
+        if (src < 0 || src >= V) {
+          atomicAdd(&g_bad_index_count, 1u);
+          continue;
+        }
+      }
+      acc += (double)load_elem(row, j) * x[src];
+    }
+    acc = warp_sum_d(acc);
+    if (lane == 0) out[b * ld_out + r] = acc;
+  }
+}
+
+// u[r][c] = sum_b A[rb, c] g[b, r]
+template <typename T>
+__global__ void sc_colsum_f64_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict__ row_idx,
+                                     int64_t n_bins, int64_t V, int n_rot, const double* __restrict__ g, int64_t ld_g,
+                                     double* __restrict__ u) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < V * n_rot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / V);
+    const int64_t c = t % V;
+    double acc = 0.0;
+    for (int64_t b = 0; b < n_bins; ++b) acc += (double)load_elem(A + (row_idx ? row_idx[b] : b) * lda, c) * g[b * ld_g + r];
+    u[(int64_t)r * V + c] = acc;
+  }
+}
+
+// weight[j] += scale * sum_r u[r][rotinv[j, r] - 1]
+__global__ void sc_gather_f64_kernel(const double* __restrict__ u, int64_t V, int n_rot,
+                                     const int64_t* __restrict__ rotinv, int64_t ld_rot, double scale,
+                                     double* __restrict__ weight) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < V; j += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int r = 0; r < n_rot; ++r) {
+      int64_t src = j;
+      if (rotinv) {
+        src = rotinv[j * ld_rot + r] - 1;
+        if (src < 0 || src >= V) {
+          atomicAdd(&g_bad_index_count, 1u);
+          continue;
+        }
+      }
+      acc += u[(int64_t)r * V + src];
+    }
+    weight[j] += scale * acc;
+  }
+}
+
 }  // namespace jscc
 
 using namespace jscc;
@@ -924,6 +991,69 @@ int jscc_sc_backproject(const void* A, int32_t a_dtype, int64_t lda, const int64
                         void* stream) {
   return sc_stage_entry("jscc_sc_backproject", 2, A, a_dtype, lda, row_idx, n_bins, n_vox, n_rot, nullptr, nullptr,
                         rotmat_inv, ld_rot, nullptr, 0, g, ld_g, scale, weight, workspace, workspace_bytes, stream);
+}
+
+size_t jscc_sc_f64_workspace_bytes(int64_t n_vox, int32_t n_rot) {
+  return align_up((size_t)(n_vox > 0 ? n_vox : 1) * (size_t)(n_rot > 0 ? n_rot : 1) * sizeof(double), 256) + 256;
+}
+
+int jscc_sc_project_f64(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx, int64_t n_bins,
+                        int64_t n_vox, int32_t n_rot, const double* img, const int64_t* rotmat, int64_t ld_rot,
+                        double* out, int64_t ld_out, void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0 && n_rot >= 1, "jscc_sc_project_f64: bad sizes");
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16, "jscc_sc_project_f64: bad a_dtype");
+  JSCC_REQUIRE(rotmat != nullptr || n_rot == 1, "jscc_sc_project_f64: n_rot > 1 needs rotmat");
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(A && img && out && lda >= n_vox && ld_out >= n_rot, "jscc_sc_project_f64: bad argument");
+  cudaStream_t st = as_stream(stream);
+  int64_t blocks = (n_bins * n_rot + 7) / 8;  // 8 warps per block
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  if (a_dtype == JSCC_DTYPE_F32)
+    JSCC_TIMED("sc_project_f64", st,
+               (sc_project_f64_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
+                   static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, n_rot, img, rotmat, ld_rot, out, ld_out)));
+  else
+    JSCC_TIMED("sc_project_f64", st,
+               (sc_project_f64_kernel<__nv_bfloat16><<<(unsigned)blocks, 256, 0, st>>>(
+                   static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox, n_rot, img, rotmat, ld_rot, out,
+                   ld_out)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_sc_backproject_f64(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx, int64_t n_bins,
+                            int64_t n_vox, int32_t n_rot, const double* g, int64_t ld_g, const int64_t* rotmat_inv,
+                            int64_t ld_rot, double scale, double* weight, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+  JSCC_REQUIRE(n_bins >= 0 && n_vox >= 0 && n_rot >= 1, "jscc_sc_backproject_f64: bad sizes");
+  JSCC_REQUIRE(a_dtype == JSCC_DTYPE_F32 || a_dtype == JSCC_DTYPE_BF16, "jscc_sc_backproject_f64: bad a_dtype");
+  JSCC_REQUIRE(rotmat_inv != nullptr || n_rot == 1, "jscc_sc_backproject_f64: n_rot > 1 needs rotmat_inv");
+  if (n_bins == 0 || n_vox == 0) return JSCC_OK;
+  JSCC_REQUIRE(A && g && weight && lda >= n_vox && ld_g >= n_rot, "jscc_sc_backproject_f64: bad argument");
+  JSCC_REQUIRE(workspace && workspace_bytes >= jscc_sc_f64_workspace_bytes(n_vox, n_rot),
+               "jscc_sc_backproject_f64: workspace too small");
+  Carver cv(workspace, workspace_bytes);
+  double* u = cv.take<double>((size_t)n_vox * n_rot);
+  JSCC_REQUIRE(cv.ok(), "jscc_sc_backproject_f64: workspace carve overflow");
+  cudaStream_t st = as_stream(stream);
+  int64_t blocks = (n_vox * n_rot + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  if (a_dtype == JSCC_DTYPE_F32)
+    JSCC_TIMED("sc_colsum_f64", st,
+               (sc_colsum_f64_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(
+                   static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, n_rot, g, ld_g, u)));
+  else
+    JSCC_TIMED("sc_colsum_f64", st,
+               (sc_colsum_f64_kernel<__nv_bfloat16><<<(unsigned)blocks, 256, 0, st>>>(
+                   static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox, n_rot, g, ld_g, u)));
+  JSCC_LAUNCH_CHECK();
+  blocks = (n_vox + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  JSCC_TIMED("sc_gather_f64", st,
+             (sc_gather_f64_kernel<<<(unsigned)blocks, 256, 0, st>>>(u, n_vox, n_rot, rotmat_inv, ld_rot, scale,
+                                                                     weight)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
 }
 
 int jscc_take_bad_index_count(unsigned int* out) {

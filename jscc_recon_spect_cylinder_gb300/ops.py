@@ -165,7 +165,7 @@ def _rot_tables(rot, n_vox, n_rot, name):
 
 def sc_project(sysmat, img, rotmat=None, n_rot=None, row_idx=None):
     """Forward SC projection ``f[b, r] = A[b] . rot_r(img)`` -> ``[n_bins, n_rot]``
-    (jscc_sc_project)."""
+    (jscc_sc_project; a float64 image selects jscc_sc_project_f64 and a float64 result)."""
     dev = _lib.require_cuda(sysmat, img, rotmat, row_idx, what="sc_project")
     A = _rows_contig(sysmat)
     n_rows, n_vox = A.shape
@@ -173,6 +173,16 @@ def sc_project(sysmat, img, rotmat=None, n_rot=None, row_idx=None):
         row_idx = row_idx.to(torch.int64).contiguous()
     n_bins = n_rows if row_idx is None else row_idx.numel()
     rm, n_rot, ld_rot = _rot_tables(rotmat, n_vox, n_rot, "rotmat")
+    if img.dtype == torch.float64:
+        x = img.reshape(-1).contiguous()
+        if x.numel() != n_vox:
+            raise ValueError(f"img has {x.numel()} voxels, sysmat has {n_vox}")
+        out = torch.empty((n_bins, n_rot), dtype=torch.float64, device=dev)
+        rc = _lib.load().jscc_sc_project_f64(A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins,
+                                             n_vox, n_rot, x.data_ptr(), _lib.ptr(rm), ld_rot, out.data_ptr(),
+                                             out.stride(0), _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_sc_project_f64")
+        return out
     x = _f32_contig(img.reshape(-1))
     if x.numel() != n_vox:
         raise ValueError(f"img has {x.numel()} voxels, sysmat has {n_vox}")
@@ -187,7 +197,8 @@ def sc_project(sysmat, img, rotmat=None, n_rot=None, row_idx=None):
 
 
 def sc_backproject(sysmat, g, rotmat_inv=None, n_rot=None, row_idx=None, scale=1.0, out=None):
-    """Adjoint of sc_project: ``out += scale * sum_r rotinv_r(A^T g[:, r])`` (jscc_sc_backproject)."""
+    """Adjoint of sc_project: ``out += scale * sum_r rotinv_r(A^T g[:, r])`` (jscc_sc_backproject;
+    a float64 ``g`` selects jscc_sc_backproject_f64 and a float64 result)."""
     dev = _lib.require_cuda(sysmat, g, rotmat_inv, row_idx, out, what="sc_backproject")
     A = _rows_contig(sysmat)
     n_rows, n_vox = A.shape
@@ -195,6 +206,19 @@ def sc_backproject(sysmat, g, rotmat_inv=None, n_rot=None, row_idx=None, scale=1
         row_idx = row_idx.to(torch.int64).contiguous()
     n_bins = n_rows if row_idx is None else row_idx.numel()
     ri, n_rot, ld_rot = _rot_tables(rotmat_inv, n_vox, n_rot, "rotmat_inv")
+    if g.dtype == torch.float64:
+        gg = g.reshape(n_bins, -1).contiguous()
+        if gg.size(1) < n_rot:
+            raise ValueError(f"g has {gg.size(1)} columns, {n_rot} rotations requested")
+        if out is None:
+            out = torch.zeros((n_vox, 1), dtype=torch.float64, device=dev)
+        lib = _lib.load()
+        ws = _lib.workspace.get(dev, lib.jscc_sc_f64_workspace_bytes(n_vox, n_rot))
+        rc = lib.jscc_sc_backproject_f64(A.data_ptr(), _dtype_code(A), A.stride(0), _lib.ptr(row_idx), n_bins, n_vox,
+                                         n_rot, gg.data_ptr(), gg.stride(0), _lib.ptr(ri), ld_rot, float(scale),
+                                         out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_sc_backproject_f64")
+        return out
     gg = _f32_contig(g.reshape(n_bins, -1))
     if gg.size(1) < n_rot:
         raise ValueError(f"g has {gg.size(1)} columns, {n_rot} rotations requested")
@@ -212,10 +236,23 @@ def sc_backproject(sysmat, g, rotmat_inv=None, n_rot=None, row_idx=None, scale=1
 def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None, use_window=False, rotmat=None,
                     rot_col=0):
     """Forward list-mode projection ``f[i] = sum_j t_ij rot(img)_j`` with T recomputed
-    (jscc_compton_project) -> ``[E]``."""
+    (jscc_compton_project) -> ``[E]``; a float64 image selects jscc_compton_project_f64 (strict
+    model, no rotation) and a float64 result."""
     dev = _lib.require_cuda(records, row_id, coor, img, eff, rotmat, what="compton_project")
     c = _f32_contig(coor)
     V = c.size(0)
+    if img.dtype == torch.float64:
+        if rotmat is not None:
+            raise ValueError("compton_project: the float64 evaluation takes no rotation table")
+        x = img.reshape(-1).contiguous()
+        e, edt, ld = _eff_args(eff)
+        n = records.size(0)
+        f = torch.empty(n, dtype=torch.float64, device=dev)
+        rc = _lib.load().jscc_compton_project_f64(records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), V, int(model),
+                                                  _lib.ptr(e), edt, ld, x.data_ptr(), f.data_ptr(),
+                                                  _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_compton_project_f64")
+        return f
     x = _f32_contig(img.reshape(-1))
     rm = _index_table(rotmat, V, "rotmat")
     e, edt, ld = _eff_args(eff)
@@ -240,10 +277,26 @@ def compton_project(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None
 
 def compton_backproject(records, row_id, coor, g, model=_lib.CONE_STRICT, eff=None, use_window=False, rotmat_inv=None,
                         rot_col=0, scale=1.0, out=None):
-    """Adjoint of compton_project: ``out += scale * rotinv(T^T g)`` (jscc_compton_backproject)."""
+    """Adjoint of compton_project: ``out += scale * rotinv(T^T g)`` (jscc_compton_backproject; a
+    float64 ``g`` selects jscc_compton_backproject_f64 and a float64 result)."""
     dev = _lib.require_cuda(records, row_id, coor, g, eff, rotmat_inv, out, what="compton_backproject")
     c = _f32_contig(coor)
     V = c.size(0)
+    if g.dtype == torch.float64:
+        if rotmat_inv is not None:
+            raise ValueError("compton_backproject: the float64 evaluation takes no rotation table")
+        e, edt, ld = _eff_args(eff)
+        n = records.size(0)
+        gg = g.reshape(-1).contiguous()
+        if gg.numel() != n:
+            raise ValueError(f"g has {gg.numel()} entries for {n} events")
+        if out is None:
+            out = torch.zeros((V, 1), dtype=torch.float64, device=dev)
+        rc = _lib.load().jscc_compton_backproject_f64(records.data_ptr(), row_id.data_ptr(), n, c.data_ptr(), V,
+                                                      int(model), _lib.ptr(e), edt, ld, gg.data_ptr(), float(scale),
+                                                      out.data_ptr(), _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_compton_backproject_f64")
+        return out
     ri = _index_table(rotmat_inv, V, "rotmat_inv")
     e, edt, ld = _eff_args(eff)
     n = records.size(0)
@@ -299,7 +352,9 @@ def rdp_prior(img, nbr, weight, gamma=2.0, beta=1.0, eps=1e-9, want_value=True, 
     ``(value, grad)``: value a float64 0-d device tensor (or None), grad [V, 1] float32
     (``grad_out`` += when ``accumulate``) or None."""
     dev = _lib.require_cuda(img, nbr, weight, grad_out, what="rdp_prior")
-    x = _f32_contig(img.reshape(-1))
+    f64 = img.dtype == torch.float64
+    x = img.reshape(-1).contiguous() if f64 else _f32_contig(img.reshape(-1))
+    rdt = torch.float64 if f64 else torch.float32
     V = x.numel()
     if nbr.dim() != 2 or nbr.size(1) != V or weight.shape != nbr.shape:
         raise ValueError(f"neighbour table {tuple(nbr.shape)} / {tuple(weight.shape)} does not match {V} voxels")
@@ -308,11 +363,11 @@ def rdp_prior(img, nbr, weight, gamma=2.0, beta=1.0, eps=1e-9, want_value=True, 
     value = torch.zeros((), dtype=torch.float64, device=dev) if want_value else None
     grad = None
     if want_grad:
-        grad = grad_out if grad_out is not None else torch.empty((V, 1), dtype=torch.float32, device=dev)
-        if grad.numel() != V or grad.dtype != torch.float32 or not grad.is_contiguous():
-            raise ValueError("grad_out must be a contiguous float32 tensor of V elements")
+        grad = grad_out if grad_out is not None else torch.empty((V, 1), dtype=rdt, device=dev)
+        if grad.numel() != V or grad.dtype != rdt or not grad.is_contiguous():
+            raise ValueError(f"grad_out must be a contiguous {rdt} tensor of V elements")
     lib = _lib.load()
-    rc = lib.jscc_rdp_prior(x.data_ptr(), nb.data_ptr(), wt.data_ptr(), V, nb.size(0), float(gamma), float(eps),
+    rc = (lib.jscc_rdp_prior_f64 if f64 else lib.jscc_rdp_prior)(x.data_ptr(), nb.data_ptr(), wt.data_ptr(), V, nb.size(0), float(gamma), float(eps),
                             float(beta), _lib.ptr(value), _lib.ptr(grad), 1 if (accumulate and grad_out is not None)
                             else 0, _lib.stream_handle(dev))
     _lib.check(rc, "jscc_rdp_prior")
