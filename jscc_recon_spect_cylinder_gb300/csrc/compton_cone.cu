@@ -411,7 +411,7 @@ __global__ void cone_ratio_kernel(const float* __restrict__ f, int64_t n, float*
 
 // ------------------------------------------------------------------ fused back projection
 // part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i
-constexpr int kBackStage = 64;
+constexpr int kBackStage = 128;
 
 template <int MODEL, bool WINDOW, typename TE>
 __global__ void __launch_bounds__(kConeThreads)
@@ -504,7 +504,8 @@ __device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, 
   // 1 / d01: one Newton-Raphson step, r (3 - d2 r^2) / 2
   const float2 h = __fmul2_rn(__fmul2_rn(d2, f2(-0.5f)), r0);
   const float2 i01 = __fmul2_rn(r0, __ffma2_rn(h, r0, f2(1.5f)));
-  const float2 bcos = __fmul2_rn(__ffma2_rn(ax, e.wx, __ffma2_rn(ay, e.wy, __fmul2_rn(az, e.wz))), i01);
+  const float2 dotw = __ffma2_rn(ax, e.wx, __ffma2_rn(ay, e.wy, __fmul2_rn(az, e.wz)));
+  const float2 bcos = __fmul2_rn(dotw, i01);
   bool in0 = true, in1 = true;
   if (WINDOW) {
     in0 = !(bcos.x < e.cos_lo.x || bcos.x > e.cos_hi.x);
@@ -516,15 +517,18 @@ __device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, 
   const float2 delta = __fadd2_rn(make_float2(acosf(c.x), acosf(c.y)), e.ntheta);
   const float2 sig_e = make_float2(delta.x >= 0.f ? e.sig_plus.x : e.sig_minus.x,
                                    delta.y >= 0.f ? e.sig_plus.y : e.sig_minus.y);
-  const float2 nb = __fmul2_rn(bcos, f2(-1.0f));
-  const float2 jx = __ffma2_rn(nb, e.wx, __fmul2_rn(ax, i01));
-  const float2 jy = __ffma2_rn(nb, e.wy, __fmul2_rn(ay, i01));
-  const float2 jz = __ffma2_rn(nb, e.wz, __fmul2_rn(az, i01));
-  float2 sb2 = __ffma2_rn(nb, bcos, f2(1.0f));
+  // grad beta per axis: (u01 - cos(beta) w) / d12 = (a - (a . w) w) / (d01 d12); the 1 / d12^2 is
+  // in q, the 1 / d01^2 is applied once to the sum
+  const float2 ndw = __fmul2_rn(dotw, f2(-1.0f));
+  const float2 jx = __ffma2_rn(ndw, e.wx, ax);
+  const float2 jy = __ffma2_rn(ndw, e.wy, ay);
+  const float2 jz = __ffma2_rn(ndw, e.wz, az);
+  float2 sb2 = __ffma2_rn(__fmul2_rn(bcos, f2(-1.0f)), bcos, f2(1.0f));
   sb2.x = fmaxf(sb2.x, 1e-12f);
   sb2.y = fmaxf(sb2.y, 1e-12f);
-  const float2 num = __ffma2_rn(__fmul2_rn(jx, jx), e.q0,
-                                __ffma2_rn(__fmul2_rn(jy, jy), e.q1, __fmul2_rn(__fmul2_rn(jz, jz), e.q2)));
+  const float2 num = __fmul2_rn(__ffma2_rn(__fmul2_rn(jx, jx), e.q0,
+                                           __ffma2_rn(__fmul2_rn(jy, jy), e.q1, __fmul2_rn(__fmul2_rn(jz, jz), e.q2))),
+                                __fmul2_rn(i01, i01));
   // sb2 * sigma^2 = max(sigma_E^2 sb2 + max(num, 1e-12 sb2), 1e-12 sb2)
   // (the outer max is implied: sigma_E^2 sb2 >= 0 and the addend is >= 1e-12 sb2, and a
   // rounded sum of the two cannot fall below the addend)
@@ -609,7 +613,7 @@ cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __res
 
 // part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i for the strict model, events in pairs.
 template <bool WINDOW, typename TE>
-__global__ void __launch_bounds__(kConeThreads)
+__global__ void __launch_bounds__(kConeThreads, 8)
 cone_back_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
                       int64_t ev_per_chunk, const float* __restrict__ q, const float* __restrict__ coor, int64_t V,
                       const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp) {
