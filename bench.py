@@ -503,6 +503,8 @@ class Batch4Bench:
     ratios as BF16 hi / lo pairs, FP32 accumulation in tensor memory), replayed as one captured
     CUDA graph. Metric: subset-iterations/s summed over the instances."""
 
+    CAPTURE = True
+
     def __init__(self, dev, n_inst=64, views=20, subsets=8, seed=None):
         from jscc_recon_spect_cylinder_gb300 import batched, synthetic
         from jscc_recon_spect_cylinder_gb300.recon_osem_plane import split_tensor_even
@@ -530,11 +532,12 @@ class Batch4Bench:
         self.s = A.sum(0)
         self.A32 = A
         self.n_inst, self.subsets, self.dev = n_inst, subsets, dev
-        self.bat = batched.BatchedScOsem(A, self.ids, self.s, n_inst, device=dev)
+        self.bat = self._make_batch(A, grid, X_true, counts, gen, gc)
         self.bat.set_projections(self.Y)
         self.bat.set_images(torch.ones((n_inst, self.V)))
         self.splits = self.bat.autotune()
-        self.bat.capture()
+        if self.CAPTURE:
+            self.bat.capture()
         self.bat.set_images(torch.ones((n_inst, self.V)))
         self.name = "batched-config4" if (views, subsets) == (20, 8) else f"batched-{views}views-{subsets}subsets"
         self.metric = ("OSEM subset-iters/s summed over 64 instances: batched BF16 tensor-core GEMM path, "
@@ -543,6 +546,11 @@ class Batch4Bench:
         self.dtypes = ("bf16",)
         self.traffic_file = "traffic_batch4.json"
         torch.cuda.synchronize(dev)
+
+    def _make_batch(self, A, grid, X_true, counts, gen, gc):
+        from jscc_recon_spect_cylinder_gb300 import batched
+
+        return batched.BatchedScOsem(A, self.ids, self.s, self.n_inst, device=self.dev)
 
     def step(self, img, dtype):
         self.bat.iterate(1)
@@ -669,6 +677,91 @@ class Batch4Bench:
                 "h2d_bytes_per_step": (y_h.numel() + x_h.numel()) * 4 // iters,
                 "d2h_bytes_per_step": out_h.numel() * 4 // iters,
                 "step": f"one job: stage projections + images, {iters} iterations, read images", "seconds": sec}
+
+
+class Batch4JointBench(Batch4Bench):
+    """Config 4, joint form: the 64 instances of Batch4Bench each with a Compton channel of
+    their own at 511 keV (events log-uniform in 50k-2M listed per instance, forward-simulated
+    from the instance's phantom on the view-0 scatter cylinder and a 150 mm absorber, energies
+    blurred as in config 2), alpha = 0.5, 8 subsets. One step = one joint OSEM iteration of
+    every instance: SC weights from the batched tensor-core GEMMs, each instance's Compton
+    weight from the fused cone kernels over its subset events, the safe joint EM update with
+    per-instance sensitivities (the Compton sensitivity rescaled as build_sparse_sensi_d does).
+    Launched kernel by kernel (the per-instance cone launches are not captured)."""
+
+    CAPTURE = False
+
+    def __init__(self, dev, n_inst=64, views=20, subsets=8, seed=None, ev_range=(5e4, 2e6)):
+        self.ev_range = ev_range
+        super().__init__(dev, n_inst=n_inst, views=views, subsets=subsets, seed=seed)
+        self.name = "batched-joint-config4"
+        self.metric = ("joint OSEM subset-iters/s summed over 64 instances: batched SC tensor-core GEMMs + "
+                       "per-instance fused Compton cone, config 4, 1xGB300")
+
+    def _make_batch(self, A, grid, X_true, counts, gen, gc):
+        from jscc_recon_spect_cylinder_gb300 import batched, ops, synthetic
+        from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+
+        e0 = 0.511
+        scat = synthetic.cylinder_pixels(120.0, 128, 32, 2.0, 0.0, self.dev)
+        absb = synthetic.cylinder_pixels(150.0, 128, 32, 2.0, 0.0, self.dev)
+        det = torch.cat((scat, absb), dim=0).to(torch.float32)
+        res = 0.08 * (0.662 / e0) ** 0.5
+        thr_max = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
+        lo, hi = math.log10(self.ev_range[0]), math.log10(self.ev_range[1])
+        n_ev = (10 ** (lo + (hi - lo) * torch.rand(self.n_inst, generator=gc, dtype=torch.float64))).long()
+        coor = grid.coor.to(torch.float32)
+        events, S = [], []
+        self.n_listed = int(n_ev.sum())
+        for n in range(self.n_inst):
+            lst = synthetic.compton_list(grid.coor, X_true[n].reshape(-1, 1), scat, 150.0, 128, 32, 2.0, e0,
+                                         int(n_ev[n] * 2.3) + 64, gen, cp1_offset=0, cp2_offset=scat.size(0))
+            lst = lst[:int(n_ev[n])]
+            noise = torch.randn((lst.size(0), 2), generator=gen, device=self.dev)
+            for k, col in ((0, 1), (1, 3)):
+                e = lst[:, col]
+                lst[:, col] = e + (e * res / 2.355 * (e0 / e) ** 0.5) * noise[:, k]
+            ev = pls.get_compton_event_params(A[:scat.size(0)], det, coor, lst, 1.0, 1.0, e0, res, thr_max, 0.05,
+                                              e0 - 0.06, window_sigmas=0.0)
+            d = ops.compton_backproject(ev.records, ev.row_id, coor, torch.ones(len(ev), device=self.dev),
+                                        model=ev.model, eff=A).reshape(-1)
+            d = d * self.s.sum() / d.sum() * (len(ev) / max(float(self.Y[n].sum()), 1.0)) if d.sum() > 0 else self.s
+            S.append(0.5 * self.s + 1.5 * d)
+            events.append(ev.split(self.subsets))
+            del lst, noise
+        self.n_kept = sum(sum(len(b) for b in ev_n) for ev_n in events)
+        return batched.BatchedJointOsem(A, self.ids, torch.stack(S), events, coor, alpha=0.5, device=self.dev)
+
+    def step(self, img, dtype):
+        self.bat.iterate(1)
+        return img
+
+    def step_eager(self, img, dtype):
+        return self.step(img, dtype)
+
+    def config(self):
+        c = super().config()
+        c.update({"workload": self.name, "compton_events_listed": self.n_listed, "compton_events_kept": self.n_kept,
+                  "compton_events_per_instance": "log-uniform 5e4-2e6 listed", "alpha": 0.5, "graph": False})
+        return c
+
+    def kernel_bytes(self, dtype):
+        return {}  # the step is the cone passes' (FP32): the roofline below, not an HBM one
+
+    def extra(self, ms_per_step):
+        """Cone pairs per second over the whole step (the cone kernels take ~99.8 % of it) and
+        the FP32 roofline at Cone2Bench's 100 operations per pair."""
+        pairs = 2 * self.n_kept * self.V  # forward + back cone pairs per iteration
+        rate = pairs / (ms_per_step / 1e3)
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        achieved = rate * Cone2Bench.K_CONE / 1e12
+        return {"compton_pairs_per_s": rate,
+                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                                  "flop_per_pair": Cone2Bench.K_CONE, "over": "the whole step"}}
+
+    def e2e(self, iters):
+        return None
 
 
 class SparseLaunchBench:
@@ -868,6 +961,8 @@ def make_workload(name, dev):
         return Map5Bench(dev)
     if name == "batch4":
         return Batch4Bench(dev)
+    if name == "batch4-joint":
+        return Batch4JointBench(dev)
     if name == "batch4-small":  # profiling case: 4 views (16,384 x 36,000), one subset, 64 instances; > L2
         return Batch4Bench(dev, views=4, subsets=1)
     if name == "sc3":
@@ -1052,7 +1147,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2", "map5", "batch4",
-                             "batch4-small"],
+                             "batch4-small", "batch4-joint"],
                     default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

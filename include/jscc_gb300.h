@@ -478,15 +478,16 @@ JSCC_API int jscc_bf16_gemm_nt(const void* P, int64_t ldp, const void* R, int64_
  * Helpers of the batched OSEM step (instances n < n_inst, padded to np rows):
  *   jscc_batch_split:  xs[n][v] = bf16(x[n][v]), xs[np + n][v] = bf16(x[n][v] - xs[n][v])
  *                      (BF16 hi / lo pairs of FP32 images; rows n_inst..np-1 zero)
- *   jscc_batch_ratio:  f = F[b][n] + F[b][np + n]; q = y[n][b0 + b] / f; qs = hi / lo of q as
- *                      above, [2 np x nb]; f_out[n][b] = f when non-NULL
+ *   jscc_batch_ratio:  f = F[b][n] + F[b][np + n] (clamped below at floor_v when use_floor);
+ *                      q = y[n][b0 + b] / f; qs = hi / lo of q as above, [2 np x nb];
+ *                      f_out[n][b] = f when non-NULL
  *   jscc_batch_weight: w_out[n][v] (+)= scale * (W[v][n] + W[v][np + n])
  */
 JSCC_API int jscc_batch_split(const float* x, int64_t ldx, int32_t n_inst, int32_t np, int64_t V, void* xs,
                    int64_t ldxs, void* stream);
 JSCC_API int jscc_batch_ratio(const float* F, int64_t ldf, const float* y, int64_t ldy, int64_t b0, int64_t nb,
                    int32_t n_inst, int32_t np, void* qs, int64_t ldqs, float* f_out, int64_t ldfo,
-                   void* stream);
+                   int32_t use_floor, float floor_v, void* stream);
 JSCC_API int jscc_batch_weight(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np, float scale,
                    float* w_out, int64_t ldwo, int32_t accumulate, void* stream);
 
@@ -498,6 +499,19 @@ JSCC_API int jscc_batch_weight(const float* W, int64_t ldw, int64_t V, int32_t n
  */
 JSCC_API int jscc_batch_em(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np, float* x,
                    int64_t ldx, const float* s_map, void* xs, int64_t ldxs, void* stream);
+
+/*
+ * Joint batched EM update (the joint loops' update per instance, recon_osem_plane.py:118 and
+ * safe_em_update of recon_osem_plane_sparse.py:60-66):
+ *   w = coef_a * (W[v][n] + W[v][np + n]) + coef_b * w_b[n][v]      (w_b may be NULL)
+ *   JSCC_EM_PLAIN: x = x * w / s;  JSCC_EM_SAFE: nan/inf -> 0 in w and s, s > eps ? x max(w, 0) / s : 0
+ * with s = s_map[n * lds + v] (lds = 0: one sensitivity for every instance), in place, and the
+ * next hi / lo pair into xs when non-NULL.
+ */
+JSCC_API int jscc_batch_em_joint(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np,
+                   float coef_a, const float* w_b, int64_t ldwb, float coef_b, float* x, int64_t ldx,
+                   const float* s_map, int64_t lds, int32_t mode, float eps, void* xs, int64_t ldxs,
+                   void* stream);
 
 /* Tensor-core GEMM waits that gave up since the last call (synchronous device read). */
 JSCC_API int jscc_take_gemm_timeout_count(unsigned int* out);

@@ -102,7 +102,12 @@ _SIGNATURES: dict[str, tuple] = {
     "jscc_batch_ratio": (
         c_int,
         [c_void_p, c_int64, c_void_p, c_int64, c_int64, c_int64, c_int32, c_int32, c_void_p, c_int64, c_void_p,
-         c_int64, c_void_p],
+         c_int64, c_int32, c_float, c_void_p],
+    ),
+    "jscc_batch_em_joint": (
+        c_int,
+        [c_void_p, c_int64, c_int64, c_int32, c_int32, c_float, c_void_p, c_int64, c_float, c_void_p, c_int64,
+         c_void_p, c_int64, c_int32, c_float, c_void_p, c_int64, c_void_p],
     ),
     "jscc_batch_weight": (
         c_int, [c_void_p, c_int64, c_int64, c_int32, c_int32, c_float, c_void_p, c_int64, c_int32, c_void_p]),

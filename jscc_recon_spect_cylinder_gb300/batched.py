@@ -16,6 +16,10 @@ GEMMs stay K-major): 2 x bins x V x 2 bytes. Instance vectors enter as hi / lo B
 (~16 significant bits), so the error is that of the BF16 matrix, as in the single-instance
 BF16 path. The K split of each GEMM shape is chosen by timing (``autotune``) and a whole
 iteration over the subsets can be captured into a CUDA graph (``capture``).
+
+BatchedJointOsem adds the Compton channel of the joint loops: each instance's own event list,
+weighted through the fused cone kernels, combined with the batched SC weights in one safe EM
+update per subset.
 """
 from __future__ import annotations
 
@@ -82,6 +86,7 @@ class BatchedScOsem:
         self.splits = {}
         self.graph = None
         self.graph_launches = 0
+        self.floor = None  # clamp_min of the forward projection (joint local loops: 1e-12)
 
     # ------------------------------------------------------------------ data
     def set_projections(self, proj):
@@ -108,7 +113,9 @@ class BatchedScOsem:
         F = self.F[:nbp]
         self._gemm(self.A[b0:b0 + nbp], self.Xs, F, ("f", nbp))
         _lib.check(lib.jscc_batch_ratio(F.data_ptr(), F.stride(0), self.Y.data_ptr(), self.Y.stride(0), b0, nb, self.n,
-                                        self.np, self.Qs[k].data_ptr(), self.Qs[k].stride(0), None, 0, st),
+                                        self.np, self.Qs[k].data_ptr(), self.Qs[k].stride(0), None, 0,
+                                        1 if self.floor is not None else 0,
+                                        float(self.floor) if self.floor is not None else 0.0, st),
                    "jscc_batch_ratio")
         self._gemm(self.AT[:, b0:b0 + nbp], self.Qs[k], self.W, ("b", nbp))
         _lib.check(lib.jscc_batch_em(self.W.data_ptr(), self.W.stride(0), self.V, self.n, self.np, self.X.data_ptr(),
@@ -197,3 +204,60 @@ def osem_bin_mode_batched(sysmat, proj, img, s_map, subsets, iterations, graph=T
     if graph:
         b.capture()
     return b.iterate(iterations).clone()
+
+
+class BatchedJointOsem(BatchedScOsem):
+    """Batched joint JSCCSD OSEM: per instance, every subset update is
+    ``w = alpha w_SC + (2 - alpha) w_C`` and ``x <- safe_em_update(x, w, s_joint)`` with the SC
+    forward projection floored at 1e-12 (osem_joint_mode_local_sparse,
+    recon_osem_local_sparse_jsccsd_only.py:58-100). The SC weights of all instances come from
+    the tensor-core GEMMs; each instance's Compton weight ``T^T (1 / T x)`` over its own events
+    of the subset comes from the fused cone kernels (T recomputed, nothing stored per event but
+    its 64-byte record), with the batch's BF16 matrix as the efficiency rows.
+
+    events:  per instance, per subset, a ComptonEvents block (row ids in the reference's bin order)
+    coor:    [V, 3] voxel centres on the device
+    s_joint: [n_inst, V] per-instance joint sensitivities
+    """
+
+    def __init__(self, sysmat, subsets, s_joint, events, coor, alpha=0.5, device="cuda"):
+        n_inst = len(events)
+        s_joint = s_joint.reshape(n_inst, -1)
+        super().__init__(sysmat, subsets, s_joint[0], n_inst, device=device)
+        if any(len(ev_n) != len(self.blocks) for ev_n in events):
+            raise ValueError("events must hold one block per subset for every instance")
+        self.floor = 1e-12
+        self.alpha = float(alpha)
+        self.S = s_joint.to(self.dev, torch.float32).contiguous()
+        self.coor = coor.to(self.dev, torch.float32).contiguous()
+        inv = torch.full((self.B,), -1, dtype=torch.int64, device=self.dev)
+        real = self.perm >= 0
+        inv[self.perm[real]] = torch.arange(self.B_pad, device=self.dev)[real]
+        self.events = []  # (records, row ids into the permuted matrix, model) per instance and subset
+        for ev_n in events:
+            per = []
+            for ev in ev_n:
+                rid = inv[ev.row_id.to(self.dev, torch.int64)].to(torch.int32).contiguous() if len(ev) else ev.row_id
+                per.append((ev.records, rid, ev.model))
+            self.events.append(per)
+        self.WC = torch.zeros((n_inst, self.V), dtype=torch.float32, device=self.dev)
+
+    def _subset(self, k):
+        b0, nb, nbp = self.blocks[k]
+        lib = _lib.load()
+        st = _lib.stream_handle(self.dev)
+        F = self.F[:nbp]
+        self._gemm(self.A[b0:b0 + nbp], self.Xs, F, ("f", nbp))
+        _lib.check(lib.jscc_batch_ratio(F.data_ptr(), F.stride(0), self.Y.data_ptr(), self.Y.stride(0), b0, nb, self.n,
+                                        self.np, self.Qs[k].data_ptr(), self.Qs[k].stride(0), None, 0, 1, self.floor,
+                                        st), "jscc_batch_ratio")
+        self._gemm(self.AT[:, b0:b0 + nbp], self.Qs[k], self.W, ("b", nbp))
+        self.WC.zero_()
+        for n in range(self.n):
+            rec, rid, model = self.events[n][k]
+            if rec.size(0):
+                ops.compton_weight(rec, rid, self.coor, self.X[n], model=model, eff=self.A, out=self.WC[n])
+        _lib.check(lib.jscc_batch_em_joint(self.W.data_ptr(), self.W.stride(0), self.V, self.n, self.np, self.alpha,
+                                           self.WC.data_ptr(), self.WC.stride(0), 2.0 - self.alpha, self.X.data_ptr(),
+                                           self.X.stride(0), self.S.data_ptr(), self.S.stride(0), _lib.EM_SAFE, 1e-12,
+                                           self.Xs.data_ptr(), self.Xs.stride(0), st), "jscc_batch_em_joint")

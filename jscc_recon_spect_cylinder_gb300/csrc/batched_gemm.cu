@@ -258,14 +258,15 @@ __global__ void batch_split_kernel(const float* __restrict__ x, int64_t ldx, int
 // q = y[n][b0 + b] / f; qs[n][b] = hi(q), qs[np + n][b] = lo(q). Optionally f_out[n][b] = f.
 __global__ void batch_ratio_kernel(const float* __restrict__ F, int64_t ldf, const float* __restrict__ y, int64_t ldy,
                                    int64_t b0, int64_t nb, int n_inst, int np, __nv_bfloat16* __restrict__ qs,
-                                   int64_t ldqs, float* __restrict__ f_out, int64_t ldfo) {
+                                   int64_t ldqs, float* __restrict__ f_out, int64_t ldfo, int use_floor, float floor_v) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)np * nb;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int n = (int)(t / nb);
     const int64_t b = t % nb;
     __nv_bfloat16 hi = __float2bfloat16_rn(0.f), lo = hi;
     if (n < n_inst) {
-      const float f = F[b * ldf + n] + F[b * ldf + np + n];
+      float f = F[b * ldf + n] + F[b * ldf + np + n];
+      if (use_floor) f = fmaxf(f, floor_v);  // clamp_min of recon_osem_local_cntstat.py:7
       if (f_out) f_out[(int64_t)n * ldfo + b] = f;
       split_bf16(__fdiv_rn(y[(int64_t)n * ldy + b0 + b], f), hi, lo);
     }
@@ -300,6 +301,40 @@ __global__ void batch_em_kernel(const float* __restrict__ W, int64_t ldw, int64_
     const float w = __fadd_rn(W[v * ldw + n], W[v * ldw + np + n]);
     float* px = x + (int64_t)n * ldx + v;
     const float xn = __fdiv_rn(__fmul_rn(*px, w), s[v]);
+    *px = xn;
+    if (xs) {
+      __nv_bfloat16 hi, lo;
+      split_bf16(xn, hi, lo);
+      xs[(int64_t)n * ldxs + v] = hi;
+      xs[(int64_t)(np + n) * ldxs + v] = lo;
+    }
+  }
+}
+
+// Joint batched EM update: w = a * (W[v][n] + W[v][np + n]) + b * wb[n][v] (wb may be NULL);
+// plain: x * w / s; safe (recon_osem_plane_sparse.py:60-66): nan/inf -> 0 in w and s, then
+// s > eps ? x * max(w, 0) / s : 0. s is per instance (lds > 0) or shared (lds = 0). Every
+// operation is rounded separately, as jscc_em_update does; the next hi / lo pair into xs.
+__global__ void batch_em_joint_kernel(const float* __restrict__ W, int64_t ldw, int64_t V, int n_inst, int np,
+                                      float a, const float* __restrict__ wb, int64_t ldwb, float b,
+                                      float* __restrict__ x, int64_t ldx, const float* __restrict__ s, int64_t lds,
+                                      int safe, float eps, __nv_bfloat16* __restrict__ xs, int64_t ldxs) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)n_inst * V;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int n = (int)(t / V);
+    const int64_t v = t % V;
+    float w = __fmul_rn(a, __fadd_rn(W[v * ldw + n], W[v * ldw + np + n]));
+    if (wb) w = __fadd_rn(w, __fmul_rn(b, wb[(int64_t)n * ldwb + v]));
+    float sv = s[(int64_t)n * lds + v];
+    float* px = x + (int64_t)n * ldx + v;
+    float xn;
+    if (!safe) {
+      xn = __fdiv_rn(__fmul_rn(*px, w), sv);
+    } else {
+      w = isfinite(w) ? w : 0.f;
+      sv = isfinite(sv) ? sv : 0.f;
+      xn = sv > eps ? __fdiv_rn(__fmul_rn(*px, fmaxf(w, 0.f)), sv) : 0.f;
+    }
     *px = xn;
     if (xs) {
       __nv_bfloat16 hi, lo;
@@ -442,14 +477,16 @@ int jscc_batch_split(const float* x, int64_t ldx, int32_t n_inst, int32_t np, in
 }
 
 int jscc_batch_ratio(const float* F, int64_t ldf, const float* y, int64_t ldy, int64_t b0, int64_t nb, int32_t n_inst,
-                     int32_t np, void* qs, int64_t ldqs, float* f_out, int64_t ldfo, void* stream) {
+                     int32_t np, void* qs, int64_t ldqs, float* f_out, int64_t ldfo, int32_t use_floor, float floor_v,
+                     void* stream) {
   JSCC_REQUIRE(n_inst >= 0 && np >= n_inst && nb >= 0 && b0 >= 0, "jscc_batch_ratio: bad sizes");
   if (np == 0 || nb == 0) return JSCC_OK;
   JSCC_REQUIRE(F && y && qs, "jscc_batch_ratio: null pointer argument");
   cudaStream_t st = as_stream(stream);
   JSCC_TIMED("batch_ratio", st,
              (batch_ratio_kernel<<<(unsigned)grid_blocks((int64_t)np * nb), 256, 0, st>>>(
-                 F, ldf, y, ldy, b0, nb, n_inst, np, static_cast<__nv_bfloat16*>(qs), ldqs, f_out, ldfo)));
+                 F, ldf, y, ldy, b0, nb, n_inst, np, static_cast<__nv_bfloat16*>(qs), ldqs, f_out, ldfo, use_floor,
+                 floor_v)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
 }
@@ -476,6 +513,22 @@ int jscc_batch_em(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_
   JSCC_TIMED("batch_em", st,
              (batch_em_kernel<<<(unsigned)grid_blocks((int64_t)n_inst * V), 256, 0, st>>>(
                  W, ldw, V, n_inst, np, x, ldx, s_map, static_cast<__nv_bfloat16*>(xs), ldxs)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
+}
+
+int jscc_batch_em_joint(const float* W, int64_t ldw, int64_t V, int32_t n_inst, int32_t np, float coef_a,
+                        const float* w_b, int64_t ldwb, float coef_b, float* x, int64_t ldx, const float* s_map,
+                        int64_t lds, int32_t mode, float eps, void* xs, int64_t ldxs, void* stream) {
+  JSCC_REQUIRE(n_inst >= 0 && np >= n_inst && V >= 0 && lds >= 0, "jscc_batch_em_joint: bad sizes");
+  JSCC_REQUIRE(mode == JSCC_EM_PLAIN || mode == JSCC_EM_SAFE, "jscc_batch_em_joint: bad mode %d", mode);
+  if (n_inst == 0 || V == 0) return JSCC_OK;
+  JSCC_REQUIRE(W && x && s_map, "jscc_batch_em_joint: null pointer argument");
+  cudaStream_t st = as_stream(stream);
+  JSCC_TIMED("batch_em", st,
+             (batch_em_joint_kernel<<<(unsigned)grid_blocks((int64_t)n_inst * V), 256, 0, st>>>(
+                 W, ldw, V, n_inst, np, coef_a, w_b, ldwb, coef_b, x, ldx, s_map, lds, mode == JSCC_EM_SAFE ? 1 : 0,
+                 eps, static_cast<__nv_bfloat16*>(xs), ldxs)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
 }

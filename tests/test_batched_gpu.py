@@ -84,3 +84,59 @@ def test_batched_osem_matches_fp64(cuda, graph):
     ref = _fp64_osem(A.double(), y.double(), x0, s, subsets, 3)
     for n in range(5):
         assert rel_l2(X[n], ref[n]) < 1e-4, n
+
+
+def test_batched_joint_matches_single_instance_loops(cuda):
+    """BatchedJointOsem (SC weights from the tensor-core GEMMs, each instance's Compton weight
+    from the fused cone kernels over its own events, safe EM with per-instance joint
+    sensitivities) against the single-instance joint loop of each instance (jscc_sc_weight with
+    the 1e-12 floor + jscc_compton_weight + safe EM) on the same BF16 matrix: 1e-4."""
+    import numpy as np
+
+    from jscc_recon_spect_cylinder_gb300 import batched, ops, synthetic
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300.recon_osem_plane import split_tensor_even
+
+    prob = synthetic.sc_problem(n_r=8, n_theta=24, n_phi=64, views=4, flat=True, total_counts=1e5)
+    A16 = prob.sysmat.to(torch.bfloat16).to(cuda)
+    B, V = A16.shape
+    coor = prob.grid.coor.to(cuda)
+    scat = synthetic.cylinder_pixels(120.0, 32, 4, 3.0)
+    absb = synthetic.cylinder_pixels(150.0, 32, 4, 3.0)
+    det = torch.cat((scat, absb)).float().to(cuda)  # 256 detectors: scatter rows index A's 256 rows
+    e0, S, alpha, n_inst = 0.511, 2, 0.5, 3
+    args = (0.8, 0.8, e0, 0.1 * (0.662 / e0) ** 0.5, 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001, 0.05, e0 - 0.06)
+    g = torch.Generator().manual_seed(31)
+    subsets = split_tensor_even(torch.randperm(B, generator=g), S)
+    mean = A16.float().cpu() @ prob.phantom.reshape(-1)
+    Y = torch.stack([torch.poisson(mean * (c / mean.sum()), generator=g) for c in (3e4, 1e5, 3e5)])
+    s_sc = A16.double().sum(0).float()
+    events, S_joint = [], []
+    for n in range(n_inst):
+        rng = np.random.default_rng(100 + n)
+        m = 400 * (n + 1)
+        L = np.stack((rng.integers(1, 129, m), rng.uniform(0.08, 0.3, m), rng.integers(129, 257, m),
+                      np.zeros(m)), axis=1).astype(np.float32)
+        L[:, 3] = e0 - L[:, 1]
+        ev = pls.get_compton_event_params(A16.float(), det, coor, torch.from_numpy(L).to(cuda), *args,
+                                          window_sigmas=0.0)
+        d = ops.compton_backproject(ev.records, ev.row_id, coor, torch.ones(len(ev), device=cuda), model=ev.model,
+                                    eff=A16).reshape(-1)
+        S_joint.append(alpha * s_sc.to(cuda) + (2 - alpha) * d)
+        events.append(ev.split(S))
+    S_joint = torch.stack(S_joint)
+    bj = batched.BatchedJointOsem(A16, subsets, S_joint, events, coor, alpha=alpha, device=cuda)
+    bj.set_projections(Y)
+    bj.set_images(torch.ones((n_inst, V)))
+    X = bj.iterate(2).cpu()
+    for n in range(n_inst):
+        x = torch.ones((V, 1), device=cuda)
+        y = Y[n].reshape(-1, 1).to(cuda)
+        for _ in range(2):
+            for k in range(S):
+                w = torch.zeros((V, 1), device=cuda)
+                ops.sc_weight(A16, y, x, floor=1e-12, scale=alpha, out=w, row_idx=subsets[k].to(cuda))
+                ev = events[n][k]
+                ops.compton_weight(ev.records, ev.row_id, coor, x, model=ev.model, eff=A16, scale=2 - alpha, out=w)
+                x = ops.em_update(x, w, S_joint[n].reshape(-1, 1), safe=True)
+        assert rel_l2(X[n], x.cpu().reshape(-1)) < 1e-4, n
