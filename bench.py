@@ -12,7 +12,10 @@ to the fine grid on the fly, alpha = 0.5, 8 subsets. One step = one OSEM iterati
 (8 subset updates). Metric: subset-iterations/s (higher is better); headline with the
 system matrix and the sparse rows stored in BF16 (FP32 accumulation), the plain FP32
 storage run beside it, plus Compton event-voxel pairs/s. Inputs are synthetic (seeded)
-and far larger than L2, so no L2 flush is needed between timed iterations.
+and far larger than L2, so no L2 flush is needed between timed iterations. After the main
+measurement the line also carries `batched_config4`: the 64-instance batched SC path of
+config 4 timed in a region of its own (subset-iterations/s summed over the instances and its
+ratio to the plain FP32 single-instance path run 64 times).
 
 Workload "sc3": the SC channel alone; "sc3-small": an 8,192-row SC case for profiling;
 "sparse-launch": one grouped sparse Compton weight launch (profiling case); "cone2": the
@@ -832,6 +835,7 @@ class JointBench:
                        "config 3), 1xGB300")
         self.traffic_file = "traffic_jsccsd3.json"
         self.dev = dev
+        self.small = small
         self.V = self.w.V
         self.subsets = self.w.subsets
 
@@ -860,7 +864,10 @@ class JointBench:
 
     def extra(self, ms_per_step):
         pairs = self.w.pair_count_per_step()
-        return {"compton_event_voxel_pairs_per_s": pairs / (ms_per_step / 1e3)}
+        out = {"compton_event_voxel_pairs_per_s": pairs / (ms_per_step / 1e3)}
+        if not self.small:
+            out["batched_config4"] = batched_summary(self.dev)
+        return out
 
     def e2e(self, iters):
         """One job with host inputs: pinned host copies of the BF16 system matrix (also the
@@ -946,6 +953,30 @@ class JointBench:
                            f"half: materialise weight of {n_sample} of the subset's {rows.size(0)} events with a "
                            f"scipy sparse upsample, scaled by events)"),
                 "seconds": time.perf_counter() - t_start}
+
+
+def batched_summary(dev, steps=5):
+    """The batched form of the SC channel (config 4: 64 instances sharing the joint
+    configuration's 81,920 x 36,000 SC matrix, one captured graph per OSEM iteration) in a
+    timed region of its own, after the main measurement: subset-iterations/s summed over the
+    instances, the plain FP32 single-instance path run 64 times for comparison, and the
+    tensor-core GEMM's HBM fraction."""
+    b = Batch4Bench(dev)
+    ms, launches, _ = timed_steps(b, "bf16", steps, 3, 1)
+    value = b.units_per_step() * steps / (ms / 1e3)
+    seq = b._sequential_fp32()
+    kt = kernel_times(b, "bf16", 2)
+    frac = None
+    if "bf16_gemm_nt" in kt:
+        n, tot = kt["bf16_gemm_nt"]
+        frac = b.kernel_bytes("bf16")["bf16_gemm_nt"] / (tot / n / 1e3) / 1e9 / measured_peaks()["hbm_gbs"]
+    res = {"value": value, "unit": "subset-iters/s summed over 64 instances", "ms_per_iteration": ms / steps,
+           "steps": steps, "gpu_launches": launches, "plain_fp32_single_instance_subset_iters_per_s": seq,
+           "speedup_vs_64_sequential_plain_fp32": value / seq, "gemm_hbm_frac_of_measured": frac,
+           "workload": "bench.py --workload batch4"}
+    del b
+    torch.cuda.empty_cache()
+    return res
 
 
 def make_workload(name, dev):
