@@ -27,6 +27,8 @@
 #include "jscc_common.cuh"
 
 #include <cuda.h>
+
+#include <atomic>
 #include <cstring>
 
 namespace jscc {
@@ -385,11 +387,16 @@ template <int NR>
 int launch_gemm(const __nv_bfloat16* P, int64_t ldp, const __nv_bfloat16* R, int64_t ldr, int64_t M, int nr, int64_t K,
                 int splits, float* out, int64_t ldo, float* part, cudaStream_t st) {
   using C = GemmCfg<NR>;
-  static bool attr_set = false;  // per process; the attribute is a property of the function
-  if (!attr_set) {
+  // the shared-memory attribute is set once per device (outside any later graph capture: the
+  // first call on a device happens eagerly)
+  static std::atomic<unsigned long long> attr_set{0};
+  int dev = 0;
+  JSCC_CUDA_CHECK(cudaGetDevice(&dev));
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(attr_set.load() & bit)) {
     JSCC_CUDA_CHECK(cudaFuncSetAttribute(bf16_gemm_nt_kernel<NR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)C::kSmem));
-    attr_set = true;
+    attr_set.fetch_or(bit);
   }
   int64_t kps = (K + splits - 1) / splits;
   kps = (kps + kGK - 1) / kGK * kGK;

@@ -166,10 +166,18 @@ def test_install_registers_reference_names():
 
 
 def test_product_path_refuses_cpu_tensors():
-    from jscc_recon_spect_cylinder_gb300 import ops
+    from jscc_recon_spect_cylinder_gb300 import batched, ops
 
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         ops.sc_weight(torch.ones((2, 3)), torch.ones((2, 1)), torch.ones((3, 1)))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        ops.sc_project(torch.ones((2, 8)), torch.ones((8, 1), dtype=torch.float64))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        ops.bf16_gemm_nt(torch.ones((4, 8), dtype=torch.bfloat16), torch.ones((2, 8), dtype=torch.bfloat16))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        ops.rdp_prior(torch.ones(4), torch.zeros((1, 4), dtype=torch.int32), torch.ones((1, 4)))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        batched.BatchedScOsem(torch.ones((8, 8)), [torch.arange(8)], torch.ones(8), 2, device="cpu")
 
 
 def test_fixed_width_adjoint_equals_dense_adjoint(golden):
