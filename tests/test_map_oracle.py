@@ -172,3 +172,43 @@ def test_adam_restatement_matches_torch():
         ((zt - tt) ** 4).sum().backward()
         opt.step()
     assert np.allclose(z, zt.detach().numpy(), rtol=1e-12, atol=1e-12)
+
+
+def test_neighbours_on_the_shipped_geometry(golden):
+    """The reference's shipped r10 polar grid (20 planes x 25 rings of 10-80 voxels): the
+    table is symmetric without duplicates or self edges, every voxel has its two in-ring
+    neighbours and its z faces and at least one neighbour in an adjacent ring, and the prior's
+    value over the table equals the direct sum over its undirected edges."""
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    coor = torch.from_numpy(golden("sparse_ops")["r10_coor_full"])
+    lay = cso._infer_polar_layout(coor)
+    n_layer, n_z = int(lay["fine_layer_num"]), int(lay["fine_z_num"])
+    lengths = [int(v) for v in lay["ring_lengths"]]
+    tb = _table(coor)
+    nbr = tb.nbr.numpy()
+    V = coor.size(0)
+    pairs = set()
+    for k in range(nbr.shape[0]):
+        for j in np.nonzero(nbr[k] >= 0)[0]:
+            pairs.add((int(j), int(nbr[k, j])))
+    assert len(pairs) == int((nbr >= 0).sum())  # no duplicates
+    assert all((b, a) in pairs for a, b in pairs)
+    assert all(a != b for a, b in pairs)
+    starts = np.concatenate(([0], np.cumsum(lengths)[:-1]))
+    for z in (0, n_z // 2, n_z - 1):
+        for r, L in enumerate(lengths):
+            for t in (0, L // 2, L - 1):
+                j = z * n_layer + starts[r] + t
+                mine = {b for a, b in pairs if a == j}
+                assert {z * n_layer + starts[r] + (t + 1) % L, z * n_layer + starts[r] + (t - 1) % L} <= mine
+                if z > 0:
+                    assert j - n_layer in mine
+                if z + 1 < n_z:
+                    assert j + n_layer in mine
+                in_plane = {b - z * n_layer for b in mine if z * n_layer <= b < (z + 1) * n_layer}
+                assert any(not starts[r] <= b < starts[r] + L for b in in_plane), (z, r, t)  # an adjacent ring
+    x = np.random.default_rng(6).uniform(0.5, 2.0, V)
+    value, _ = om.rdp(x, nbr, tb.weight.numpy(), 2.0)
+    direct = sum(1.0 * (x[a] - x[b]) ** 2 / (x[a] + x[b] + 2.0 * abs(x[a] - x[b]) + 1e-9) for a, b in pairs if a < b)
+    assert abs(value - direct) < 1e-9 * direct
