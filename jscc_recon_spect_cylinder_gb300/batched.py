@@ -32,6 +32,22 @@ def _pad8(n: int) -> int:
     return (n + 7) // 8 * 8
 
 
+def subset_blocks(subsets):
+    """Layout of the bin-permuted matrix: ``(blocks, perm)`` with one ``(row offset, bins,
+    padded bins)`` block per subset (padded to a multiple of 8 rows, so every block and every
+    column block of the transpose starts 16-byte aligned) and ``perm[row]`` = the reference's
+    bin index held by that row (-1 on padding rows)."""
+    blocks, off = [], 0
+    for ids in subsets:
+        nb = int(ids.numel())
+        blocks.append((off, nb, _pad8(nb)))
+        off += _pad8(nb)
+    perm = torch.full((off,), -1, dtype=torch.int64)
+    for (b0, nb, _), ids in zip(blocks, subsets):
+        perm[b0:b0 + nb] = ids.to(torch.int64).cpu()
+    return blocks, perm
+
+
 class BatchedScOsem:
     """Batched plain SC OSEM over fixed subsets.
 
@@ -56,18 +72,11 @@ class BatchedScOsem:
         self.dev, self.V, self.B, self.n = dev, V, B, n_inst
         self.np = _pad8(n_inst)
         self.nr = 2 * self.np
-        self.blocks = []  # (row offset in the permuted matrix, real bins, padded bins)
-        off = 0
-        for ids in subsets:
-            nb = int(ids.numel())
-            self.blocks.append((off, nb, _pad8(nb)))
-            off += _pad8(nb)
-        self.B_pad = off
-        perm = torch.full((self.B_pad,), -1, dtype=torch.int64)
+        self.blocks, perm = subset_blocks(subsets)  # (row offset, real bins, padded bins) per subset
+        self.B_pad = perm.numel()
         A = torch.zeros((self.B_pad, V), dtype=torch.bfloat16, device=dev)
         for (b0, nb, _), ids in zip(self.blocks, subsets):
             ids = ids.to(torch.int64).cpu()
-            perm[b0:b0 + nb] = ids
             A[b0:b0 + nb] = sysmat[ids.to(sysmat.device)].to(dev, torch.bfloat16)
         self.perm = perm.to(dev)
         self.A = A
