@@ -189,6 +189,8 @@ JSCC_API int jscc_sc_weight_noalloc(const void* A, int32_t a_dtype, int64_t lda,
 
 #define JSCC_CONE_STRICT 0 /* process_list_plane_strict.py (kinematic filter, clamped angles) */
 #define JSCC_CONE_LEGACY 1 /* process_list_plane.py (derivative sigma_E, atan sigma_pos, no clamps) */
+#define JSCC_CONE_SIMPLE 2 /* exp(-(beta - theta)^2 / (2 sigma_E^2)) / d01^2 on strict records (no sigma_pos,
+                              no Klein-Nishina factor): the simplified list-mode kernel */
 #define JSCC_CONE_RECORD_FLOATS 16 /* floats per event record (64 bytes, 16-byte aligned) */
 
 /*

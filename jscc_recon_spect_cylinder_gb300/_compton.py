@@ -59,7 +59,7 @@ def select_events(list_smeared, detector, delta_r1, delta_r2, e0, ene_resolution
     """Run the selection kernel on a smeared list and compact the survivors.
     Returns ``(kept list indices int64, records [E', 16], row_id int32 [E'])``."""
     det = detector[:, :3].to(torch.float32).contiguous()
-    if model == _lib.CONE_STRICT:
+    if model != _lib.CONE_LEGACY:  # strict and simple records carry the strict fields
         s1 = detector_pos_sigma_sq(det, delta_r1).to(torch.float32).contiguous()
         s2 = detector_pos_sigma_sq(det, delta_r2).to(torch.float32).contiguous()
     else:

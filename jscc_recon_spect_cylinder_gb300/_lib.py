@@ -27,6 +27,7 @@ EM_SAFE = 1
 
 CONE_STRICT = 0
 CONE_LEGACY = 1
+CONE_SIMPLE = 2
 CONE_RECORD_FLOATS = 16
 
 SPARSE_MATERIALIZE = 0

@@ -5,6 +5,8 @@
 //   strict:  process_list_plane_strict.py:151-253 (filters :164-189, theta :24-27, sigma_E
 //            :39-52, sigma_pos :59-134, kernel :228), t = cone * sysmat[cp1 - 1] (:240)
 //   legacy:  process_list_plane.py:17-107 (derivative sigma_E :66-74, atan sigma_pos :77-80)
+//   simple:  exp(-(beta - theta)^2 / (2 sigma_E^2)) / d01^2 (the simplified kernel of the
+//            list-mode benchmark description; strict records, no sigma_pos, no Klein-Nishina)
 //   weight:  recon_osem_plane.py:33-42 (get_weight_compton) over the builder's rows; rows are
 //            normalised there, and the list-mode weight is invariant to a row's scale, so the
 //            fused form skips the normalisation.
@@ -83,7 +85,7 @@ __global__ void compton_event_prep_kernel(const float* __restrict__ list, int64_
     const int cp2 = (int)L[2];
     const float e1 = L[1], e2 = L[3];
     bool k = (e1 < thr_max) && (e1 > thr_min) && (e2 > thr_min) && (__fadd_rn(e1, e2) > thr_sum);
-    if (model == 0) {
+    if (model != 1) {
       const float c = compton_cos_f32(e1, e0);
       k = k && (c > -1.0f + 1e-6f) && (c < 1.0f - 1e-6f);
     }
@@ -106,7 +108,7 @@ __global__ void compton_event_prep_kernel(const float* __restrict__ list, int64_
     r.vy = __fsub_rn(b[1], a[1]);
     r.vz = __fsub_rn(b[2], a[2]);
     r.d12 = sqrtf(r.vx * r.vx + r.vy * r.vy + r.vz * r.vz);
-    if (model == 0) {
+    if (model != 1) {
       // sigma_E: e1 -/+ e1 * res / 2.355 * sqrt(e0 / e1), clamped to (1e-7, e0 - 1e-7)
       if (theta_fp64) {
         const double E0 = (double)e0, E1 = (double)e1;
@@ -198,6 +200,15 @@ __device__ __forceinline__ float cone_value(const ConeEvent& e, float cx, float 
     const float sig2 = fmaxf(sig_pos * sig_pos + sig_e * sig_e, 1e-12f);
     const float sinb2 = (1.0f - c) * (1.0f + c);
     return expf(-(delta * delta) / (2.0f * sig2)) * (e.kn - sinb2);
+  } else if (MODEL == 2) {
+    // simple: exp(-(beta - theta)^2 / (2 sigma_E^2)) / d01^2 with the two-sided sigma_E of the
+    // record (the energy resolution propagated through the Compton formula)
+    const float bcos = dot / fmaxf(d01 * e.d12, 1e-7f);
+    if (WINDOW && (bcos < e.cos_lo || bcos > e.cos_hi)) return 0.f;
+    const float c = fminf(fmaxf(bcos, -1.0f + 1e-7f), 1.0f - 1e-7f);
+    const float delta = acosf(c) - e.theta;
+    const float sig_e = delta >= 0.f ? e.sig_plus : e.sig_minus;
+    return expf(-(delta * delta) / (2.0f * sig_e * sig_e)) / fmaxf(d01sq, 1e-14f);
   } else {
     const float beta = acosf(dot / (d01 * e.d12));
     const float delta = beta - e.theta;
@@ -824,7 +835,8 @@ int jscc_compton_event_prep(const float* list, int64_t ld_list, int64_t n_events
                             int32_t theta_fp64, float window_sigmas, float delta_r1, float delta_r2,
                             uint8_t* keep, float* records, int32_t* row_id, void* stream) {
   JSCC_REQUIRE(n_events >= 0 && n_det >= 0, "jscc_compton_event_prep: negative size");
-  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_event_prep: bad model %d",
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY || model == JSCC_CONE_SIMPLE,
+               "jscc_compton_event_prep: bad model %d",
                model);
   if (n_events == 0) return JSCC_OK;
   JSCC_REQUIRE(list && det_pos && keep && records && row_id, "jscc_compton_event_prep: null pointer argument");
@@ -848,7 +860,8 @@ int jscc_compton_cone_rows(const float* records, const int32_t* row_id, int64_t 
                            int32_t model, const void* eff, int32_t eff_dtype, int64_t ld_eff, float* t_compton,
                            float* t, void* stream) {
   JSCC_REQUIRE(n_ev >= 0 && V >= 0, "jscc_compton_cone_rows: negative size");
-  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_cone_rows: bad model");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY || model == JSCC_CONE_SIMPLE,
+               "jscc_compton_cone_rows: bad model");
   JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_cone_rows: bad dtype");
   if (n_ev == 0 || V == 0) return JSCC_OK;
   JSCC_REQUIRE(records && coor && (t_compton || t), "jscc_compton_cone_rows: null pointer argument");
@@ -864,6 +877,9 @@ int jscc_compton_cone_rows(const float* records, const int32_t* row_id, int64_t 
     if (model == JSCC_CONE_STRICT)
       JSCC_TIMED("cone_rows", st, (cone_rows_kernel<0, float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, V, e,
                                                                                         ld_eff, t_compton, t)));
+    else if (model == JSCC_CONE_SIMPLE)
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<2, float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, V, e,
+                                                                                        ld_eff, t_compton, t)));
     else
       JSCC_TIMED("cone_rows", st, (cone_rows_kernel<1, float><<<grid, 256, 0, st>>>(rec, row_id, n_ev, coor, V, e,
                                                                                         ld_eff, t_compton, t)));
@@ -871,6 +887,9 @@ int jscc_compton_cone_rows(const float* records, const int32_t* row_id, int64_t 
     const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
     if (model == JSCC_CONE_STRICT)
       JSCC_TIMED("cone_rows", st, (cone_rows_kernel<0, __nv_bfloat16><<<grid, 256, 0, st>>>(
+                                      rec, row_id, n_ev, coor, V, e, ld_eff, t_compton, t)));
+    else if (model == JSCC_CONE_SIMPLE)
+      JSCC_TIMED("cone_rows", st, (cone_rows_kernel<2, __nv_bfloat16><<<grid, 256, 0, st>>>(
                                       rec, row_id, n_ev, coor, V, e, ld_eff, t_compton, t)));
     else
       JSCC_TIMED("cone_rows", st, (cone_rows_kernel<1, __nv_bfloat16><<<grid, 256, 0, st>>>(
@@ -884,7 +903,8 @@ int jscc_compton_row_stats(const float* records, const int32_t* row_id, int64_t 
                            int32_t model, int32_t use_window, const void* eff, int32_t eff_dtype, int64_t ld_eff,
                            float* s1, float* s2, int32_t* nan_flag, void* stream) {
   JSCC_REQUIRE(n_ev >= 0 && V >= 0, "jscc_compton_row_stats: negative size");
-  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "jscc_compton_row_stats: bad model");
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY || model == JSCC_CONE_SIMPLE,
+               "jscc_compton_row_stats: bad model");
   JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "jscc_compton_row_stats: bad dtype");
   if (n_ev == 0) return JSCC_OK;
   JSCC_REQUIRE(records && coor && s1 && s2 && nan_flag, "jscc_compton_row_stats: null pointer argument");
@@ -900,10 +920,12 @@ int jscc_compton_row_stats(const float* records, const int32_t* row_id, int64_t 
                  nan_flag)))
   if (eff_dtype == JSCC_DTYPE_F32) {
     if (model == JSCC_CONE_LEGACY) JSCC_STATS_LAUNCH(1, false, float);
+    else if (model == JSCC_CONE_SIMPLE) JSCC_STATS_LAUNCH(2, false, float);
     else if (use_window) JSCC_STATS_LAUNCH(0, true, float);
     else JSCC_STATS_LAUNCH(0, false, float);
   } else {
     if (model == JSCC_CONE_LEGACY) JSCC_STATS_LAUNCH(1, false, __nv_bfloat16);
+    else if (model == JSCC_CONE_SIMPLE) JSCC_STATS_LAUNCH(2, false, __nv_bfloat16);
     else if (use_window) JSCC_STATS_LAUNCH(0, true, __nv_bfloat16);
     else JSCC_STATS_LAUNCH(0, false, __nv_bfloat16);
   }
@@ -924,7 +946,8 @@ static int compton_stage_entry(const char* what, int stage, const float* records
                                float* f_out, float scale, float* weight, void* workspace, size_t workspace_bytes,
                                void* stream) {
   JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0, "%s: negative size", what);
-  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY, "%s: bad model", what);
+  JSCC_REQUIRE(model == JSCC_CONE_STRICT || model == JSCC_CONE_LEGACY || model == JSCC_CONE_SIMPLE,
+               "%s: bad model", what);
   JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "%s: bad dtype", what);
   if (n_ev == 0 || n_vox == 0) return JSCC_OK;
   JSCC_REQUIRE(records && coor, "%s: null pointer argument", what);
@@ -962,6 +985,8 @@ static int compton_stage_entry(const char* what, int stage, const float* records
     const float* e = static_cast<const float*>(eff);
     if (model == JSCC_CONE_LEGACY)
       rc = launch_cone_weight<1, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
+    else if (model == JSCC_CONE_SIMPLE)
+      rc = launch_cone_weight<2, false, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
     else if (win)
       rc = launch_cone_weight<0, true, float>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p, st, stage);
     else
@@ -970,6 +995,9 @@ static int compton_stage_entry(const char* what, int stage, const float* records
     const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
     if (model == JSCC_CONE_LEGACY)
       rc = launch_cone_weight<1, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
+                                                       st, stage);
+    else if (model == JSCC_CONE_SIMPLE)
+      rc = launch_cone_weight<2, false, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,
                                                        st, stage);
     else if (win)
       rc = launch_cone_weight<0, true, __nv_bfloat16>(rec, row_id, n_ev, coor, n_vox, x, e, ld_eff, f, q, part, p,

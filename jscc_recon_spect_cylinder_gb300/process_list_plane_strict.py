@@ -216,7 +216,7 @@ def get_compton_event_params(sysmat, detector, coor, list_smeared, delta_r1, del
     s1, s2, nan = ops.compton_row_stats(rec, rid, coor.to(dev, torch.float32), model=model, eff=sysmat.to(dev),
                                         use_window=window_sigmas > 0)
     ok = (~nan) & (s1 != 0)
-    if stability and model == _lib.CONE_STRICT:
+    if stability and model != _lib.CONE_LEGACY:
         ok &= (s1 * s1 / s2) >= MIN_EVENT_EFFECTIVE_SUPPORT
     keep = torch.nonzero(ok).flatten()
     return ComptonEvents(rec.index_select(0, keep).contiguous(), rid.index_select(0, keep).contiguous(),

@@ -122,6 +122,33 @@ def cone_rows_strict(pos1, pos2, e1, s1sq, s2sq, coor, e0, ene_resolution, dtype
     return np.exp(-(delta ** 2) / (d(2) * sig ** 2)) * (kn[:, None] - np.sin(beta) ** 2)
 
 
+def cone_rows_simple(pos1, pos2, e1, coor, e0, ene_resolution, dtype=np.float64):
+    """Simple cone kernel: exp(-(beta - theta)^2 / (2 sigma_E^2)) / d01^2, with theta and the
+    two-sided sigma_E of the strict model (process_list_plane_strict.py:24-27, :39-52) and
+    neither sigma_pos nor the Klein-Nishina factor (the simplified list-mode kernel)."""
+    d = dtype
+    pos1 = np.asarray(pos1, dtype=d)
+    pos2 = np.asarray(pos2, dtype=d)
+    e1 = np.asarray(e1, dtype=d)
+    coor = np.asarray(coor, dtype=d)
+    v01 = pos1[:, None, :] - coor[None, :, :]
+    v12 = (pos2 - pos1)[:, None, :]
+    d01sq = (v01 * v01).sum(-1)
+    d01 = np.sqrt(d01sq)
+    d12 = np.sqrt((v12 * v12).sum(-1))
+    theta = compton_theta(e1, e0, d)
+    bcos = (v01 * v12).sum(-1) / np.maximum(d01 * d12, d(1e-7))
+    beta = np.arccos(np.clip(bcos, d(-1.0 + 1e-7), d(1.0 - 1e-7)))
+    sig_e = e1 * d(ene_resolution) / d(2.355) * np.sqrt(d(e0) / e1)
+    lo = np.clip(e1 - sig_e, d(1e-7), d(e0) - d(1e-7))
+    hi = np.clip(e1 + sig_e, d(1e-7), d(e0) - d(1e-7))
+    s_minus = np.maximum(theta - compton_theta(lo, e0, d), d(1e-7))
+    s_plus = np.maximum(compton_theta(hi, e0, d) - theta, d(1e-7))
+    delta = beta - theta[:, None]
+    sig = np.where(delta >= 0, s_plus[:, None], s_minus[:, None])
+    return np.exp(-(delta ** 2) / (d(2) * sig ** 2)) / np.maximum(d01sq, d(1e-14))
+
+
 def cone_rows_legacy(pos1, pos2, e1, coor, e0, ene_resolution, delta_r1, delta_r2, dtype=np.float64):
     """Legacy cone kernel (process_list_plane.py:56-83): derivative-based sigma_E, atan sigma_pos,
     no clamps."""

@@ -495,3 +495,32 @@ def test_plan_groups_ahead_of_the_weight_call(cuda):
     assert torch.equal(w, w_fresh)
     with pytest.raises(ValueError):
         ops.plan_groups(ids.long(), n_det)
+
+
+def test_simple_model_rows_and_fused_weight(cuda):
+    """The simple kernel (JSCC_CONE_SIMPLE: exp(-(beta - theta)^2 / 2 sigma_E^2) / d01^2 on the
+    strict records): materialised rows against the float32 oracle restatement (per row,
+    relative to the row maximum), and the fused on-the-fly weight against the stored rows'."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300 import recon_osem_plane as rop
+
+    grid, det, sysmat, L, args = _cone_problem(cuda, n_events=1500)
+    A, coor = sysmat.to(cuda), grid.coor.to(cuda)
+    ev = pls.get_compton_event_params(A, det.to(cuda), coor, torch.from_numpy(L).to(cuda), *args,
+                                      model=_lib.CONE_SIMPLE, theta_fp64=False, window_sigmas=0.0)
+    assert len(ev) > 100
+    tc, t = ops.compton_cone_rows(ev.records, ev.row_id, coor, model=_lib.CONE_SIMPLE, eff=A)
+    ids = ev.list_index.cpu().numpy()
+    cp1, cp2 = L[ids, 0].astype(np.int64), L[ids, 2].astype(np.int64)
+    d = det.numpy()
+    ref = oc.cone_rows_simple(d[cp1 - 1], d[cp2 - 1], L[ids, 1], grid.coor.numpy(), args[2], args[3],
+                              dtype=np.float32)
+    # without sigma_pos the Gaussian is only sigma_E wide, so an ulp of cos(beta) (amplified by
+    # acos) moves t further than in the strict model: float32 and float64 evaluations of this
+    # formula differ by up to 3e-4 per row on these events, two float32 ones by ~1e-4
+    _rows_close(tc.cpu(), ref, 3e-4)
+    x = torch.rand((grid.n_vox, 1), generator=torch.Generator().manual_seed(3)).to(cuda) + 0.5
+    w_fused = ops.compton_weight(ev.records, ev.row_id, coor, x, model=_lib.CONE_SIMPLE, eff=A)
+    w_stored = rop.get_weight_compton(t, x)
+    assert rel_l2(w_fused.cpu(), w_stored.cpu()) < TOL_W
