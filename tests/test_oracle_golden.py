@@ -235,3 +235,31 @@ def test_sensitivity_builders_match_reference(golden):
     r = osp.sensitivity_d_rescale(d, s, 1000, 250)
     np.testing.assert_allclose(r.sum(), s.sum() * 250 / 1000, rtol=1e-12)
     assert np.array_equal(osp.sensitivity_d_rescale(np.zeros_like(d), s, 1, 1), np.zeros_like(d))
+
+
+def test_simple_cone_oracle_is_the_strict_kernel_without_sigma_pos():
+    """The simple restatement against the golden-pinned strict one: with zero position
+    variance the strict kernel is exp(-(beta - theta)^2 / 2 sigma_E^2) (kn - sin^2 beta), so
+    strict = simple * d01^2 * (kn - sin^2 beta) (float64, relative to each row's maximum; the
+    strict kernel's floor of sigma_pos^2 at 1e-12 is the only difference, ~1e-8 here)."""
+    from oracle import compton as oc
+
+    rng = np.random.default_rng(8)
+    n, e0 = 40, 0.511
+    pos1 = rng.uniform(-120, 120, (n, 3))
+    pos2 = rng.uniform(-150, 150, (n, 3))
+    e1 = rng.uniform(0.08, 0.3, n)
+    coor = rng.uniform(-40, 40, (300, 3))
+    res = 0.1
+    zero = np.zeros((n, 3))
+    strict = oc.cone_rows_strict(pos1, pos2, e1, zero, zero, coor, e0, res)
+    simple = oc.cone_rows_simple(pos1, pos2, e1, coor, e0, res)
+    v01 = pos1[:, None, :] - coor[None, :, :]
+    v12 = (pos2 - pos1)[:, None, :]
+    d01 = np.linalg.norm(v01, axis=-1)
+    bcos = (v01 * v12).sum(-1) / np.maximum(d01 * np.linalg.norm(v12, axis=-1), 1e-7)
+    c = np.clip(bcos, -1 + 1e-7, 1 - 1e-7)
+    kn = e0 / (e0 - e1) + (e0 - e1) / e0
+    expect = simple * d01 ** 2 * (kn[:, None] - (1 - c) * (1 + c))
+    scale = np.maximum(np.abs(strict).max(axis=1, keepdims=True), 1e-300)  # rows that underflow entirely
+    assert np.max(np.abs(strict - expect) / scale) < 1e-6
