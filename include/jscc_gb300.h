@@ -17,6 +17,9 @@
  *    jscc_last_error() (thread-local).
  *  - Results are deterministic: reductions run in a fixed order and no float
  *    atomics are used, so repeated calls give bit-identical outputs.
+ *  - Per-device state is cached for the life of the process (kernel attributes set
+ *    once per device, the no-allocation scratch address): after cudaDeviceReset on a
+ *    device, do not use the library on that device again in the same process.
  */
 #ifndef JSCC_GB300_H
 #define JSCC_GB300_H
@@ -172,7 +175,10 @@ JSCC_API int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, co
  * 16 MiB covers e.g. a 10,240-bin x 36,000-voxel subset block with one rotation
  * (about 5 MiB); scratch grows with the rotations handled per pass (up to 8).
  * The first call on each device looks up the array's device address (with that
- * device current); make that first call before any stream capture. All calls share
+ * device current); make that first call before any stream capture. The address is
+ * kept for the life of the process: after cudaDeviceReset on a device, do not call this
+ * entry point on that device again in the same process (the array may then live at
+ * another address). All calls share
  * the one array, so calls that can overlap on the GPU (other streams, other host
  * threads) race and must be serialised by the caller. Nothing in the scratch needs
  * clearing between calls: each call writes every scratch byte it later reads.
@@ -397,6 +403,17 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  */
 JSCC_API int jscc_take_wait_timeout_count(unsigned int* out);
 
+/*
+ * Poll bound of every bounded pipeline wait on the current device: the bulk sparse kernels
+ * (jscc_sparse_weight_grouped) and the tensor-core GEMM (jscc_bf16_gemm_nt). polls < 0
+ * restores the default (2^22 polls per wait); 0 makes each such wait give up at once. A CTA
+ * that gives up still waits, with a fixed bound of its own, for the copies and MMAs it has
+ * in flight, frees its tensor memory and is counted (jscc_take_wait_timeout_count,
+ * jscc_take_gemm_timeout_count); the results of that call are invalid. For tests of the
+ * give-up path; synchronous. No counterpart in the reference.
+ */
+JSCC_API int jscc_set_wait_limit(int64_t polls);
+
 JSCC_API size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int64_t n_coarse,
                    int32_t n_groups, int32_t adj_width);
 JSCC_API int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype,
@@ -457,7 +474,7 @@ JSCC_API int jscc_compton_backproject_f64(const float* records, const int32_t* r
                    int64_t ld_eff, const double* g, double scale, double* weight, void* stream);
 JSCC_API int jscc_rdp_prior_f64(const double* img, const int32_t* nbr, const float* weight, int64_t n_vox,
                    int32_t n_nbr, double gamma, double eps, double beta, double* value, double* grad,
-                   int32_t accumulate, void* stream);
+                   int32_t accumulate, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ------------------------------------------------ batched (multi-instance) SC path */
 
@@ -527,13 +544,17 @@ JSCC_API int jscc_take_gemm_timeout_count(unsigned int* out);
  *   R(x) = 1/2 sum_j sum_{k in N(j)} w_jk (x_j - x_k)^2 / (x_j + x_k + gamma |x_j - x_k| + eps)
  * nbr / weight are neighbour-major [n_nbr, n_vox] (entry k * n_vox + j is the k-th neighbour
  * of voxel j, -1 = none); every edge must appear in both directions with the same weight.
- * value (may be NULL): *value += beta * R(x) (double, device memory; the caller zeroes it).
+ * value (may be NULL): *value += beta * R(x) (double, device memory; the caller zeroes it),
+ * reduced in a fixed order (per-block sums in the workspace, then one block adds them in
+ * order), so repeated calls give bit-identical values. The workspace (8-byte aligned, at least
+ * jscc_rdp_prior_workspace_bytes(n_vox) bytes) is only needed when value is non-NULL.
  * grad  (may be NULL): grad[j] = (accumulate ? grad[j] : 0) + beta * dR/dx_j.
  * Out-of-range neighbour indices are skipped and counted (jscc_take_bad_index_count).
  */
+JSCC_API size_t jscc_rdp_prior_workspace_bytes(int64_t n_vox);
 JSCC_API int jscc_rdp_prior(const float* img, const int32_t* nbr, const float* weight, int64_t n_vox,
                    int32_t n_nbr, float gamma, float eps, float beta, double* value, float* grad,
-                   int32_t accumulate, void* stream);
+                   int32_t accumulate, void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -91,7 +91,7 @@ _SIGNATURES: dict[str, tuple] = {
     "jscc_rdp_prior_f64": (
         c_int,
         [c_void_p, c_void_p, c_void_p, c_int64, c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-         c_void_p, c_void_p, c_int32, c_void_p],
+         c_void_p, c_void_p, c_int32, c_void_p, c_size_t, c_void_p],
     ),
     "jscc_bf16_gemm_workspace_bytes": (c_size_t, [c_int64, c_int32, c_int64, c_int32]),
     "jscc_bf16_gemm_nt": (
@@ -116,10 +116,12 @@ _SIGNATURES: dict[str, tuple] = {
         c_int, [c_void_p, c_int64, c_int64, c_int32, c_int32, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                 c_void_p]),
     "jscc_take_gemm_timeout_count": (c_int, [POINTER(c_uint)]),
+    "jscc_set_wait_limit": (c_int, [c_int64]),
+    "jscc_rdp_prior_workspace_bytes": (c_size_t, [c_int64]),
     "jscc_rdp_prior": (
         c_int,
         [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_float, c_float, c_float, c_void_p, c_void_p, c_int32,
-         c_void_p],
+         c_void_p, c_size_t, c_void_p],
     ),
     "jscc_sc_sensitivity": (
         c_int,
@@ -265,6 +267,30 @@ def take_gemm_timeout_count() -> int:
     out = c_uint(0)
     check(load().jscc_take_gemm_timeout_count(ctypes.byref(out)), "jscc_take_gemm_timeout_count")
     return int(out.value)
+
+
+def set_wait_limit(polls: int | None) -> None:
+    """Poll bound of every bounded pipeline wait (bulk sparse kernels and tensor-core GEMM)
+    on the current device; None restores the default. 0 makes each wait give up at once:
+    the give-up path then runs while every copy still completes."""
+    check(load().jscc_set_wait_limit(-1 if polls is None else int(polls)), "jscc_set_wait_limit")
+
+
+# Bumped whenever a give-up is detected: per-plan event sums computed before it may come from
+# a call whose waits gave up, so ops keys its cached sums by this epoch.
+timeout_epoch = 0
+
+
+def check_wait_timeouts() -> None:
+    """Raise RuntimeError when a bounded device wait gave up since the last check (the
+    results of the calls made meanwhile are then invalid, and cached per-plan event sums are
+    dropped); resets both counters."""
+    global timeout_epoch
+    bulk, gemm = take_wait_timeout_count(), take_gemm_timeout_count()
+    if bulk or gemm:
+        timeout_epoch += 1
+        raise RuntimeError(f"device pipeline waits gave up: {bulk} in the sparse bulk kernels, {gemm} in the "
+                           "tensor-core GEMM; the results computed since the last check are invalid")
 
 
 def take_bad_index_count() -> int:

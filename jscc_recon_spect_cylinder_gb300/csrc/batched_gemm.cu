@@ -22,8 +22,11 @@
 //     before refilling it; a last commit signals the epilogue;
 //   * epilogue (all four warps): each warp reads its 32 TMEM lanes with tcgen05.ld and writes
 //     FP32 rows.
-//   Every wait is bounded and polls a CTA abort flag; a CTA that gives up is counted
-//   (jscc_take_gemm_timeout_count) and still frees its TMEM.
+//   Every wait is bounded (jscc_set_wait_limit) and polls a CTA abort flag. A CTA that gives
+//   up first waits, with a fixed bound of its own, for the work it already issued: the TMA
+//   loads that the MMA issuer did not consume (they still write shared memory) and the MMAs
+//   it committed (they still write TMEM and read shared memory). Only then is it counted
+//   (jscc_take_gemm_timeout_count), skips the epilogue and frees its TMEM.
 #include "jscc_common.cuh"
 
 #include <cuda.h>
@@ -36,9 +39,13 @@ namespace jscc {
 constexpr int kGM = 128;          // tile rows = MMA M
 constexpr int kGK = 64;           // K per stage (128 bytes of BF16 per row)
 constexpr int kGThreads = 128;
-constexpr uint32_t kGemmPolls = 1u << 22;
+constexpr uint32_t kGemmPolls = 1u << 22;       // default bound of a role's wait
+constexpr uint32_t kGemmDrainPolls = 1u << 24;  // bound of the drain after a give-up
 
 __device__ unsigned int g_gemm_timeout_count = 0;
+// Poll bound of the role waits, settable from the host (jscc_set_wait_limit): 0 makes every
+// role wait give up at once, which exercises the give-up path with all copies completing.
+__device__ uint32_t g_gemm_poll_limit = kGemmPolls;
 
 // tcgen05 shared-memory matrix descriptor for a K-major tile written by TMA with 128-byte
 // swizzle (rows of 64 BF16 = 128 bytes, 8-row atoms of 1024 bytes): start address >> 4
@@ -99,8 +106,9 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 // Bounded wait that also gives up when another role of the CTA raised the abort flag.
-__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  for (uint32_t i = 0; i < kGemmPolls; ++i) {
+__device__ __forceinline__ bool role_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((i & 255) == 255 && *abort_flag) return false;
   }
@@ -137,6 +145,10 @@ bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_consta
   uint64_t* done = empty + S;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  int* loads_issued = reinterpret_cast<int*>(tmem_slot + 2);    // K steps loaded
+  int* loads_consumed = reinterpret_cast<int*>(tmem_slot + 3);  // K steps handed to the MMA
+  int* mma_committed = reinterpret_cast<int*>(tmem_slot + 4);   // `done` committed
+  const uint32_t polls = g_gemm_poll_limit;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t m0 = (int64_t)blockIdx.x * kGM;
@@ -151,6 +163,7 @@ bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_consta
     }
     mbar_init(done, 1);
     *abort_flag = 0;
+    *loads_issued = *loads_consumed = *mma_committed = 0;
     mbar_init_fence();
   }
   if (warp == 0) {
@@ -169,11 +182,12 @@ bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_consta
     // producer
     for (int t = 0; t < nk; ++t) {
       const int s = t % S;
-      if (t >= S && !role_wait(&empty[s], (uint32_t)(((t / S) - 1) & 1), abort_flag)) break;
+      if (t >= S && !role_wait(&empty[s], (uint32_t)(((t / S) - 1) & 1), abort_flag, polls)) break;
       mbar_arrive_expect_tx(&full[s], C::kStage);
       const int x = (int)(kb + (int64_t)t * kGK);
       tma_load_2d(sbase + s * C::kStage, &tmP, x, (int)m0, &full[s]);
       tma_load_2d(sbase + s * C::kStage + C::kA, &tmR, x, 0, &full[s]);
+      *loads_issued = t + 1;
     }
   } else if (nk > 0 && warp == 1 && lane == 0) {
     // MMA issuer
@@ -181,7 +195,8 @@ bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_consta
     int t = 0;
     for (; t < nk; ++t) {
       const int s = t % S;
-      if (!role_wait(&full[s], (uint32_t)((t / S) & 1), abort_flag)) break;
+      if (!role_wait(&full[s], (uint32_t)((t / S) & 1), abort_flag, polls)) break;
+      *loads_consumed = t + 1;
       tc_fence_after();
       const uint32_t a = sbase + s * C::kStage, b = a + C::kA;
 #pragma unroll
@@ -190,10 +205,20 @@ bf16_gemm_nt_kernel(const __grid_constant__ CUtensorMap tmP, const __grid_consta
       tc_commit(&empty[s]);
     }
     tc_commit(done);  // arrives when every MMA issued above has completed
+    *mma_committed = 1;
   }
   bool ok = true;
-  if (nk > 0) ok = role_wait(done, 0u, abort_flag) && !*abort_flag;
-  ok = __syncthreads_and(ok);
+  if (nk > 0) ok = role_wait(done, 0u, abort_flag, polls) && !*abort_flag;
+  ok = __syncthreads_and(ok);  // every role has left its loop: nothing more is issued
+  if (!ok && tid == 0) {
+    // Work issued before the give-up still runs: wait (bounded) for the TMA loads the MMA
+    // issuer did not consume (each stage holds at most one such load, so its parity is
+    // unambiguous) and for the committed MMAs, before shared memory and TMEM are released.
+    for (int t = *loads_consumed; t < *loads_issued; ++t)
+      mbar_wait_bounded(&full[t % S], (uint32_t)((t / S) & 1), kGemmDrainPolls);
+    if (*mma_committed) mbar_wait_bounded(done, 0u, kGemmDrainPolls);
+  }
+  __syncthreads();
   tc_fence_after();
   const int64_t row = m0 + warp * 32 + lane;
   float* orow = out + (int64_t)blockIdx.y * split_stride + row * ldo;
@@ -539,6 +564,19 @@ int jscc_batch_em_joint(const float* W, int64_t ldw, int64_t V, int32_t n_inst, 
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
 }
+
+}  // extern "C"
+
+namespace jscc {
+// Poll bound of the GEMM's role waits on the current device (`reset` restores the default).
+int set_gemm_poll_limit(uint32_t polls, bool reset) {
+  const uint32_t v = reset ? kGemmPolls : polls;
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_gemm_poll_limit, &v, sizeof(v)));
+  return JSCC_OK;
+}
+}  // namespace jscc
+
+extern "C" {
 
 int jscc_take_gemm_timeout_count(unsigned int* out) {
   JSCC_REQUIRE(out, "jscc_take_gemm_timeout_count: null pointer argument");

@@ -78,9 +78,21 @@ void timing_end(const char* name, cudaStream_t st) {
   g_pending_start = nullptr;
 }
 
+int set_bulk_poll_limit(uint32_t polls, bool reset);  // sparse_ops.cu
+int set_gemm_poll_limit(uint32_t polls, bool reset);  // batched_gemm.cu
+
 }  // namespace jscc
 
 extern "C" {
+
+int jscc_set_wait_limit(int64_t polls) {
+  JSCC_REQUIRE(polls <= (int64_t)UINT32_MAX, "jscc_set_wait_limit: %lld polls is above 2^32 - 1", (long long)polls);
+  const bool reset = polls < 0;
+  const uint32_t v = reset ? 0u : (uint32_t)polls;
+  int rc = jscc::set_bulk_poll_limit(v, reset);
+  if (rc != JSCC_OK) return rc;
+  return jscc::set_gemm_poll_limit(v, reset);
+}
 
 void jscc_kernel_timing_enable(int enable) {
   std::lock_guard<std::mutex> lk(jscc::g_tmu);
@@ -122,7 +134,7 @@ int jscc_kernel_timing_collect(char* buf, size_t buf_bytes) {
 
 const char* jscc_last_error(void) { return jscc::g_err; }
 
-int jscc_abi_version(void) { return 6; }
+int jscc_abi_version(void) { return 7; }
 
 unsigned long long jscc_launch_count(void) { return jscc::launch_counter().load(); }
 

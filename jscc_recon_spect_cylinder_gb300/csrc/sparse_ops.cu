@@ -688,10 +688,15 @@ constexpr int kBkMaxBatch = 2;
 constexpr int kBkQ = 10;  // q registers: chunks of four coarse values per event thread
 constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkEvents;
 constexpr int kBkHeader = 2048;  // barriers, flags, dot partials, coefficients, group event sums
-constexpr uint32_t kBkMaxPolls = 1u << 22;  // per wait
+constexpr uint32_t kBkMaxPolls = 1u << 22;    // default bound of a pipeline wait
+constexpr uint32_t kBkDrainPolls = 1u << 24;  // bound of the drain of a CTA that gave up
 static_assert(kBkProducerWarp * 32 + 32 == kBkThreads, "warp roles");
 
 __device__ unsigned int g_wait_timeout_count = 0;
+// Poll bound of the pipeline waits of the bulk kernels, settable from the host
+// (jscc_set_wait_limit): 0 makes every such wait give up at once, which exercises the
+// give-up path while every copy still completes. The drains keep their own fixed bound.
+__device__ uint32_t g_bk_poll_limit = kBkMaxPolls;
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
@@ -715,8 +720,8 @@ __device__ __forceinline__ bool role_sync_or(int id, int count, bool v) {
 }
 
 // bounded wait that also gives up once another thread has flagged an abort
-__device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  for (uint32_t i = 0; i < kBkMaxPolls; ++i) {
+__device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((i & 31u) == 31u && *abort_flag) return false;
   }
@@ -903,6 +908,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
   float* s_grp = reinterpret_cast<float*>(smem + 1024);  // [kBkEvents] event sums of the group
   TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t polls = g_bk_poll_limit;
   const int G = gridDim.x;
   auto bbuf = [&](int k) { return reinterpret_cast<float*>(smem + b_off + (size_t)(k & 1) * b_stride); };
   auto slot = [&](int s) { return reinterpret_cast<const TC*>(smem + slot_off + (size_t)s * slot_stride); };
@@ -987,7 +993,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       }
       if (progress) {
         idle = 0;
-      } else if (++idle > kBkMaxPolls || *abort_flag) {
+      } else if (++idle > polls || *abort_flag) {
         ok = false;
       } else {
         __nanosleep(64);  // neither buffer is free yet: leave the issue slots to the other warps
@@ -1000,8 +1006,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     bool bad = false, aborted = false;
     int kg = 0;
     for (int gi = blockIdx.x; gi < n_groups; gi += G, ++kg) {
-      if (!bk_wait(erow_full, kg & 1, abort_flag)) bad = true;
-      if (kg >= 2 && !bk_wait(b_empty + (kg & 1), ((kg >> 1) - 1) & 1, abort_flag)) bad = true;
+      if (!bk_wait(erow_full, kg & 1, abort_flag, polls)) bad = true;
+      if (kg >= 2 && !bk_wait(b_empty + (kg & 1), ((kg >> 1) - 1) & 1, abort_flag, polls)) bad = true;
       float* b = bbuf(kg);
       if (RS == 4) group_adjoint_ring4<kBkAdj, TE>(b, vc, xs, ring_len, erow, at);
       else group_adjoint_packed<KT, kBkAdj, TE>(b, vc, tp, M, erow, at);
@@ -1042,7 +1048,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       s_next = (MODE == 0 && r0a + et < r0e) ? s_ev[r0a + et] : 0.f;
       if (MODE == 0) s_grp[et] = s_mine;  // read after the first batch barrier
       const float* b = bbuf(kg);
-      if (!bk_wait(b_full + (kg & 1), (kg >> 1) & 1, abort_flag)) bad = true;
+      if (!bk_wait(b_full + (kg & 1), (kg >> 1) & 1, abort_flag, polls)) bad = true;
       float4 qa[kBkQ];
 #pragma unroll
       for (int u = 0; u < kBkQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1059,7 +1065,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k)
           if (k < n) {
-            if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag)) bad = true;
+            if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag, polls)) bad = true;
             cphase ^= 1u << sl[k];
           }
         // ---- dots f_i = t_i . b; BF16 rows stay in registers for the q pass
@@ -1176,8 +1182,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     atomicAdd(&g_wait_timeout_count, 1u);
     // copies still in flight write this CTA's shared memory: wait (bounded) for them
     for (int sq = *rows_used; sq < *rows_issued; ++sq)
-      mbar_wait_bounded(full + sq % n_slots, (sq / n_slots) & 1, kBkMaxPolls);
-    if (*erows_issued > *erows_used) mbar_wait_bounded(erow_full, *erows_used & 1, kBkMaxPolls);
+      mbar_wait_bounded(full + sq % n_slots, (sq / n_slots) & 1, kBkDrainPolls);
+    if (*erows_issued > *erows_used) mbar_wait_bounded(erow_full, *erows_used & 1, kBkDrainPolls);
   }
 }
 
@@ -1264,6 +1270,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   int* used = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 8);
   int* span = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 12);  // [lmin, lmax]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t polls = g_bk_poll_limit;
   const int n_lf = taps.n_lf, n_lc = taps.n_lc;
   const int tiles_per_plane = (n_lf + kScTile - 1) / kScTile;
   const int zf = blockIdx.x / tiles_per_plane;
@@ -1373,7 +1380,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
           const int kk = w - g_begin + k;
           if (lane == 0) {
             if (kk >= n_stages) {
-              ok = bk_wait(empty + s, (eph >> s) & 1u, abort_flag);
+              ok = bk_wait(empty + s, (eph >> s) & 1u, abort_flag, polls);
               eph ^= 1u << s;
             }
             if (ok) {
@@ -1440,7 +1447,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
       uint32_t fph = 0;       // bit s: parity of the next phase of full[s]
       for (int g = g_begin; g < g_end; ++g, s = s + 1 == n_stages ? 0 : s + 1) {
         const int kk = g - g_begin;
-        if (!bk_wait(full + s, (fph >> s) & 1u, abort_flag)) {
+        if (!bk_wait(full + s, (fph >> s) & 1u, abort_flag, polls)) {
           bad = true;
           break;
         }
@@ -1489,7 +1496,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   if (*abort_flag && tid == 0) {
     atomicAdd(&g_wait_timeout_count, 1u);
     for (int kk = *used; kk < *issued; ++kk)
-      mbar_wait_bounded(full + kk % n_stages, (kk / n_stages) & 1, kBkMaxPolls);
+      mbar_wait_bounded(full + kk % n_stages, (kk / n_stages) & 1, kBkDrainPolls);
   }
 }
 
@@ -1929,6 +1936,20 @@ int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int3
                                         : JSCC_GROUPED(__nv_bfloat16, __nv_bfloat16, r);
 #undef JSCC_GROUPED
 }
+
+}  // extern "C"
+
+namespace jscc {
+// Poll bound of the bulk kernels' pipeline waits on the current device (`reset` restores
+// the default).
+int set_bulk_poll_limit(uint32_t polls, bool reset) {
+  const uint32_t v = reset ? kBkMaxPolls : polls;
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_bk_poll_limit, &v, sizeof(v)));
+  return JSCC_OK;
+}
+}  // namespace jscc
+
+extern "C" {
 
 int jscc_take_wait_timeout_count(unsigned int* out) {
   JSCC_REQUIRE(out, "jscc_take_wait_timeout_count: null pointer argument");

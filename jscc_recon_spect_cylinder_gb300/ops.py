@@ -367,9 +367,11 @@ def rdp_prior(img, nbr, weight, gamma=2.0, beta=1.0, eps=1e-9, want_value=True, 
         if grad.numel() != V or grad.dtype != rdt or not grad.is_contiguous():
             raise ValueError(f"grad_out must be a contiguous {rdt} tensor of V elements")
     lib = _lib.load()
-    rc = (lib.jscc_rdp_prior_f64 if f64 else lib.jscc_rdp_prior)(x.data_ptr(), nb.data_ptr(), wt.data_ptr(), V, nb.size(0), float(gamma), float(eps),
-                            float(beta), _lib.ptr(value), _lib.ptr(grad), 1 if (accumulate and grad_out is not None)
-                            else 0, _lib.stream_handle(dev))
+    ws = _lib.workspace.get(dev, lib.jscc_rdp_prior_workspace_bytes(V)) if want_value else None
+    rc = (lib.jscc_rdp_prior_f64 if f64 else lib.jscc_rdp_prior)(
+        x.data_ptr(), nb.data_ptr(), wt.data_ptr(), V, nb.size(0), float(gamma), float(eps), float(beta),
+        _lib.ptr(value), _lib.ptr(grad), 1 if (accumulate and grad_out is not None) else 0, _lib.ptr(ws),
+        0 if ws is None else ws.numel(), _lib.stream_handle(dev))
     _lib.check(rc, "jscc_rdp_prior")
     return value, grad
 
@@ -931,7 +933,7 @@ def sparse_weight_grouped(sysmat, tables: SparseTables, img, rows=None, row_id=N
     ws = _lib.workspace.get(dev, lib.jscc_sparse_grouped_workspace_bytes(n, vf, vc, plan.n_groups,
                                                                          tables.adj_width))
     # S_i = t_i . adj(A_g) depends on the rows and the sysmat only: kept on the plan per sysmat
-    skey = (A.data_ptr(), A._version, A.dtype, tuple(A.shape))
+    skey = (A.data_ptr(), A._version, A.dtype, tuple(A.shape), _lib.timeout_epoch)
     sums = plan.sums.get(skey)
     have = sums is not None
     if not have:

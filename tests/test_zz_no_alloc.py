@@ -21,21 +21,29 @@ pytestmark = pytest.mark.gpu
 TOL_F32 = 1e-5
 
 
-def _call_with_workspace(lib, A, y, x, w, floor=None):
+def _rot_args(rot, inv, n_rot):
+    if rot is None:
+        return None, None, 0
+    return rot.data_ptr(), inv.data_ptr(), rot.stride(0)
+
+
+def _call_with_workspace(lib, A, y, x, w, floor=None, rot=None, inv=None, n_rot=1):
     B, V = A.shape
-    nbytes = lib.jscc_sc_weight_workspace_bytes(B, V, 1)
+    nbytes = lib.jscc_sc_weight_workspace_bytes(B, V, n_rot)
     ws = torch.empty(nbytes, dtype=torch.uint8, device=A.device)
+    rp, ip, ld_rot = _rot_args(rot, inv, n_rot)
     rc = lib.jscc_sc_weight(A.data_ptr(), 0 if A.dtype == torch.float32 else 1, A.stride(0), None, B, V,
-                            y.data_ptr(), y.stride(0), 1, x.data_ptr(), None, None, 0,
+                            y.data_ptr(), y.stride(0), n_rot, x.data_ptr(), rp, ip, ld_rot,
                             1 if floor is not None else 0, floor or 0.0, 1.0, w.data_ptr(), ws.data_ptr(),
                             nbytes, torch.cuda.current_stream().cuda_stream)
     assert rc == 0, lib.jscc_last_error()
 
 
-def _call_noalloc(lib, A, y, x, w, floor=None):
+def _call_noalloc(lib, A, y, x, w, floor=None, rot=None, inv=None, n_rot=1):
     B, V = A.shape
+    rp, ip, ld_rot = _rot_args(rot, inv, n_rot)
     return lib.jscc_sc_weight_noalloc(A.data_ptr(), 0 if A.dtype == torch.float32 else 1, A.stride(0), None, B,
-                                      V, y.data_ptr(), y.stride(0), 1, x.data_ptr(), None, None, 0,
+                                      V, y.data_ptr(), y.stride(0), n_rot, x.data_ptr(), rp, ip, ld_rot,
                                       1 if floor is not None else 0, floor or 0.0, 1.0, w.data_ptr(),
                                       torch.cuda.current_stream().cuda_stream)
 
@@ -67,6 +75,39 @@ def test_noalloc_matches_workspace_entry_two_calls(cuda, lib):
     assert _call_noalloc(lib, A, y, x, w2) == 0
     torch.cuda.synchronize()
     assert torch.equal(w1, w2)
+
+
+def test_noalloc_rotation_blocks_after_direct_call(cuda, lib):
+    """The rotated form (gather through rotmat, scatter back through rotmat_inv) with 8 and
+    then 4 rotations per pass, straight after a one-rotation direct call: the scratch holds
+    up to 8 rotated images and their partial sums, laid out differently for each rotation
+    count, and what a larger call left behind must not leak into a smaller one."""
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    A1, y1, x1 = _problem(cuda, 2048, 4800, 3)
+    w_ref = torch.zeros((4800, 1), device=cuda)
+    _call_with_workspace(lib, A1, y1, x1, w_ref)
+    w = torch.zeros_like(w_ref)
+    assert _call_noalloc(lib, A1, y1, x1, w) == 0, lib.jscc_last_error()
+    torch.cuda.synchronize()
+    assert rel_l2(w.cpu(), w_ref.cpu()) < TOL_F32
+    for views in (8, 4):
+        prob = synthetic.sc_problem(n_r=40, n_theta=120, n_phi=1024, views=views, flat=False, total_counts=1e6)
+        A = prob.sysmat.to(cuda)
+        y = prob.proj.to(cuda).contiguous()          # [bins, views]: column r is view r
+        rot, inv = prob.rotmat.to(cuda), prob.rotmat_inv.to(cuda)
+        x = (torch.rand((A.size(1), 1), generator=torch.Generator().manual_seed(views)) + 0.1).to(cuda)
+        assert lib.jscc_sc_weight_workspace_bytes(A.size(0), A.size(1), views) <= 16 * 1024 * 1024
+        for floor in (None, 1e-12):
+            w_ref = torch.zeros((A.size(1), 1), device=cuda)
+            _call_with_workspace(lib, A, y, x, w_ref, floor, rot, inv, views)
+            w1 = torch.zeros_like(w_ref)
+            w2 = torch.zeros_like(w_ref)
+            assert _call_noalloc(lib, A, y, x, w1, floor, rot, inv, views) == 0, lib.jscc_last_error()
+            assert _call_noalloc(lib, A, y, x, w2, floor, rot, inv, views) == 0, lib.jscc_last_error()
+            torch.cuda.synchronize()
+            assert rel_l2(w1.cpu(), w_ref.cpu()) < TOL_F32
+            assert torch.equal(w1, w2)
 
 
 def test_noalloc_rejects_problems_beyond_scratch(cuda, lib):
