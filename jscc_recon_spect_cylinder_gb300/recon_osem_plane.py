@@ -313,6 +313,53 @@ def run_recon_osem(sysmat_all, rotmat_all, rotmat_inv_all, proj_all, proj_d_all,
              img_jsccsd_iter, iter_arg, save_path)
 
 
+WORKER_POLL_S = 1.0  # how often a wait for worker results checks that the workers are alive
+
+
+def collect_worker_weights(weight_queue, procs, count, what):
+    """``count`` weight images from ``weight_queue``, in arrival order. Instead of blocking
+    forever on a worker that died (the reference's ``weight_queue.get()``), the wait checks
+    the workers every WORKER_POLL_S seconds: a worker that exited with a non-zero code, or
+    exited while results are still owed, stops every worker and raises RuntimeError, as the
+    reference's entry points do for their T-builder workers (main_plane_sparse.py:194-203)."""
+    import queue as _queue
+
+    out = []
+    while len(out) < count:
+        try:
+            out.append(weight_queue.get(timeout=WORKER_POLL_S))
+            continue
+        except _queue.Empty:
+            pass
+        dead = [(g, p.exitcode) for g, p in enumerate(procs) if p.exitcode is not None and p.exitcode != 0]
+        if not dead and all(p.exitcode is not None for p in procs):
+            dead = [(g, p.exitcode) for g, p in enumerate(procs)]
+        if dead:
+            stop_workers(procs)
+            g, code = dead[0]
+            raise RuntimeError(f"{what} worker {g} exited with code {code} while {count - len(out)} of {count} "
+                               "weight images were still owed")
+    return out
+
+
+def stop_workers(procs, timeout=5.0):
+    """Terminate and reap every worker that is still running."""
+    for p in procs:
+        if p.is_alive():
+            p.terminate()
+    for p in procs:
+        p.join(timeout)
+
+
+def join_workers(procs, what):
+    """Join the workers and raise if any exited with a non-zero code."""
+    for g, p in enumerate(procs):
+        p.join()
+        if p.exitcode != 0:
+            stop_workers(procs)
+            raise RuntimeError(f"{what} worker {g} exited with code {p.exitcode}")
+
+
 def _run_multi_gpu_compton(t_list_all, sysmat_list_all, proj_list_all, rotmat_all, rotmat_inv_all, img_jsccd,
                            img_jsccsd, s_map_arg, alpha, iter_arg, num_gpus, rotate_num, img_jsccd_iter,
                            img_jsccsd_iter, model_denoiser):
@@ -333,8 +380,8 @@ def _run_multi_gpu_compton(t_list_all, sysmat_list_all, proj_list_all, rotmat_al
                 for _ in range(num_gpus):
                     img_queue.put(img)
                 w_c = torch.zeros_like(img)
-                for _ in range(num_gpus):
-                    w_c = w_c + weight_queue.get()
+                for w in collect_worker_weights(weight_queue, procs, num_gpus, "list-mode OSEM"):
+                    w_c = w_c + w
                 if joint:
                     w_s = torch.zeros_like(img)
                     _accumulate_sc(w_s, sysmat_list_all[s], proj_list_all[s], rotmat_all, rotmat_inv_all,
@@ -346,8 +393,7 @@ def _run_multi_gpu_compton(t_list_all, sysmat_list_all, proj_list_all, rotmat_al
             if (it + 1) % step == 0:
                 snapshots[k, :] = torch.squeeze(img).cpu()
                 k += 1
-        for p in procs:
-            p.join()
+        join_workers(procs, "list-mode OSEM")
         return img
 
     img_jsccd = phase(iter_arg.jsccd, img_jsccd, img_jsccd_iter, joint=False)

@@ -17,6 +17,7 @@ import torch.multiprocessing as mp
 
 from . import compton_sparse_ops as cso
 from . import ops
+from .recon_osem_plane import collect_worker_weights, join_workers
 from .recon_osem_plane import (  # noqa: F401  (re-exported, as the reference does)
     get_gpu_memory_usage,
     get_t_budget_bytes_per_gpu,
@@ -196,8 +197,8 @@ def run_recon_osem_sparse(sysmat_all, rotmat_all, rotmat_inv_all, proj_all, proj
                     for _ in range(num_gpus):
                         img_queue.put(img)
                     w_c = torch.zeros_like(img)
-                    for _ in range(num_gpus):
-                        w_c = w_c + weight_queue.get()
+                    for w in collect_worker_weights(weight_queue, procs, num_gpus, "sparse list-mode OSEM"):
+                        w_c = w_c + w
                     if joint:
                         w_s = torch.zeros_like(img)
                         for sysmat, proj, rotmat, rotmat_inv in zip(sysmat_list_all[s], proj_list_all[s], rotmat_all,
@@ -210,8 +211,7 @@ def run_recon_osem_sparse(sysmat_all, rotmat_all, rotmat_inv_all, proj_all, proj
                 if (it + 1) % step == 0:
                     snaps[k, :] = torch.squeeze(img).cpu()
                     k += 1
-            for p in procs:
-                p.join()
+            join_workers(procs, "sparse list-mode OSEM")
             return img
 
         img_jsccd = mp_phase(iter_arg.jsccd, img_jsccd, img_jsccd_iter, joint=False)

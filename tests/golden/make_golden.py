@@ -322,12 +322,167 @@ def golden_sensitivity(ref):
          sc_codes=codes.numpy(), sc_s=s.numpy())  # rotation tables: sparse_ops r10_rotmat_inv
 
 
+# ----------------------------------------------------------------------------- runners
+class _CudaAsCpu:
+    """Runs the reference's runners, which pin "cuda:0" (recon_osem_plane.py:168-171,
+    recon_osem_plane_sparse.py:150-153), on the CPU: every tensor / projector move to a CUDA
+    device stays on the CPU, the T-memory budget is unbounded (so nothing is pinned) and the
+    GPU memory report is skipped. The runners' own code (staging, permutation, phase order,
+    snapshots, save_img) runs unchanged."""
+
+    def __init__(self, ref):
+        self.mods = [ref["recon_osem_plane"], ref["recon_osem_plane_sparse"]]
+
+    @staticmethod
+    def _cuda(a):
+        return (isinstance(a, str) and a.startswith("cuda")) or (isinstance(a, torch.device) and a.type == "cuda")
+
+    def __enter__(self):
+        self.orig_to = torch.Tensor.to
+        orig_to = self.orig_to
+        cuda = self._cuda
+
+        def to(t, *args, **kwargs):
+            args = tuple("cpu" if cuda(a) else a for a in args)
+            if cuda(kwargs.get("device")):
+                kwargs["device"] = "cpu"
+            return orig_to(t, *args, **kwargs)
+
+        torch.Tensor.to = to
+        self.saved = []
+        for m in self.mods:
+            for name, fn in (("get_t_budget_bytes_per_gpu", lambda n: [1 << 62] * n),
+                             ("get_gpu_memory_usage", lambda n: None)):
+                self.saved.append((m, name, getattr(m, name)))
+                setattr(m, name, fn)
+        return self
+
+    def __exit__(self, *exc):
+        torch.Tensor.to = self.orig_to
+        for m, name, fn in self.saved:
+            setattr(m, name, fn)
+        return False
+
+
+def _read_images(path, names):
+    return {n: np.fromfile(path / n, dtype=np.float32) for n in names}
+
+
+def golden_runners(ref):
+    """The reference's four runners on small seeded problems, with the files they write:
+    run_recon_osem (dense T, recon_osem_plane.py:161-403) and run_recon_osem_sparse
+    (recon_osem_plane_sparse.py:144-348) on one GPU's path, run on the CPU through
+    _CudaAsCpu; run_recon_osem_local_cntstat (recon_osem_local_cntstat.py:56-100) and
+    run_recon_osem_local_sparse_jsccsd_only (recon_osem_local_sparse_jsccsd_only.py:111-202)
+    with device=cpu. Two energies, two rotations, 3 subsets, 2 divides, snapshots every 2
+    iterations. The global and per-runner permutations are recorded so that tests replay
+    them (the local runners draw theirs on the device they run on)."""
+    import tempfile
+    from types import SimpleNamespace
+
+    rop = ref["recon_osem_plane"]
+    rsp = ref["recon_osem_plane_sparse"]
+    cso = ref["compton_sparse_ops"]
+    lcs = ref["recon_osem_local_cntstat"]
+    ljs = ref["recon_osem_local_sparse_jsccsd_only"]
+    E, R, S, D = 2, 2, 3, 2
+    probs = [synthetic.sc_problem(n_r=6, n_theta=24, disk_radius=20.0, n_phi=48, views=R, flat=False,
+                                  total_counts=2e4, seed=synthetic.SEED + 10 + e) for e in range(E)]
+    V = probs[0].grid.n_vox
+    B = probs[0].sysmat.size(0)
+    g = torch.Generator().manual_seed(404)
+    sysmat = [p.sysmat.clone() for p in probs]
+    rot = [p.rotmat.clone() for p in probs]
+    inv = [p.rotmat_inv.clone() for p in probs]
+    proj = [p.proj.clone() for p in probs]
+    proj_d = [torch.poisson(p.proj, generator=g) for p in probs]
+    s = sum(p.s_map for p in probs)
+    d = torch.rand((V, 1), generator=g) + 0.5
+    # dense T per energy and rotation (normalised rows, uneven counts)
+    t_dense = []
+    for e in range(E):
+        blocks = []
+        for r in range(R):
+            t = torch.rand((23 + 7 * e + 3 * r, V), generator=g) ** 4
+            blocks.append(t / t.sum(dim=1, keepdim=True))
+        t_dense.append(blocks)
+    # sparse packed rows per energy and rotation (cp1 indexes the SC matrix rows, 1-based)
+    proj_sp = cso.build_compton_sparse_projector(probs[0].grid.coor, theta_stride=4, z_stride=1, rotate_num=R)
+    vc = proj_sp.coarse_pixel_num
+    t_sparse = []
+    for e in range(E):
+        blocks = []
+        for r in range(R):
+            n = 31 + 5 * e + 4 * r
+            cp1 = torch.randint(1, B + 1, (n,), generator=g)
+            tc = torch.rand((n, vc), generator=g) ** 3
+            blocks.append(cso.pack_sparse_event_rows(cp1, tc))
+        t_sparse.append(blocks)
+    iter_arg = SimpleNamespace(sc=4, jsccd=4, jsccsd=4, save_iter_step=2, osem_subset_num=S, t_divide_num=D,
+                               ene_num=E, mode=0, seed=20260331)
+    alpha = 0.5
+    names = ["Image_SC", "Image_SCD", "Image_JSCCD", "Image_JSCCSD", "Image_SC_Iter_4_2", "Image_SCD_Iter_4_2",
+             "Image_JSCCD_Iter_4_2", "Image_JSCCSD_Iter_4_2"]
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp, torch.no_grad():
+        tmp = Path(tmp)
+        for tag, runner, t_all, extra in (("dense", rop.run_recon_osem, t_dense, ()),
+                                          ("sparse", rsp.run_recon_osem_sparse, t_sparse, ([proj_sp, proj_sp],))):
+            torch.manual_seed(2718)
+            perm = torch.randperm(B)
+            torch.manual_seed(2718)
+            smap = SimpleNamespace(s=s.clone(), d=d.clone())
+            path = tmp / tag
+            path.mkdir()
+            with _CudaAsCpu(ref):
+                runner([a.clone() for a in sysmat], [r.clone() for r in rot], [r.clone() for r in inv],
+                       [p.clone() for p in proj], [p.clone() for p in proj_d], [[t.clone() for t in ts] for ts in t_all],
+                       *extra, iter_arg, smap, alpha, str(path) + "/", 1)
+            for n, a in _read_images(path, names).items():
+                out[f"{tag}_{n}"] = a
+            out[f"{tag}_perm"] = perm.numpy()
+        # local runners: device = cpu, CPU generator; the permutations of every iteration
+        for tag in ("cntstat", "jsccsd"):
+            gen = torch.Generator().manual_seed(iter_arg.seed)
+            n_it = iter_arg.sc if tag == "cntstat" else iter_arg.jsccsd
+            out[f"{tag}_perms"] = np.stack([torch.randperm(B, generator=gen).numpy() for _ in range(n_it)])
+        path = tmp / "cntstat"
+        path.mkdir()
+        try:
+            lcs.run_recon_osem_local_cntstat([a.clone() for a in sysmat], [r.clone() for r in rot],
+                                             [r.clone() for r in inv], [p.clone() for p in proj], iter_arg,
+                                             SimpleNamespace(s=s.clone()), str(path) + "/", torch.device("cpu"))
+        except NameError:
+            pass  # the runner returns an undefined name after writing its files (recon_osem_local_cntstat.py:100)
+        for n, a in _read_images(path, ["Image_SC", "Image_SC_Iter_4_2"]).items():
+            out[f"cntstat_{n}"] = a
+        path = tmp / "jsccsd"
+        path.mkdir()
+        j = alpha * s + (2 - alpha) * d
+        t_local = [[t.clone() for t in ts] for ts in t_sparse]
+        ljs.run_recon_osem_local_sparse_jsccsd_only([a.clone() for a in sysmat], [a.clone() for a in sysmat],
+                                                    [r.clone() for r in rot], [r.clone() for r in inv],
+                                                    [p.clone() for p in proj], t_local, [proj_sp, proj_sp], iter_arg,
+                                                    SimpleNamespace(j=j.clone()), alpha, str(path) + "/",
+                                                    torch.device("cpu"))
+        for n, a in _read_images(path, ["Image_JSCCSD", "Image_JSCCSD_Iter_4_2"]).items():
+            out[f"jsccsd_{n}"] = a
+    save("runners", sysmat=np.stack([_np(a) for a in sysmat]), rot=np.stack([_np(r) for r in rot]),
+         inv=np.stack([_np(r) for r in inv]), proj=np.stack([_np(p) for p in proj]),
+         proj_d=np.stack([_np(p) for p in proj_d]), s=_np(s), d=_np(d), coor=_np(probs[0].grid.coor),
+         **{f"t_dense_{e}_{r}": _np(t_dense[e][r]) for e in range(E) for r in range(R)},
+         **{f"t_sparse_{e}_{r}": _np(t_sparse[e][r]) for e in range(E) for r in range(R)},
+         iter_arg=np.array([iter_arg.sc, iter_arg.jsccd, iter_arg.jsccsd, iter_arg.save_iter_step, S, D, E]),
+         alpha=np.array(alpha), **out)
+
+
 GENERATORS = {
     "sc_osem": golden_sc,
     "dense_compton": golden_dense_compton,
     "compton_builders": golden_compton,
     "sparse_ops": golden_sparse,
     "sensitivity": golden_sensitivity,
+    "runners": golden_runners,
 }
 
 
