@@ -822,8 +822,22 @@ class SparseLaunchBench:
         return {}
 
 
+JOINT_METRIC = ("OSEM subset-iters/s: BF16-stored vs plain FP32 joint JSCCSD (SC + sparse Compton, config 3), "
+                "1xGB300")
+
+
+def joint_config(name, bins, voxels, coarse, listed, kept, subsets, groups, alpha, views):
+    """The `config` of the joint workload, the same dict on both arms."""
+    return {"workload": name, "sc_bins": bins, "voxels": voxels, "coarse_voxels": coarse,
+            "compton_events_listed": listed, "compton_events_kept": kept, "subsets": subsets,
+            "groups_per_subset": groups, "alpha": alpha, "views": views,
+            "l2": "inputs larger than L2 (no flush)", "parallelism": "single"}
+
+
 class JointBench:
     """workloads.JointWorkload behind the bench interface."""
+
+    storage = "bf16 system matrix + bf16 sparse rows (int32 ids split out); fp32 arm: fp32 matrix + packed fp32 rows"
 
     def __init__(self, dev, small=False):
         from jscc_recon_spect_cylinder_gb300 import workloads
@@ -831,8 +845,7 @@ class JointBench:
         kw = dict(views=2, n_events=60000, subsets=2) if small else {}
         self.w = workloads.JointWorkload(dev, **kw)
         self.name = "jsccsd-config3" if not small else "jsccsd-small"
-        self.metric = ("OSEM subset-iters/s: BF16-stored vs plain FP32 joint JSCCSD (SC + sparse Compton, "
-                       "config 3), 1xGB300")
+        self.metric = JOINT_METRIC
         self.traffic_file = "traffic_jsccsd3.json"
         self.dev = dev
         self.small = small
@@ -852,12 +865,8 @@ class JointBench:
 
     def config(self):
         w = self.w
-        return {"workload": self.name, "sc_bins": w.B, "voxels": w.V, "coarse_voxels": w.Vc,
-                "compton_events_listed": w.n_list, "compton_events_kept": w.n_events, "subsets": w.subsets,
-                "groups_per_subset": round(w.group_count(), 1),
-                "alpha": w.alpha, "views": w.views,
-                "storage": "bf16 system matrix + bf16 sparse rows (int32 ids split out)",
-                "l2": "inputs larger than L2 (no flush)"}
+        return joint_config(self.name, w.B, w.V, w.Vc, w.n_list, w.n_events, w.subsets, round(w.group_count(), 1),
+                            w.alpha, w.views)
 
     def fp64_reference(self, iters):
         return self.w.fp64_reference(iters)
@@ -866,8 +875,28 @@ class JointBench:
         pairs = self.w.pair_count_per_step()
         out = {"compton_event_voxel_pairs_per_s": pairs / (ms_per_step / 1e3)}
         if not self.small:
+            out["plain_fp32_gpu_reference"] = self.plain_fp32_gpu_reference()
+            ref = out["plain_fp32_gpu_reference"]
+            if "value" in ref:
+                out["speedup_vs_plain_fp32_gpu"] = self.units_per_step() / (ms_per_step / 1e3) / ref["value"]
             out["batched_config4"] = batched_summary(self.dev)
         return out
+
+    def plain_fp32_gpu_reference(self):
+        """The reference's own PyTorch FP32 joint loop on this GPU (whole subset updates of
+        the same workload, its float32 inputs), and how far its image after one subset update
+        is from the product's float32 path from the same start."""
+        from oracle import reference_timing as rt
+
+        torch.cuda.empty_cache()
+        res = rt.run_gpu_plain_fp32(self.w)
+        img = res.pop("image", None)
+        if img is not None:
+            ours = self.w.subset_update(torch.ones((self.w.V, 1), device=self.dev), 0, "f32")
+            d = (ours.double() - img.double())
+            res["image_rel_l2_vs_product_fp32_after_one_subset"] = float(d.norm() / img.double().norm())
+        torch.cuda.empty_cache()
+        return res
 
     def e2e(self, iters):
         """One job with host inputs: pinned host copies of the BF16 system matrix (also the
@@ -906,53 +935,18 @@ class JointBench:
         sec = time.perf_counter() - t0
         return {"value": iters * w.subsets / sec, "unit": "subset-iters/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(w.V * 4),
-                "step": f"one job: stage inputs + {iters} iterations + read image", "seconds": sec}
+                "step": (f"one job: stage inputs + {iters} iterations + read image (the sparse T rows are built "
+                         "beforehand by the GPU T builder, outside the timed job)"), "seconds": sec}
 
-    def cpu_rate(self, budget_s=20.0):
-        """Oracle port on the host cores for one subset update: the SC half with numpy
-        float32 BLAS on subset 0's rows, the Compton half with the oracle's sparse (scipy)
-        restatement of the materialise weight on a sample of subset 0's events, scaled to
-        the subset's event count."""
-        from oracle import osem_sc
-        from oracle import sparse as osp
-        import scipy.sparse as sp
+    def cpu_rate(self, steps=2, warmup=1):
+        """The reference's own functions on the host cores (oracle.reference_timing): whole-
+        subset SC half, sampled Compton half; a bounded run of a few steps."""
+        from oracle import reference_timing as rt
 
-        w = self.w
-        ids = w.subset_ids[0]
-        A = w.A["f32"][ids].cpu().numpy()
-        y = w.proj[ids].cpu().numpy()
-        x = np.ones((w.V, 1), dtype=np.float32)
-        ptr, idx, val = (t.cpu().numpy() for t in w.tables.up[1])
-        U = sp.csr_matrix((val.astype(np.float64), idx, ptr), shape=(w.tables.n_lf, w.tables.n_lc))
-        rows = w.rows_f32[0]
-        n_sample = min(rows.size(0), 2000)
-        sample = rows[torch.randperm(rows.size(0), generator=torch.Generator(device=w.dev).manual_seed(0),
-                                     device=w.dev)[:n_sample]].cpu().numpy()
-        Afull = w.A["f32"]
-        eff = Afull[torch.from_numpy(np.clip(np.round(sample[:, 0]).astype(np.int64) - 1, 0, Afull.size(0) - 1))
-                    .to(w.dev)].cpu().numpy()
-        sample_local = sample.copy()
-        sample_local[:, 0] = np.arange(1, n_sample + 1)
-        t_sc = t_c = 0.0
-        n = 0
-        t_start = time.perf_counter()
-        while True:
-            t0 = time.perf_counter()
-            osem_sc.get_weight_single(A, y, x, floor=1e-12, dtype=np.float32)
-            t1 = time.perf_counter()
-            osp.weight_materialize_csr(sample_local, eff, x, U, dtype=np.float32)
-            t2 = time.perf_counter()
-            t_sc += t1 - t0
-            t_c += (t2 - t1) * (rows.size(0) / n_sample)
-            n += 1
-            if time.perf_counter() - t_start >= budget_s or n >= 20:
-                break
-        per_update = (t_sc + t_c) / n
-        return {"value": 1.0 / per_update, "unit": "subset-iters/s", "cores": os.cpu_count(), "kind": "port",
-                "sample": (f"{n} x (SC half on subset 0: {A.shape[0]} x {A.shape[1]} float32 numpy BLAS; Compton "
-                           f"half: materialise weight of {n_sample} of the subset's {rows.size(0)} events with a "
-                           f"scipy sparse upsample, scaled by events)"),
-                "seconds": time.perf_counter() - t_start}
+        r = rt.run_host(steps, warmup)
+        return {"value": r["value"], "unit": r["unit"], "cores": r["cores"], "cpu_model": r["cpu_model"],
+                "kind": r["kind"], "sample": r["sample"], "seconds_per_subset_update": r["seconds_per_subset_update"],
+                "parts_s": r["parts_s"]}
 
 
 def batched_summary(dev, steps=5):
@@ -1065,25 +1059,34 @@ def image_errors(ref64, images):
 
 # ----------------------------------------------------------------------------- arms
 def reference_arm(args):
+    """The reference's own CPU implementation of the joint subset update on this machine's
+    host cores (oracle.reference_timing: the staged reference modules, else the oracle's
+    numpy port). No kernel of this repository runs and its library is not loaded: the inputs
+    are built on the host. Each step is one bounded sample of the workload (the SC half on a
+    whole subset, the Compton half on a fixed sample of whole groups); `value` is the
+    resulting subset-update rate and `ms_per_step` the wall time a step actually took."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
-    work = make_workload(args.workload, dev)
-    rates = []
-    for i in range(args.warmup + args.steps):
-        r = work.cpu_rate(budget_s=max(2.0, 60.0 / max(1, args.steps + args.warmup)))
-        if i >= args.warmup:
-            rates.append(r["value"])
-    value = float(np.median(rates))
+    if args.workload != "jsccsd3":
+        print(json.dumps({"impl": "reference", "unavailable": f"no reference arm for workload {args.workload}"}))
+        return
+    from oracle import reference_timing as rt
+
+    c = rt.CONFIG3
+    r = rt.run_host(args.steps, args.warmup)
     line = {
-        "impl": "reference", "metric": work.metric, "value": value, "unit": "subset-iters/s", "n_gpus": 0,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * work.subsets / value,
+        "impl": "reference", "metric": JOINT_METRIC, "value": r["value"], "unit": r["unit"], "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": work.config(),
-        "cpu_baseline": {"value": value, "unit": "subset-iters/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": r["sample"]},
-        "e2e": {"value": value, "unit": "subset-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": joint_config("jsccsd-config3", c["views"] * c["n_phi"] * c["n_axial"], c["n_r"] * c["n_theta"],
+                               c["n_r"] * c["n_theta"] // c["theta_stride"], c["events_listed"], c["events_kept"],
+                               c["subsets"], c["groups_per_subset"], c["alpha"], c["views"]),
+        "cpu_baseline": {"value": r["value"], "unit": r["unit"], "cores": r["cores"], "cpu_model": r["cpu_model"],
+                         "kind": r["kind"], "sample": r["sample"]},
+        "seconds_per_subset_update": r["seconds_per_subset_update"], "parts_s": r["parts_s"],
+        "setup_s": r["setup_s"],
+        "e2e": {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
@@ -1148,12 +1151,15 @@ def ours_arm(args):
             errors = image_errors(work.fp64_reference(err_iters), imgs)
         e2e = work.e2e(30) if not args.no_e2e and hasattr(work, "e2e") else None
         cpu = work.cpu_rate() if (world == 1 and not args.no_cpu_baseline and hasattr(work, "cpu_rate")) else None
+        cfg = work.config()
+        cfg["parallelism"] = "replicas" if world > 1 else "single"
         line = {
             "metric": work.metric, "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_main / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": dtypes[0], "data": "synthetic",
-            "config": dict(work.config(), parallelism="replicas" if world > 1 else "single"),
+            "vs_baseline": None, "dtype": dtypes[0], "data": "synthetic", "config": cfg,
         }
+        if hasattr(work, "storage"):
+            line["storage"] = work.storage
         if second is not None:
             line[dtypes[1] if dtypes[1] != "f32" else "fp32"] = second
             line["speedup_bf16_vs_fp32"] = value / second["value"]

@@ -131,19 +131,22 @@ class JointWorkload:
         torch.cuda.synchronize(device)
 
     # -------------------------------------------------------------------------------- step
+    def subset_update(self, img, s, dtype="bf16"):
+        """One subset update: w = alpha w_SC + (2 - alpha) w_Compton, safe EM update."""
+        A_eff = self.A[dtype]
+        w = torch.zeros_like(img)
+        ops.sc_weight(A_eff, self.proj, img, floor=1e-12, scale=self.alpha, out=w, row_idx=self.subset_ids[s])
+        if dtype == "bf16":
+            ops.sparse_weight_split(self.ids[s], self.tc_bf16[s], A_eff, self.tables, img, grouped=False,
+                                    scale=2 - self.alpha, out=w)
+        else:
+            ops.sparse_weight(self.rows_f32[s], A_eff, self.tables, img, grouped=False, scale=2 - self.alpha, out=w)
+        return ops.em_update(img, w, self.s_joint, safe=True)
+
     def step(self, img, dtype="bf16"):
         """One OSEM iteration (every subset updated once)."""
-        A_eff = self.A[dtype]
         for s in range(self.subsets):
-            w = torch.zeros_like(img)
-            ops.sc_weight(A_eff, self.proj, img, floor=1e-12, scale=self.alpha, out=w, row_idx=self.subset_ids[s])
-            if dtype == "bf16":
-                ops.sparse_weight_split(self.ids[s], self.tc_bf16[s], A_eff, self.tables, img, grouped=False,
-                                        scale=2 - self.alpha, out=w)
-            else:
-                ops.sparse_weight(self.rows_f32[s], A_eff, self.tables, img, grouped=False, scale=2 - self.alpha,
-                                  out=w)
-            img = ops.em_update(img, w, self.s_joint, safe=True)
+            img = self.subset_update(img, s, dtype)
         return img
 
     def fp64_reference(self, iters):
