@@ -687,19 +687,20 @@ class Batch4JointBench(Batch4Bench):
     their own at 511 keV (events log-uniform in 50k-2M listed per instance, forward-simulated
     from the instance's phantom on the view-0 scatter cylinder and a 150 mm absorber, energies
     blurred as in config 2), alpha = 0.5, 8 subsets. One step = one joint OSEM iteration of
-    every instance: SC weights from the batched tensor-core GEMMs, each instance's Compton
-    weight from the fused cone kernels over its subset events, the safe joint EM update with
-    per-instance sensitivities (the Compton sensitivity rescaled as build_sparse_sensi_d does).
-    Launched kernel by kernel (the per-instance cone launches are not captured)."""
+    every instance: SC weights from the batched tensor-core GEMMs, the Compton weights of all
+    64 instances from one batched fused-cone launch per direction over the subset's events
+    (device segment tables), the safe joint EM update with per-instance sensitivities (the
+    Compton sensitivity rescaled as build_sparse_sensi_d does); the iteration is replayed as
+    one captured CUDA graph."""
 
-    CAPTURE = False
+    CAPTURE = True
 
     def __init__(self, dev, n_inst=64, views=20, subsets=8, seed=None, ev_range=(5e4, 2e6)):
         self.ev_range = ev_range
         super().__init__(dev, n_inst=n_inst, views=views, subsets=subsets, seed=seed)
         self.name = "batched-joint-config4"
         self.metric = ("joint OSEM subset-iters/s summed over 64 instances: batched SC tensor-core GEMMs + "
-                       "per-instance fused Compton cone, config 4, 1xGB300")
+                       "batched fused Compton cone, config 4, 1xGB300")
 
     def _make_batch(self, A, grid, X_true, counts, gen, gc):
         from jscc_recon_spect_cylinder_gb300 import batched, ops, synthetic
@@ -733,38 +734,115 @@ class Batch4JointBench(Batch4Bench):
             events.append(ev.split(self.subsets))
             del lst, noise
         self.n_kept = sum(sum(len(b) for b in ev_n) for ev_n in events)
-        return batched.BatchedJointOsem(A, self.ids, torch.stack(S), events, coor, alpha=0.5, device=self.dev)
-
-    def step(self, img, dtype):
-        self.bat.iterate(1)
-        return img
-
-    def step_eager(self, img, dtype):
-        return self.step(img, dtype)
+        self.events, self.S_joint, self.coor, self.n_ev_listed = events, torch.stack(S), coor, n_ev
+        return batched.BatchedJointOsem(A, self.ids, self.S_joint, events, coor, alpha=0.5, device=self.dev)
 
     def config(self):
         c = super().config()
         c.update({"workload": self.name, "compton_events_listed": self.n_listed, "compton_events_kept": self.n_kept,
-                  "compton_events_per_instance": "log-uniform 5e4-2e6 listed", "alpha": 0.5, "graph": False})
+                  "compton_events_per_instance": "log-uniform 5e4-2e6 listed", "alpha": 0.5,
+                  "sc_kev": 140, "compton_kev": 511, "graph": True})
         return c
+
+    def _joint_step_fp(self, n, x, dtype=torch.float32):
+        """One joint iteration of instance n alone on the FP32 matrix (the original bin order):
+        float32 through the library (jscc_sc_weight + jscc_compton_weight + safe EM), or, for
+        float64 images, the library's FP64 projector halves (the reference definitions with every
+        sum in double) and float64 SC products."""
+        from jscc_recon_spect_cylinder_gb300 import ops
+
+        y = self.Y[n].reshape(-1, 1)
+        s = self.S_joint[n].reshape(-1, 1)
+        for k in range(self.subsets):
+            ids = self.ids[k].to(self.dev)
+            ev = self.events[n][k]
+            if dtype == torch.float32:
+                w = torch.zeros_like(x)
+                ops.sc_weight(self.A32, y, x, floor=1e-12, scale=0.5, out=w, row_idx=ids)
+                if len(ev):
+                    ops.compton_weight(ev.records, ev.row_id, self.coor, x, model=ev.model, eff=self.A32, scale=1.5,
+                                       out=w)
+                x = ops.em_update(x, w, s, safe=True)
+            else:
+                As = self.A32[ids].double()
+                w = 0.5 * (As.T @ (y[ids].double() / torch.clamp(As @ x, min=1e-12)))
+                if len(ev):
+                    f = ops.compton_project(ev.records, ev.row_id, self.coor, x, model=ev.model, eff=self.A32)
+                    w = w + 1.5 * ops.compton_backproject(ev.records, ev.row_id, self.coor,
+                                                          1.0 / f.reshape(-1), model=ev.model,
+                                                          eff=self.A32).reshape(-1, 1)
+                w = torch.nan_to_num(w, nan=0.0, posinf=0.0, neginf=0.0)
+                sd = s.double()
+                valid = sd > 1e-12
+                x = torch.where(valid, x * torch.clamp(w, min=0.0) / torch.where(valid, sd, torch.ones_like(sd)),
+                                torch.zeros_like(x))
+        return x
+
+    def _sequential_fp32(self, iters=1):
+        """The plain FP32 single-instance joint path run for the 64 instances one after the
+        other: subset-iterations/s summed over the instances."""
+        xs = [torch.ones((self.V, 1), device=self.dev) for _ in range(self.n_inst)]
+        self._joint_step_fp(0, xs[0])  # warm-up (workspaces, cached event orders)
+        torch.cuda.synchronize(self.dev)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(iters):
+            for n in range(self.n_inst):
+                xs[n] = self._joint_step_fp(n, xs[n])
+        t1.record()
+        torch.cuda.synchronize(self.dev)
+        return self.n_inst * self.subsets / (t0.elapsed_time(t1) / iters / 1e3)
+
+    def _errors(self, iters=2, max_listed=4e5, n_pick=4):
+        """Per-instance relative L2 / max-voxel error of the batched BF16 path after `iters`
+        iterations from x = 1 against a float64 joint OSEM on the FP32 matrix, for `n_pick`
+        instances spread over the event counts up to `max_listed` listed events (the float64
+        cone evaluation costs seconds per 100k events)."""
+        order = [int(i) for i in torch.argsort(self.n_ev_listed) if self.n_ev_listed[i] <= max_listed]
+        pick = sorted({order[int(round(q * (len(order) - 1)))] for q in np.linspace(0, 1, n_pick)}) if order else []
+        self.bat.set_images(torch.ones((self.n_inst, self.V)))
+        X = self.bat.iterate(iters).double().clone()
+        self.bat.set_images(torch.ones((self.n_inst, self.V)))
+        rel, mx = [], []
+        for n in pick:
+            x64 = torch.ones((self.V, 1), dtype=torch.float64, device=self.dev)
+            for _ in range(iters):
+                x64 = self._joint_step_fp(n, x64, torch.float64)
+            x64 = x64.reshape(-1)
+            rel.append(float((X[n] - x64).norm() / x64.norm()))
+            mx.append(float((X[n] - x64).abs().max() / x64.abs().max()))
+        return {"iterations": iters, "instances": pick, "listed_events": [int(self.n_ev_listed[n]) for n in pick],
+                "rel_l2": rel, "max_voxel_rel": mx,
+                "rel_l2_median": float(np.median(rel)) if rel else None, "rel_l2_max": max(rel) if rel else None,
+                "reference": "float64 joint OSEM per instance on the FP32 matrix (float64 SC products, the "
+                             "library's FP64 cone projector halves)"}
 
     def kernel_bytes(self, dtype):
         return {}  # the step is the cone passes' (FP32): the roofline below, not an HBM one
 
     def extra(self, ms_per_step):
-        """Cone pairs per second over the whole step (the cone kernels take ~99.8 % of it) and
-        the FP32 roofline at Cone2Bench's 100 operations per pair."""
+        """Cone pairs per second over the whole step (the cone kernels take nearly all of it),
+        the FP32 roofline at Cone2Bench's operations per pair, the plain FP32 single-instance
+        joint path run for the 64 instances in turn, and per-instance errors against float64."""
         pairs = 2 * self.n_kept * self.V  # forward + back cone pairs per iteration
         rate = pairs / (ms_per_step / 1e3)
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         achieved = rate * Cone2Bench.K_CONE / 1e12
+        value = self.units_per_step() / (ms_per_step / 1e3)
+        seq = self._sequential_fp32()
         return {"compton_pairs_per_s": rate,
                 "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                                   "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
-                                  "flop_per_pair": Cone2Bench.K_CONE, "over": "the whole step"}}
+                                  "flop_per_pair": Cone2Bench.K_CONE, "over": "the whole step"},
+                "sequential_fp32_joint_64_instances": {"subset_iters_per_s": seq,
+                                                       "batched_speedup_vs_64_sequential": value / seq},
+                "errors_vs_fp64": self._errors()}
 
     def e2e(self, iters):
-        return None
+        """Batch4Bench's job (projections and initial images staged from pinned host memory,
+        the captured iterations, images read back) with at most two iterations: one joint
+        iteration of the 64 instances takes seconds."""
+        return super().e2e(min(iters, 2))
 
 
 class SparseLaunchBench:

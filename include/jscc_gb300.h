@@ -271,6 +271,32 @@ JSCC_API int jscc_compton_weight(const float* records, const int32_t* row_id, in
 JSCC_API int jscc_take_bad_detector_count(unsigned int* out);
 
 /*
+ * jscc_compton_weight (strict model, every pair) for several instances in one launch per
+ * direction: instance b's events reweight its own image, W[b] += scale * T_b^T (1 / T_b X[b])
+ * (recon_osem_plane.py:33-42 per instance, as the joint loops use it, with T recomputed on the
+ * fly). The events of all instances are concatenated; the device tables describe the segments:
+ *   event_inst  [n_ev]          instance of each event, -1 for padding events (no contribution)
+ *   block_inst  [n_ev / 16]     instance of each 16-event forward block (each block holds events of
+ *                               one instance and padding only; pad every instance to a multiple of 16)
+ *   chunk_range [n_chunks + 1]  event offsets of the back-projection chunks (a chunk holds events
+ *                               of one instance only)
+ *   inst_chunk  [n_inst + 1]    chunk offsets of each instance (its chunks are consecutive)
+ * X [n_inst, ldx] images, W [n_inst, ldw] accumulated (the caller zeroes it). Chunk partial
+ * images are summed per instance in chunk order (no float atomics). Out-of-range instance ids
+ * in the tables are skipped and counted (jscc_take_bad_detector_count). Workspace:
+ * jscc_compton_batch_workspace_bytes(n_ev, n_chunks, n_vox). No counterpart in the reference,
+ * which runs one instance at a time: the batched joint reconstruction of many Poisson
+ * realisations or count levels.
+ */
+JSCC_API size_t jscc_compton_batch_workspace_bytes(int64_t n_ev, int64_t n_chunks, int64_t n_vox);
+JSCC_API int jscc_compton_weight_batched(const float* records, const int32_t* row_id, int64_t n_ev,
+                   const int32_t* event_inst, const int32_t* block_inst, const int64_t* chunk_range,
+                   const int32_t* inst_chunk, int64_t n_chunks, int32_t n_inst, const float* coor,
+                   int64_t n_vox, const void* eff, int32_t eff_dtype, int64_t ld_eff, const float* X,
+                   int64_t ldx, float scale, float* W, int64_t ldw, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/*
  * The two halves of jscc_compton_weight on their own (T recomputed in both, never stored):
  *   jscc_compton_project:     f_out[i] = sum_j t_ij * rot(img)_j
  *   jscc_compton_backproject: weight[j] += scale * rotinv(sum_i t_ij * g_i)

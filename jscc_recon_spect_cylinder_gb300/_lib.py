@@ -161,6 +161,12 @@ _SIGNATURES: dict[str, tuple] = {
          c_void_p, c_void_p, c_int64, c_float, c_void_p, c_void_p, c_size_t, c_void_p],
     ),
     "jscc_take_bad_detector_count": (c_int, [POINTER(c_uint)]),
+    "jscc_compton_batch_workspace_bytes": (c_size_t, [c_int64, c_int64, c_int64]),
+    "jscc_compton_weight_batched": (
+        c_int,
+        [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_int64,
+         c_void_p, c_int32, c_int64, c_void_p, c_int64, c_float, c_void_p, c_int64, c_void_p, c_size_t, c_void_p],
+    ),
     "jscc_take_wait_timeout_count": (c_int, [POINTER(c_uint)]),
     "jscc_sparse_map": (
         c_int,

@@ -18,8 +18,9 @@ BF16 path. The K split of each GEMM shape is chosen by timing (``autotune``) and
 iteration over the subsets can be captured into a CUDA graph (``capture``).
 
 BatchedJointOsem adds the Compton channel of the joint loops: each instance's own event list,
-weighted through the fused cone kernels, combined with the batched SC weights in one safe EM
-update per subset.
+weighted through the fused cone kernels (all instances of a subset in one launch per direction,
+jscc_compton_weight_batched with device segment tables), combined with the batched SC weights
+in one safe EM update per subset; the whole iteration can be captured in one CUDA graph.
 """
 from __future__ import annotations
 
@@ -222,7 +223,10 @@ class BatchedJointOsem(BatchedScOsem):
     recon_osem_local_sparse_jsccsd_only.py:58-100). The SC weights of all instances come from
     the tensor-core GEMMs; each instance's Compton weight ``T^T (1 / T x)`` over its own events
     of the subset comes from the fused cone kernels (T recomputed, nothing stored per event but
-    its 64-byte record), with the batch's BF16 matrix as the efficiency rows.
+    its 64-byte record), with the batch's BF16 matrix as the efficiency rows. With the strict
+    model, every subset's events of all instances form one ops.ComptonBatch (one forward and
+    one back launch for the whole batch, partial images summed per instance in a fixed order);
+    other models go instance by instance through ops.compton_weight.
 
     events:  per instance, per subset, a ComptonEvents block (row ids in the reference's bin order)
     coor:    [V, 3] voxel centres on the device
@@ -250,6 +254,11 @@ class BatchedJointOsem(BatchedScOsem):
                 per.append((ev.records, rid, ev.model))
             self.events.append(per)
         self.WC = torch.zeros((n_inst, self.V), dtype=torch.float32, device=self.dev)
+        self.cbatch = None
+        if all(m == _lib.CONE_STRICT for per in self.events for _, _, m in per):
+            self.cbatch = [ops.ComptonBatch([(per[k][0], per[k][1]) for per in self.events], self.V, self.dev)
+                           for k in range(len(self.blocks))]
+            self.events = None  # the batches hold their own (sorted, padded) copies
 
     def _subset(self, k):
         b0, nb, nbp = self.blocks[k]
@@ -262,10 +271,13 @@ class BatchedJointOsem(BatchedScOsem):
                                         st), "jscc_batch_ratio")
         self._gemm(self.AT[:, b0:b0 + nbp], self.Qs[k], self.W, ("b", nbp))
         self.WC.zero_()
-        for n in range(self.n):
-            rec, rid, model = self.events[n][k]
-            if rec.size(0):
-                ops.compton_weight(rec, rid, self.coor, self.X[n], model=model, eff=self.A, out=self.WC[n])
+        if self.cbatch is not None:
+            self.cbatch[k].weight(self.X, self.A, self.coor, out=self.WC)
+        else:
+            for n in range(self.n):
+                rec, rid, model = self.events[n][k]
+                if rec.size(0):
+                    ops.compton_weight(rec, rid, self.coor, self.X[n], model=model, eff=self.A, out=self.WC[n])
         _lib.check(lib.jscc_batch_em_joint(self.W.data_ptr(), self.W.stride(0), self.V, self.n, self.np, self.alpha,
                                            self.WC.data_ptr(), self.WC.stride(0), 2.0 - self.alpha, self.X.data_ptr(),
                                            self.X.stride(0), self.S.data_ptr(), self.S.stride(0), _lib.EM_SAFE, 1e-12,

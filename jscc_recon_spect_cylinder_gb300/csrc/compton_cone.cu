@@ -420,6 +420,40 @@ __global__ void cone_ratio_kernel(const float* __restrict__ f, int64_t n, float*
     q[i] = 1.0f / f[i];
 }
 
+// Batched form: q[i] = 1 / f[i] for events of an instance in [0, n_inst), 0 for padding events
+// (event_inst = -1) and, counted, for instance ids out of range.
+__global__ void cone_ratio_batch_kernel(const float* __restrict__ f, const int32_t* __restrict__ event_inst,
+                                        int64_t n, int n_inst, float* __restrict__ q) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = event_inst[i];
+    if (b >= n_inst) atomicAdd(&g_bad_detector_count, 1u);
+    q[i] = (b >= 0 && b < n_inst) ? 1.0f / f[i] : 0.f;
+  }
+}
+
+// W[b][j] += scale * sum_{c = inst_chunk[b]}^{inst_chunk[b + 1] - 1} part[c][j] (chunks in
+// order; chunk offsets clamped to [0, n_chunks], a reversed range counted and skipped).
+__global__ void cone_batch_reduce_kernel(const float* __restrict__ part, int64_t ldp, int64_t n_chunks,
+                                         const int32_t* __restrict__ inst_chunk, int n_inst, int64_t V, int has_scale,
+                                         float scale, float* __restrict__ W, int64_t ldw) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)n_inst * V;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(t / V);
+    const int64_t j = t % V;
+    int64_t c0 = inst_chunk[b], c1 = inst_chunk[b + 1];
+    c0 = c0 < 0 ? 0 : (c0 > n_chunks ? n_chunks : c0);
+    c1 = c1 < 0 ? 0 : (c1 > n_chunks ? n_chunks : c1);
+    if (c1 < c0) {
+      if (j == 0) atomicAdd(&g_bad_detector_count, 1u);
+      continue;
+    }
+    float s = 0.f;
+    for (int64_t c = c0; c < c1; ++c) s += part[c * ldp + j];
+    float* w = W + (int64_t)b * ldw + j;
+    *w = has_scale ? __fadd_rn(*w, __fmul_rn(scale, s)) : __fadd_rn(*w, s);
+  }
+}
+
 // ------------------------------------------------------------------ fused back projection
 // part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i
 constexpr int kBackStage = 128;
@@ -559,17 +593,31 @@ __device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, 
 }
 
 // f[i] = sum_j t_ij eff_ij x_j for the strict model, 16 events (8 pairs) per CTA.
-template <bool WINDOW, typename TE>
+// BATCH: several instances' events in one launch; every 16-event block belongs to one
+// instance (block_inst[block]), whose image is x + instance * ldx; a block whose instance is
+// outside [0, n_inst) is skipped (f = 0) and counted.
+template <bool WINDOW, typename TE, bool BATCH = false>
 __global__ void __launch_bounds__(kConeThreads, 5)
 cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
                          const float* __restrict__ coor, int64_t V, const float* __restrict__ x,
-                         const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ f_out) {
+                         const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ f_out,
+                         const int32_t* __restrict__ block_inst, int64_t ldx, int n_inst) {
   constexpr int EB = 16, NP = EB / 2;
   __shared__ ConePair sev[NP];
   __shared__ int64_t srow[EB];
   __shared__ float red[kConeThreads / 32][EB];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i0 = (int64_t)blockIdx.x * EB;
+  int64_t v_end = V;
+  if (BATCH) {
+    const int b = block_inst[blockIdx.x];
+    if (b < 0 || b >= n_inst) {
+      if (tid == 0) atomicAdd(&g_bad_detector_count, 1u);
+      v_end = 0;  // no voxel: f = 0
+    } else {
+      x += (int64_t)b * ldx;
+    }
+  }
   if (tid < EB) {
     const int64_t i = i0 + tid < n_ev ? i0 + tid : n_ev - 1;  // padding repeats a valid event
     stage_pair_half(&sev[tid >> 1], tid & 1, rec[i]);
@@ -581,7 +629,7 @@ cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __res
   float2 af[NP];
 #pragma unroll
   for (int k = 0; k < NP; ++k) af[k] = make_float2(0.f, 0.f);
-  for (int64_t j = tid; j < V; j += kConeThreads) {
+  for (int64_t j = tid; j < v_end; j += kConeThreads) {
     const float2 ncx = f2(-coor[3 * j]), ncy = f2(-coor[3 * j + 1]), ncz = f2(-coor[3 * j + 2]);
     const float2 xj = f2(x ? __ldg(x + j) : 0.f);
 #pragma unroll
@@ -623,19 +671,29 @@ cone_forward_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __res
 }
 
 // part[chunk][j] = sum_{i in chunk} t_ij eff_ij q_i for the strict model, events in pairs.
-template <bool WINDOW, typename TE>
+// BATCH: chunk c holds events chunk_range[c] .. chunk_range[c + 1] (clamped to [0, n_ev]).
+template <bool WINDOW, typename TE, bool BATCH = false>
 __global__ void __launch_bounds__(kConeThreads, 8)
 cone_back_pair_kernel(const ConeEvent* __restrict__ rec, const int32_t* __restrict__ row_id, int64_t n_ev,
                       int64_t ev_per_chunk, const float* __restrict__ q, const float* __restrict__ coor, int64_t V,
-                      const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp) {
+                      const TE* __restrict__ eff, int64_t ld_eff, float* __restrict__ part, int64_t ldp,
+                      const int64_t* __restrict__ chunk_range) {
   __shared__ ConePair sev[kBackStage / 2];
   __shared__ int64_t srow[kBackStage];
   __shared__ float sq[kBackStage];
   const int tid = threadIdx.x;
   const int64_t j = (int64_t)blockIdx.x * kConeThreads + tid;
-  const int64_t e_begin = (int64_t)blockIdx.y * ev_per_chunk;
-  int64_t e_end = e_begin + ev_per_chunk;
-  if (e_end > n_ev) e_end = n_ev;
+  int64_t e_begin, e_end;
+  if (BATCH) {
+    e_begin = chunk_range[blockIdx.y];
+    e_end = chunk_range[blockIdx.y + 1];
+    e_begin = e_begin < 0 ? 0 : (e_begin > n_ev ? n_ev : e_begin);
+    e_end = e_end < e_begin ? e_begin : (e_end > n_ev ? n_ev : e_end);
+  } else {
+    e_begin = (int64_t)blockIdx.y * ev_per_chunk;
+    e_end = e_begin + ev_per_chunk;
+    if (e_end > n_ev) e_end = n_ev;
+  }
   float2 ncx = f2(0.f), ncy = f2(0.f), ncz = f2(0.f);
   if (j < V) {
     ncx = f2(-coor[3 * j]);
@@ -798,7 +856,8 @@ static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t 
     if (MODEL == 0)
       JSCC_TIMED("cone_forward", st,
                  (cone_forward_pair_kernel<WINDOW, TE><<<fgrid, kConeThreads, 0, st>>>(rec, rid, n_ev, coor, V, x,
-                                                                                       eff, ld_eff, f)));
+                                                                                       eff, ld_eff, f, nullptr, 0,
+                                                                                       0)));
     else
       JSCC_TIMED("cone_forward", st,
                  (cone_forward_kernel<MODEL, WINDOW, EB, false, TE><<<fgrid, kConeThreads, 0, st>>>(
@@ -814,7 +873,7 @@ static int launch_cone_weight(const ConeEvent* rec, const int32_t* rid, int64_t 
   if (MODEL == 0)
     JSCC_TIMED("cone_back", st,
                (cone_back_pair_kernel<WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
-                   rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp)));
+                   rec, rid, n_ev, p.ev_per_chunk, q, coor, V, eff, ld_eff, part, p.ldp, nullptr)));
   else
     JSCC_TIMED("cone_back", st,
                (cone_back_kernel<MODEL, WINDOW, TE><<<bgrid, kConeThreads, 0, st>>>(
@@ -1025,6 +1084,80 @@ int jscc_compton_weight(const float* records, const int32_t* row_id, int64_t n_e
   return compton_stage_entry("jscc_compton_weight", 0, records, row_id, n_ev, coor, n_vox, model, use_window, eff,
                              eff_dtype, ld_eff, img, rotmat, rotmat_inv, ld_rot, nullptr, nullptr, scale, weight,
                              workspace, workspace_bytes, stream);
+}
+
+size_t jscc_compton_batch_workspace_bytes(int64_t n_ev, int64_t n_chunks, int64_t n_vox) {
+  if (n_ev < 0 || n_chunks < 0 || n_vox < 0) return 0;
+  const int64_t ldp = (int64_t)align_up((size_t)(n_vox > 0 ? n_vox : 1), 8);
+  return align_up((size_t)(n_ev > 0 ? n_ev : 1) * sizeof(float), 256) * 2 +
+         align_up((size_t)(n_chunks > 0 ? n_chunks : 1) * ldp * sizeof(float), 256) + 256;
+}
+
+int jscc_compton_weight_batched(const float* records, const int32_t* row_id, int64_t n_ev, const int32_t* event_inst,
+                                const int32_t* block_inst, const int64_t* chunk_range, const int32_t* inst_chunk,
+                                int64_t n_chunks, int32_t n_inst, const float* coor, int64_t n_vox, const void* eff,
+                                int32_t eff_dtype, int64_t ld_eff, const float* X, int64_t ldx, float scale, float* W,
+                                int64_t ldw, void* workspace, size_t workspace_bytes, void* stream) {
+  const char* what = "jscc_compton_weight_batched";
+  JSCC_REQUIRE(n_ev >= 0 && n_vox >= 0 && n_chunks >= 0 && n_inst >= 0, "%s: negative size", what);
+  JSCC_REQUIRE(eff_dtype == JSCC_DTYPE_F32 || eff_dtype == JSCC_DTYPE_BF16, "%s: bad dtype", what);
+  if (n_ev == 0 || n_vox == 0 || n_inst == 0 || n_chunks == 0) return JSCC_OK;
+  JSCC_REQUIRE(n_ev % 16 == 0, "%s: n_ev (%lld) must be a multiple of 16 (pad each instance)", what,
+               (long long)n_ev);
+  JSCC_REQUIRE(records && coor && event_inst && block_inst && chunk_range && inst_chunk && X && W,
+               "%s: null pointer argument", what);
+  JSCC_REQUIRE(!eff || (row_id && ld_eff >= n_vox), "%s: efficiency rows need row ids, ld >= V", what);
+  JSCC_REQUIRE(ldx >= n_vox && ldw >= n_vox, "%s: ldx / ldw < n_vox", what);
+  JSCC_REQUIRE(n_chunks <= 65535, "%s: %lld chunks exceed the grid's y extent", what, (long long)n_chunks);
+  const size_t need = jscc_compton_batch_workspace_bytes(n_ev, n_chunks, n_vox);
+  JSCC_REQUIRE(workspace && workspace_bytes >= need, "%s: workspace too small (%zu < %zu)", what, workspace_bytes,
+               need);
+  Carver cv(workspace, workspace_bytes);
+  const int64_t ldp = (int64_t)align_up((size_t)n_vox, 8);
+  float* f = cv.take<float>((size_t)n_ev);
+  float* q = cv.take<float>((size_t)n_ev);
+  float* part = cv.take<float>((size_t)n_chunks * ldp);
+  JSCC_REQUIRE(cv.ok(), "%s: workspace carve overflow", what);
+  cudaStream_t st = as_stream(stream);
+  const ConeEvent* rec = reinterpret_cast<const ConeEvent*>(records);
+  const unsigned fgrid = (unsigned)(n_ev / 16);
+  dim3 bgrid((unsigned)((n_vox + kConeThreads - 1) / kConeThreads), (unsigned)n_chunks);
+  int64_t rb = (n_ev + 255) / 256;
+  if (rb > 4096) rb = 4096;
+  if (eff_dtype == JSCC_DTYPE_F32) {
+    const float* e = static_cast<const float*>(eff);
+    JSCC_TIMED("cone_forward", st,
+               (cone_forward_pair_kernel<false, float, true><<<fgrid, kConeThreads, 0, st>>>(
+                   rec, row_id, n_ev, coor, n_vox, X, e, ld_eff, f, block_inst, ldx, n_inst)));
+    JSCC_LAUNCH_CHECK();
+    JSCC_TIMED("cone_ratio", st,
+               (cone_ratio_batch_kernel<<<(unsigned)rb, 256, 0, st>>>(f, event_inst, n_ev, n_inst, q)));
+    JSCC_LAUNCH_CHECK();
+    JSCC_TIMED("cone_back", st,
+               (cone_back_pair_kernel<false, float, true><<<bgrid, kConeThreads, 0, st>>>(
+                   rec, row_id, n_ev, 0, q, coor, n_vox, e, ld_eff, part, ldp, chunk_range)));
+  } else {
+    const __nv_bfloat16* e = static_cast<const __nv_bfloat16*>(eff);
+    JSCC_TIMED("cone_forward", st,
+               (cone_forward_pair_kernel<false, __nv_bfloat16, true><<<fgrid, kConeThreads, 0, st>>>(
+                   rec, row_id, n_ev, coor, n_vox, X, e, ld_eff, f, block_inst, ldx, n_inst)));
+    JSCC_LAUNCH_CHECK();
+    JSCC_TIMED("cone_ratio", st,
+               (cone_ratio_batch_kernel<<<(unsigned)rb, 256, 0, st>>>(f, event_inst, n_ev, n_inst, q)));
+    JSCC_LAUNCH_CHECK();
+    JSCC_TIMED("cone_back", st,
+               (cone_back_pair_kernel<false, __nv_bfloat16, true><<<bgrid, kConeThreads, 0, st>>>(
+                   rec, row_id, n_ev, 0, q, coor, n_vox, e, ld_eff, part, ldp, chunk_range)));
+  }
+  JSCC_LAUNCH_CHECK();
+  int64_t blocks = ((int64_t)n_inst * n_vox + 255) / 256;
+  if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+  JSCC_TIMED("cone_batch_reduce", st,
+             (cone_batch_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, n_chunks, inst_chunk, n_inst,
+                                                                          n_vox, scale != 1.0f ? 1 : 0, scale, W,
+                                                                          ldw)));
+  JSCC_LAUNCH_CHECK();
+  return JSCC_OK;
 }
 
 int jscc_compton_project(const float* records, const int32_t* row_id, int64_t n_ev, const float* coor, int64_t n_vox,

@@ -563,6 +563,88 @@ def compton_weight(records, row_id, coor, img, model=_lib.CONE_STRICT, eff=None,
     return out
 
 
+class ComptonBatch:
+    """Several instances' Compton event blocks as one batch for jscc_compton_weight_batched
+    (strict model, every pair). ``blocks`` holds one ``(records, row_id)`` pair per instance
+    (records [E_b, 16] float32, row_id [E_b] int32 efficiency rows). Each instance's events are
+    visited sorted by efficiency row (a stable sort: as compton_weight does, only float32
+    rounding changes) and padded to a multiple of 16 with copies of its first event that carry
+    no weight; the back projection splits each instance's events into chunks of about
+    ``ev_per_chunk`` (default: the batch's events over 256, at least 64). The tables are
+    built once; ``weight`` can then be captured in a CUDA graph."""
+
+    def __init__(self, blocks, n_vox, device, ev_per_chunk=None):
+        dev = torch.device(device)
+        recs, rids, insts, binst, ranges, ichunk = [], [], [], [], [0], [0]
+        counts = [int(r.size(0)) for r, _ in blocks]
+        total = sum(-(-n // 16) * 16 for n in counts)
+        if ev_per_chunk is None:
+            ev_per_chunk = max(64, -(-total // 256))
+        off = 0
+        for b, (rec, rid) in enumerate(blocks):
+            n = counts[b]
+            if n == 0:
+                ichunk.append(ichunk[-1])
+                continue
+            rec = rec.to(dev, torch.float32).reshape(n, _lib.CONE_RECORD_FLOATS)
+            rid = rid.to(dev, torch.int32).reshape(n)
+            order = torch.argsort(rid.to(torch.int64), stable=True)
+            rec, rid = rec[order], rid[order]
+            pad = -(-n // 16) * 16 - n
+            if pad:
+                rec = torch.cat((rec, rec[:1].expand(pad, -1)))
+                rid = torch.cat((rid, rid[:1].expand(pad)))
+            npad = n + pad
+            recs.append(rec)
+            rids.append(rid)
+            ev_inst = torch.full((npad,), b, dtype=torch.int32, device=dev)
+            ev_inst[n:] = -1
+            insts.append(ev_inst)
+            binst.append(torch.full((npad // 16,), b, dtype=torch.int32, device=dev))
+            k = max(1, -(-npad // ev_per_chunk))
+            edges = [off + (npad * i) // k for i in range(1, k + 1)]
+            ranges.extend(edges)
+            ichunk.append(ichunk[-1] + k)
+            off += npad
+        self.n_inst = len(blocks)
+        self.V = int(n_vox)
+        self.dev = dev
+        self.n_ev = off
+        self.counts = counts
+        empty_f = torch.zeros((0, _lib.CONE_RECORD_FLOATS), dtype=torch.float32, device=dev)
+        empty_i = torch.zeros(0, dtype=torch.int32, device=dev)
+        self.records = torch.cat(recs).contiguous() if recs else empty_f
+        self.row_id = torch.cat(rids).contiguous() if rids else empty_i
+        self.event_inst = torch.cat(insts).contiguous() if insts else empty_i
+        self.block_inst = torch.cat(binst).contiguous() if binst else empty_i
+        self.chunk_range = torch.tensor(ranges, dtype=torch.int64, device=dev)
+        self.inst_chunk = torch.tensor(ichunk, dtype=torch.int32, device=dev)
+        self.n_chunks = len(ranges) - 1
+
+    def weight(self, X, eff, coor, scale=1.0, out=None):
+        """``out[b] += scale * T_b^T (1 / T_b X[b])`` for every instance b; X [n_inst, V]."""
+        dev = _lib.require_cuda(X, eff, coor, out, what="ComptonBatch.weight")
+        c = _f32_contig(coor)
+        if c.size(0) != self.V:
+            raise ValueError(f"coor has {c.size(0)} voxels, the batch was built for {self.V}")
+        if X.dim() != 2 or X.shape != (self.n_inst, self.V) or X.dtype != torch.float32 or X.stride(1) != 1:
+            raise ValueError(f"X must be a float32 [{self.n_inst}, {self.V}] tensor with unit column stride")
+        if out is None:
+            out = torch.zeros((self.n_inst, self.V), dtype=torch.float32, device=dev)
+        if out.shape != (self.n_inst, self.V) or out.dtype != torch.float32 or out.stride(1) != 1:
+            raise ValueError(f"out must be a float32 [{self.n_inst}, {self.V}] tensor with unit column stride")
+        e, edt, ld = _eff_args(eff)
+        lib = _lib.load()
+        ws = _lib.workspace.get(dev, lib.jscc_compton_batch_workspace_bytes(self.n_ev, self.n_chunks, self.V))
+        rc = lib.jscc_compton_weight_batched(
+            self.records.data_ptr(), self.row_id.data_ptr(), self.n_ev, self.event_inst.data_ptr(),
+            self.block_inst.data_ptr(), self.chunk_range.data_ptr(), self.inst_chunk.data_ptr(), self.n_chunks,
+            self.n_inst, c.data_ptr(), self.V, _lib.ptr(e), edt, ld, X.data_ptr(), X.stride(0), float(scale),
+            out.data_ptr(), out.stride(0), ws.data_ptr(), ws.numel(), _lib.stream_handle(dev))
+        _lib.check(rc, "jscc_compton_weight_batched")
+        return out
+
+
 # ============================================================================ sparse rows
 def _padded_rows(m):
     """Non-zeros of each row of m as padded [rows, width] (index, weight); padding weight 0."""

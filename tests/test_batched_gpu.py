@@ -86,11 +86,65 @@ def test_batched_osem_matches_fp64(cuda, graph):
         assert rel_l2(X[n], ref[n]) < 1e-4, n
 
 
-def test_batched_joint_matches_single_instance_loops(cuda):
-    """BatchedJointOsem (SC weights from the tensor-core GEMMs, each instance's Compton weight
-    from the fused cone kernels over its own events, safe EM with per-instance joint
-    sensitivities) against the single-instance joint loop of each instance (jscc_sc_weight with
-    the 1e-12 floor + jscc_compton_weight + safe EM) on the same BF16 matrix: 1e-4."""
+def _cone_events(cuda, A, coor, n_ev, seed):
+    import numpy as np
+
+    from jscc_recon_spect_cylinder_gb300 import process_list_plane_strict as pls
+    from jscc_recon_spect_cylinder_gb300 import synthetic
+
+    scat = synthetic.cylinder_pixels(120.0, 32, 4, 3.0)
+    absb = synthetic.cylinder_pixels(150.0, 32, 4, 3.0)
+    det = torch.cat((scat, absb)).float().to(cuda)
+    e0 = 0.511
+    args = (0.8, 0.8, e0, 0.1 * (0.662 / e0) ** 0.5, 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001, 0.05, e0 - 0.06)
+    rng = np.random.default_rng(seed)
+    L = np.stack((rng.integers(1, 129, n_ev), rng.uniform(0.08, 0.3, n_ev), rng.integers(129, 257, n_ev),
+                  np.zeros(n_ev)), axis=1).astype(np.float32)
+    L[:, 3] = e0 - L[:, 1]
+    return pls.get_compton_event_params(A.float(), det, coor, torch.from_numpy(L).to(cuda), *args, window_sigmas=0.0)
+
+
+@pytest.mark.parametrize("ev_per_chunk", [None, 64])
+def test_compton_batch_matches_per_instance_weights(cuda, ev_per_chunk):
+    """ops.ComptonBatch (jscc_compton_weight_batched: one forward and one back launch for all
+    instances, device segment tables) against jscc_compton_weight run instance by instance,
+    with uneven instances: none, one event, counts that are not multiples of 16, several back
+    chunks per instance; BF16 and FP32 efficiency rows; 1e-5, repeated calls bit-identical."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
+
+    prob = synthetic.sc_problem(n_r=8, n_theta=24, n_phi=64, views=4, flat=True, total_counts=1e5)
+    coor = prob.grid.coor.to(cuda)
+    V = coor.size(0)
+    evs = [(torch.zeros((0, 16), device=cuda), torch.zeros(0, dtype=torch.int32, device=cuda))]
+    for n in (1, 37, 700, 2000):
+        e = _cone_events(cuda, prob.sysmat.to(cuda), coor, n, 7 + n)
+        evs.append((e.records, e.row_id))
+    g = torch.Generator().manual_seed(3)
+    X = (torch.rand((len(evs), V), generator=g) + 0.2).to(cuda)
+    _lib.take_bad_detector_count()
+    for A in (prob.sysmat.to(cuda), prob.sysmat.to(torch.bfloat16).to(cuda)):
+        cb = ops.ComptonBatch(evs, V, cuda, ev_per_chunk=ev_per_chunk)
+        assert cb.n_ev % 16 == 0 and cb.n_chunks >= len([r for r, _ in evs if r.size(0)])
+        W = cb.weight(X, A, coor, scale=1.5)
+        W2 = cb.weight(X, A, coor, scale=1.5)
+        torch.cuda.synchronize()
+        assert torch.equal(W, W2)
+        for b, (rec, rid) in enumerate(evs):
+            if rec.size(0) == 0:
+                assert torch.count_nonzero(W[b]) == 0
+                continue
+            ref = ops.compton_weight(rec, rid, coor, X[b], eff=A, scale=1.5)
+            assert rel_l2(W[b].cpu(), ref.cpu()) < 1e-5, b
+    assert _lib.take_bad_detector_count() == 0
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batched_joint_matches_single_instance_loops(cuda, graph):
+    """BatchedJointOsem (SC weights from the tensor-core GEMMs, the Compton weights of all
+    instances from one batched cone launch per direction, safe EM with per-instance joint
+    sensitivities; eager and captured in one CUDA graph) against the single-instance joint loop
+    of each instance (jscc_sc_weight with the 1e-12 floor + jscc_compton_weight + safe EM) on
+    the same BF16 matrix: 1e-4."""
     import numpy as np
 
     from jscc_recon_spect_cylinder_gb300 import batched, ops, synthetic
@@ -126,8 +180,12 @@ def test_batched_joint_matches_single_instance_loops(cuda):
         events.append(ev.split(S))
     S_joint = torch.stack(S_joint)
     bj = batched.BatchedJointOsem(A16, subsets, S_joint, events, coor, alpha=alpha, device=cuda)
+    assert bj.cbatch is not None  # strict events: the batched cone launches
     bj.set_projections(Y)
     bj.set_images(torch.ones((n_inst, V)))
+    if graph:
+        bj.capture()
+        bj.set_images(torch.ones((n_inst, V)))
     X = bj.iterate(2).cpu()
     for n in range(n_inst):
         x = torch.ones((V, 1), device=cuda)
