@@ -961,18 +961,12 @@ class JointBench:
         return out
 
     def plain_fp32_gpu_reference(self):
-        """The reference's own PyTorch FP32 joint loop on this GPU (whole subset updates of
-        the same workload, its float32 inputs), and how far its image after one subset update
-        is from the product's float32 path from the same start."""
+        """The reference's own PyTorch FP32 joint subset update on this GPU (oracle.
+        reference_timing.run_gpu_plain_fp32: the same workload's float32 inputs)."""
         from oracle import reference_timing as rt
 
         torch.cuda.empty_cache()
         res = rt.run_gpu_plain_fp32(self.w)
-        img = res.pop("image", None)
-        if img is not None:
-            ours = self.w.subset_update(torch.ones((self.w.V, 1), device=self.dev), 0, "f32")
-            d = (ours.double() - img.double())
-            res["image_rel_l2_vs_product_fp32_after_one_subset"] = float(d.norm() / img.double().norm())
         torch.cuda.empty_cache()
         return res
 
@@ -1049,6 +1043,33 @@ def batched_summary(dev, steps=5):
     del b
     torch.cuda.empty_cache()
     return res
+
+
+SUMMARY_KEYS = {
+    "cone2": ("window_9sigma", "stored_t", "fp32_roofline"),
+    "map5": ("cone_pass", "fp32_roofline"),
+    "batch4-joint": ("compton_pairs_per_s", "fp32_roofline", "sequential_fp32_joint_64_instances", "errors_vs_fp64"),
+}
+
+
+def workload_summary(name, dev, steps=3, warmup=3):
+    """Another configuration's workload measured in a timed region of its own (CUDA events on
+    the launch stream around `steps` steps after `warmup` untimed ones), with the figures of its
+    own bench line that explain it; the workload is freed afterwards."""
+    t0 = time.perf_counter()
+    work = make_workload(name, dev)
+    setup_s = time.perf_counter() - t0
+    dt = getattr(work, "dtypes", ("bf16",))[0]
+    ms, launches, _ = timed_steps(work, dt, steps, warmup, 1)
+    out = {"workload": f"bench.py --workload {name}", "metric": work.metric,
+           "value": work.units_per_step() * steps / (ms / 1e3), "unit": getattr(work, "unit", "subset-iters/s"),
+           "ms_per_step": ms / steps, "steps": steps, "warmup": warmup, "gpu_launches": launches,
+           "config": work.config(), "setup_s": setup_s}
+    extra = work.extra(ms / steps)
+    out.update({k: extra[k] for k in SUMMARY_KEYS.get(name, ()) if k in extra})
+    del work, extra
+    torch.cuda.empty_cache()
+    return out
 
 
 def make_workload(name, dev):
@@ -1248,6 +1269,13 @@ def ours_arm(args):
             top = max(kernels, key=lambda k: kernels[k]["avg_ms"] * kernels[k]["launches"]) if kernels else None
             line["roofline"] = dict(extra.pop("fp32_roofline"), kernel=top, traffic=None)
         line.update(extra)
+        if args.workload == "jsccsd3" and not args.no_extra and not args.no_other_workloads:
+            # the other configurations, each in a timed region of its own after the main
+            # measurement (the joint workload is freed first)
+            del work
+            torch.cuda.empty_cache()
+            line["other_workloads"] = {name.replace("-", "_"): workload_summary(name, dev)
+                                       for name in ("cone2", "map5", "batch4-joint")}
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
@@ -1269,6 +1297,8 @@ def main():
     ap.add_argument("--no-errors", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the workload's extra figures (e.g. cone2's stored-T arm): small profiling runs")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="jsccsd3: skip the summaries of the cone2 / map5 / batch4-joint workloads")
     ap.add_argument("--error-iters", type=int, default=10,
                     help="iterations (from a uniform image) at which BF16 / FP32 images are compared with FP64")
     args = ap.parse_args()

@@ -117,6 +117,7 @@ _SIGNATURES: dict[str, tuple] = {
                 c_void_p]),
     "jscc_take_gemm_timeout_count": (c_int, [POINTER(c_uint)]),
     "jscc_set_wait_limit": (c_int, [c_int64]),
+    "jscc_set_fused_cluster": (c_int, [c_int32]),
     "jscc_rdp_prior_workspace_bytes": (c_size_t, [c_int64]),
     "jscc_rdp_prior": (
         c_int,
@@ -285,6 +286,12 @@ def set_wait_limit(polls: int | None) -> None:
 # Bumped whenever a give-up is detected: per-plan event sums computed before it may come from
 # a call whose waits gave up, so ops keys its cached sums by this epoch.
 timeout_epoch = 0
+
+
+def set_fused_cluster(enable: bool) -> None:
+    """Let the grouped sparse weight use its fused cluster kernel where it applies (default),
+    or always run the two-kernel pipeline."""
+    check(load().jscc_set_fused_cluster(1 if enable else 0), "jscc_set_fused_cluster")
 
 
 def check_wait_timeouts() -> None:

@@ -1,0 +1,582 @@
+// Fused grouped sparse Compton weight on thread-block clusters (included by sparse_ops.cu).
+//
+// The grouped weight (recon_osem_plane_sparse.py:22-57 and the materialise form of
+// recon_osem_local_sparse_jsccsd_only.py:13-19, see sparse_group_coef_bulk_kernel) in ONE
+// kernel: per group g (events sharing the first-hit sysmat row A_g)
+//   b_g = adj(A_g . x)          f_i = t_i . b_g          c_i = coefficient of f_i
+//   q_g = sum_i c_i t_i         w  += A_g . up(q_g)
+// Each byte of the event rows and of the group's sysmat row is read from HBM once, and q never
+// leaves the chip (the two-kernel form writes q and reads every sysmat row a second time).
+//
+// Data split: a cluster of kCfCluster CTAs (one per SM) works on the same groups; CTA r owns
+// the rings [R0, R1) of the polar grid (one z plane, the stride-4 ring stencil: coarse voxel
+// th of a ring has the fine taps 4 th + d, d = -3..3, with the polar projector's linear
+// weights 1 - |d| / 4, periodic in the ring), so its fine voxels [J0, J1) and coarse voxels
+// [C0, C1) close under adj and up. Every CTA stages its slice of x once, and per group its
+// slice of A_g and of each event row (bulk copies of the 16-byte-aligned windows [jw0, jw1)
+// and [cw0, cw1) around the slices). The only cross-CTA step is f_i = sum over the cluster
+// of the CTAs' partial dots: each team's lead thread stores its partials into every CTA of
+// the cluster (distributed shared memory) and signals that CTA's exchange mbarrier; partials
+// are added in CTA order, so every CTA derives the same f_i and coefficient.
+//
+// Warp roles (512 threads, one CTA per SM):
+//   warp 15       producer: bulk copies of the A_g slices (three buffers) and of the event row
+//                 slices (a ring of slots), each issued as soon as its buffer is free;
+//   warps 8-14    group warps: b_g for the slice into one of two buffers, then the scatter of
+//                 the previous group, w_j += A_g[j] up(q_g)[j], into a partial image held in
+//                 registers (kCfM fine voxels per thread);
+//   warps 0-7     two teams of four event warps taking alternate batches of up to kCfNB
+//                 events, so one team computes while the other waits for its exchange: dots
+//                 (four partial sums per event), the exchange, coefficients, q in registers;
+//                 at the end of a group team 0 stores its q, team 1 adds its own.
+// Every wait is bounded (g_bk_poll_limit): a CTA that gives up raises its abort flag, its
+// roles leave their loops, its peers give up on their exchange waits, and every CTA waits
+// (bounded) for its own copies in flight, arrives at the closing cluster barrier and counts
+// the give-up (jscc_take_wait_timeout_count). Partial images: one per cluster, summed in
+// cluster order by sparse_reduce_kernel. No float atomics.
+
+constexpr int kCfCluster = 4;
+constexpr int kCfThreads = 512;
+constexpr int kCfTeamWarps = 4;
+constexpr int kCfTeam = kCfTeamWarps * 32;  // threads per event team
+constexpr int kCfGroupWarps = 7;
+constexpr int kCfGroup = kCfGroupWarps * 32;
+constexpr int kCfProducerWarp = 15;
+constexpr int kCfNB = 4;       // events per batch
+constexpr int kCfQ = 5;        // chunks of four coarse voxels per team thread (window <= 2,560)
+constexpr int kCfM = 48;       // fine voxels per group thread (slice <= 10,752)
+constexpr int kCfNX = 4;       // exchange slots
+constexpr int kCfMaxSlots = 16;
+constexpr int kCfHeader = 4096;
+constexpr int kCfMaxWindowC = kCfTeam * 4 * kCfQ;
+constexpr int kCfMaxSliceF = kCfGroup * kCfM;
+static_assert(kCfProducerWarp * 32 + 32 == kCfThreads && 2 * kCfTeam + kCfGroup + 32 == kCfThreads, "roles");
+
+// header layout (bytes)
+constexpr int kCfOffFull = 0;                       // [kCfMaxSlots] u64
+constexpr int kCfOffEmpty = 128;                    // [kCfMaxSlots]
+constexpr int kCfOffErowFull = 256;                 // [3]
+constexpr int kCfOffErowEmpty = 280;                // [3]
+constexpr int kCfOffBFull = 304;                    // [2]
+constexpr int kCfOffBEmpty = 320;                   // [2]
+constexpr int kCfOffQFull = 336;                    // [2]
+constexpr int kCfOffQEmpty = 352;                   // [2]
+constexpr int kCfOffXFull = 368;                    // [kCfNX]
+constexpr int kCfOffXEmpty = 400;                   // [kCfNX]
+constexpr int kCfOffFlags = 512;                    // abort
+constexpr int kCfOffSlotIssued = 576;               // [kCfMaxSlots] int
+constexpr int kCfOffSlotWaited = 640;               // [kCfMaxSlots] int
+constexpr int kCfOffErowIssued = 704;               // [3] int
+constexpr int kCfOffErowWaited = 720;               // [3] int
+constexpr int kCfOffRed = 1024;                     // [2][kCfTeamWarps][kCfNB] float
+constexpr int kCfOffCs = 1280;                      // [2][kCfNB] float
+constexpr int kCfOffXval = 1536;                    // [kCfNX][kCfCluster][kCfNB] float
+static_assert(kCfOffXEmpty + 8 * kCfNX <= kCfOffFlags, "barriers");
+static_assert(kCfOffXval + 4 * kCfNX * kCfCluster * kCfNB <= kCfHeader, "header");
+
+// ------------------------------------------------------------------ cluster primitives
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_id_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t n_clusters_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// all threads of every CTA of the cluster
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// the address of this CTA's shared variable at `p` in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_to_rank(const void* p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_cluster_v4(uint32_t addr, float a, float b, float c, float d) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
+}
+// a wait that sees arrivals (and the stores before them) from other CTAs of the cluster
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool cf_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
+    if ((i & 31u) == 31u && *abort_flag) return false;
+  }
+  return false;
+}
+
+struct CfArgs {
+  const __nv_bfloat16* tc;  // split coarse rows [E, ld]
+  int64_t ld;
+  int64_t n_det;
+  const int32_t* order;
+  const int32_t* goff;
+  const int32_t* grow;
+  int n_groups;
+  const __nv_bfloat16* eff;
+  int64_t ld_eff;
+  const float* x;      // fine image (already rotated)
+  const float* s_ev;   // event sums by position in `order` (materialise form)
+  float* part;         // [clusters][ldp] partial images
+  int64_t ldp;
+  int vf, vc, ring_len, n_rings;
+  int n_slots;
+  uint32_t x_off, erow_off, erow_stride, b_off, b_stride, q_off, q_stride, slot_off, slot_stride;
+  int max_wf, max_wc;  // largest window lengths (elements) over the cluster's CTAs
+};
+
+// slice of CTA r: rings [R0, R1), fine [J0, J1), coarse [C0, C1), 16-byte windows
+struct CfSlice {
+  int J0, J1, C0, C1, jw0, jw1, cw0, cw1;
+};
+__host__ __device__ inline CfSlice cf_slice(int r, int n_rings, int ring_len, int vf, int vc) {
+  CfSlice s;
+  const int R0 = (int)((int64_t)n_rings * r / kCfCluster), R1 = (int)((int64_t)n_rings * (r + 1) / kCfCluster);
+  const int nthc = ring_len / 4;
+  s.J0 = R0 * ring_len;
+  s.J1 = R1 * ring_len;
+  s.C0 = R0 * nthc;
+  s.C1 = R1 * nthc;
+  s.jw0 = s.J0 & ~7;
+  s.jw1 = ((s.J1 + 7) & ~7) < vf ? ((s.J1 + 7) & ~7) : vf;
+  s.cw0 = s.C0 & ~7;
+  s.cw1 = ((s.C1 + 7) & ~7) < vc ? ((s.C1 + 7) & ~7) : vc;
+  return s;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kCfOffFull);
+  uint64_t* empty = reinterpret_cast<uint64_t*>(smem + kCfOffEmpty);
+  uint64_t* erow_full = reinterpret_cast<uint64_t*>(smem + kCfOffErowFull);
+  uint64_t* erow_empty = reinterpret_cast<uint64_t*>(smem + kCfOffErowEmpty);
+  uint64_t* b_full = reinterpret_cast<uint64_t*>(smem + kCfOffBFull);
+  uint64_t* b_empty = reinterpret_cast<uint64_t*>(smem + kCfOffBEmpty);
+  uint64_t* q_full = reinterpret_cast<uint64_t*>(smem + kCfOffQFull);
+  uint64_t* q_empty = reinterpret_cast<uint64_t*>(smem + kCfOffQEmpty);
+  uint64_t* xfull = reinterpret_cast<uint64_t*>(smem + kCfOffXFull);
+  uint64_t* xempty = reinterpret_cast<uint64_t*>(smem + kCfOffXEmpty);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + kCfOffFlags);
+  int* slot_issued = reinterpret_cast<int*>(smem + kCfOffSlotIssued);
+  int* slot_waited = reinterpret_cast<int*>(smem + kCfOffSlotWaited);
+  int* erow_issued = reinterpret_cast<int*>(smem + kCfOffErowIssued);
+  int* erow_waited = reinterpret_cast<int*>(smem + kCfOffErowWaited);
+  float* red = reinterpret_cast<float*>(smem + kCfOffRed);
+  float* cs = reinterpret_cast<float*>(smem + kCfOffCs);
+  float* xval = reinterpret_cast<float*>(smem + kCfOffXval);
+  float* xs = reinterpret_cast<float*>(smem + a.x_off);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t polls = g_bk_poll_limit;
+  const uint32_t rank = cluster_rank();
+  const int G = (int)n_clusters_x(), cid = (int)cluster_id_x();
+  const CfSlice sl = cf_slice((int)rank, a.n_rings, a.ring_len, a.vf, a.vc);
+  const int nthc = a.ring_len / 4;
+  const uint32_t erow_bytes = (uint32_t)(sl.jw1 - sl.jw0) * 2u, row_bytes = (uint32_t)(sl.cw1 - sl.cw0) * 2u;
+  auto erow = [&](int k) { return reinterpret_cast<__nv_bfloat16*>(smem + a.erow_off + (size_t)k * a.erow_stride); };
+  auto bbuf = [&](int k) { return reinterpret_cast<float*>(smem + a.b_off + (size_t)k * a.b_stride); };
+  auto qbuf = [&](int k) { return reinterpret_cast<float*>(smem + a.q_off + (size_t)k * a.q_stride); };
+  auto slot = [&](int s) { return reinterpret_cast<__nv_bfloat16*>(smem + a.slot_off + (size_t)s * a.slot_stride); };
+  if (tid == 0) {
+    for (int s = 0; s < kCfMaxSlots; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, 1);
+      slot_issued[s] = slot_waited[s] = 0;
+    }
+    for (int k = 0; k < 3; ++k) {
+      mbar_init(erow_full + k, 1);
+      mbar_init(erow_empty + k, 1);
+      erow_issued[k] = erow_waited[k] = 0;
+    }
+    for (int k = 0; k < 2; ++k) {
+      mbar_init(b_full + k, 1);
+      mbar_init(b_empty + k, 1);
+      mbar_init(q_full + k, 1);
+      mbar_init(q_empty + k, 1);
+    }
+    for (int k = 0; k < kCfNX; ++k) {
+      mbar_init(xfull + k, kCfCluster);
+      mbar_init(xempty + k, kCfCluster);
+    }
+    *abort_flag = 0;
+    mbar_init_fence();
+  }
+  // the image slice, once: xs[j - jw0] = x[j]
+  for (int j = sl.jw0 + tid; j < sl.jw1; j += kCfThreads) xs[j - sl.jw0] = __ldg(a.x + j);
+  __syncthreads();
+  cluster_sync_all();  // every CTA's barriers exist before any remote arrival
+  const int n_mine = cid < a.n_groups ? (a.n_groups - 1 - cid) / G + 1 : 0;  // groups of this cluster
+
+  if (warp == kCfProducerWarp) {
+    // ------------------------------------------------------------ producer
+    int ek = 0;                        // next group whose A_g slice is issued
+    int rk = 0, re = 0, re_end = 0;    // group and event position of the next row
+    if (n_mine > 0) {
+      re = a.goff[cid];
+      re_end = a.goff[cid + 1];
+    }
+    int seq = 0;
+    uint32_t idle = 0;
+    bool ok = true;
+    while (ok) {
+      while (rk < n_mine && re >= re_end) {
+        ++rk;
+        if (rk < n_mine) {
+          const int gi = cid + rk * G;
+          re = a.goff[gi];
+          re_end = a.goff[gi + 1];
+        }
+      }
+      const bool rows_left = rk < n_mine, erows_left = ek < n_mine;
+      if (!rows_left && !erows_left) break;
+      bool progress = false;
+      if (erows_left) {
+        const int k3 = ek % 3;
+        bool ready = ek < 3 || mbar_test_wait(erow_empty + k3, (uint32_t)((ek / 3) - 1) & 1u);
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (ready) {
+          if (lane == 0) {
+            const int gi = cid + ek * G;
+            const __nv_bfloat16* src = a.eff + clamp_row(a.grow[gi], a.n_det) * a.ld_eff + sl.jw0;
+            mbar_arrive_expect_tx(erow_full + k3, erow_bytes);
+            bulk_copy_g2s(erow(k3), src, erow_bytes, erow_full + k3);
+            erow_issued[k3] += 1;
+          }
+          ++ek;
+          progress = true;
+        }
+      }
+      if (rows_left) {
+        const int s = seq % a.n_slots;
+        bool ready = seq < a.n_slots || mbar_test_wait(empty + s, (uint32_t)((seq / a.n_slots) - 1) & 1u);
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (ready) {
+          if (lane == 0) {
+            const int i = a.order[re];
+            mbar_arrive_expect_tx(full + s, row_bytes);
+            bulk_copy_g2s(slot(s), a.tc + (int64_t)i * a.ld + sl.cw0, row_bytes, full + s);
+            slot_issued[s] += 1;
+          }
+          ++seq;
+          ++re;
+          progress = true;
+        }
+      }
+      if (progress) {
+        idle = 0;
+      } else if (++idle > polls || *abort_flag) {
+        ok = false;
+      } else {
+        __nanosleep(64);
+      }
+    }
+    if (!ok && lane == 0) *abort_flag = 1;
+  } else if (warp >= 2 * kCfTeamWarps) {
+    // ------------------------------------------------------------ group warps
+    const int gt = tid - 2 * kCfTeam;
+    float acc[kCfM];
+#pragma unroll
+    for (int m = 0; m < kCfM; ++m) acc[m] = 0.f;
+    // this thread's first fine voxel (J0 + gt) as ring position and coarse base
+    const int nf = sl.J1 - sl.J0;
+    int p0 = gt, r0 = 0;
+    while (p0 >= a.ring_len) {
+      p0 -= a.ring_len;
+      ++r0;
+    }
+    const int cbase0 = (sl.J0 / a.ring_len + r0) * nthc;  // coarse index of theta 0 of the ring
+    bool bad = false, aborted = false;
+    // scatter of group k: acc[m] += A_g[j] (w_lo q[c_lo] + w_hi q[c_hi]) for j = J0 + gt + m * kCfGroup
+    auto scatter = [&](int k) {
+      if (!cf_wait_cluster(q_full + (k & 1), (uint32_t)(k >> 1) & 1u, abort_flag, polls)) bad = true;
+      const __nv_bfloat16* er = erow(k % 3);
+      const float* q = qbuf(k & 1);
+      int p = p0, cb = cbase0;
+#pragma unroll
+      for (int m = 0; m < kCfM; ++m) {
+        const int jj = gt + m * kCfGroup;
+        if (jj < nf) {
+          const int th = p >> 2, kk = p & 3;
+          const int clo = cb + th;
+          const int chi = cb + (th + 1 == nthc ? 0 : th + 1);
+          const float A = __bfloat162float(er[sl.J0 + jj - sl.jw0]);
+          float up = q[clo - sl.cw0];
+          if (kk) {
+            const float wh = 0.25f * (float)kk;
+            up = fmaf(wh, q[chi - sl.cw0], (1.0f - wh) * up);
+          }
+          acc[m] = fmaf(A, up, acc[m]);
+        }
+        p += kCfGroup;
+        while (p >= a.ring_len) {
+          p -= a.ring_len;
+          cb += nthc;
+        }
+      }
+      if (role_sync_or(5, kCfGroup, bad)) return false;
+      if (gt == 0) {
+        mbar_arrive(q_empty + (k & 1));
+        mbar_arrive(erow_empty + (k % 3));
+      }
+      return true;
+    };
+    for (int kg = 0; kg < n_mine; ++kg) {
+      const int k3 = kg % 3;
+      if (!cf_wait_cluster(erow_full + k3, (uint32_t)(kg / 3) & 1u, abort_flag, polls)) bad = true;
+      else if (gt == 0) erow_waited[k3] += 1;  // counted only when the copy is known complete
+      if (kg >= 2 && !cf_wait_cluster(b_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls))
+        bad = true;
+      // b[c - cw0] = sum_d (w_d x_j) A_j over the taps j of coarse c (zero outside [C0, C1))
+      float* b = bbuf(kg & 1);
+      const __nv_bfloat16* er = erow(k3);
+      for (int c = sl.cw0 + gt; c < sl.cw1; c += kCfGroup) {
+        float v = 0.f;
+        if (c >= sl.C0 && c < sl.C1) {
+          const int ring = c / nthc, th = c - ring * nthc;
+          const int jr = ring * a.ring_len;  // first fine voxel of the ring
+#pragma unroll
+          for (int d = -3; d <= 3; ++d) {
+            int pj = 4 * th + d;
+            if (pj < 0) pj += a.ring_len;
+            const int j = jr + pj - sl.jw0;
+            const float w = 1.0f - 0.25f * (float)(d < 0 ? -d : d);
+            v = fmaf(w * xs[j], __bfloat162float(er[j]), v);
+          }
+        }
+        b[c - sl.cw0] = v;
+      }
+      if (role_sync_or(5, kCfGroup, bad)) {
+        aborted = true;
+        break;
+      }
+      if (gt == 0) mbar_arrive(b_full + (kg & 1));
+      if (kg >= 1 && !scatter(kg - 1)) {
+        aborted = true;
+        break;
+      }
+    }
+    if (!aborted && n_mine > 0 && !scatter(n_mine - 1)) aborted = true;
+    if (aborted) {
+      *abort_flag = 1;
+    } else {
+      float* out = a.part + (int64_t)cid * a.ldp + sl.J0;
+#pragma unroll
+      for (int m = 0; m < kCfM; ++m) {
+        const int jj = gt + m * kCfGroup;
+        if (jj < nf) out[jj] = acc[m];
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ event teams
+    const int team = warp / kCfTeamWarps, tw = warp % kCfTeamWarps, lt = tid - team * kCfTeam;
+    const int bar_team = 1 + team;  // named barriers 1, 2: one team; 3: both teams
+    const int wc = sl.cw1 - sl.cw0;
+    float* redt = red + team * kCfTeamWarps * kCfNB;
+    float* cst = cs + team * kCfNB;
+    float4 qa[kCfQ];
+    bool bad = false, aborted = false;
+    int bs = 0;   // batch counter over the cluster's groups (both teams count every batch)
+    int seq = 0;  // event counter (slot sequence)
+    for (int kg = 0; kg < n_mine; ++kg) {
+      const int gi = cid + kg * G;
+      const int e0 = a.goff[gi], e1 = a.goff[gi + 1];
+      if (!cf_wait_cluster(b_full + (kg & 1), (uint32_t)(kg >> 1) & 1u, abort_flag, polls)) bad = true;
+      const float* b = bbuf(kg & 1);
+#pragma unroll
+      for (int u = 0; u < kCfQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int eb = e0; eb < e1; eb += kCfNB, ++bs) {
+        const int n = min(kCfNB, e1 - eb);
+        const int seq_b = seq;
+        seq += n;
+        if ((bs & 1) != team) continue;  // the other team's batch
+        int sk[kCfNB];
+#pragma unroll
+        for (int k = 0; k < kCfNB; ++k) {
+          sk[k] = (seq_b + k) % a.n_slots;
+          if (k < n) {
+            if (!cf_wait_cluster(full + sk[k], (uint32_t)((seq_b + k) / a.n_slots) & 1u, abort_flag, polls))
+              bad = true;
+            else if (lt == 0)
+              slot_waited[sk[k]] += 1;  // counted only when the copy is known complete
+          }
+        }
+        // ---- partial dots over this CTA's window (b is zero outside [C0, C1))
+        uint2 rc[kCfNB][kCfQ];
+        float4 ac[kCfNB];
+#pragma unroll
+        for (int k = 0; k < kCfNB; ++k) ac[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kCfQ; ++u) {
+          const int c = 4 * lt + u * (4 * kCfTeam);
+          if (c < wc) {
+            const float4 bv = *reinterpret_cast<const float4*>(b + c);
+#pragma unroll
+            for (int k = 0; k < kCfNB; ++k)
+              if (k < n) {
+                rc[k][u] = *reinterpret_cast<const uint2*>(slot(sk[k]) + c);
+                ac[k].x = fmaf(bf16_lo(rc[k][u].x), bv.x, ac[k].x);
+                ac[k].y = fmaf(bf16_hi(rc[k][u].x), bv.y, ac[k].y);
+                ac[k].z = fmaf(bf16_lo(rc[k][u].y), bv.z, ac[k].z);
+                ac[k].w = fmaf(bf16_hi(rc[k][u].y), bv.w, ac[k].w);
+              }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < kCfNB; ++k)
+          if (k < n) {
+            const float f = warp_sum((ac[k].x + ac[k].y) + (ac[k].z + ac[k].w));
+            if (lane == 0) redt[tw * kCfNB + k] = f;
+          }
+        if (role_sync_or(bar_team, kCfTeam, bad)) {
+          aborted = true;  // leaves this team's batches; both teams decide at the group's end
+          break;
+        }
+        if (lt == 0) {
+          // ---- exchange: this CTA's partials to every CTA of the cluster; f = sum in CTA order
+          float fr[kCfNB] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+          for (int k = 0; k < kCfNB; ++k)
+            if (k < n) {
+              float f = 0.f;
+              for (int w = 0; w < kCfTeamWarps; ++w) f += redt[w * kCfNB + k];
+              fr[k] = f;
+            }
+          float si[kCfNB] = {1.f, 1.f, 1.f, 1.f};
+          if (MODE == 0) {
+#pragma unroll
+            for (int k = 0; k < kCfNB; ++k)
+              if (k < n) si[k] = a.s_ev[eb + k];
+          }
+          const int x = bs % kCfNX;
+          bool ok = bs < kCfNX ||
+                    cf_wait_cluster(xempty + x, (uint32_t)((bs / kCfNX) - 1) & 1u, abort_flag, polls);
+          if (ok) {
+            float* dst = xval + (x * kCfCluster + (int)rank) * kCfNB;
+            for (uint32_t d = 0; d < (uint32_t)kCfCluster; ++d) {
+              st_cluster_v4(map_to_rank(dst, d), fr[0], fr[1], fr[2], fr[3]);
+              mbar_arrive_cluster(map_to_rank(xfull + x, d));
+            }
+            ok = cf_wait_cluster(xfull + x, (uint32_t)(bs / kCfNX) & 1u, abort_flag, polls);
+          }
+          if (ok) {
+#pragma unroll
+            for (int k = 0; k < kCfNB; ++k) {
+              float f = 0.f;
+              for (int r = 0; r < kCfCluster; ++r) f += xval[(x * kCfCluster + r) * kCfNB + k];
+              float c = 0.f;
+              if (k < n) {
+                if (MODE == 0) c = (isfinite(si[k]) && si[k] > 0.f) ? 1.0f / fmaxf(f, 1e-12f * si[k]) : 0.f;
+                else c = 1.0f / fmaxf(f, 1e-12f);
+              }
+              cst[k] = c;
+            }
+            for (uint32_t d = 0; d < (uint32_t)kCfCluster; ++d) mbar_arrive_cluster(map_to_rank(xempty + x, d));
+          } else {
+            bad = true;
+          }
+        }
+        if (role_sync_or(bar_team, kCfTeam, bad)) {
+          aborted = true;
+          break;
+        }
+        // ---- q += c_i t_i over the batch, events in order
+#pragma unroll
+        for (int k = 0; k < kCfNB; ++k)
+          if (k < n) {
+            const float ck = cst[k];
+            if (ck != 0.f) {
+#pragma unroll
+              for (int u = 0; u < kCfQ; ++u) {
+                const int c = 4 * lt + u * (4 * kCfTeam);
+                if (c < wc) {
+                  qa[u].x = fmaf(ck, bf16_lo(rc[k][u].x), qa[u].x);
+                  qa[u].y = fmaf(ck, bf16_hi(rc[k][u].x), qa[u].y);
+                  qa[u].z = fmaf(ck, bf16_lo(rc[k][u].y), qa[u].z);
+                  qa[u].w = fmaf(ck, bf16_hi(rc[k][u].y), qa[u].w);
+                }
+              }
+            }
+          }
+        role_sync(bar_team, kCfTeam);  // the batch's slots, partials and coefficients are free
+        if (lt == 0) {
+#pragma unroll
+          for (int k = 0; k < kCfNB; ++k)
+            if (k < n) mbar_arrive(empty + sk[k]);
+        }
+      }
+      // ---- end of the group: q = q(team 0) + q(team 1) into the q buffer (both teams reach
+      // this barrier, also a team that gave up, so the decision is uniform)
+      if (!aborted && kg >= 2 &&
+          !cf_wait_cluster(q_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls))
+        bad = true;
+      if (role_sync_or(3, 2 * kCfTeam, bad || aborted)) {
+        aborted = true;
+        break;
+      }
+      float* q = qbuf(kg & 1);
+      if (team == 0) {
+#pragma unroll
+        for (int u = 0; u < kCfQ; ++u) {
+          const int c = 4 * lt + u * (4 * kCfTeam);
+          if (c < wc) *reinterpret_cast<float4*>(q + c) = qa[u];
+        }
+      }
+      role_sync(3, 2 * kCfTeam);
+      if (team == 1) {
+#pragma unroll
+        for (int u = 0; u < kCfQ; ++u) {
+          const int c = 4 * lt + u * (4 * kCfTeam);
+          if (c < wc) {
+            float4 v = *reinterpret_cast<const float4*>(q + c);
+            v.x += qa[u].x;
+            v.y += qa[u].y;
+            v.z += qa[u].z;
+            v.w += qa[u].w;
+            *reinterpret_cast<float4*>(q + c) = v;
+          }
+        }
+      }
+      role_sync(3, 2 * kCfTeam);
+      if (tid == 0) {
+        mbar_arrive(q_full + (kg & 1));
+        mbar_arrive(b_empty + (kg & 1));
+      }
+    }
+    if (aborted) *abort_flag = 1;
+  }
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
+    atomicAdd(&g_wait_timeout_count, 1u);
+    // bulk copies still in flight write this CTA's shared memory: wait (bounded) for them
+    for (int s = 0; s < a.n_slots; ++s)
+      if (slot_issued[s] > slot_waited[s])
+        mbar_wait_bounded(full + s, (uint32_t)slot_waited[s] & 1u, kBkDrainPolls);
+    for (int k = 0; k < 3; ++k)
+      if (erow_issued[k] > erow_waited[k])
+        mbar_wait_bounded(erow_full + k, (uint32_t)erow_waited[k] & 1u, kBkDrainPolls);
+  }
+  __syncthreads();
+  cluster_sync_all();  // no CTA leaves while a peer may still write its shared memory
+}

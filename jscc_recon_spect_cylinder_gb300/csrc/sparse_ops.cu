@@ -14,6 +14,9 @@
 #include <climits>
 #include "jscc_common.cuh"
 
+#include <algorithm>
+#include <type_traits>
+
 namespace jscc {
 
 // ------------------------------------------------------------------ separable map
@@ -1500,6 +1503,43 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   }
 }
 
+#include "sparse_cluster.cuh"
+
+constexpr int kCfMaxClusters = 64;  // partial images reserved in the workspace for the cluster path
+static bool g_cluster_fused = true;
+
+// Co-resident clusters of the fused kernel for this device and shared-memory size (cached).
+template <int MODE>
+static int cf_max_clusters(size_t smem) {
+  static int cache_dev[64] = {0};
+  static size_t cache_smem[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  if (cache_dev[dev] > 0 && cache_smem[dev] == smem) return cache_dev[dev];
+  if (cudaFuncSetAttribute(sparse_cluster_fused_kernel<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(num_sms() / kCfCluster * kCfCluster));
+  cfg.blockDim = dim3(kCfThreads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kCfCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, sparse_cluster_fused_kernel<MODE>, &cfg) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  cache_dev[dev] = n;
+  cache_smem[dev] = smem;
+  return n;
+}
+
 static int64_t group_chunks(int64_t n_groups, int64_t vf) {
   const int64_t tiles = (vf + 255) / 256;
   int64_t chunks = (2432 + tiles - 1) / (tiles > 0 ? tiles : 1);  // ~16 CTAs x 152 SMs
@@ -1562,6 +1602,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   int4* tpw = cv.take<int4>((size_t)M * vc);  // packed taps, weights only (row sums)
   float4* xsx = cv.take<float4>((size_t)2 * vc);  // ring stencil, x folded in
   float4* xsw = cv.take<float4>((size_t)2 * vc);  // ring stencil, weights only
+  float* part_cf = cv.take<float>((size_t)kCfMaxClusters * ldp);  // cluster path partial images
   JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
   // stride-4 ring stencil (checked by the caller against the tap table): centres multiples of 4
   const bool ring = bulk && ring_stride == 4 && K == 7 && ring_len >= 8 && ring_len % 4 == 0 &&
@@ -1630,6 +1671,101 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
     else JSCC_GC_K(MODE, 0, TW);                                                                                 \
   } while (0)
+  // ---- fused cluster path (one kernel: coefficients and scatter; see sparse_cluster.cuh):
+  // BF16 split rows and sysmat, one plane of rings under the stride-4 ring stencil, slices
+  // and windows that fit the kernel's registers and shared memory
+  if constexpr (std::is_same<TE, __nv_bfloat16>::value && std::is_same<TC, __nv_bfloat16>::value) {
+    const int n_rings = ring ? (int)(vf / ring_len) : 0;
+    bool cf_ok = g_cluster_fused && ring && taps.n_lf == vf && vf % 8 == 0 && vc % 8 == 0 && n_rings >= kCfCluster &&
+                 vf < (1 << 24);
+    int max_wf = 0, max_wc = 0;
+    if (cf_ok) {
+      for (int r = 0; r < kCfCluster; ++r) {
+        const CfSlice s = cf_slice(r, n_rings, ring_len, (int)vf, (int)vc);
+        max_wf = std::max(max_wf, s.jw1 - s.jw0);
+        max_wc = std::max(max_wc, s.cw1 - s.cw0);
+        cf_ok = cf_ok && (s.J1 - s.J0) <= kCfMaxSliceF;
+      }
+      cf_ok = cf_ok && max_wc <= kCfMaxWindowC;
+    }
+    CfArgs ca{};
+    size_t cf_smem = 0;
+    if (cf_ok) {
+      ca.x_off = kCfHeader;
+      ca.erow_off = ca.x_off + (uint32_t)align_up((size_t)max_wf * 4, 128);
+      ca.erow_stride = (uint32_t)align_up((size_t)max_wf * 2, 128);
+      ca.b_off = ca.erow_off + 3 * ca.erow_stride;
+      ca.b_stride = (uint32_t)align_up((size_t)max_wc * 4, 128);
+      ca.q_off = ca.b_off + 2 * ca.b_stride;
+      ca.q_stride = ca.b_stride;
+      ca.slot_off = ca.q_off + 2 * ca.q_stride;
+      ca.slot_stride = (uint32_t)align_up((size_t)max_wc * 2, 128);
+      const size_t limit = 227 * 1024;
+      int ns = ca.slot_off < limit ? (int)((limit - ca.slot_off) / ca.slot_stride) : 0;
+      ns = std::min(ns, kCfMaxSlots);
+      ca.n_slots = ns;
+      cf_smem = (size_t)ca.slot_off + (size_t)ns * ca.slot_stride;
+      cf_ok = ns >= 2 * kCfNB;
+    }
+    int n_clusters = 0;
+    if (cf_ok) {
+      n_clusters = mode == JSCC_SPARSE_MATERIALIZE ? cf_max_clusters<0>(cf_smem) : cf_max_clusters<1>(cf_smem);
+      n_clusters = std::min(std::min(n_clusters, kCfMaxClusters), (int)n_groups);
+      cf_ok = n_clusters >= 1;
+    }
+    if (cf_ok) {
+      if (mode == JSCC_SPARSE_MATERIALIZE && !have_sums) {
+        JSCC_GC(2, tw, tpw, xsw);  // S_i = t_i . adj(A_g), kept by the caller across calls
+        JSCC_CUDA_CHECK(attr);
+        JSCC_LAUNCH_CHECK();
+      }
+      ca.tc = rows.tc;
+      ca.ld = rows.ld;
+      ca.n_det = rows.n_det;
+      ca.order = order;
+      ca.goff = goff;
+      ca.grow = grow;
+      ca.n_groups = n_groups;
+      ca.eff = eff;
+      ca.ld_eff = ld_eff;
+      ca.x = x;
+      ca.s_ev = s_ev;
+      ca.part = part_cf;
+      ca.ldp = ldp;
+      ca.vf = (int)vf;
+      ca.vc = (int)vc;
+      ca.ring_len = ring_len;
+      ca.n_rings = n_rings;
+      ca.max_wf = max_wf;
+      ca.max_wc = max_wc;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)(n_clusters * kCfCluster));
+      cfg.blockDim = dim3(kCfThreads);
+      cfg.dynamicSmemBytes = cf_smem;
+      cfg.stream = st;
+      cudaLaunchAttribute cattr[1];
+      cattr[0].id = cudaLaunchAttributeClusterDimension;
+      cattr[0].val.clusterDim.x = kCfCluster;
+      cattr[0].val.clusterDim.y = 1;
+      cattr[0].val.clusterDim.z = 1;
+      cfg.attrs = cattr;
+      cfg.numAttrs = 1;
+      if (mode == JSCC_SPARSE_MATERIALIZE)
+        JSCC_TIMED("sparse_group_fused", st, (attr = cudaLaunchKernelEx(&cfg, sparse_cluster_fused_kernel<0>, ca)));
+      else
+        JSCC_TIMED("sparse_group_fused", st, (attr = cudaLaunchKernelEx(&cfg, sparse_cluster_fused_kernel<1>, ca)));
+      JSCC_CUDA_CHECK(attr);
+      JSCC_LAUNCH_CHECK();
+      int64_t blocks = (vf + 255) / 256;
+      if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
+      const int has_scale = scale != 1.0f;
+      JSCC_TIMED("sparse_reduce", st,
+                 (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part_cf, ldp, n_clusters, rotmat_inv, ld_rot,
+                                                                         vf, has_scale, scale, weight)));
+      JSCC_LAUNCH_CHECK();
+      return JSCC_OK;
+    }
+  }
   if (mode == JSCC_SPARSE_MATERIALIZE) {
     if (!have_sums) {
       JSCC_GC(2, tw, tpw, xsw);  // S_i = t_i . adj(A_g), kept by the caller across calls
@@ -1865,7 +2001,13 @@ size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int
          align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) +
          align_up((size_t)chunks * ldp * sizeof(float), 256) +
          2 * align_up((size_t)((adj_width > 0 ? adj_width : 1) + 1) / 2 * (n_coarse > 0 ? n_coarse : 1) * 16, 256) +
-         2 * align_up((size_t)(n_coarse > 0 ? n_coarse : 1) * 32, 256) + 256;
+         2 * align_up((size_t)(n_coarse > 0 ? n_coarse : 1) * 32, 256) +
+         align_up((size_t)kCfMaxClusters * ldp * sizeof(float), 256) + 256;
+}
+
+int jscc_set_fused_cluster(int32_t enable) {
+  jscc::g_cluster_fused = enable != 0;
+  return JSCC_OK;
 }
 
 int jscc_sparse_weight_grouped(const int32_t* row_id, const void* t_coarse, int32_t tc_dtype, int64_t ld_tc,

@@ -682,8 +682,8 @@ def _ring_stencil(z_expand, layer_expand):
     """(ring_len, 4) when the upsample's adjoint is a stride-4 ring stencil: z the identity
     and, within each fine plane, rings of ring_len theta voxels where coarse voxel
     lc = r * (ring_len / 4) + th has exactly the taps r * ring_len + (4 th + d) mod ring_len,
-    d = -3..3 (linear theta interpolation with stride 4, as the polar projector builds it);
-    else (0, 0)."""
+    d = -3..3, with the weights 1 - |d| / 4 (linear theta interpolation with stride 4, as the
+    polar projector builds it, compton_sparse_ops.py:132-154); else (0, 0)."""
     ze = z_expand.detach().to("cpu", torch.float32)
     le = layer_expand.detach().to("cpu", torch.float32)
     if ze.size(0) != ze.size(1) or not torch.equal(ze, torch.eye(ze.size(0))):
@@ -703,6 +703,11 @@ def _ring_stencil(z_expand, layer_expand):
     d = torch.arange(-3, 4)
     expect = r[:, None] * ring_len + (4 * th[:, None] + d[None, :]) % ring_len
     if not torch.equal(torch.sort(expect, dim=1).values, torch.sort(li, dim=1).values):
+        return 0, 0
+    # the polar projector's linear interpolation weights, 1 - |d| / 4 on tap d
+    pos = (li - r[:, None] * ring_len - 4 * th[:, None]) % ring_len
+    dd = torch.where(pos > ring_len // 2, pos - ring_len, pos)
+    if not torch.equal(lw, 1.0 - 0.25 * dd.abs().to(lw.dtype)):
         return 0, 0
     return ring_len, 4
 

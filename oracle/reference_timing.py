@@ -28,11 +28,11 @@ from the SC matrix formula, efficiency rows the same way, the projector by the r
 build_compton_sparse_projector, coarse event rows seeded random (the reference's cost does not
 depend on their values).
 
-GPU (comparison point: the reference's PyTorch FP32 path on the same GB300). The reference's
-osem_joint_mode_local_sparse (recon_osem_local_sparse_jsccsd_only.py:58-100) runs whole
-subset updates of the full workload on the device, on the float32 inputs the bench built; its
-grouped Compton weight (recon_osem_plane_sparse.py:22-57) runs on a sample of whole groups of
-the same subset, scaled by groups; the faster form is the comparison point.
+GPU (comparison point: the reference's PyTorch FP32 path on the same GB300). The parts of the
+reference's osem_joint_mode_local_sparse (recon_osem_local_sparse_jsccsd_only.py:58-100) run
+on the device on the float32 inputs the bench built: the SC half on a whole subset, the
+Compton half in both of the reference's forms on samples of the same subset scaled to it, as
+on the host; the faster form is the comparison point.
 
 When oracle/_ref/ holds no staged copies, the same steps run through the oracle's numpy
 restatement of the same functions (cpu kind "port").
@@ -227,79 +227,58 @@ def run_host(steps, warmup, threads=None):
 
 
 # ------------------------------------------------------------------ the reference's PyTorch path on the GPU
-def run_gpu_plain_fp32(work, subsets=(0, 1), warmup=1, block_events=8192, group_sample=1000):
-    """Whole subset updates of the reference's osem_joint_mode_local_sparse on the GPU, float32,
-    on the bench workload's inputs (the float32 SC matrix, packed float32 event rows, joint
-    sensitivity). Returns a dict for the bench line, with the image after the first timed
-    subset (for a parity check against the product path)."""
+def run_gpu_plain_fp32(work, subset=0, block_events=8192, sample_blocks=2, group_sample=1000):
+    """The reference's own float32 torch path for one subset update of the bench workload on
+    the GPU (its inputs: the float32 SC matrix, packed float32 event rows, joint sensitivity):
+    the SC half (get_weight_single of recon_osem_local_sparse_jsccsd_only.py:8-10) on the whole
+    subset, each Compton form on a sample scaled to the subset (the materialise form,
+    osem_joint_mode_local_sparse's get_weight_compton_sparse, on `sample_blocks` blocks of
+    `block_events` events, by events; the grouped form of recon_osem_plane_sparse.py:22-57 on
+    the first `group_sample` groups, by groups), and safe_em_update. Each part is timed after
+    one untimed call; the faster Compton form is the comparison point."""
     ref = reference_modules()
     if ref is None:
         return {"unavailable": "the reference's modules are not staged in oracle/_ref (oracle/stage_ref.py)"}
-    ljs, cso = ref["recon_osem_local_sparse_jsccsd_only"], ref["compton_sparse_ops"]
+    ljs, rsp, cso = ref["recon_osem_local_sparse_jsccsd_only"], ref["recon_osem_plane_sparse"], ref["compton_sparse_ops"]
     dev = work.dev
     proj = cso.build_compton_sparse_projector(work.grid.coor.cpu(), theta_stride=4, z_stride=1, rotate_num=1).to(dev)
     A = work.A["f32"]
-    ident = torch.arange(1, work.V + 1, device=dev, dtype=torch.int64).unsqueeze(1)
-
-    def inputs(s):
-        ids = work.subset_ids[s]
-        rows = work.rows_f32[s]
-        blocks = list(torch.split(rows, block_events, dim=0))
-        return [[A[ids]]], [[work.proj[ids]]], [[[[b] for b in blocks]]]
-
+    ids = work.subset_ids[subset]
+    rows = work.rows_f32[subset]
     x0 = torch.ones((work.V, 1), device=dev)
-    times = []
-    img_first = None
-    with torch.no_grad():
-        for i, s in enumerate([subsets[0]] * warmup + list(subsets)):
-            A_l, y_l, t_l = inputs(s)
+
+    def timed(fn, reps=2):
+        out = None
+        for _ in range(reps):
             torch.cuda.synchronize(dev)
             t0 = time.perf_counter()
-            img = ljs.osem_joint_mode_local_sparse(A_l, y_l, t_l, [A], [proj], [ident], [ident], x0, work.s_joint,
-                                                   work.alpha, 1, dev)
+            out = fn()
             torch.cuda.synchronize(dev)
-            if i >= warmup:
-                times.append(time.perf_counter() - t0)
-                if img_first is None:
-                    img_first = img
-            del A_l, y_l, t_l
-    sec = float(np.mean(times))
-    # the reference's other Compton form, the grouped weight (recon_osem_plane_sparse.py:22-57),
-    # on a sample of whole groups of the same subset (its cost is linear in the groups), with the
-    # SC half and the update of the materialise run above
-    rsp = ref["recon_osem_plane_sparse"]
-    rows = work.rows_f32[subsets[0]]
-    cp1 = torch.round(rows[:, 0]).to(torch.int64)
-    uniq, counts = torch.unique_consecutive(cp1, return_counts=True)  # rows are sorted by first-hit row
-    g_total = int(uniq.numel())
-    g_sample = min(group_sample, g_total)
-    n_rows = int(counts[:g_sample].sum())
-    block = rows[:n_rows]
+            dt = time.perf_counter() - t0
+        return dt, out
+
     with torch.no_grad():
-        for i in range(2):
-            torch.cuda.synchronize(dev)
-            t0 = time.perf_counter()
-            rsp.get_weight_compton_sparse(block, A, x0, proj)
-            torch.cuda.synchronize(dev)
-            t_g = time.perf_counter() - t0
-    with torch.no_grad():
-        A_l, y_l, _ = inputs(subsets[0])
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        ljs.get_weight_single(A_l[0][0], y_l[0][0], x0)
-        torch.cuda.synchronize(dev)
-        t_sc = time.perf_counter() - t0
-        del A_l, y_l
-    grouped = t_sc + t_g * g_total / g_sample
-    best = min(sec, grouped)
-    return {"value": 1.0 / best, "unit": "subset-iters/s", "seconds_per_subset_update": best,
-            "materialise_form": {"seconds_per_subset_update": sec, "subset_updates_timed": len(times),
-                                 "block_events": block_events,
-                                 "path": "recon_osem_local_sparse_jsccsd_only.osem_joint_mode_local_sparse"},
-            "grouped_form": {"seconds_per_subset_update": grouped, "sc_half_s": t_sc, "groups_timed": g_sample,
-                             "groups_per_subset": g_total, "events_timed": n_rows,
-                             "path": ("recon_osem_plane_sparse.get_weight_compton_sparse on the first "
-                                      f"{g_sample} groups, scaled by groups, + get_weight_single")},
+        A_s, y_s = A[ids], work.proj[ids]
+        t_sc, w = timed(lambda: ljs.get_weight_single(A_s, y_s, x0))
+        del A_s, y_s
+        n_mat = min(rows.size(0), block_events * sample_blocks)
+        t_mat, _ = timed(lambda: [ljs.get_weight_compton_sparse(b, A, x0, proj)
+                                  for b in torch.split(rows[:n_mat], block_events, dim=0)])
+        cp1 = torch.round(rows[:, 0]).to(torch.int64)
+        _, counts = torch.unique_consecutive(cp1, return_counts=True)  # rows are sorted by first-hit row
+        g_total = int(counts.numel())
+        g_sample = min(group_sample, g_total)
+        n_grp = int(counts[:g_sample].sum())
+        t_grp, _ = timed(lambda: rsp.get_weight_compton_sparse(rows[:n_grp], A, x0, proj))
+        t_em, _ = timed(lambda: ljs.safe_em_update(x0, w, work.s_joint))
+    n_ev = rows.size(0)
+    mat = t_mat * n_ev / n_mat
+    grp = t_grp * g_total / g_sample
+    sec = t_sc + min(mat, grp) + t_em
+    return {"value": 1.0 / sec, "unit": "subset-iters/s", "seconds_per_subset_update": sec,
+            "parts_s": {"sc_half": t_sc, "em": t_em, "materialise_subset": mat, "grouped_subset": grp},
+            "sample": (f"SC half on the whole subset ({ids.numel()} bins); materialise form on {n_mat} of the "
+                       f"subset's {n_ev} events in blocks of {block_events}, scaled by events; grouped form on "
+                       f"{g_sample} of its {g_total} groups ({n_grp} events), scaled by groups"),
             "path": ("the reference's float32 torch code on the GPU (cuBLAS GEMV for SC; Compton: the faster of "
-                     "its two sparse forms, both through the dense [36,000 x 9,000] coarse-to-fine matrix)"),
-            "image": img_first}
+                     "its two sparse forms, both through the dense [36,000 x 9,000] coarse-to-fine matrix)")}
