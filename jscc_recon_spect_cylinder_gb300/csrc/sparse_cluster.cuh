@@ -15,16 +15,21 @@
 // [C0, C1) close under adj and up. Every CTA stages its slice of x once, and per group its
 // slice of A_g and of each event row (bulk copies of the 16-byte-aligned windows [jw0, jw1)
 // and [cw0, cw1) around the slices). The only cross-CTA step is f_i = sum over the cluster
-// of the CTAs' partial dots: each team's lead thread stores its partials into every CTA of
-// the cluster (distributed shared memory) and signals that CTA's exchange mbarrier; partials
-// are added in CTA order, so every CTA derives the same f_i and coefficient.
+// of the CTAs' partial dots: each team's lead thread arms its own exchange mbarrier for the
+// batch and writes its partials into the same exchange slot of every CTA of the cluster with
+// st.async (distributed shared memory; each store completes 16 transaction bytes on the
+// receiving CTA's mbarrier, so no fence is needed); partials are added in CTA order, so every
+// CTA derives the same f_i and coefficient. An exchange slot is reused every kCfNX = 4
+// batches, always by the same team (teams alternate batches): before a CTA writes batch b + 4
+// into a peer's slot it has received that peer's partials of batch b + 2, which the peer's
+// lead thread sent after reading batch b from the slot, so no slot is overwritten unread.
 //
 // Warp roles (512 threads, one CTA per SM):
 //   warp 15       producer: bulk copies of the A_g slices (three buffers) and of the event row
 //                 slices (a ring of slots), each issued as soon as its buffer is free;
 //   warps 8-14    group warps: b_g for the slice into one of two buffers, then the scatter of
 //                 the previous group, w_j += A_g[j] up(q_g)[j], into a partial image held in
-//                 registers (kCfM fine voxels per thread);
+//                 registers (kCfRuns runs of four fine voxels per thread);
 //   warps 0-7     two teams of four event warps taking alternate batches of up to kCfNB
 //                 events, so one team computes while the other waits for its exchange: dots
 //                 (four partial sums per event), the exchange, coefficients, q in registers;
@@ -44,12 +49,12 @@ constexpr int kCfGroup = kCfGroupWarps * 32;
 constexpr int kCfProducerWarp = 15;
 constexpr int kCfNB = 4;       // events per batch
 constexpr int kCfQ = 5;        // chunks of four coarse voxels per team thread (window <= 2,560)
-constexpr int kCfM = 48;       // fine voxels per group thread (slice <= 10,752)
+constexpr int kCfRuns = 12;    // runs of four fine voxels per group thread (slice <= 10,752)
 constexpr int kCfNX = 4;       // exchange slots
 constexpr int kCfMaxSlots = 16;
 constexpr int kCfHeader = 4096;
 constexpr int kCfMaxWindowC = kCfTeam * 4 * kCfQ;
-constexpr int kCfMaxSliceF = kCfGroup * kCfM;
+constexpr int kCfMaxSliceF = kCfGroup * kCfRuns * 4;
 static_assert(kCfProducerWarp * 32 + 32 == kCfThreads && 2 * kCfTeam + kCfGroup + 32 == kCfThreads, "roles");
 
 // header layout (bytes)
@@ -62,7 +67,6 @@ constexpr int kCfOffBEmpty = 320;                   // [2]
 constexpr int kCfOffQFull = 336;                    // [2]
 constexpr int kCfOffQEmpty = 352;                   // [2]
 constexpr int kCfOffXFull = 368;                    // [kCfNX]
-constexpr int kCfOffXEmpty = 400;                   // [kCfNX]
 constexpr int kCfOffFlags = 512;                    // abort
 constexpr int kCfOffSlotIssued = 576;               // [kCfMaxSlots] int
 constexpr int kCfOffSlotWaited = 640;               // [kCfMaxSlots] int
@@ -71,7 +75,8 @@ constexpr int kCfOffErowWaited = 720;               // [3] int
 constexpr int kCfOffRed = 1024;                     // [2][kCfTeamWarps][kCfNB] float
 constexpr int kCfOffCs = 1280;                      // [2][kCfNB] float
 constexpr int kCfOffXval = 1536;                    // [kCfNX][kCfCluster][kCfNB] float
-static_assert(kCfOffXEmpty + 8 * kCfNX <= kCfOffFlags, "barriers");
+static_assert(kCfOffXFull + 8 * kCfNX <= kCfOffFlags, "barriers");
+static_assert(kCfNX == 4, "slot reuse argument: two alternating teams, four slots");
 static_assert(kCfOffXval + 4 * kCfNX * kCfCluster * kCfNB <= kCfHeader, "header");
 
 // ------------------------------------------------------------------ cluster primitives
@@ -100,12 +105,13 @@ __device__ __forceinline__ uint32_t map_to_rank(const void* p, uint32_t rank) {
   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
   return r;
 }
-__device__ __forceinline__ void st_cluster_v4(uint32_t addr, float a, float b, float c, float d) {
-  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+// 16 bytes into another CTA's shared memory, completing 16 transaction bytes on that CTA's
+// mbarrier (no fence: the receiver's wait on its own mbarrier sees the data)
+__device__ __forceinline__ void st_async_v4(uint32_t addr, float a, float b, float c, float d, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   addr),
+               "f"(a), "f"(b), "f"(c), "f"(d), "r"(bar)
                : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
 }
 // a wait that sees arrivals (and the stores before them) from other CTAs of the cluster
 __device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
@@ -178,7 +184,6 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
   uint64_t* q_full = reinterpret_cast<uint64_t*>(smem + kCfOffQFull);
   uint64_t* q_empty = reinterpret_cast<uint64_t*>(smem + kCfOffQEmpty);
   uint64_t* xfull = reinterpret_cast<uint64_t*>(smem + kCfOffXFull);
-  uint64_t* xempty = reinterpret_cast<uint64_t*>(smem + kCfOffXEmpty);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + kCfOffFlags);
   int* slot_issued = reinterpret_cast<int*>(smem + kCfOffSlotIssued);
   int* slot_waited = reinterpret_cast<int*>(smem + kCfOffSlotWaited);
@@ -216,10 +221,7 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
       mbar_init(q_full + k, 1);
       mbar_init(q_empty + k, 1);
     }
-    for (int k = 0; k < kCfNX; ++k) {
-      mbar_init(xfull + k, kCfCluster);
-      mbar_init(xempty + k, kCfCluster);
-    }
+    for (int k = 0; k < kCfNX; ++k) mbar_init(xfull + k, 1);  // the local arm; the peers' bytes complete it
     *abort_flag = 0;
     mbar_init_fence();
   }
@@ -296,42 +298,54 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
   } else if (warp >= 2 * kCfTeamWarps) {
     // ------------------------------------------------------------ group warps
     const int gt = tid - 2 * kCfTeam;
-    float acc[kCfM];
+    // the partial image of this CTA's slice in registers: runs of four fine voxels (one
+    // coarse theta step of a ring: the same two coarse taps), run rho = gt + m * kCfGroup
+    float acc[kCfRuns][4];
 #pragma unroll
-    for (int m = 0; m < kCfM; ++m) acc[m] = 0.f;
-    // this thread's first fine voxel (J0 + gt) as ring position and coarse base
-    const int nf = sl.J1 - sl.J0;
-    int p0 = gt, r0 = 0;
-    while (p0 >= a.ring_len) {
-      p0 -= a.ring_len;
-      ++r0;
+    for (int m = 0; m < kCfRuns; ++m)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[m][i] = 0.f;
+    const int n_runs = (sl.J1 - sl.J0) / 4;
+    // run gt: theta index and the coarse index of theta 0 of its ring
+    int th0 = gt, cb0 = sl.C0;
+    while (th0 >= nthc) {
+      th0 -= nthc;
+      cb0 += nthc;
     }
-    const int cbase0 = (sl.J0 / a.ring_len + r0) * nthc;  // coarse index of theta 0 of the ring
+    // this thread's first coarse voxel c = cw0 + gt: ring-relative theta and ring start
+    int ath0 = sl.cw0 + gt - sl.C0, ar0 = sl.C0 / nthc;
+    while (ath0 >= nthc) {
+      ath0 -= nthc;
+      ++ar0;
+    }
+    while (ath0 < 0) {
+      ath0 += nthc;
+      --ar0;
+    }
     bool bad = false, aborted = false;
-    // scatter of group k: acc[m] += A_g[j] (w_lo q[c_lo] + w_hi q[c_hi]) for j = J0 + gt + m * kCfGroup
+    // scatter of group k: for each run, w[4th + i] += A[4th + i] ((1 - i/4) q[th] + (i/4) q[th + 1])
     auto scatter = [&](int k) {
       if (!cf_wait_cluster(q_full + (k & 1), (uint32_t)(k >> 1) & 1u, abort_flag, polls)) bad = true;
       const __nv_bfloat16* er = erow(k % 3);
       const float* q = qbuf(k & 1);
-      int p = p0, cb = cbase0;
+      int th = th0, cb = cb0;
 #pragma unroll
-      for (int m = 0; m < kCfM; ++m) {
-        const int jj = gt + m * kCfGroup;
-        if (jj < nf) {
-          const int th = p >> 2, kk = p & 3;
-          const int clo = cb + th;
-          const int chi = cb + (th + 1 == nthc ? 0 : th + 1);
-          const float A = __bfloat162float(er[sl.J0 + jj - sl.jw0]);
-          float up = q[clo - sl.cw0];
-          if (kk) {
-            const float wh = 0.25f * (float)kk;
-            up = fmaf(wh, q[chi - sl.cw0], (1.0f - wh) * up);
-          }
-          acc[m] = fmaf(A, up, acc[m]);
+      for (int m = 0; m < kCfRuns; ++m) {
+        const int rho = gt + m * kCfGroup;
+        if (rho < n_runs) {
+          const int clo = cb + th, chi = cb + (th + 1 == nthc ? 0 : th + 1);
+          const float ql = q[clo - sl.cw0], qh = q[chi - sl.cw0];
+          const uint2 ar = *reinterpret_cast<const uint2*>(er + (sl.J0 + 4 * rho - sl.jw0));
+          const float up[4] = {ql, fmaf(0.25f, qh, 0.75f * ql), fmaf(0.5f, qh, 0.5f * ql),
+                               fmaf(0.75f, qh, 0.25f * ql)};
+          acc[m][0] = fmaf(bf16_lo(ar.x), up[0], acc[m][0]);
+          acc[m][1] = fmaf(bf16_hi(ar.x), up[1], acc[m][1]);
+          acc[m][2] = fmaf(bf16_lo(ar.y), up[2], acc[m][2]);
+          acc[m][3] = fmaf(bf16_hi(ar.y), up[3], acc[m][3]);
         }
-        p += kCfGroup;
-        while (p >= a.ring_len) {
-          p -= a.ring_len;
+        th += kCfGroup;
+        while (th >= nthc) {
+          th -= nthc;
           cb += nthc;
         }
       }
@@ -342,6 +356,8 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
       }
       return true;
     };
+    // taps of the stride-4 ring stencil, d = -3..3 at positions 4 th - 4 + i, i = 1..7
+    constexpr float kW[8] = {0.f, 0.25f, 0.5f, 0.75f, 1.0f, 0.75f, 0.5f, 0.25f};
     for (int kg = 0; kg < n_mine; ++kg) {
       const int k3 = kg % 3;
       if (!cf_wait_cluster(erow_full + k3, (uint32_t)(kg / 3) & 1u, abort_flag, polls)) bad = true;
@@ -351,21 +367,34 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
       // b[c - cw0] = sum_d (w_d x_j) A_j over the taps j of coarse c (zero outside [C0, C1))
       float* b = bbuf(kg & 1);
       const __nv_bfloat16* er = erow(k3);
+      int th = ath0, ring = ar0;
       for (int c = sl.cw0 + gt; c < sl.cw1; c += kCfGroup) {
         float v = 0.f;
         if (c >= sl.C0 && c < sl.C1) {
-          const int ring = c / nthc, th = c - ring * nthc;
-          const int jr = ring * a.ring_len;  // first fine voxel of the ring
+          const int jr = ring * a.ring_len - sl.jw0;  // first fine voxel of the ring, window-relative
+          if (th > 0) {
+            const int o = jr + 4 * th - 4;  // a multiple of 4: 16-byte x loads, 8-byte A loads
+            const float4 x0 = *reinterpret_cast<const float4*>(xs + o), x1 = *reinterpret_cast<const float4*>(xs + o + 4);
+            const uint2 a0 = *reinterpret_cast<const uint2*>(er + o), a1 = *reinterpret_cast<const uint2*>(er + o + 4);
+            const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+            const float av[8] = {bf16_lo(a0.x), bf16_hi(a0.x), bf16_lo(a0.y), bf16_hi(a0.y),
+                                 bf16_lo(a1.x), bf16_hi(a1.x), bf16_lo(a1.y), bf16_hi(a1.y)};
 #pragma unroll
-          for (int d = -3; d <= 3; ++d) {
-            int pj = 4 * th + d;
-            if (pj < 0) pj += a.ring_len;
-            const int j = jr + pj - sl.jw0;
-            const float w = 1.0f - 0.25f * (float)(d < 0 ? -d : d);
-            v = fmaf(w * xs[j], __bfloat162float(er[j]), v);
+            for (int i = 1; i < 8; ++i) v = fmaf(kW[i] * xv[i], av[i], v);
+          } else {
+#pragma unroll
+            for (int i = 1; i < 8; ++i) {
+              const int pj = i - 4 < 0 ? i - 4 + a.ring_len : i - 4;
+              v = fmaf(kW[i] * xs[jr + pj], __bfloat162float(er[jr + pj]), v);
+            }
           }
         }
         b[c - sl.cw0] = v;
+        th += kCfGroup;
+        while (th >= nthc) {
+          th -= nthc;
+          ++ring;
+        }
       }
       if (role_sync_or(5, kCfGroup, bad)) {
         aborted = true;
@@ -383,9 +412,9 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
     } else {
       float* out = a.part + (int64_t)cid * a.ldp + sl.J0;
 #pragma unroll
-      for (int m = 0; m < kCfM; ++m) {
-        const int jj = gt + m * kCfGroup;
-        if (jj < nf) out[jj] = acc[m];
+      for (int m = 0; m < kCfRuns; ++m) {
+        const int rho = gt + m * kCfGroup;
+        if (rho < n_runs) *reinterpret_cast<float4*>(out + 4 * rho) = make_float4(acc[m][0], acc[m][1], acc[m][2], acc[m][3]);
       }
     }
   } else {
@@ -470,16 +499,11 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
               if (k < n) si[k] = a.s_ev[eb + k];
           }
           const int x = bs % kCfNX;
-          bool ok = bs < kCfNX ||
-                    cf_wait_cluster(xempty + x, (uint32_t)((bs / kCfNX) - 1) & 1u, abort_flag, polls);
-          if (ok) {
-            float* dst = xval + (x * kCfCluster + (int)rank) * kCfNB;
-            for (uint32_t d = 0; d < (uint32_t)kCfCluster; ++d) {
-              st_cluster_v4(map_to_rank(dst, d), fr[0], fr[1], fr[2], fr[3]);
-              mbar_arrive_cluster(map_to_rank(xfull + x, d));
-            }
-            ok = cf_wait_cluster(xfull + x, (uint32_t)(bs / kCfNX) & 1u, abort_flag, polls);
-          }
+          mbar_arrive_expect_tx(xfull + x, (uint32_t)(kCfCluster * kCfNB * sizeof(float)));
+          float* dst = xval + (x * kCfCluster + (int)rank) * kCfNB;
+          for (uint32_t d = 0; d < (uint32_t)kCfCluster; ++d)
+            st_async_v4(map_to_rank(dst, d), fr[0], fr[1], fr[2], fr[3], map_to_rank(xfull + x, d));
+          const bool ok = cf_wait_cluster(xfull + x, (uint32_t)(bs / kCfNX) & 1u, abort_flag, polls);
           if (ok) {
 #pragma unroll
             for (int k = 0; k < kCfNB; ++k) {
@@ -492,7 +516,6 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
               }
               cst[k] = c;
             }
-            for (uint32_t d = 0; d < (uint32_t)kCfCluster; ++d) mbar_arrive_cluster(map_to_rank(xempty + x, d));
           } else {
             bad = true;
           }
