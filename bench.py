@@ -889,7 +889,8 @@ class SparseLaunchBench:
     def kernel_bytes(self, dtype):
         coef = self.n_events * (self.Vc * 2 + 4) + self.n_groups * (self.V * 2 + self.Vc * 4)
         scatter = self.n_groups * (self.V * 2 + self.Vc * 4) + 16 * self.V * 4
-        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter}
+        fused = self.n_events * (self.Vc * 2 + 4) + self.n_groups * self.V * 2 + 38 * self.V * 4
+        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter, "sparse_group_fused": fused}
 
     def config(self):
         return {"workload": self.name, "events": self.n_events, "groups": self.n_groups, "voxels": self.V,

@@ -422,11 +422,12 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * d = -3..3, with the polar projector's linear weights 1 - |d| / 4, in each plane (the
  * caller checks the table; the kernels then compute the tap indices, and the weights where
  * they need them, instead of loading them).
- * With BF16 split rows and a BF16 sysmat on one plane of at least four such rings, the
- * per-iteration weight (mode GROUPED, or MATERIALIZE with have_sums) runs as one fused kernel
- * on clusters of four CTAs that split the rings: each event row and each group's sysmat row
- * is read from HBM once and the per-group coarse sums stay on chip (the per-event sums of
- * MATERIALIZE are computed beforehand by the two-kernel pipeline when have_sums == 0).
+ * With BF16 split rows and a BF16 sysmat on one plane of at least four such rings, and the
+ * fused cluster kernel enabled (jscc_set_fused_cluster), the per-iteration weight (mode
+ * GROUPED, or MATERIALIZE with have_sums) runs as one kernel on clusters of four CTAs that
+ * split the rings: each event row and each group's sysmat row is read from HBM once and the
+ * per-group coarse sums stay on chip (the per-event sums of MATERIALIZE are computed
+ * beforehand by the two-kernel pipeline when have_sums == 0).
  */
 /*
  * Number of bounded device waits that gave up since the last call (then reset to 0).
@@ -436,9 +437,10 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
 JSCC_API int jscc_take_wait_timeout_count(unsigned int* out);
 
 /*
- * Whether jscc_sparse_weight_grouped may use the fused cluster kernel where it applies
- * (enable != 0, the default) or always runs the two-kernel pipeline (coefficients, then the
- * scatter). Process-wide; for comparisons of the two forms. No counterpart in the reference.
+ * Whether jscc_sparse_weight_grouped uses the fused cluster kernel where it applies
+ * (enable != 0) or the two-kernel pipeline (coefficients, then the scatter; the default, as it
+ * is the faster of the two on GB300 at the joint configuration's sizes). Process-wide. No
+ * counterpart in the reference.
  */
 JSCC_API int jscc_set_fused_cluster(int32_t enable);
 

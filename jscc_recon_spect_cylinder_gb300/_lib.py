@@ -289,8 +289,8 @@ timeout_epoch = 0
 
 
 def set_fused_cluster(enable: bool) -> None:
-    """Let the grouped sparse weight use its fused cluster kernel where it applies (default),
-    or always run the two-kernel pipeline."""
+    """Let the grouped sparse weight use its fused cluster kernel where it applies, or (the
+    default) the two-kernel pipeline."""
     check(load().jscc_set_fused_cluster(1 if enable else 0), "jscc_set_fused_cluster")
 
 

@@ -33,7 +33,8 @@
 //   warps 0-7     two teams of four event warps taking alternate batches of up to kCfNB
 //                 events, so one team computes while the other waits for its exchange: dots
 //                 (four partial sums per event), the exchange, coefficients, q in registers;
-//                 at the end of a group team 0 stores its q, team 1 adds its own.
+//                 at the end of a group each team stores its q into a buffer of its own, and
+//                 the scatter adds the two (team 0 first).
 // Every wait is bounded (g_bk_poll_limit): a CTA that gives up raises its abort flag, its
 // roles leave their loops, its peers give up on their exchange waits, and every CTA waits
 // (bounded) for its own copies in flight, arrives at the closing cluster barrier and counts
@@ -202,7 +203,10 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
   const uint32_t erow_bytes = (uint32_t)(sl.jw1 - sl.jw0) * 2u, row_bytes = (uint32_t)(sl.cw1 - sl.cw0) * 2u;
   auto erow = [&](int k) { return reinterpret_cast<__nv_bfloat16*>(smem + a.erow_off + (size_t)k * a.erow_stride); };
   auto bbuf = [&](int k) { return reinterpret_cast<float*>(smem + a.b_off + (size_t)k * a.b_stride); };
-  auto qbuf = [&](int k) { return reinterpret_cast<float*>(smem + a.q_off + (size_t)k * a.q_stride); };
+  // q buffers: [group parity][event team]
+  auto qbuf = [&](int k, int team) {
+    return reinterpret_cast<float*>(smem + a.q_off + (size_t)(2 * k + team) * a.q_stride);
+  };
   auto slot = [&](int s) { return reinterpret_cast<__nv_bfloat16*>(smem + a.slot_off + (size_t)s * a.slot_stride); };
   if (tid == 0) {
     for (int s = 0; s < kCfMaxSlots; ++s) {
@@ -217,8 +221,8 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
     }
     for (int k = 0; k < 2; ++k) {
       mbar_init(b_full + k, 1);
-      mbar_init(b_empty + k, 1);
-      mbar_init(q_full + k, 1);
+      mbar_init(b_empty + k, 2);  // one arrival per event team
+      mbar_init(q_full + k, 2);   // one arrival per event team
       mbar_init(q_empty + k, 1);
     }
     for (int k = 0; k < kCfNX; ++k) mbar_init(xfull + k, 1);  // the local arm; the peers' bytes complete it
@@ -325,16 +329,17 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
     bool bad = false, aborted = false;
     // scatter of group k: for each run, w[4th + i] += A[4th + i] ((1 - i/4) q[th] + (i/4) q[th + 1])
     auto scatter = [&](int k) {
-      if (!cf_wait_cluster(q_full + (k & 1), (uint32_t)(k >> 1) & 1u, abort_flag, polls)) bad = true;
+      if (!bk_wait(q_full + (k & 1), (uint32_t)(k >> 1) & 1u, abort_flag, polls)) bad = true;
       const __nv_bfloat16* er = erow(k % 3);
-      const float* q = qbuf(k & 1);
+      const float* q0 = qbuf(k & 1, 0);
+      const float* q1 = qbuf(k & 1, 1);
       int th = th0, cb = cb0;
 #pragma unroll
       for (int m = 0; m < kCfRuns; ++m) {
         const int rho = gt + m * kCfGroup;
         if (rho < n_runs) {
           const int clo = cb + th, chi = cb + (th + 1 == nthc ? 0 : th + 1);
-          const float ql = q[clo - sl.cw0], qh = q[chi - sl.cw0];
+          const float ql = q0[clo - sl.cw0] + q1[clo - sl.cw0], qh = q0[chi - sl.cw0] + q1[chi - sl.cw0];
           const uint2 ar = *reinterpret_cast<const uint2*>(er + (sl.J0 + 4 * rho - sl.jw0));
           const float up[4] = {ql, fmaf(0.25f, qh, 0.75f * ql), fmaf(0.5f, qh, 0.5f * ql),
                                fmaf(0.75f, qh, 0.25f * ql)};
@@ -360,9 +365,9 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
     constexpr float kW[8] = {0.f, 0.25f, 0.5f, 0.75f, 1.0f, 0.75f, 0.5f, 0.25f};
     for (int kg = 0; kg < n_mine; ++kg) {
       const int k3 = kg % 3;
-      if (!cf_wait_cluster(erow_full + k3, (uint32_t)(kg / 3) & 1u, abort_flag, polls)) bad = true;
+      if (!bk_wait(erow_full + k3, (uint32_t)(kg / 3) & 1u, abort_flag, polls)) bad = true;
       else if (gt == 0) erow_waited[k3] += 1;  // counted only when the copy is known complete
-      if (kg >= 2 && !cf_wait_cluster(b_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls))
+      if (kg >= 2 && !bk_wait(b_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls))
         bad = true;
       // b[c - cw0] = sum_d (w_d x_j) A_j over the taps j of coarse c (zero outside [C0, C1))
       float* b = bbuf(kg & 1);
@@ -420,7 +425,7 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
   } else {
     // ------------------------------------------------------------ event teams
     const int team = warp / kCfTeamWarps, tw = warp % kCfTeamWarps, lt = tid - team * kCfTeam;
-    const int bar_team = 1 + team;  // named barriers 1, 2: one team; 3: both teams
+    const int bar_team = 1 + team;  // named barriers 1, 2: one team each
     const int wc = sl.cw1 - sl.cw0;
     float* redt = red + team * kCfTeamWarps * kCfNB;
     float* cst = cs + team * kCfNB;
@@ -431,7 +436,7 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
     for (int kg = 0; kg < n_mine; ++kg) {
       const int gi = cid + kg * G;
       const int e0 = a.goff[gi], e1 = a.goff[gi + 1];
-      if (!cf_wait_cluster(b_full + (kg & 1), (uint32_t)(kg >> 1) & 1u, abort_flag, polls)) bad = true;
+      if (!bk_wait(b_full + (kg & 1), (uint32_t)(kg >> 1) & 1u, abort_flag, polls)) bad = true;
       const float* b = bbuf(kg & 1);
 #pragma unroll
       for (int u = 0; u < kCfQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -445,7 +450,7 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
         for (int k = 0; k < kCfNB; ++k) {
           sk[k] = (seq_b + k) % a.n_slots;
           if (k < n) {
-            if (!cf_wait_cluster(full + sk[k], (uint32_t)((seq_b + k) / a.n_slots) & 1u, abort_flag, polls))
+            if (!bk_wait(full + sk[k], (uint32_t)((seq_b + k) / a.n_slots) & 1u, abort_flag, polls))
               bad = true;
             else if (lt == 0)
               slot_waited[sk[k]] += 1;  // counted only when the copy is known complete
@@ -479,7 +484,7 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
             if (lane == 0) redt[tw * kCfNB + k] = f;
           }
         if (role_sync_or(bar_team, kCfTeam, bad)) {
-          aborted = true;  // leaves this team's batches; both teams decide at the group's end
+          aborted = true;
           break;
         }
         if (lt == 0) {
@@ -549,40 +554,22 @@ __global__ void __launch_bounds__(kCfThreads, 1) sparse_cluster_fused_kernel(CfA
             if (k < n) mbar_arrive(empty + sk[k]);
         }
       }
-      // ---- end of the group: q = q(team 0) + q(team 1) into the q buffer (both teams reach
-      // this barrier, also a team that gave up, so the decision is uniform)
-      if (!aborted && kg >= 2 &&
-          !cf_wait_cluster(q_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls))
-        bad = true;
-      if (role_sync_or(3, 2 * kCfTeam, bad || aborted)) {
+      if (aborted) break;
+      // ---- end of the group: this team's q into its own buffer (the scatter adds the two
+      // teams' buffers, team 0 first)
+      if (kg >= 2 && !bk_wait(q_empty + (kg & 1), (uint32_t)((kg >> 1) - 1) & 1u, abort_flag, polls)) bad = true;
+      if (role_sync_or(bar_team, kCfTeam, bad)) {
         aborted = true;
         break;
       }
-      float* q = qbuf(kg & 1);
-      if (team == 0) {
+      float* q = qbuf(kg & 1, team);
 #pragma unroll
-        for (int u = 0; u < kCfQ; ++u) {
-          const int c = 4 * lt + u * (4 * kCfTeam);
-          if (c < wc) *reinterpret_cast<float4*>(q + c) = qa[u];
-        }
+      for (int u = 0; u < kCfQ; ++u) {
+        const int c = 4 * lt + u * (4 * kCfTeam);
+        if (c < wc) *reinterpret_cast<float4*>(q + c) = qa[u];
       }
-      role_sync(3, 2 * kCfTeam);
-      if (team == 1) {
-#pragma unroll
-        for (int u = 0; u < kCfQ; ++u) {
-          const int c = 4 * lt + u * (4 * kCfTeam);
-          if (c < wc) {
-            float4 v = *reinterpret_cast<const float4*>(q + c);
-            v.x += qa[u].x;
-            v.y += qa[u].y;
-            v.z += qa[u].z;
-            v.w += qa[u].w;
-            *reinterpret_cast<float4*>(q + c) = v;
-          }
-        }
-      }
-      role_sync(3, 2 * kCfTeam);
-      if (tid == 0) {
+      role_sync(bar_team, kCfTeam);
+      if (lt == 0) {
         mbar_arrive(q_full + (kg & 1));
         mbar_arrive(b_empty + (kg & 1));
       }

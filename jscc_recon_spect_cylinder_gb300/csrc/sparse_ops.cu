@@ -1506,7 +1506,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
 #include "sparse_cluster.cuh"
 
 constexpr int kCfMaxClusters = 64;  // partial images reserved in the workspace for the cluster path
-static bool g_cluster_fused = true;
+static bool g_cluster_fused = false;  // opt-in (jscc_set_fused_cluster)
 
 // Co-resident clusters of the fused kernel for this device and shared-memory size (cached).
 template <int MODE>
@@ -1698,7 +1698,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
       ca.b_stride = (uint32_t)align_up((size_t)max_wc * 4, 128);
       ca.q_off = ca.b_off + 2 * ca.b_stride;
       ca.q_stride = ca.b_stride;
-      ca.slot_off = ca.q_off + 2 * ca.q_stride;
+      ca.slot_off = ca.q_off + 4 * ca.q_stride;  // q: [group parity][event team]
       ca.slot_stride = (uint32_t)align_up((size_t)max_wc * 2, 128);
       const size_t limit = 227 * 1024;
       int ns = ca.slot_off < limit ? (int)((limit - ca.slot_off) / ca.slot_stride) : 0;

@@ -204,7 +204,10 @@ class JointWorkload:
         groups = float(sum(torch.unique(i).numel() for i in self.ids)) / self.subsets
         coef = ev * (self.Vc * b + 4) + groups * (self.V * b + self.Vc * 4)
         scatter = groups * (self.V * b + self.Vc * 4) + 16 * self.V * 4
-        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter}
+        # the fused cluster kernel: every coarse row and its event sum once, one sysmat row per
+        # group, one float32 partial image per cluster (at most 38 clusters of four CTAs)
+        fused = ev * (self.Vc * b + 4) + groups * self.V * b + 38 * self.V * 4
+        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter, "sparse_group_fused": fused}
 
     def group_count(self):
         """Mean number of groups (distinct first-hit rows) per subset."""

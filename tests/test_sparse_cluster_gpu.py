@@ -18,6 +18,16 @@ pytestmark = pytest.mark.gpu
 TOL_W = 1e-5
 
 
+@pytest.fixture
+def fused(cuda):
+    """The fused cluster kernel switched on for the test (it is opt-in), off again after."""
+    from jscc_recon_spect_cylinder_gb300 import _lib
+
+    _lib.set_fused_cluster(True)
+    yield
+    _lib.set_fused_cluster(False)
+
+
 def _problem(cuda, n_r, n_theta, n_det, n_events, seed, big_group=0):
     from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
     from jscc_recon_spect_cylinder_gb300 import synthetic
@@ -42,7 +52,7 @@ def _problem(cuda, n_r, n_theta, n_det, n_events, seed, big_group=0):
     (16, 96, 300, 2000, 77),      # one group of 77 events (> the 16 row slots)
     (13, 64, 200, 1500, 0),       # 13 rings: slices of 3 and 4 rings, coarse windows past the slices
 ])
-def test_fused_cluster_matches_two_kernel_and_event(cuda, n_r, n_theta, n_det, n_events, big):
+def test_fused_cluster_matches_two_kernel_and_event(cuda, fused, n_r, n_theta, n_det, n_events, big):
     from jscc_recon_spect_cylinder_gb300 import _lib, ops
 
     A, tb, tc, ids, x, _ = _problem(cuda, n_r, n_theta, n_det, n_events, n_r + n_det, big)
@@ -63,7 +73,7 @@ def test_fused_cluster_matches_two_kernel_and_event(cuda, n_r, n_theta, n_det, n
     _lib.check_wait_timeouts()
 
 
-def test_fused_cluster_rotated_views(cuda):
+def test_fused_cluster_rotated_views(cuda, fused):
     """Rotation tables (gather the image through rotmat, scatter the weight through
     rotmat_inv) around the fused kernel, as the joint loops call it per view."""
     from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
@@ -79,7 +89,7 @@ def test_fused_cluster_rotated_views(cuda):
     _lib.check_wait_timeouts()
 
 
-def test_fused_cluster_waits_give_up_and_recover(cuda):
+def test_fused_cluster_waits_give_up_and_recover(cuda, fused):
     """With the poll bound at 0 every wait of the fused kernel gives up at once (the bulk
     copies still complete; the peers give up on their exchanges): the launch returns, the
     give-up is counted and reported, and with the default bound the result is exact again."""
