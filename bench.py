@@ -241,6 +241,38 @@ class Sc3Workload:
                 "seconds": el}
 
 
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+FP32_PEAK_SOURCE = ("nominal: 152 SMs x 128 FP32 lanes x 2 FLOP per FMA x 2.07 GHz (no measured FP32 figure on "
+                    "this pool)")
+
+
+def cone_flop_per_pair():
+    """FP32 FLOPs per fully evaluated event-voxel pair of the strict fused cone passes, from
+    ncu's FP32 instruction counters on the config-2 forward and back launches
+    (profiles/cone_flops_jsccd2.json: FADD, FMUL = 1, FFMA, FADD2, FMUL2 = 2, FFMA2 = 4 per
+    thread instruction, over the launch's event-voxel pairs; the special-function unit's
+    instructions, compares and selects are not counted), averaged over the two directions;
+    the formula's hand count (Cone2Bench.K_CONE) when no capture is committed."""
+    f = REPO / "profiles" / "cone_flops_jsccd2.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        vals = [d[k]["flop_per_pair"] for k in ("cone_forward_pair", "cone_back_pair") if k in d]
+        if vals:
+            return float(np.mean(vals)), "ncu FP32 instruction counters (profiles/cone_flops_jsccd2.json)"
+    return float(Cone2Bench.K_CONE), "hand count of the strict formula"
+
+
+def cone_roofline(pairs_per_s, over=None):
+    fpp, src = cone_flop_per_pair()
+    achieved = pairs_per_s * fpp / 1e12
+    out = {"bound": "fp32", "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+           "frac": achieved / FP32_PEAK_TFLOPS, "peak_source": FP32_PEAK_SOURCE, "flop_per_pair": fpp,
+           "flop_source": src}
+    if over:
+        out["over"] = over
+    return out
+
+
 class Cone2Bench:
     """Config 2 (JSCCD list mode, FP32): the fused strict cone weight w = T^T (1 / T x) with
     T recomputed on the fly from 64-byte event records. 100 x 360 polar grid (36,000 voxels);
@@ -367,14 +399,9 @@ class Cone2Bench:
         torch.cuda.synchronize(self.dev)
         ms_w = t0.elapsed_time(t1) / n
         pairs = self.units_per_step() / (ms_per_step / 1e3)
-        peak = 152 * 128 * 2 * 2.07e9 / 1e12  # nominal FP32 FMA peak, TFLOP/s (no measured figure)
-        achieved = pairs * self.K_CONE / 1e12
         stored = self.stored_t(img)
         return {"window_9sigma": {"pairs_per_s": self.units_per_step() / (ms_w / 1e3), "ms_per_step": ms_w},
-                "stored_t": stored,
-                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
-                                  "flop_per_pair": self.K_CONE}}
+                "stored_t": stored, "fp32_roofline": cone_roofline(pairs)}
 
 
 class Map5Bench:
@@ -489,12 +516,8 @@ class Map5Bench:
         torch.cuda.synchronize(self.dev)
         ms = t0.elapsed_time(t1)
         pairs = 2 * len(self.ev) * self.V
-        peak = 152 * 128 * 2 * 2.07e9 / 1e12
-        achieved = pairs / (ms / 1e3) * self.K_CONE / 1e12
         return {"cone_pass": {"pairs_per_s": pairs / (ms / 1e3), "ms": ms},
-                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
-                                  "flop_per_pair": self.K_CONE}}
+                "fp32_roofline": cone_roofline(pairs / (ms / 1e3))}
 
 
 class Batch4Bench:
@@ -826,14 +849,9 @@ class Batch4JointBench(Batch4Bench):
         joint path run for the 64 instances in turn, and per-instance errors against float64."""
         pairs = 2 * self.n_kept * self.V  # forward + back cone pairs per iteration
         rate = pairs / (ms_per_step / 1e3)
-        peak = 152 * 128 * 2 * 2.07e9 / 1e12
-        achieved = rate * Cone2Bench.K_CONE / 1e12
         value = self.units_per_step() / (ms_per_step / 1e3)
         seq = self._sequential_fp32()
-        return {"compton_pairs_per_s": rate,
-                "fp32_roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                                  "frac": achieved / peak, "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
-                                  "flop_per_pair": Cone2Bench.K_CONE, "over": "the whole step"},
+        return {"compton_pairs_per_s": rate, "fp32_roofline": cone_roofline(rate, over="the whole step"),
                 "sequential_fp32_joint_64_instances": {"subset_iters_per_s": seq,
                                                        "batched_speedup_vs_64_sequential": value / seq},
                 "errors_vs_fp64": self._errors()}
