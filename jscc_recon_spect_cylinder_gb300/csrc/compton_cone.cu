@@ -538,6 +538,32 @@ __device__ __forceinline__ float ex2_approx(float z) {
 
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 
+// arccos of two cosines (|c| < 1) by the rational-free approximation of Abramowitz & Stegun,
+// Handbook of Mathematical Functions, 4.4.46 (after Hastings): acos(x) = sqrt(1 - x) P7(x) on
+// [0, 1], |error| <= 2e-8 in exact arithmetic, and acos(x) = pi - acos(-x) below 0. The
+// square root is 1 - |x| times its reciprocal square root refined by one Newton step, in
+// packed f32x2 arithmetic (float32 evaluation error: a few 1e-7 rad; checked against acosf by
+// the cone tests through the fused-versus-stored weights).
+__device__ __forceinline__ float2 acos2_as4446(float2 c) {
+  const float2 a = make_float2(fabsf(c.x), fabsf(c.y));
+  float2 p = f2(-0.0012624911f);
+  p = __ffma2_rn(p, a, f2(0.0066700901f));
+  p = __ffma2_rn(p, a, f2(-0.0170881256f));
+  p = __ffma2_rn(p, a, f2(0.0308918810f));
+  p = __ffma2_rn(p, a, f2(-0.0501743046f));
+  p = __ffma2_rn(p, a, f2(0.0889789874f));
+  p = __ffma2_rn(p, a, f2(-0.2145988016f));
+  p = __ffma2_rn(p, a, f2(1.5707963050f));
+  const float2 om = __ffma2_rn(a, f2(-1.0f), f2(1.0f));  // 1 - |x| (exact for |x| >= 1/2)
+  const float2 r = make_float2(rsqrtf(om.x), rsqrtf(om.y));
+  float2 sq = __fmul2_rn(om, r);
+  const float2 err = __ffma2_rn(__fmul2_rn(sq, f2(-1.0f)), sq, om);  // om - sq^2
+  sq = __ffma2_rn(err, __fmul2_rn(r, f2(0.5f)), sq);
+  const float2 v = __fmul2_rn(sq, p);
+  const float2 w = __fadd2_rn(f2(3.14159265358979f), __fmul2_rn(v, f2(-1.0f)));  // pi - v
+  return make_float2(c.x < 0.f ? w.x : v.x, c.y < 0.f ? w.y : v.y);
+}
+
 // t for the two events of a staged pair at one voxel (ncx.. = minus the voxel centre).
 template <bool WINDOW>
 __device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, float2 ncy, float2 ncz) {
@@ -559,7 +585,7 @@ __device__ __forceinline__ float2 cone_pair_fast(const ConePair& e, float2 ncx, 
   }
   const float2 c = make_float2(fminf(fmaxf(bcos.x, -1.0f + 1e-7f), 1.0f - 1e-7f),
                                fminf(fmaxf(bcos.y, -1.0f + 1e-7f), 1.0f - 1e-7f));
-  const float2 delta = __fadd2_rn(make_float2(acosf(c.x), acosf(c.y)), e.ntheta);
+  const float2 delta = __fadd2_rn(acos2_as4446(c), e.ntheta);
   const float2 sig_e = make_float2(delta.x >= 0.f ? e.sig_plus.x : e.sig_minus.x,
                                    delta.y >= 0.f ? e.sig_plus.y : e.sig_minus.y);
   // grad beta per axis: (u01 - cos(beta) w) / d12 = (a - (a . w) w) / (d01 d12); the 1 / d12^2 is
