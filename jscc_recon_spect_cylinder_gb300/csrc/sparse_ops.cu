@@ -795,6 +795,7 @@ __device__ __forceinline__ void smem8(const float* p, float (&v)[8]) {
 template <int NT, typename TE, int U = 4>
 __device__ __forceinline__ void group_adjoint_ring4(float* b, int vc, const float4* __restrict__ xs, int ring_len,
                                                     const TE* er, int tid) {
+  static_assert(U % 2 == 0, "coarse voxels are processed in pairs");
   for (int c0 = tid; c0 < vc; c0 += U * NT) {
     float4 wa[U], wb[U];
 #pragma unroll
@@ -803,28 +804,51 @@ __device__ __forceinline__ void group_adjoint_ring4(float* b, int vc, const floa
       wa[u] = c < vc ? __ldg(xs + 2 * c) : make_float4(0.f, 0.f, 0.f, 0.f);
       wb[u] = c < vc ? __ldg(xs + 2 * c + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    // two coarse voxels per packed f32x2 FMA chain (per lane the same fmaf sequence)
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int c = c0 + u * NT;
-      if (c < vc) {
-        const int info = __float_as_int(wb[u].w);
+    for (int u = 0; u < U; u += 2) {
+      float v[2][8];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int c = c0 + (u + h) * NT;
+        const int info = __float_as_int(wb[u + h].w);
         const int jb = info & 0x3fffffff;
-        float v[8];
-        if ((info >> 30) == 0) {
-          smem8(er + jb - 4, v);
+        if (c >= vc) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k) v[h][k] = 0.f;
+        } else if ((info >> 30) == 0) {
+          smem8(er + jb - 4, v[h]);
         } else {
-          v[0] = 0.f;
+          v[h][0] = 0.f;
 #pragma unroll
-          for (int k = 1; k < 8; ++k) v[k] = to_float(er[jb + k - 4 + (k < 4 ? ring_len : 0)]);
+          for (int k = 1; k < 8; ++k) v[h][k] = to_float(er[jb + k - 4 + (k < 4 ? ring_len : 0)]);
         }
-        const float w[7] = {wa[u].x, wa[u].y, wa[u].z, wa[u].w, wb[u].x, wb[u].y, wb[u].z};
-        float acc = 0.f;
-#pragma unroll
-        for (int d = 0; d < 7; ++d) acc = fmaf(w[d], v[d + 1], acc);
-        b[c] = acc;
       }
+      const float w0[7] = {wa[u].x, wa[u].y, wa[u].z, wa[u].w, wb[u].x, wb[u].y, wb[u].z};
+      const float w1[7] = {wa[u + 1].x, wa[u + 1].y, wa[u + 1].z, wa[u + 1].w, wb[u + 1].x, wb[u + 1].y, wb[u + 1].z};
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int d = 0; d < 7; ++d)
+        acc = __ffma2_rn(make_float2(w0[d], w1[d]), make_float2(v[0][d + 1], v[1][d + 1]), acc);
+      if (c0 + u * NT < vc) b[c0 + u * NT] = acc.x;
+      if (c0 + (u + 1) * NT < vc) b[c0 + (u + 1) * NT] = acc.y;
     }
   }
+}
+
+// acc.xyzw += v[0..3] * b.xyzw as two packed f32x2 FMAs: per lane the same round-to-nearest FMA
+// as fmaf, in half the issued instructions
+__device__ __forceinline__ void ffma4(float4& acc, const float (&v)[4], const float4& b) {
+  const float2 lo = __ffma2_rn(make_float2(v[0], v[1]), make_float2(b.x, b.y), make_float2(acc.x, acc.y));
+  const float2 hi = __ffma2_rn(make_float2(v[2], v[3]), make_float2(b.z, b.w), make_float2(acc.z, acc.w));
+  acc = make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+// acc.xyzw += c * v[0..3] (packed, as ffma4)
+__device__ __forceinline__ void ffma4s(float4& acc, float c, const float (&v)[4]) {
+  const float2 cc = make_float2(c, c);
+  const float2 lo = __ffma2_rn(cc, make_float2(v[0], v[1]), make_float2(acc.x, acc.y));
+  const float2 hi = __ffma2_rn(cc, make_float2(v[2], v[3]), make_float2(acc.z, acc.w));
+  acc = make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
 // coarse rows of a batch held in registers between the dot and the q pass: four BF16 values
@@ -1099,10 +1123,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
                 float v[4];
                 if (RowChunk<TC>::kKeep) rc[k][u].get(rp[k], c, v);
                 else smem4(rp[k], c, v);
-                acc[k].x = fmaf(v[0], bv.x, acc[k].x);
-                acc[k].y = fmaf(v[1], bv.y, acc[k].y);
-                acc[k].z = fmaf(v[2], bv.z, acc[k].z);
-                acc[k].w = fmaf(v[3], bv.w, acc[k].w);
+                ffma4(acc[k], v, bv);
               }
           }
         }
@@ -1144,10 +1165,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
                   if (c < vc) {
                     float v[4];
                     rc[k][u].get(rp[k], c, v);
-                    qa[u].x = fmaf(ck, v[0], qa[u].x);
-                    qa[u].y = fmaf(ck, v[1], qa[u].y);
-                    qa[u].z = fmaf(ck, v[2], qa[u].z);
-                    qa[u].w = fmaf(ck, v[3], qa[u].w);
+                    ffma4s(qa[u], ck, v);
                   }
                 }
               }
@@ -1410,6 +1428,25 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     bool bad = false;
     // acc[v] += a[v] * (u0 * (w0 q0[l0] + w1 q0[l1]) + u1 * (w0 q1[l0] + w1 q1[l1]))
     auto accumulate = [&](const float (&a)[kScVox], const float* q0, const float* q1) {
+      if (pair && !two_z) {
+        // one z plane: per voxel acc += a * (u0 * (ra qa + rb qb)), two voxels per packed f32x2
+        // operation (per lane the same rounded operations as the scalar form below)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const float2 qa = make_float2(q0[pc0[r]], q0[pc0[r]]), qb = make_float2(q0[pc1[r]], q0[pc1[r]]);
+#pragma unroll
+          for (int i = 0; i < 4; i += 2) {
+            const int v = 4 * r + i;
+            float2 t = __fmul2_rn(make_float2(ra[v], ra[v + 1]), qa);
+            t = __ffma2_rn(make_float2(rb[v], rb[v + 1]), qb, t);
+            const float2 val = __fmul2_rn(make_float2(u0, u0), t);
+            const float2 nw = __ffma2_rn(make_float2(a[v], a[v + 1]), val, make_float2(acc[v], acc[v + 1]));
+            if (val.x != 0.f) acc[v] = nw.x;
+            if (val.y != 0.f) acc[v + 1] = nw.y;
+          }
+        }
+        return;
+      }
       if (pair) {
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
