@@ -1447,6 +1447,25 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
         }
         return;
       }
+      if (pair && !two_z) {
+        // one z plane: per voxel acc += a * (u0 * (ra qa + rb qb)), two voxels per packed f32x2
+        // operation (per lane the same rounded operations as the scalar form below)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          const float2 qa = make_float2(q0[pc0[r]], q0[pc0[r]]), qb = make_float2(q0[pc1[r]], q0[pc1[r]]);
+#pragma unroll
+          for (int i = 0; i < 4; i += 2) {
+            const int v = 4 * r + i;
+            float2 t = __fmul2_rn(make_float2(ra[v], ra[v + 1]), qa);
+            t = __ffma2_rn(make_float2(rb[v], rb[v + 1]), qb, t);
+            const float2 val = __fmul2_rn(make_float2(u0, u0), t);
+            const float2 nw = __ffma2_rn(make_float2(a[v], a[v + 1]), val, make_float2(acc[v], acc[v + 1]));
+            if (val.x != 0.f) acc[v] = nw.x;
+            if (val.y != 0.f) acc[v + 1] = nw.y;
+          }
+        }
+        return;
+      }
       if (pair) {
 #pragma unroll
         for (int r = 0; r < 2; ++r) {

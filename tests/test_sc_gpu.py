@@ -1,9 +1,9 @@
 """GPU parity of the SC projector (kernel b) and EM update against the oracle and the
-reference's golden outputs. Float32 path: rel-L2 <= 1e-5 (spec tolerance for the
+reference's golden outputs. Float32 path: rel-L2 <= 1e-5 (the stated tolerance for the
 FP32 path). BF16-stored matrix: the kernels' arithmetic is checked at the FP32 tolerance
 against the FP64 oracle run on the same BF16-rounded matrix; the storage error itself
 (~2^-9 per element, averaged by the projections, growing by ~2e-4 relative L2 per iteration
-on config 1) against the FP64 oracle on the float32 matrix at the benchmark spec's bound of 1e-3."""
+on config 1) against the FP64 oracle on the float32 matrix at the BF16 storage bound of 1e-3."""
 from __future__ import annotations
 
 import numpy as np
@@ -109,7 +109,7 @@ def test_config1_sc_osem_vs_fp64_oracle(cuda):
 
     # BF16-stored matrix, FP32 accumulation: (a) the kernels' arithmetic against the FP64
     # oracle on the same BF16-rounded matrix, 20 iterations, FP32 tolerance; (b) the storage
-    # error against the FP64 oracle on the float32 matrix, spec bound
+    # error against the FP64 oracle on the float32 matrix, BF16 storage bound of 1e-3
     A_bf = [[a[0].to(torch.bfloat16)] for a in A_l]
     A_bf_np = [[a[0].to(torch.bfloat16).float().cpu().numpy()] for a in A_l]
     img_bf = torch.ones((V, 1), device=cuda)
