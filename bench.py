@@ -905,10 +905,12 @@ class SparseLaunchBench:
         return 1
 
     def kernel_bytes(self, dtype):
-        coef = self.n_events * (self.Vc * 2 + 4) + self.n_groups * (self.V * 2 + self.Vc * 4)
+        adjoint = self.n_groups * (self.V * 2 + self.Vc * 4)
+        coef = self.n_events * (self.Vc * 2 + 4) + self.n_groups * 2 * self.Vc * 4
         scatter = self.n_groups * (self.V * 2 + self.Vc * 4) + 16 * self.V * 4
         fused = self.n_events * (self.Vc * 2 + 4) + self.n_groups * self.V * 2 + 38 * self.V * 4
-        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter, "sparse_group_fused": fused}
+        return {"sparse_group_adjoint": adjoint, "sparse_group_coef": coef, "sparse_group_scatter": scatter,
+                "sparse_group_fused": fused}
 
     def config(self):
         return {"workload": self.name, "events": self.n_events, "groups": self.n_groups, "voxels": self.V,
@@ -934,7 +936,7 @@ def joint_config(name, bins, voxels, coarse, listed, kept, subsets, groups, alph
 class JointBench:
     """workloads.JointWorkload behind the bench interface."""
 
-    storage = "bf16 system matrix + bf16 sparse rows (int32 ids split out); fp32 arm: fp32 matrix + packed fp32 rows"
+    storage = "bf16 system matrix + bf16 sparse rows (int32 ids split out); fp32 arm: fp32 matrix + fp32 sparse rows (the same split layout and kernels)"
 
     def __init__(self, dev, small=False):
         from jscc_recon_spect_cylinder_gb300 import workloads

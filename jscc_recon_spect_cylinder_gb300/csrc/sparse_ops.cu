@@ -661,39 +661,40 @@ sparse_group_coef_kernel(SpRows<TC> rows, bool vec_rows, const int32_t* __restri
 }
 
 // ------------------------------------------------------------------ grouped coefficients, bulk-copy pipeline
-// The same per-group computation with its operands staged in shared memory by bulk copies
-// (cp.async.bulk completing on mbarriers): each byte is read from HBM once, and the adjoint
-// gather, the event dots and the q accumulation read shared memory. One persistent CTA per
-// SM walks its groups gi = blockIdx.x, + gridDim.x, ... (group k of the CTA) with three
-// warp roles that overlap:
-//   producer (warp 15): two copy streams, each issued as soon as its buffer is free: the
-//     group's sysmat row into `erow` (after the adjoint of group k - 1 released it) and
-//     every event's coarse row, in order, into a ring of `n_slots` slots;
-//   adjoint warps (7-14): b[k & 1] = adjoint of erow for group k, once the event warps
-//     have released that buffer (group k - 2);
-//   event warps (0-7): per group, batches of up to `batch` events: dots f_i = t_i . b
-//     (each thread four coarse values per 1,024, reduced per warp and then over warps in
-//     warp order), coefficients, q += c_i t_i in registers (events in order); q_g stored at
-//     the end of the group, then b[k & 1] released.
-// So group k + 1's adjoint and the copies of later rows proceed while group k's events are
-// processed. Shared memory: header (barriers, flags, dot partials, coefficients),
-// erow[vf] TE, b[2][vc] float, slots[n_slots][vc] TC. Every wait is bounded: on a timeout
-// the CTA counts it (jscc_take_wait_timeout_count), waits (bounded) for the copies it still
-// has in flight and returns.
+// The per-group computation in two kernels whose operands move by bulk copies
+// (cp.async.bulk completing on mbarriers), each byte read from HBM once:
+//   sparse_group_adjoint: b_g = adjoint of (A_g o x) for every group into `bq` (float,
+//     [n_groups][ldq]). For the stride-4 ring stencil a CTA takes one tile of whole rings and
+//     one chunk of the groups: its threads keep the tile's folded taps (x folded in) in
+//     registers for the whole chunk while thread 0 streams the groups' sysmat-row segments
+//     through a ring of shared-memory stages, so the taps are read once per CTA rather than
+//     once per group. Other tap tables: one thread per coarse voxel gathering the sysmat row
+//     from global memory.
+//   sparse_group_coef (this kernel): one persistent CTA per SM walks its groups
+//     gi = blockIdx.x, + gridDim.x, ... (group k of the CTA) with two warp roles:
+//     producer (warp 15): b_g into one shared buffer (once the event warps have taken the
+//       previous group's b into registers) and every event's coarse row, in order, into a
+//       ring of `n_slots` slots;
+//     event warps (0-14): each thread holds b and q of its coarse values c = 4 t + 1,920 u in
+//       registers for the group; chunks of up to `batch` events: dots f_i = t_i . b (per
+//       thread, then per warp, then over warps in warp order after one named barrier),
+//       coefficients, q += c_i t_i (events in order); q_g stored at the end of the group.
+// Shared memory: header (barriers, flags, dot partials), b[vc] float, slots[n_slots][vc] TC.
+// Every wait is bounded: on a timeout the CTA counts it (jscc_take_wait_timeout_count),
+// waits (bounded) for the copies it still has in flight and returns.
 constexpr int kBkThreads = 512;
-constexpr int kBkEventWarps = 8;
+constexpr int kBkEventWarps = 15;
 constexpr int kBkEvents = kBkEventWarps * 32;
-constexpr int kBkAdjWarps = 7;
-constexpr int kBkAdj = kBkAdjWarps * 32;
-constexpr int kBkProducerWarp = kBkEventWarps + kBkAdjWarps;
-constexpr int kBkMaxSlots = 8;
-constexpr int kBkMaxBatch = 2;
-constexpr int kBkQ = 10;  // q registers: chunks of four coarse values per event thread
+constexpr int kBkProducerWarp = kBkEventWarps;
+constexpr int kBkMaxSlots = 16;
+constexpr int kBkMaxBatch = 4;  // events of a chunk
+constexpr int kBkQ = 5;         // b and q registers: chunks of four coarse values per event thread
 constexpr int64_t kBkMaxCoarse = (int64_t)kBkQ * 4 * kBkEvents;
-constexpr int kBkHeader = 2048;  // barriers, flags, dot partials, coefficients, group event sums
+constexpr int kBkHeader = 1024;  // barriers, flags, dot partials
 constexpr uint32_t kBkMaxPolls = 1u << 22;    // default bound of a pipeline wait
 constexpr uint32_t kBkDrainPolls = 1u << 24;  // bound of the drain of a CTA that gave up
 static_assert(kBkProducerWarp * 32 + 32 == kBkThreads, "warp roles");
+static_assert(2 * kBkMaxSlots * 8 + 64 + 2 * kBkEventWarps * kBkMaxBatch * 4 <= kBkHeader, "header");
 
 __device__ unsigned int g_wait_timeout_count = 0;
 // Poll bound of the pipeline waits of the bulk kernels, settable from the host
@@ -731,51 +732,6 @@ __device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile
   return false;
 }
 
-// Adjoint of one group from the shared-memory sysmat row by NT threads: b[c] = sum over the
-// packed taps of w' * erow[j] (plain shared loads), two coarse voxels per thread at a time;
-// with MT = KT / 2 > 0 all tap loads are issued before the first gather (MT = 0: runtime M).
-template <int KT, int NT, typename TE>
-__device__ __forceinline__ void group_adjoint_packed(float* b, int vc, const int4* __restrict__ tp, int M,
-                                                     const TE* er, int tid) {
-  constexpr int MT = KT / 2;
-  for (int c0 = tid; c0 < vc; c0 += 2 * NT) {
-    float acc[2] = {0.f, 0.f};
-    if (MT > 0) {
-      int4 t[2][MT > 0 ? MT : 1];
-#pragma unroll
-      for (int m = 0; m < MT; ++m)
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int c = c0 + u * NT;
-          t[u][m] = (c < vc && m < M) ? __ldg(tp + (size_t)m * vc + c) : make_int4(0, 0, 0, 0);
-        }
-#pragma unroll
-      for (int m = 0; m < MT; ++m)
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          acc[u] = fmaf(__int_as_float(t[u][m].y), to_float(er[t[u][m].x]), acc[u]);
-          acc[u] = fmaf(__int_as_float(t[u][m].w), to_float(er[t[u][m].z]), acc[u]);
-        }
-    } else {
-      for (int m = 0; m < M; ++m)
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const int c = c0 + u * NT;
-          if (c < vc) {
-            const int4 tt = __ldg(tp + (size_t)m * vc + c);
-            acc[u] = fmaf(__int_as_float(tt.y), to_float(er[tt.x]), acc[u]);
-            acc[u] = fmaf(__int_as_float(tt.w), to_float(er[tt.z]), acc[u]);
-          }
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const int c = c0 + u * NT;
-      if (c < vc) b[c] = acc[u];
-    }
-  }
-}
-
 // eight consecutive sysmat-row values from shared memory starting at p (p 8-byte aligned for
 // BF16, 16-byte aligned for float)
 __device__ __forceinline__ void smem8(const __nv_bfloat16* p, float (&v)[8]) {
@@ -786,54 +742,6 @@ __device__ __forceinline__ void smem8(const __nv_bfloat16* p, float (&v)[8]) {
 __device__ __forceinline__ void smem8(const float* p, float (&v)[8]) {
   const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-
-// Adjoint of one group for the stride-4 ring stencil (sparse_fold_ring_kernel's table):
-// b[c] = sum_{d=-3..3} xs[c][d] * erow[jb + d]; a centre away from theta 0 reads
-// erow[jb - 4 .. jb + 3] with two vector loads (jb is a multiple of 4). U coarse voxels per
-// thread at a time, all their table loads issued first.
-template <int NT, typename TE, int U = 4>
-__device__ __forceinline__ void group_adjoint_ring4(float* b, int vc, const float4* __restrict__ xs, int ring_len,
-                                                    const TE* er, int tid) {
-  static_assert(U % 2 == 0, "coarse voxels are processed in pairs");
-  for (int c0 = tid; c0 < vc; c0 += U * NT) {
-    float4 wa[U], wb[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int c = c0 + u * NT;
-      wa[u] = c < vc ? __ldg(xs + 2 * c) : make_float4(0.f, 0.f, 0.f, 0.f);
-      wb[u] = c < vc ? __ldg(xs + 2 * c + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    // two coarse voxels per packed f32x2 FMA chain (per lane the same fmaf sequence)
-#pragma unroll
-    for (int u = 0; u < U; u += 2) {
-      float v[2][8];
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int c = c0 + (u + h) * NT;
-        const int info = __float_as_int(wb[u + h].w);
-        const int jb = info & 0x3fffffff;
-        if (c >= vc) {
-#pragma unroll
-          for (int k = 0; k < 8; ++k) v[h][k] = 0.f;
-        } else if ((info >> 30) == 0) {
-          smem8(er + jb - 4, v[h]);
-        } else {
-          v[h][0] = 0.f;
-#pragma unroll
-          for (int k = 1; k < 8; ++k) v[h][k] = to_float(er[jb + k - 4 + (k < 4 ? ring_len : 0)]);
-        }
-      }
-      const float w0[7] = {wa[u].x, wa[u].y, wa[u].z, wa[u].w, wb[u].x, wb[u].y, wb[u].z};
-      const float w1[7] = {wa[u + 1].x, wa[u + 1].y, wa[u + 1].z, wa[u + 1].w, wb[u + 1].x, wb[u + 1].y, wb[u + 1].z};
-      float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int d = 0; d < 7; ++d)
-        acc = __ffma2_rn(make_float2(w0[d], w1[d]), make_float2(v[0][d + 1], v[1][d + 1]), acc);
-      if (c0 + u * NT < vc) b[c0 + u * NT] = acc.x;
-      if (c0 + (u + 1) * NT < vc) b[c0 + (u + 1) * NT] = acc.y;
-    }
-  }
 }
 
 // acc.xyzw += v[0..3] * b.xyzw as two packed f32x2 FMAs: per lane the same round-to-nearest FMA
@@ -851,29 +759,6 @@ __device__ __forceinline__ void ffma4s(float4& acc, float c, const float (&v)[4]
   acc = make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
-// coarse rows of a batch held in registers between the dot and the q pass: four BF16 values
-// per chunk as a uint2 (float rows are re-read from shared memory instead)
-template <typename TC>
-struct RowChunk;
-template <>
-struct RowChunk<__nv_bfloat16> {
-  static constexpr bool kKeep = true;
-  uint2 v;
-  __device__ __forceinline__ void load(const __nv_bfloat16* p, int c) { v = *reinterpret_cast<const uint2*>(p + c); }
-  __device__ __forceinline__ void get(const __nv_bfloat16*, int, float (&f)[4]) const {
-    f[0] = bf16_lo(v.x); f[1] = bf16_hi(v.x); f[2] = bf16_lo(v.y); f[3] = bf16_hi(v.y);
-  }
-};
-template <>
-struct RowChunk<float> {
-  static constexpr bool kKeep = false;
-  __device__ __forceinline__ void load(const float*, int) {}
-  __device__ __forceinline__ void get(const float* p, int c, float (&f)[4]) const {
-    const float4 u = *reinterpret_cast<const float4*>(p + c);
-    f[0] = u.x; f[1] = u.y; f[2] = u.z; f[3] = u.w;
-  }
-};
-
 // four consecutive coarse values from shared memory (c a multiple of 4)
 __device__ __forceinline__ void smem4(const __nv_bfloat16* p, int64_t c, float (&v)[4]) {
   const uint2 u = *reinterpret_cast<const uint2*>(p + c);
@@ -884,12 +769,6 @@ __device__ __forceinline__ void smem4(const float* p, int64_t c, float (&v)[4]) 
   v[0] = u.x; v[1] = u.y; v[2] = u.z; v[3] = u.w;
 }
 
-// eight consecutive values (16-byte aligned; shared or global memory, plain loads)
-__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&v)[8]) {
-  const uint4 u = *reinterpret_cast<const uint4*>(p);
-  v[0] = bf16_lo(u.x); v[1] = bf16_hi(u.x); v[2] = bf16_lo(u.y); v[3] = bf16_hi(u.y);
-  v[4] = bf16_lo(u.z); v[5] = bf16_hi(u.z); v[6] = bf16_lo(u.w); v[7] = bf16_hi(u.w);
-}
 // two runs of four consecutive values at p and p + 128 (plain loads; p 8-byte aligned for
 // BF16, 16-byte aligned for float)
 template <typename T>
@@ -904,61 +783,211 @@ __device__ __forceinline__ void load4x2(const T* p, float (&v)[8]) {
   }
 }
 
-__device__ __forceinline__ void load8(const float* p, float (&v)[8]) {
-  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+// ---- sparse_group_adjoint, stride-4 ring stencil
+constexpr int kAdWarps = 8;  // compute warps; one more warp streams the segments
+constexpr int kAdThreads = kAdWarps * 32 + 32;
+constexpr int kAdCompute = kAdWarps * 32;
+constexpr int kAdVox = 4;  // coarse voxels per compute thread: a tile holds at most 1,024
+constexpr int kAdMaxStages = 8;
+constexpr int kAdHeader = 256;
+
+// Coarse voxel c of the tile [c0, c1) (whole rings: a voxel at theta 0 takes its taps
+// d = -3..-1 from the end of its own ring, inside the tile): taps xs[c] (x folded in) and, in
+// the eighth float, jb | (th == 0) << 30 with jb = 4 c. b[c] = sum_{d=-3..3} xs[c][d] *
+// seg[jb - 4 c0 + d], the taps in d order as one packed f32x2 chain per pair of voxels (the
+// same fmaf sequence per lane). The producer warp issues group k + n_stages's segment into a
+// stage once every compute warp has released it (empty[s], one arrival per warp).
+template <typename TE>
+__global__ void __launch_bounds__(kAdThreads)
+sparse_group_adjoint_ring_kernel(const int32_t* __restrict__ grow, int n_groups, int gpc, const TE* __restrict__ eff,
+                                 int64_t ld_eff, int64_t n_det, const float4* __restrict__ xs, int vc, int tile_c,
+                                 int ring_len, float* __restrict__ bq, int64_t ldq, int n_stages,
+                                 uint32_t stage_stride) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kAdMaxStages]
+  uint64_t* empty = full + kAdMaxStages;                // [kAdMaxStages]
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * kAdMaxStages * 8);
+  int* issued = reinterpret_cast<int*>(smem + 2 * kAdMaxStages * 8 + 4);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c0 = blockIdx.x * tile_c, c1 = min(vc, c0 + tile_c);
+  const int g0 = blockIdx.y * gpc, g1 = min(n_groups, g0 + gpc);
+  if (c0 >= c1 || g0 >= g1) return;
+  const uint32_t seg_bytes = (uint32_t)(c1 - c0) * 4u * (uint32_t)sizeof(TE);
+  auto stage = [&](int s) { return reinterpret_cast<const TE*>(smem + kAdHeader + (size_t)s * stage_stride); };
+  const uint32_t polls = g_bk_poll_limit;
+  const int n_k = g1 - g0;
+  if (tid == 0) {
+    for (int s = 0; s < kAdMaxStages; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, kAdWarps);
+    }
+    *abort_flag = 0;
+    *issued = 0;
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (warp == kAdWarps) {
+    // ---- producer: segment of group k into stage k mod n_stages; 32 row indices per window
+    int win_base = INT_MIN, win_val = 0;
+    for (int k = 0; k < n_k; ++k) {
+      const int s = k % n_stages;
+      bool ok = k < n_stages || bk_wait(empty + s, (uint32_t)(k / n_stages - 1) & 1u, abort_flag, polls);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      if (k >= win_base + 32 || win_base == INT_MIN) {
+        win_base = k;
+        win_val = k + lane < n_k ? grow[g0 + k + lane] : 0;
+      }
+      const int row = __shfl_sync(0xffffffffu, win_val, k - win_base);
+      if (lane == 0) {
+        mbar_arrive_expect_tx(full + s, seg_bytes);
+        bulk_copy_g2s(const_cast<TE*>(stage(s)), eff + clamp_row(row, n_det) * ld_eff + 4 * (int64_t)c0, seg_bytes,
+                      full + s);
+        *issued = k + 1;
+      }
+    }
+  } else {
+    // ---- compute warps: the tile's taps in registers, one group per stage
+    float4 wa[kAdVox], wb[kAdVox];
+#pragma unroll
+    for (int u = 0; u < kAdVox; ++u) {
+      const int c = c0 + tid + u * kAdCompute;
+      wa[u] = c < c1 ? __ldg(xs + 2 * c) : make_float4(0.f, 0.f, 0.f, 0.f);
+      wb[u] = c < c1 ? __ldg(xs + 2 * c + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    for (int k = 0; k < n_k; ++k) {
+      const int s = k % n_stages;
+      bool ok = bk_wait(full + s, (uint32_t)(k / n_stages) & 1u, abort_flag, polls);
+      if (!__all_sync(0xffffffffu, ok)) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      const TE* seg = stage(s);
+      float* out = bq + (int64_t)(g0 + k) * ldq;
+#pragma unroll
+      for (int u = 0; u < kAdVox; u += 2) {
+        float v[2][8];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int c = c0 + tid + (u + h) * kAdCompute;
+          if (c < c1) {
+            const int info = __float_as_int(wb[u + h].w);
+            const int jl = (info & 0x3fffffff) - 4 * c0;  // centre within the segment
+            float a4[4], b4[4];
+            smem4(seg + ((info >> 30) ? jl - 4 + ring_len : jl - 4), 0, a4);
+            smem4(seg + jl, 0, b4);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              v[h][i] = a4[i];
+              v[h][4 + i] = b4[i];
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[h][i] = 0.f;
+          }
+        }
+        const float w0[7] = {wa[u].x, wa[u].y, wa[u].z, wa[u].w, wb[u].x, wb[u].y, wb[u].z};
+        const float w1[7] = {wa[u + 1].x, wa[u + 1].y, wa[u + 1].z, wa[u + 1].w, wb[u + 1].x, wb[u + 1].y,
+                             wb[u + 1].z};
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int d = 0; d < 7; ++d)
+          acc = __ffma2_rn(make_float2(w0[d], w1[d]), make_float2(v[0][d + 1], v[1][d + 1]), acc);
+        const int ca = c0 + tid + u * kAdCompute, cb = ca + kAdCompute;
+        if (ca < c1) out[ca] = acc.x;
+        if (cb < c1) out[cb] = acc.y;
+      }
+      __syncwarp();  // every lane is past its reads of stage s
+      if (lane == 0) mbar_arrive(empty + s);
+    }
+  }
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
+    atomicAdd(&g_wait_timeout_count, 1u);
+    // copies still in flight write this CTA's shared memory: wait (bounded) for them
+    for (int k = max(0, *issued - n_stages); k < *issued; ++k)
+      mbar_wait_bounded(full + k % n_stages, (uint32_t)(k / n_stages) & 1u, kBkDrainPolls);
+  }
 }
 
-template <int MODE, int KT, int RS, typename TE, typename TC>
+// ---- sparse_group_adjoint, packed tap table (any upsample): b[c] = sum over the packed
+// taps (index, w x) of w' * A_g[j], one thread per coarse voxel, the sysmat row gathered
+// from global memory (cached); with MT = KT / 2 > 0 all tap loads are issued first.
+template <int KT, typename TE>
+__global__ void __launch_bounds__(256)
+sparse_group_adjoint_taps_kernel(const int32_t* __restrict__ grow, int n_groups, const TE* __restrict__ eff,
+                                 int64_t ld_eff, int64_t n_det, const int4* __restrict__ tp, int M, int vc,
+                                 float* __restrict__ bq, int64_t ldq) {
+  constexpr int MT = KT / 2;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= vc) return;
+  int4 t[MT > 0 ? MT : 1];
+  if (MT > 0) {
+#pragma unroll
+    for (int m = 0; m < MT; ++m) t[m] = m < M ? __ldg(tp + (size_t)m * vc + c) : make_int4(0, 0, 0, 0);
+  }
+  for (int g = blockIdx.y; g < n_groups; g += gridDim.y) {
+    const TE* er = eff + clamp_row(grow[g], n_det) * ld_eff;
+    float acc = 0.f;
+    if (MT > 0) {
+#pragma unroll
+      for (int m = 0; m < MT; ++m) {
+        acc = fmaf(__int_as_float(t[m].y), load_elem(er, t[m].x), acc);
+        acc = fmaf(__int_as_float(t[m].w), load_elem(er, t[m].z), acc);
+      }
+    } else {
+      for (int m = 0; m < M; ++m) {
+        const int4 tt = __ldg(tp + (size_t)m * vc + c);
+        acc = fmaf(__int_as_float(tt.y), load_elem(er, tt.x), acc);
+        acc = fmaf(__int_as_float(tt.w), load_elem(er, tt.z), acc);
+      }
+    }
+    bq[(int64_t)g * ldq + c] = acc;
+  }
+}
+
+// ---- sparse_group_coef (bulk): MODE 0 materialise coefficients, 1 grouped, 2 event sums
+template <int MODE, typename TC>
 __global__ void __launch_bounds__(kBkThreads, 1)
 sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
-                              const int32_t* __restrict__ grow, int n_groups, int vc,
-                              const int4* __restrict__ tp, int M, const float4* __restrict__ xs, int ring_len,
-                              const TE* __restrict__ eff, int64_t ld_eff,
-                              float* __restrict__ s_ev, float* __restrict__ q, int64_t ldq, int n_slots, int batch,
-                              uint32_t erow_bytes, uint32_t row_bytes, uint32_t b_off, uint32_t b_stride,
-                              uint32_t slot_off, uint32_t slot_stride) {
+                              int n_groups, int vc, const float* __restrict__ bq, float* __restrict__ s_ev,
+                              float* __restrict__ q, int64_t ldq, int n_slots, int batch, uint32_t b_bytes,
+                              uint32_t row_bytes, uint32_t slot_off, uint32_t slot_stride) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kBkMaxSlots]
   uint64_t* empty = full + kBkMaxSlots;                // [kBkMaxSlots]
-  uint64_t* erow_full = empty + kBkMaxSlots;
-  uint64_t* erow_empty = erow_full + 1;
-  uint64_t* b_full = erow_empty + 1;  // [2]
-  uint64_t* b_empty = b_full + 2;     // [2]
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 192);
-  int* rows_issued = reinterpret_cast<int*>(smem + 196);
-  int* erows_issued = reinterpret_cast<int*>(smem + 200);
-  int* rows_used = reinterpret_cast<int*>(smem + 204);
-  int* erows_used = reinterpret_cast<int*>(smem + 208);
-  float* red = reinterpret_cast<float*>(smem + 256);  // [kBkEventWarps][kBkMaxBatch]
-  float* cs = reinterpret_cast<float*>(smem + 512);   // [kBkMaxBatch]
-  float* s_grp = reinterpret_cast<float*>(smem + 1024);  // [kBkEvents] event sums of the group
-  TE* erow = reinterpret_cast<TE*>(smem + kBkHeader);
+  uint64_t* b_full = empty + kBkMaxSlots;
+  uint64_t* b_empty = b_full + 1;
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * kBkMaxSlots * 8 + 16);
+  int* rows_issued = reinterpret_cast<int*>(smem + 2 * kBkMaxSlots * 8 + 20);
+  int* b_issued = reinterpret_cast<int*>(smem + 2 * kBkMaxSlots * 8 + 24);
+  int* rows_used = reinterpret_cast<int*>(smem + 2 * kBkMaxSlots * 8 + 28);
+  int* b_used = reinterpret_cast<int*>(smem + 2 * kBkMaxSlots * 8 + 32);
+  float* red = reinterpret_cast<float*>(smem + 2 * kBkMaxSlots * 8 + 64);  // [2][kBkEventWarps][kBkMaxBatch]
+  float* b = reinterpret_cast<float*>(smem + kBkHeader);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t polls = g_bk_poll_limit;
   const int G = gridDim.x;
-  auto bbuf = [&](int k) { return reinterpret_cast<float*>(smem + b_off + (size_t)(k & 1) * b_stride); };
   auto slot = [&](int s) { return reinterpret_cast<const TC*>(smem + slot_off + (size_t)s * slot_stride); };
   if (tid == 0) {
     for (int s = 0; s < kBkMaxSlots; ++s) {
       mbar_init(full + s, 1);
-      mbar_init(empty + s, 1);
+      mbar_init(empty + s, kBkEventWarps);  // every event warp releases a slot after its reads
     }
-    mbar_init(erow_full, 1);
-    mbar_init(erow_empty, 1);
-    for (int h = 0; h < 2; ++h) {
-      mbar_init(b_full + h, 1);
-      mbar_init(b_empty + h, 1);
-    }
+    mbar_init(b_full, 1);
+    mbar_init(b_empty, kBkEventWarps);
     *abort_flag = 0;
-    *rows_issued = *erows_issued = *rows_used = *erows_used = 0;
+    *rows_issued = *b_issued = *rows_used = *b_used = 0;
     mbar_init_fence();
   }
   __syncthreads();
   if (warp == kBkProducerWarp) {
     // ------------------------------------------------------------ producer warp
-    // erow stream: group eg (k-th of the CTA: ek); row stream: event re of group rg
-    int eg = blockIdx.x, ek = 0;
+    // b stream: group bg (k-th of the CTA: bk); row stream: event re of group rg
+    int bg = blockIdx.x, bk = 0;
     int rg = blockIdx.x, re = 0, re_end = 0, pseq = 0;
     if (rg < n_groups) {
       re = goff[rg];
@@ -978,20 +1007,21 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
           win_base = INT_MIN;  // the window holds one group's events only
         }
       }
-      const bool rows_left = rg < n_groups, erows_left = eg < n_groups;
-      if (!rows_left && !erows_left) break;
+      const bool rows_left = rg < n_groups, b_left = bg < n_groups;
+      if (!rows_left && !b_left) break;
       bool progress = false;
-      if (erows_left) {
-        bool ready = ek == 0 || mbar_test_wait(erow_empty, (ek - 1) & 1);
+      if (b_left) {
+        // the event warps have taken group bk - 1's b into registers: phase bk - 1 of b_empty
+        bool ready = bk == 0 || mbar_test_wait(b_empty, (bk - 1) & 1);
         ready = __shfl_sync(0xffffffffu, ready, 0);
         if (ready) {
           if (lane == 0) {
-            mbar_arrive_expect_tx(erow_full, erow_bytes);
-            bulk_copy_g2s(erow, eff + clamp_row(grow[eg], rows.n_det) * ld_eff, erow_bytes, erow_full);
-            *erows_issued = ek + 1;
+            mbar_arrive_expect_tx(b_full, b_bytes);
+            bulk_copy_g2s(b, bq + (int64_t)bg * ldq, b_bytes, b_full);
+            *b_issued = bk + 1;
           }
-          eg += G;
-          ++ek;
+          bg += G;
+          ++bk;
           progress = true;
         }
       }
@@ -1027,37 +1057,14 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       }
     }
     if (!ok && lane == 0) *abort_flag = 1;
-  } else if (warp >= kBkEventWarps) {
-    // ------------------------------------------------------------ adjoint warps
-    const int at = tid - kBkEvents;
-    bool bad = false, aborted = false;
-    int kg = 0;
-    for (int gi = blockIdx.x; gi < n_groups; gi += G, ++kg) {
-      if (!bk_wait(erow_full, kg & 1, abort_flag, polls)) bad = true;
-      if (kg >= 2 && !bk_wait(b_empty + (kg & 1), ((kg >> 1) - 1) & 1, abort_flag, polls)) bad = true;
-      float* b = bbuf(kg);
-      if (RS == 4) group_adjoint_ring4<kBkAdj, TE>(b, vc, xs, ring_len, erow, at);
-      else group_adjoint_packed<KT, kBkAdj, TE>(b, vc, tp, M, erow, at);
-      if (role_sync_or(2, kBkAdj, bad)) {
-        aborted = true;
-        break;
-      }
-      if (at == 0) {
-        *erows_used = kg + 1;
-        mbar_arrive(erow_empty);  // the producer may refill erow
-        mbar_arrive(b_full + (kg & 1));
-      }
-    }
-    if (aborted) *abort_flag = 1;
   } else {
     // ------------------------------------------------------------ event warps
     const int et = tid;
-    int seq = 0, kg = 0;
+    int seq = 0, kg = 0, par = 0;
     int cs_slot = 0;         // slot of event seq (seq mod n_slots, kept incrementally)
     uint32_t cphase = 0;     // bit s: parity of the next phase of full[s]
     bool aborted = false, bad = false;  // bad: one of this thread's waits gave up
-    // software pipeline over groups: the event range of group k + 2 and the event sums of
-    // group k + 1 (this thread's event of it) are loaded while group k is processed
+    // the event ranges of the next two groups are loaded while a group is processed
     auto range = [&](int g, int& a, int& e) {
       a = g < n_groups ? goff[g] : 0;
       e = g < n_groups ? goff[g + 1] : 0;
@@ -1065,24 +1072,29 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     int r0a, r0e, r1a, r1e;
     range(blockIdx.x, r0a, r0e);
     range(blockIdx.x + G, r1a, r1e);
-    float s_next = (MODE == 0 && r0a + et < r0e) ? s_ev[r0a + et] : 0.f;
     for (int gi = blockIdx.x; gi < n_groups && !aborted; gi += G, ++kg) {
       const int e0 = r0a, e1 = r0e;
-      const float s_mine = s_next;
       r0a = r1a;
       r0e = r1e;
       range(gi + 2 * G, r1a, r1e);
-      s_next = (MODE == 0 && r0a + et < r0e) ? s_ev[r0a + et] : 0.f;
-      if (MODE == 0) s_grp[et] = s_mine;  // read after the first batch barrier
-      const float* b = bbuf(kg);
-      if (!bk_wait(b_full + (kg & 1), (kg >> 1) & 1, abort_flag, polls)) bad = true;
-      float4 qa[kBkQ];
+      // b of this thread's coarse values into registers, then the buffer goes back
+      if (!bk_wait(b_full, kg & 1, abort_flag, polls)) bad = true;
+      float4 bv[kBkQ], qa[kBkQ];
 #pragma unroll
-      for (int u = 0; u < kBkQ; ++u) qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int u = 0; u < kBkQ; ++u) {
+        const int c = et * 4 + u * (kBkEvents * 4);
+        bv[u] = c < vc ? *reinterpret_cast<const float4*>(b + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+        qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      __syncwarp();
+      if (__all_sync(0xffffffffu, !bad) && lane == 0) {
+        if (et == 0) *b_used = kg + 1;
+        mbar_arrive(b_empty);
+      }
       for (int bs = e0; bs < e1; bs += batch) {
         const int n = min(batch, e1 - bs);
-        // event sums beyond the first kBkEvents of a group are read here (issued before the dots)
-        const float s_far = (MODE == 0 && et < n && bs + et - e0 >= kBkEvents) ? s_ev[bs + et] : 0.f;
+        // the event sum of lane k's event of the chunk, read before the dots
+        const float s_lane = (MODE == 0 && lane < n) ? s_ev[bs + lane] : 0.f;
         int sl[kBkMaxBatch];
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k) {
@@ -1095,12 +1107,8 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
             if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag, polls)) bad = true;
             cphase ^= 1u << sl[k];
           }
-        // ---- dots f_i = t_i . b; BF16 rows stay in registers for the q pass
-        const TC* rp[kBkMaxBatch];
-#pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k) rp[k] = slot(sl[k]);
-        RowChunk<TC> rc[kBkMaxBatch][kBkQ];
-        float4 acc[kBkMaxBatch];  // four independent partial sums per event
+        // ---- dots f_i = t_i . b: this thread's values, then the warp's
+        float4 acc[kBkMaxBatch];
 #pragma unroll
         for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
@@ -1109,21 +1117,10 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
           if (c < vc) {
 #pragma unroll
             for (int k = 0; k < kBkMaxBatch; ++k)
-              if (k < n) rc[k][u].load(rp[k], c);
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < kBkQ; ++u) {
-          const int c = et * 4 + u * (kBkEvents * 4);
-          if (c < vc) {
-            const float4 bv = *reinterpret_cast<const float4*>(b + c);
-#pragma unroll
-            for (int k = 0; k < kBkMaxBatch; ++k)
               if (k < n) {
                 float v[4];
-                if (RowChunk<TC>::kKeep) rc[k][u].get(rp[k], c, v);
-                else smem4(rp[k], c, v);
-                ffma4(acc[k], v, bv);
+                smem4(slot(sl[k]), c, v);
+                ffma4(acc[k], v, bv[u]);
               }
           }
         }
@@ -1131,62 +1128,63 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         for (int k = 0; k < kBkMaxBatch; ++k)
           if (k < n) {
             const float f = warp_sum((acc[k].x + acc[k].y) + (acc[k].z + acc[k].w));
-            if (lane == 0) red[warp * kBkMaxBatch + k] = f;
+            if (lane == 0) red[(par * kBkEventWarps + warp) * kBkMaxBatch + k] = f;
           }
         if (role_sync_or(1, kBkEvents, bad)) {
           aborted = true;
           break;
         }
-        if (et < n) {
+        // ---- coefficients: lane k sums event k's partials over the warps in order (every
+        // warp the same values), then broadcasts
+        float cl = 0.f;
+        if (lane < n) {
           float f = 0.f;
-          for (int w = 0; w < kBkEventWarps; ++w) f += red[w * kBkMaxBatch + et];
+          for (int w = 0; w < kBkEventWarps; ++w) f += red[(par * kBkEventWarps + w) * kBkMaxBatch + lane];
           if (MODE == 2) {
-            s_ev[bs + et] = f;  // event sums are kept by position in `order`
+            if (warp == 0) s_ev[bs + lane] = f;  // event sums are kept by position in `order`
           } else if (MODE == 0) {
-            const int p = bs + et - e0;
-            const float si = p < kBkEvents ? s_grp[p] : s_far;
             // (1 / max(f / S, 1e-12)) / S = 1 / max(f, 1e-12 S) for S > 0: one division
-            cs[et] = (isfinite(si) && si > 0.f) ? 1.0f / fmaxf(f, 1e-12f * si) : 0.f;
+            cl = (isfinite(s_lane) && s_lane > 0.f) ? 1.0f / fmaxf(f, 1e-12f * s_lane) : 0.f;
           } else {
-            cs[et] = 1.0f / fmaxf(f, 1e-12f);
+            cl = 1.0f / fmaxf(f, 1e-12f);
           }
         }
+        // ---- q_g += c_i t_i over the chunk, events in order
         if (MODE != 2) {
-          role_sync(1, kBkEvents);
-          // ---- q_g += c_i t_i over the batch, events in order
 #pragma unroll
           for (int k = 0; k < kBkMaxBatch; ++k)
             if (k < n) {
-              const float ck = cs[k];
+              const float ck = __shfl_sync(0xffffffffu, cl, k);
               if (ck != 0.f) {
 #pragma unroll
                 for (int u = 0; u < kBkQ; ++u) {
                   const int c = et * 4 + u * (kBkEvents * 4);
                   if (c < vc) {
                     float v[4];
-                    rc[k][u].get(rp[k], c, v);
+                    smem4(slot(sl[k]), c, v);
                     ffma4s(qa[u], ck, v);
                   }
                 }
               }
             }
         }
-        role_sync(1, kBkEvents);  // the batch's slots, partials and coefficients are free
-        if (et == 0) {
+        // ---- this warp is past its last read of the chunk's rows: release the slots (a
+        // warp with a lane whose wait gave up keeps them: its copy may still be in flight)
+        __syncwarp();
+        if (__all_sync(0xffffffffu, !bad) && lane == 0) {
+          if (et == 0) *rows_used = seq + n;  // before the slots can be refilled
 #pragma unroll
           for (int k = 0; k < kBkMaxBatch; ++k)
             if (k < n) mbar_arrive(empty + sl[k]);
-          *rows_used = seq + n;
         }
         seq += n;
+        par ^= 1;
       }
       if (aborted) break;
-      if (e0 == e1 && role_sync_or(1, kBkEvents, bad)) {  // no batch consumed the b wait's status
+      if (e0 == e1 && role_sync_or(1, kBkEvents, bad)) {  // no chunk consumed the b wait's status
         aborted = true;
         break;
       }
-      // every event thread is past its last read of b (the last batch's barrier)
-      if (et == 0) mbar_arrive(b_empty + (kg & 1));
       if (MODE != 2) {
         float* qg = q + (int64_t)gi * ldq;
 #pragma unroll
@@ -1196,7 +1194,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         }
       }
     }
-    if (aborted) *abort_flag = 1;  // stops the other roles
+    if (aborted) *abort_flag = 1;  // stops the producer
   }
   __syncthreads();
   if (*abort_flag && tid == 0) {
@@ -1204,7 +1202,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
     // copies still in flight write this CTA's shared memory: wait (bounded) for them
     for (int sq = *rows_used; sq < *rows_issued; ++sq)
       mbar_wait_bounded(full + sq % n_slots, (sq / n_slots) & 1, kBkDrainPolls);
-    if (*erows_issued > *erows_used) mbar_wait_bounded(erow_full, *erows_used & 1, kBkDrainPolls);
+    if (*b_issued > *b_used) mbar_wait_bounded(b_full, *b_used & 1, kBkDrainPolls);
   }
 }
 
@@ -1631,12 +1629,10 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   int64_t grid = (int64_t)num_sms() * per_sm;
   if (grid > n_groups) grid = n_groups;
   // bulk-copy pipeline when every row start and length is 16-byte aligned (split storage),
-  // q fits the consumer registers and a sysmat row, b and at least two coarse rows fit in
+  // b and q fit the event threads' registers and b plus at least two coarse rows fit in
   // shared memory
-  const uint32_t erow_bytes = (uint32_t)((size_t)vf * sizeof(TE)), row_bytes = (uint32_t)((size_t)vc * sizeof(TC));
-  const uint32_t b_off = (uint32_t)align_up(kBkHeader + align_up(erow_bytes, 128), 128);
-  const uint32_t b_stride = (uint32_t)align_up((size_t)vc * 4, 128);
-  const uint32_t slot_off = b_off + 2 * b_stride;
+  const uint32_t row_bytes = (uint32_t)((size_t)vc * sizeof(TC)), b_bytes = (uint32_t)((size_t)vc * 4);
+  const uint32_t slot_off = (uint32_t)align_up(kBkHeader + align_up(b_bytes, 128), 128);
   const uint32_t slot_stride = (uint32_t)align_up(row_bytes, 128);
   const size_t bk_limit = 227 * 1024;
   int n_slots = 0;
@@ -1644,12 +1640,13 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     n_slots = (int)((bk_limit - slot_off) / (size_t)slot_stride);
     if (n_slots > kBkMaxSlots) n_slots = kBkMaxSlots;
   }
-  const int batch = n_slots / 2 < kBkMaxBatch ? n_slots / 2 : kBkMaxBatch;
+  // events of a chunk: a power of two leaving as many slots in flight as it holds
+  int batch = 1;
+  while (batch * 2 <= kBkMaxBatch && batch * 2 <= n_slots / 2) batch *= 2;
   const bool bulk = rows.packed == nullptr && n_slots >= 2 && vc <= kBkMaxCoarse &&
-                    (size_t)vf * sizeof(TE) < (1u << 20) && reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 &&
-                    (rows.ld * sizeof(TC)) % 16 == 0 && row_bytes % 16 == 0 &&
-                    reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
-                    erow_bytes % 16 == 0;
+                    reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 && (rows.ld * sizeof(TC)) % 16 == 0 &&
+                    row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(eff) % 16 == 0 &&
+                    (ld_eff * sizeof(TE)) % 16 == 0 && ((size_t)vf * sizeof(TE)) % 16 == 0 && ldq % 4 == 0;
   const size_t bk_smem = (size_t)slot_off + (size_t)n_slots * slot_stride;
   int64_t bk_grid = num_sms();
   if (bk_grid > n_groups) bk_grid = n_groups;
@@ -1659,11 +1656,43 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   float4* xsx = cv.take<float4>((size_t)2 * vc);  // ring stencil, x folded in
   float4* xsw = cv.take<float4>((size_t)2 * vc);  // ring stencil, weights only
   float* part_cf = cv.take<float>((size_t)kCfMaxClusters * ldp);  // cluster path partial images
+  float* bq = cv.take<float>((size_t)n_groups * ldq);             // group adjoints b_g (bulk path)
   JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
   // stride-4 ring stencil (checked by the caller against the tap table): centres multiples of 4
-  const bool ring = bulk && ring_stride == 4 && K == 7 && ring_len >= 8 && ring_len % 4 == 0 &&
-                    taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf && vf / taps.n_lf == vc / taps.n_lc &&
-                    vf < (1 << 30);
+  bool ring = bulk && ring_stride == 4 && K == 7 && ring_len >= 8 && ring_len % 4 == 0 &&
+              taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf && vf / taps.n_lf == vc / taps.n_lc &&
+              vf < (1 << 30);
+  // adjoint tiles of whole rings (at most kAdVox * kAdCompute coarse voxels, an even number so
+  // that every segment starts on a 16-byte boundary), chunks of groups for about two CTAs per SM
+  int ad_tile = 0, ad_tiles = 0, ad_chunks = 1, ad_gpc = 0, ad_stages = 0;
+  uint32_t ad_stride = 0;
+  size_t ad_smem = 0;
+  if (ring) {
+    const int n_thc = ring_len / 4;
+    const int n_blocks = (int)(vc / n_thc);
+    const int rmax = (kAdVox * kAdCompute) / n_thc;
+    if (rmax >= 1) {
+      ad_tiles = (n_blocks + rmax - 1) / rmax;
+      int r = (n_blocks + ad_tiles - 1) / ad_tiles;
+      if ((r * n_thc) % 2 != 0) ++r;
+      if (r * n_thc > kAdVox * kAdCompute) r -= 2;
+      ad_tile = r * n_thc;
+    }
+    ring = ad_tile > 0 && ad_tile % 2 == 0;
+    if (ring) {
+      ad_tiles = (int)((vc + ad_tile - 1) / ad_tile);
+      ad_stride = (uint32_t)align_up((size_t)ad_tile * 4 * sizeof(TE), 128);
+      ad_stages = (int)((110u * 1024u - kAdHeader) / ad_stride);
+      if (ad_stages > kAdMaxStages) ad_stages = kAdMaxStages;
+      if (ad_stages < 2) ad_stages = 2;
+      ad_smem = kAdHeader + (size_t)ad_stages * ad_stride;
+      ring = ad_smem <= 227 * 1024;
+      int64_t ch = (2 * (int64_t)num_sms() + ad_tiles - 1) / ad_tiles;
+      if (ch > n_groups) ch = n_groups;
+      ad_chunks = (int)(ch < 1 ? 1 : ch);
+      ad_gpc = (int)((n_groups + ad_chunks - 1) / ad_chunks);
+    }
+  }
   {
     int64_t blocks = ((int64_t)K * vc + 255) / 256;
     if (blocks > (int64_t)num_sms() * 8) blocks = (int64_t)num_sms() * 8;
@@ -1694,16 +1723,48 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     }
   }
   cudaError_t attr = cudaSuccess;
-#define JSCC_GC_BK(MODE, KT, RS, TP, XS)                                                                         \
+#define JSCC_GA(TP, XS)                                                                                          \
   do {                                                                                                           \
-    attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, KT, RS, TE, TC>,                             \
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                      \
+    if (ring) {                                                                                                  \
+      attr = cudaFuncSetAttribute(sparse_group_adjoint_ring_kernel<TE>,                                          \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ad_smem);                    \
+      if (attr == cudaSuccess)                                                                                   \
+        JSCC_TIMED("sparse_group_adjoint", st,                                                                   \
+                   (sparse_group_adjoint_ring_kernel<TE><<<dim3((unsigned)ad_tiles, (unsigned)ad_chunks),        \
+                                                           kAdThreads, ad_smem, st>>>(                           \
+                       grow, n_groups, ad_gpc, eff, ld_eff, rows.n_det, XS, (int)vc, ad_tile, ring_len, bq, ldq, \
+                       ad_stages, ad_stride)));                                                                  \
+    } else {                                                                                                     \
+      const dim3 ag((unsigned)((vc + 255) / 256), (unsigned)(n_groups < 65535 ? n_groups : 65535));            \
+      if (K <= 4)                                                                                                \
+        JSCC_TIMED("sparse_group_adjoint", st,                                                                   \
+                   (sparse_group_adjoint_taps_kernel<4, TE><<<ag, 256, 0, st>>>(grow, n_groups, eff, ld_eff,     \
+                                                                             rows.n_det, TP, M, (int)vc, bq,    \
+                                                                             ldq)));                            \
+      else if (K <= 8)                                                                                           \
+        JSCC_TIMED("sparse_group_adjoint", st,                                                                   \
+                   (sparse_group_adjoint_taps_kernel<8, TE><<<ag, 256, 0, st>>>(grow, n_groups, eff, ld_eff,     \
+                                                                             rows.n_det, TP, M, (int)vc, bq,    \
+                                                                             ldq)));                            \
+      else                                                                                                       \
+        JSCC_TIMED("sparse_group_adjoint", st,                                                                   \
+                   (sparse_group_adjoint_taps_kernel<0, TE><<<ag, 256, 0, st>>>(grow, n_groups, eff, ld_eff,     \
+                                                                             rows.n_det, TP, M, (int)vc, bq,    \
+                                                                             ldq)));                            \
+    }                                                                                                            \
+  } while (0)
+#define JSCC_GC_BK(MODE, TP, XS)                                                                                 \
+  do {                                                                                                           \
+    JSCC_GA(TP, XS);                                                                                             \
+    if (attr == cudaSuccess) attr = cudaGetLastError();                                                          \
+    if (attr == cudaSuccess)                                                                                     \
+      attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, TC>,                                       \
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                    \
     if (attr == cudaSuccess)                                                                                     \
       JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
-                 (sparse_group_coef_bulk_kernel<MODE, KT, RS, TE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem,  \
-                                                                         st>>>(                                  \
-                     rows, order, goff, grow, n_groups, (int)vc, TP, M, XS, ring_len, eff, ld_eff, s_ev, q, ldq, \
-                     n_slots, batch, erow_bytes, row_bytes, b_off, b_stride, slot_off, slot_stride)));           \
+                 (sparse_group_coef_bulk_kernel<MODE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem, st>>>(       \
+                     rows, order, goff, n_groups, (int)vc, bq, s_ev, q, ldq, n_slots, batch, b_bytes, row_bytes, \
+                     slot_off, slot_stride)));                                                                   \
   } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
@@ -1717,12 +1778,8 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   } while (0)
 #define JSCC_GC(MODE, TW, TP, XS)                                                                                \
   do {                                                                                                           \
-    if (ring) {                                                                                                  \
-      JSCC_GC_BK(MODE, 0, 4, TP, XS);                                                                            \
-    } else if (bulk) {                                                                                           \
-      if (K <= 4) JSCC_GC_BK(MODE, 4, 0, TP, XS);                                                                \
-      else if (K <= 8) JSCC_GC_BK(MODE, 8, 0, TP, XS);                                                           \
-      else JSCC_GC_BK(MODE, 0, 0, TP, XS);                                                                       \
+    if (bulk) {                                                                                                  \
+      JSCC_GC_BK(MODE, TP, XS);                                                                                  \
     } else if (K <= 4) JSCC_GC_K(MODE, 4, TW);                                                                   \
     else if (K <= 8) JSCC_GC_K(MODE, 8, TW);                                                                     \
     else JSCC_GC_K(MODE, 0, TW);                                                                                 \
@@ -1835,6 +1892,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
 #undef JSCC_GC
 #undef JSCC_GC_K
 #undef JSCC_GC_BK
+#undef JSCC_GA
   JSCC_CUDA_CHECK(attr);
   JSCC_LAUNCH_CHECK();
   const int gpc = (int)((n_groups + chunks - 1) / chunks);
@@ -2058,7 +2116,8 @@ size_t jscc_sparse_grouped_workspace_bytes(int64_t n_events, int64_t n_fine, int
          align_up((size_t)chunks * ldp * sizeof(float), 256) +
          2 * align_up((size_t)((adj_width > 0 ? adj_width : 1) + 1) / 2 * (n_coarse > 0 ? n_coarse : 1) * 16, 256) +
          2 * align_up((size_t)(n_coarse > 0 ? n_coarse : 1) * 32, 256) +
-         align_up((size_t)kCfMaxClusters * ldp * sizeof(float), 256) + 256;
+         align_up((size_t)kCfMaxClusters * ldp * sizeof(float), 256) +
+         align_up((size_t)(n_groups > 0 ? n_groups : 1) * ldq * sizeof(float), 256) + 256;
 }
 
 int jscc_set_fused_cluster(int32_t enable) {

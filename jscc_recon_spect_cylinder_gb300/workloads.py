@@ -107,10 +107,14 @@ class JointWorkload:
             # is then reused from L2 by consecutive events; the weight is a sum over the
             # subset's events, so the order only changes float32 rounding
             parts = [p[torch.argsort(p[:, 0], stable=True)] for p in parts]
+        # packed float32 rows (the reference's layout: the float64 reference and the oracle
+        # read them) and split storage for the product path, float32 and BF16 coarse rows
+        # behind the same int32 row ids
         self.rows_f32 = [p.contiguous() for p in parts] if with_fp32 else None
         split = [ops.split_sparse_rows(p, torch.bfloat16) for p in parts]
         self.ids = [s[0] for s in split]
         self.tc_bf16 = [s[1] for s in split]
+        self.tc_f32 = [p[:, 1:].contiguous() for p in parts] if with_fp32 else None
         del rows, parts
         # ---------------- sensitivities: s (SC column sums), d (Compton, build_sparse_sensi_d
         # rescaling: sum(d) = sum(s) * E_C / E_S), joint s_j = alpha s + (2 - alpha) d
@@ -136,11 +140,8 @@ class JointWorkload:
         A_eff = self.A[dtype]
         w = torch.zeros_like(img)
         ops.sc_weight(A_eff, self.proj, img, floor=1e-12, scale=self.alpha, out=w, row_idx=self.subset_ids[s])
-        if dtype == "bf16":
-            ops.sparse_weight_split(self.ids[s], self.tc_bf16[s], A_eff, self.tables, img, grouped=False,
-                                    scale=2 - self.alpha, out=w)
-        else:
-            ops.sparse_weight(self.rows_f32[s], A_eff, self.tables, img, grouped=False, scale=2 - self.alpha, out=w)
+        tc = self.tc_bf16[s] if dtype == "bf16" else self.tc_f32[s]
+        ops.sparse_weight_split(self.ids[s], tc, A_eff, self.tables, img, grouped=False, scale=2 - self.alpha, out=w)
         return ops.em_update(img, w, self.s_joint, safe=True)
 
     def step(self, img, dtype="bf16"):
@@ -195,19 +196,22 @@ class JointWorkload:
 
     def sparse_kernel_bytes(self, dtype):
         """Algorithmic bytes of one launch of the grouped sparse kernels (one subset, the
-        subset's mean event and group counts): sparse_group_coef reads every coarse row and
-        its event sum once and one sysmat row per group (distinct first-hit row), and writes
-        q (float32 [groups, V_c]); sparse_group_scatter reads one sysmat row and one q row per
-        group and writes one float32 partial image per group chunk (16 chunks)."""
+        subset's mean event and group counts): sparse_group_adjoint reads one sysmat row per
+        group (distinct first-hit row) and writes its float32 adjoint b_g [V_c];
+        sparse_group_coef reads every coarse row and its event sum once and b_g per group, and
+        writes q (float32 [groups, V_c]); sparse_group_scatter reads one sysmat row and one q
+        row per group and writes one float32 partial image per group chunk (16 chunks)."""
         b = 2 if dtype == "bf16" else 4
         ev = self.n_events / self.subsets
         groups = float(sum(torch.unique(i).numel() for i in self.ids)) / self.subsets
-        coef = ev * (self.Vc * b + 4) + groups * (self.V * b + self.Vc * 4)
+        adjoint = groups * (self.V * b + self.Vc * 4)
+        coef = ev * (self.Vc * b + 4) + groups * 2 * self.Vc * 4
         scatter = groups * (self.V * b + self.Vc * 4) + 16 * self.V * 4
         # the fused cluster kernel: every coarse row and its event sum once, one sysmat row per
         # group, one float32 partial image per cluster (at most 38 clusters of four CTAs)
         fused = ev * (self.Vc * b + 4) + groups * self.V * b + 38 * self.V * 4
-        return {"sparse_group_coef": coef, "sparse_group_scatter": scatter, "sparse_group_fused": fused}
+        return {"sparse_group_adjoint": adjoint, "sparse_group_coef": coef, "sparse_group_scatter": scatter,
+                "sparse_group_fused": fused}
 
     def group_count(self):
         """Mean number of groups (distinct first-hit rows) per subset."""
