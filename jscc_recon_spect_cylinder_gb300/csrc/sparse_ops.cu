@@ -803,7 +803,7 @@ sparse_group_adjoint_ring_kernel(const int32_t* __restrict__ grow, int n_groups,
                                  int64_t ld_eff, int64_t n_det, const float4* __restrict__ xs, int vc, int tile_c,
                                  int ring_len, float* __restrict__ bq, int64_t ldq, int n_stages,
                                  uint32_t stage_stride) {
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kAdMaxStages]
   uint64_t* empty = full + kAdMaxStages;                // [kAdMaxStages]
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 2 * kAdMaxStages * 8);
@@ -956,6 +956,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
                               int n_groups, int vc, const float* __restrict__ bq, float* __restrict__ s_ev,
                               float* __restrict__ q, int64_t ldq, int n_slots, int batch, uint32_t b_bytes,
                               uint32_t row_bytes, uint32_t slot_off, uint32_t slot_stride) {
+  constexpr int MB = kBkMaxBatch;  // events of a chunk at most
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kBkMaxSlots]
   uint64_t* empty = full + kBkMaxSlots;                // [kBkMaxSlots]
@@ -1091,54 +1092,51 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         if (et == 0) *b_used = kg + 1;
         mbar_arrive(b_empty);
       }
-      for (int bs = e0; bs < e1; bs += batch) {
-        const int n = min(batch, e1 - bs);
+      // one chunk of NE events, NE known when compiled (no issue slots for absent events);
+      // false: one of the waits gave up
+      auto chunk = [&](auto ne_tag, int bs) -> bool {
+        constexpr int NE = decltype(ne_tag)::value;
         // the event sum of lane k's event of the chunk, read before the dots
-        const float s_lane = (MODE == 0 && lane < n) ? s_ev[bs + lane] : 0.f;
-        int sl[kBkMaxBatch];
+        const float s_lane = (MODE == 0 && lane < NE) ? s_ev[bs + lane] : 0.f;
+        int sl[NE];
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k) {
+        for (int k = 0; k < NE; ++k) {
           sl[k] = cs_slot;
-          if (k < n) cs_slot = cs_slot + 1 == n_slots ? 0 : cs_slot + 1;
+          cs_slot = cs_slot + 1 == n_slots ? 0 : cs_slot + 1;
         }
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k)
-          if (k < n) {
-            if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag, polls)) bad = true;
-            cphase ^= 1u << sl[k];
-          }
+        for (int k = 0; k < NE; ++k) {
+          if (!bk_wait(full + sl[k], (cphase >> sl[k]) & 1u, abort_flag, polls)) bad = true;
+          cphase ^= 1u << sl[k];
+        }
         // ---- dots f_i = t_i . b: this thread's values, then the warp's
-        float4 acc[kBkMaxBatch];
+        float4 acc[NE];
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < NE; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int u = 0; u < kBkQ; ++u) {
           const int c = et * 4 + u * (kBkEvents * 4);
           if (c < vc) {
 #pragma unroll
-            for (int k = 0; k < kBkMaxBatch; ++k)
-              if (k < n) {
-                float v[4];
-                smem4(slot(sl[k]), c, v);
-                ffma4(acc[k], v, bv[u]);
-              }
+            for (int k = 0; k < NE; ++k) {
+              float v[4];
+              smem4(slot(sl[k]), c, v);
+              ffma4(acc[k], v, bv[u]);
+            }
           }
         }
 #pragma unroll
-        for (int k = 0; k < kBkMaxBatch; ++k)
-          if (k < n) {
-            const float f = warp_sum((acc[k].x + acc[k].y) + (acc[k].z + acc[k].w));
-            if (lane == 0) red[(par * kBkEventWarps + warp) * kBkMaxBatch + k] = f;
-          }
-        if (role_sync_or(1, kBkEvents, bad)) {
-          aborted = true;
-          break;
+        for (int k = 0; k < NE; ++k) {
+          const float f = warp_sum((acc[k].x + acc[k].y) + (acc[k].z + acc[k].w));
+          if (lane == 0) red[(par * kBkEventWarps + warp) * kBkMaxBatch + k] = f;
         }
+        if (role_sync_or(1, kBkEvents, bad)) return false;
         // ---- coefficients: lane k sums event k's partials over the warps in order (every
         // warp the same values), then broadcasts
         float cl = 0.f;
-        if (lane < n) {
+        if (lane < NE) {
           float f = 0.f;
+#pragma unroll
           for (int w = 0; w < kBkEventWarps; ++w) f += red[(par * kBkEventWarps + w) * kBkMaxBatch + lane];
           if (MODE == 2) {
             if (warp == 0) s_ev[bs + lane] = f;  // event sums are kept by position in `order`
@@ -1152,33 +1150,49 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
         // ---- q_g += c_i t_i over the chunk, events in order
         if (MODE != 2) {
 #pragma unroll
-          for (int k = 0; k < kBkMaxBatch; ++k)
-            if (k < n) {
-              const float ck = __shfl_sync(0xffffffffu, cl, k);
-              if (ck != 0.f) {
+          for (int k = 0; k < NE; ++k) {
+            const float ck = __shfl_sync(0xffffffffu, cl, k);
+            if (ck != 0.f) {
 #pragma unroll
-                for (int u = 0; u < kBkQ; ++u) {
-                  const int c = et * 4 + u * (kBkEvents * 4);
-                  if (c < vc) {
-                    float v[4];
-                    smem4(slot(sl[k]), c, v);
-                    ffma4s(qa[u], ck, v);
-                  }
+              for (int u = 0; u < kBkQ; ++u) {
+                const int c = et * 4 + u * (kBkEvents * 4);
+                if (c < vc) {
+                  float v[4];
+                  smem4(slot(sl[k]), c, v);
+                  ffma4s(qa[u], ck, v);
                 }
               }
             }
+          }
         }
         // ---- this warp is past its last read of the chunk's rows: release the slots (a
         // warp with a lane whose wait gave up keeps them: its copy may still be in flight)
         __syncwarp();
         if (__all_sync(0xffffffffu, !bad) && lane == 0) {
-          if (et == 0) *rows_used = seq + n;  // before the slots can be refilled
+          if (et == 0) *rows_used = seq + NE;  // before the slots can be refilled
 #pragma unroll
-          for (int k = 0; k < kBkMaxBatch; ++k)
-            if (k < n) mbar_arrive(empty + sl[k]);
+          for (int k = 0; k < NE; ++k) mbar_arrive(empty + sl[k]);
         }
-        seq += n;
+        seq += NE;
         par ^= 1;
+        return true;
+      };
+      for (int bs = e0; bs < e1; bs += batch) {
+        const int n = min(batch, e1 - bs);
+        bool ok;
+        if (n == 1) {
+          ok = chunk(std::integral_constant<int, 1>{}, bs);
+        } else if (n == 2) {
+          ok = chunk(std::integral_constant<int, 2>{}, bs);
+        } else if (n == 3) {
+          ok = chunk(std::integral_constant<int, 3>{}, bs);
+        } else {
+          ok = chunk(std::integral_constant<int, MB>{}, bs);
+        }
+        if (!ok) {
+          aborted = true;
+          break;
+        }
       }
       if (aborted) break;
       if (e0 == e1 && role_sync_or(1, kBkEvents, bad)) {  // no chunk consumed the b wait's status
@@ -1271,16 +1285,16 @@ constexpr int kScThreads = kScConsumers + 32;
 constexpr int kScVox = 8;
 constexpr int kScTile = kScConsumers * kScVox;
 constexpr int kScSeg = 1024;  // coarse values per staged q segment
-constexpr int kScMaxStages = 16;
-constexpr int kScHeader = 384;  // 2 x kScMaxStages barriers, flags, tap span
+constexpr int kScMaxStages = 24;
+constexpr int kScHeader = 512;  // 2 x kScMaxStages barriers, flags, tap span
 static_assert(16 * kScMaxStages + 20 <= kScHeader, "scatter header");
 
 template <typename TE>
 __global__ void __launch_bounds__(kScThreads, 2)
 sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const int32_t* __restrict__ grow,
                                  int n_groups, int groups_per_chunk, const TE* __restrict__ eff, int64_t ld_eff,
-                                 int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp, int n_stages,
-                                 uint32_t stage_bytes, uint32_t seg_off) {
+                                 int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp,
+                                 uint32_t stage_space, uint32_t seg_off) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kScMaxStages]
   uint64_t* empty = full + kScMaxStages;               // [kScMaxStages]
@@ -1384,6 +1398,12 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   const bool staged = seg_len <= kScSeg;
   const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
   const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
+  // stages sized to this tile's segment: the sysmat tile (seg_off bytes) and one q segment per
+  // z tap, as many as the shared memory holds
+  const uint32_t stage_bytes = (seg_off + seg_bytes * (two_z ? 2u : 1u) + 127u) & ~127u;
+  int n_stages = (int)(stage_space / stage_bytes);
+  if (n_stages > kScMaxStages) n_stages = kScMaxStages;
+  if (n_stages < 1) n_stages = 1;  // (a tile that is not staged uses none)
   auto stage = [&](int s) { return smem + kScHeader + (size_t)s * stage_bytes; };
   if (warp == kScConsumers / 32) {
     // ------------------------------------------------------------ producer warp
@@ -1408,7 +1428,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
               mbar_arrive_expect_tx(full + s, a_bytes + seg_bytes * (two_z ? 2u : 1u));
               bulk_copy_g2s(st, eff + clamp_row(row, n_det) * ld_eff + j0, a_bytes, full + s);
               bulk_copy_g2s(st + seg_off, qg + (int64_t)z0 * n_lc + cs0, seg_bytes, full + s);
-              if (two_z) bulk_copy_g2s(st + seg_off + kScSeg * 4, qg + (int64_t)z1 * n_lc + cs0, seg_bytes, full + s);
+              if (two_z) bulk_copy_g2s(st + seg_off + seg_bytes, qg + (int64_t)z1 * n_lc + cs0, seg_bytes, full + s);
               *issued = kk + 1;
             }
           }
@@ -1426,25 +1446,6 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
     bool bad = false;
     // acc[v] += a[v] * (u0 * (w0 q0[l0] + w1 q0[l1]) + u1 * (w0 q1[l0] + w1 q1[l1]))
     auto accumulate = [&](const float (&a)[kScVox], const float* q0, const float* q1) {
-      if (pair && !two_z) {
-        // one z plane: per voxel acc += a * (u0 * (ra qa + rb qb)), two voxels per packed f32x2
-        // operation (per lane the same rounded operations as the scalar form below)
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-          const float2 qa = make_float2(q0[pc0[r]], q0[pc0[r]]), qb = make_float2(q0[pc1[r]], q0[pc1[r]]);
-#pragma unroll
-          for (int i = 0; i < 4; i += 2) {
-            const int v = 4 * r + i;
-            float2 t = __fmul2_rn(make_float2(ra[v], ra[v + 1]), qa);
-            t = __ffma2_rn(make_float2(rb[v], rb[v + 1]), qb, t);
-            const float2 val = __fmul2_rn(make_float2(u0, u0), t);
-            const float2 nw = __ffma2_rn(make_float2(a[v], a[v + 1]), val, make_float2(acc[v], acc[v + 1]));
-            if (val.x != 0.f) acc[v] = nw.x;
-            if (val.y != 0.f) acc[v + 1] = nw.y;
-          }
-        }
-        return;
-      }
       if (pair && !two_z) {
         // one z plane: per voxel acc += a * (u0 * (ra qa + rb qb)), two voxels per packed f32x2
         // operation (per lane the same rounded operations as the scalar form below)
@@ -1515,7 +1516,7 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
           float a[kScVox];
           load4x2(at, a);
           accumulate(a, reinterpret_cast<const float*>(st + seg_off) - cs0,
-                     reinterpret_cast<const float*>(st + seg_off + kScSeg * 4) - cs0);
+                     reinterpret_cast<const float*>(st + seg_off + seg_bytes) - cs0);
         }
         __syncwarp();
         if (lane == 0) {
@@ -1663,7 +1664,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
               taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf && vf / taps.n_lf == vc / taps.n_lc &&
               vf < (1 << 30);
   // adjoint tiles of whole rings (at most kAdVox * kAdCompute coarse voxels, an even number so
-  // that every segment starts on a 16-byte boundary), chunks of groups for about two CTAs per SM
+  // that every segment starts on a 16-byte boundary), chunks of groups for about three CTAs per SM
   int ad_tile = 0, ad_tiles = 0, ad_chunks = 1, ad_gpc = 0, ad_stages = 0;
   uint32_t ad_stride = 0;
   size_t ad_smem = 0;
@@ -1682,12 +1683,12 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     if (ring) {
       ad_tiles = (int)((vc + ad_tile - 1) / ad_tile);
       ad_stride = (uint32_t)align_up((size_t)ad_tile * 4 * sizeof(TE), 128);
-      ad_stages = (int)((110u * 1024u - kAdHeader) / ad_stride);
+      ad_stages = (int)((74u * 1024u - kAdHeader) / ad_stride);  // three CTAs per SM
       if (ad_stages > kAdMaxStages) ad_stages = kAdMaxStages;
       if (ad_stages < 2) ad_stages = 2;
       ad_smem = kAdHeader + (size_t)ad_stages * ad_stride;
       ring = ad_smem <= 227 * 1024;
-      int64_t ch = (2 * (int64_t)num_sms() + ad_tiles - 1) / ad_tiles;
+      int64_t ch = (3 * (int64_t)num_sms()) / ad_tiles;  // one wave of about three CTAs per SM
       if (ch > n_groups) ch = n_groups;
       ad_chunks = (int)(ch < 1 ? 1 : ch);
       ad_gpc = (int)((n_groups + ad_chunks - 1) / ad_chunks);
@@ -1901,12 +1902,11 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   // ~98 KB so that two CTAs share an SM)
   const int n_zc = (int)(vc / taps.n_lc);
   const uint32_t sc_a = (uint32_t)align_up((size_t)kScTile * sizeof(TE), 128);
-  const uint32_t sc_stage = sc_a + (n_zc > 1 ? 2u : 1u) * kScSeg * 4u;
-  int sc_stages = (int)((98u * 1024u - kScHeader) / sc_stage);
-  if (sc_stages > kScMaxStages) sc_stages = kScMaxStages;
-  if (sc_stages < 2) sc_stages = 2;
-  const size_t sc_smem = kScHeader + (size_t)sc_stages * sc_stage;
-  const bool sc_bulk = reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
+  const uint32_t sc_stage = sc_a + (n_zc > 1 ? 2u : 1u) * kScSeg * 4u;  // largest stage
+  // two CTAs per SM: the kernel packs its stages into the space (at least two of the largest)
+  const size_t sc_smem = 110u * 1024u;
+  const uint32_t sc_space = (uint32_t)(sc_smem - kScHeader);
+  const bool sc_bulk = sc_space >= 2 * sc_stage && reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
                        ((size_t)taps.n_lf * sizeof(TE)) % 16 == 0 && taps.n_lf % kScVox == 0 && taps.n_lc % 4 == 0 &&
                        reinterpret_cast<uintptr_t>(q) % 16 == 0 && ldq % 4 == 0;
   int64_t n_part = chunks;
@@ -1922,8 +1922,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     JSCC_TIMED("sparse_group_scatter", st,
                (sparse_group_scatter_bulk_kernel<TE><<<dim3((unsigned)tiles, (unsigned)sc_chunks), kScThreads,
                                                        sc_smem, st>>>(q, ldq, grow, n_groups, sc_gpc, eff, ld_eff,
-                                                                      rows.n_det, taps, part, ldp, sc_stages, sc_stage,
-                                                                      sc_a)));
+                                                                      rows.n_det, taps, part, ldp, sc_space, sc_a)));
     n_part = sc_chunks;
   } else {
     dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
