@@ -1558,9 +1558,263 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
   }
 }
 
+// Scatter for the stride-4 ring stencil: the same CTA layout as the bulk scatter with
+// sixteen voxels per thread (runs of four at stride 128, tiles of kSpTile fine voxels, q
+// segments up to kSpSeg coarse values). Every run of four theta-consecutive voxels of a ring
+// interpolates between two coarse voxels, so each voxel keeps two folded weights (ra, rb) and
+// its sum in registers and a run reads two q values per z tap; the arithmetic per voxel is the
+// bulk scatter's pair form (the same result). A thread whose runs are not pairs (tap tables
+// that do not follow the stencil) reads its taps from global memory on every group instead.
+constexpr int kSpVox = 16;
+constexpr int kSpRuns = kSpVox / 4;
+constexpr int kSpTile = kScConsumers * kSpVox;
+constexpr int kSpSeg = 2048;
+
+template <typename TE>
+__global__ void __launch_bounds__(kScThreads, 2)
+sparse_group_scatter_pair_kernel(const float* __restrict__ q, int64_t ldq, const int32_t* __restrict__ grow,
+                                 int n_groups, int groups_per_chunk, const TE* __restrict__ eff, int64_t ld_eff,
+                                 int64_t n_det, UpTaps taps, float* __restrict__ part, int64_t ldp,
+                                 uint32_t stage_space, uint32_t seg_off) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);  // [kScMaxStages]
+  uint64_t* empty = full + kScMaxStages;               // [kScMaxStages]
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 16 * kScMaxStages);
+  int* issued = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 4);
+  int* used = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 8);
+  int* span = reinterpret_cast<int*>(smem + 16 * kScMaxStages + 12);  // [lmin, lmax]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t polls = g_bk_poll_limit;
+  const int n_lf = taps.n_lf, n_lc = taps.n_lc;
+  const int tiles_per_plane = (n_lf + kSpTile - 1) / kSpTile;
+  const int zf = blockIdx.x / tiles_per_plane;
+  const int l_begin = (blockIdx.x - zf * tiles_per_plane) * kSpTile;
+  const int l_end = min(l_begin + kSpTile, n_lf);
+  const int64_t j0 = (int64_t)zf * n_lf + l_begin;
+  const int z0 = taps.zt[2 * zf], z1 = taps.zt[2 * zf + 1];
+  const float u0 = taps.zwt[2 * zf], u1 = taps.zwt[2 * zf + 1];
+  const bool two_z = u1 != 0.f;
+  const int g_begin = blockIdx.y * groups_per_chunk;
+  const int g_end = min(g_begin + groups_per_chunk, n_groups);
+  if (tid == 0) {
+    for (int s = 0; s < kScMaxStages; ++s) {
+      mbar_init(full + s, 1);
+      mbar_init(empty + s, kScConsumers / 32);
+    }
+    *abort_flag = 0;
+    *issued = *used = 0;
+    span[0] = INT_MAX;
+    span[1] = -1;
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // this thread's voxels: runs r of four at lf0 + 128 r (one tap of the warp's voxels reads
+  // consecutive q words; each run is one 8-byte sysmat load)
+  const int lf0 = l_begin + warp * (32 * kSpVox) + lane * 4;
+  auto vox = [&](int v) { return lf0 + (v >> 2) * 128 + (v & 3); };
+  int pc0[kSpRuns], pc1[kSpRuns];
+  float ra[kSpVox], rb[kSpVox];
+  bool pair = true;
+  if (tid < kScConsumers) {
+    int mn = INT_MAX, mx = -1;
+#pragma unroll
+    for (int r = 0; r < kSpRuns; ++r) {
+      int a = -1, b = -1;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int v = 4 * r + i, lf = vox(v);
+        ra[v] = rb[v] = 0.f;
+        if (lf >= l_end) continue;
+        const int t[2] = {taps.lt[2 * lf], taps.lt[2 * lf + 1]};
+        const float w[2] = {taps.lwt[2 * lf], taps.lwt[2 * lf + 1]};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          mn = min(mn, t[h]);
+          mx = max(mx, t[h]);
+          if (a < 0) a = t[h];
+          if (t[h] == a) {
+            ra[v] += w[h];
+          } else {
+            if (b < 0) b = t[h];
+            if (t[h] == b) rb[v] += w[h];
+            else pair = false;
+          }
+        }
+      }
+      pc0[r] = a < 0 ? 0 : a;
+      pc1[r] = b < 0 ? pc0[r] : b;
+    }
+    if (mx >= 0) {
+      atomicMin(span, mn);
+      atomicMax(span + 1, mx);
+    }
+  }
+  __syncthreads();
+  const int cs0 = span[0] & ~3;
+  const int seg_len = span[1] < 0 ? 4 : ((span[1] + 1 - cs0 + 3) & ~3);
+  if (pair && tid < kScConsumers) {
+#pragma unroll
+    for (int r = 0; r < kSpRuns; ++r) {  // runs past the tile: indices inside the segment (weight 0)
+      if (vox(4 * r) >= l_end) pc0[r] = pc1[r] = cs0;
+    }
+  }
+  const bool staged = seg_len <= kSpSeg;
+  const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
+  const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
+  const uint32_t stage_bytes = (seg_off + seg_bytes * (two_z ? 2u : 1u) + 127u) & ~127u;
+  int n_stages = (int)(stage_space / stage_bytes);
+  if (n_stages > kScMaxStages) n_stages = kScMaxStages;
+  if (n_stages < 1) n_stages = 1;  // (a tile that is not staged uses none)
+  auto stage = [&](int s) { return smem + kScHeader + (size_t)s * stage_bytes; };
+  if (warp == kScConsumers / 32) {
+    // ------------------------------------------------------------ producer warp
+    if (staged) {
+      bool ok = true;
+      int s = 0;
+      uint32_t eph = 0;  // bit s: parity of the next phase of empty[s] to wait for
+      for (int w = g_begin; w < g_end && ok; w += 32) {
+        const int gv = w + lane < g_end ? grow[w + lane] : 0;  // 32 group rows per load
+        const int m = min(32, g_end - w);
+        for (int k = 0; k < m && ok; ++k) {
+          const int row = __shfl_sync(0xffffffffu, gv, k);
+          const int kk = w - g_begin + k;
+          if (lane == 0) {
+            if (kk >= n_stages) {
+              ok = bk_wait(empty + s, (eph >> s) & 1u, abort_flag, polls);
+              eph ^= 1u << s;
+            }
+            if (ok) {
+              unsigned char* st = stage(s);
+              const float* qg = q + (int64_t)(w + k) * ldq;
+              mbar_arrive_expect_tx(full + s, a_bytes + seg_bytes * (two_z ? 2u : 1u));
+              bulk_copy_g2s(st, eff + clamp_row(row, n_det) * ld_eff + j0, a_bytes, full + s);
+              bulk_copy_g2s(st + seg_off, qg + (int64_t)z0 * n_lc + cs0, seg_bytes, full + s);
+              if (two_z) bulk_copy_g2s(st + seg_off + seg_bytes, qg + (int64_t)z1 * n_lc + cs0, seg_bytes, full + s);
+              *issued = kk + 1;
+            }
+          }
+          s = s + 1 == n_stages ? 0 : s + 1;
+          ok = __shfl_sync(0xffffffffu, ok, 0);
+        }
+      }
+      if (!ok && lane == 0) *abort_flag = 1;
+    }
+  } else {
+    // ------------------------------------------------------------ consumer warps
+    float acc[kSpVox];
+#pragma unroll
+    for (int v = 0; v < kSpVox; ++v) acc[v] = 0.f;
+    bool bad = false;
+    // acc[v] += a[v] * (u0 * (ra qa + rb qb) + u1 * (ra qa1 + rb qb1)) per run (a: the run's
+    // four sysmat values at ar), the scalar form of the bulk scatter's pair branch
+    auto run = [&](int r, const float (&a)[4], const float* q0, const float* q1) {
+      if (pair) {
+        if (!two_z) {
+          const float2 qa = make_float2(q0[pc0[r]], q0[pc0[r]]), qb = make_float2(q0[pc1[r]], q0[pc1[r]]);
+#pragma unroll
+          for (int i = 0; i < 4; i += 2) {
+            const int v = 4 * r + i;
+            float2 t = __fmul2_rn(make_float2(ra[v], ra[v + 1]), qa);
+            t = __ffma2_rn(make_float2(rb[v], rb[v + 1]), qb, t);
+            const float2 val = __fmul2_rn(make_float2(u0, u0), t);
+            const float2 nw = __ffma2_rn(make_float2(a[i], a[i + 1]), val, make_float2(acc[v], acc[v + 1]));
+            if (val.x != 0.f) acc[v] = nw.x;
+            if (val.y != 0.f) acc[v + 1] = nw.y;
+          }
+        } else {
+          const float qa = q0[pc0[r]], qb = q0[pc1[r]], qa1 = q1[pc0[r]], qb1 = q1[pc1[r]];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int v = 4 * r + i;
+            float t = ra[v] * qa;
+            t = fmaf(rb[v], qb, t);
+            float val = u0 * t;
+            float bb = ra[v] * qa1;
+            bb = fmaf(rb[v], qb1, bb);
+            val = fmaf(u1, bb, val);
+            if (val != 0.f) acc[v] = fmaf(a[i], val, acc[v]);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int v = 4 * r + i, lf = vox(v);
+          if (lf >= l_end) continue;
+          const int l0 = taps.lt[2 * lf], l1 = taps.lt[2 * lf + 1];
+          const float w0 = taps.lwt[2 * lf], w1 = taps.lwt[2 * lf + 1];
+          float t = w0 * q0[l0];
+          t = fmaf(w1, q0[l1], t);
+          float val = u0 * t;
+          if (two_z) {
+            float bb = w0 * q1[l0];
+            bb = fmaf(w1, q1[l1], bb);
+            val = fmaf(u1, bb, val);
+          }
+          if (val != 0.f) acc[v] = fmaf(a[i], val, acc[v]);
+        }
+      }
+    };
+    if (staged) {
+      // shared-memory operands only (the pointers below are derived from the shared array)
+      int s = 0;
+      uint32_t fph = 0;  // bit s: parity of the next phase of full[s]
+      for (int g = g_begin; g < g_end; ++g, s = s + 1 == n_stages ? 0 : s + 1) {
+        const int kk = g - g_begin;
+        if (!bk_wait(full + s, (fph >> s) & 1u, abort_flag, polls)) {
+          bad = true;
+          break;
+        }
+        fph ^= 1u << s;
+        unsigned char* st = stage(s);
+        const TE* at = reinterpret_cast<const TE*>(st) + (lf0 - l_begin);
+        const float* q0 = reinterpret_cast<const float*>(st + seg_off) - cs0;
+        const float* q1 = reinterpret_cast<const float*>(st + seg_off + seg_bytes) - cs0;
+#pragma unroll
+        for (int r = 0; r < kSpRuns; ++r)
+          if (vox(4 * r) < l_end) {
+            float a[4];
+            smem4(at + 128 * r, 0, a);
+            run(r, a, q0, q1);
+          }
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(empty + s);
+          if (warp == 0) *used = kk + 1;
+        }
+      }
+    } else {
+      for (int g = g_begin; g < g_end; ++g) {
+        const TE* ag = eff + clamp_row(grow[g], n_det) * ld_eff + j0 + (lf0 - l_begin);
+        const float* q0 = q + (int64_t)g * ldq + (int64_t)z0 * n_lc;
+        const float* q1 = q + (int64_t)g * ldq + (int64_t)z1 * n_lc;
+#pragma unroll
+        for (int r = 0; r < kSpRuns; ++r)
+          if (vox(4 * r) < l_end) {  // (runs are whole: the plane's length is a multiple of 4)
+            float a[4];
+            smem4(ag + 128 * r, 0, a);
+            run(r, a, q0, q1);
+          }
+      }
+    }
+    if (bad) *abort_flag = 1;
+    if (!bad) {
+      float* out = part + (int64_t)blockIdx.y * ldp + (int64_t)zf * n_lf;
+#pragma unroll
+      for (int v = 0; v < kSpVox; ++v)
+        if (vox(v) < l_end) out[vox(v)] = acc[v];
+    }
+  }
+  __syncthreads();
+  if (*abort_flag && tid == 0) {
+    atomicAdd(&g_wait_timeout_count, 1u);
+    for (int kk = *used; kk < *issued; ++kk)
+      mbar_wait_bounded(full + kk % n_stages, (kk / n_stages) & 1, kBkDrainPolls);
+  }
+}
+
 #include "sparse_cluster.cuh"
 
-constexpr int kCfMaxClusters = 64;  // partial images reserved in the workspace for the cluster path
+constexpr int kCfMaxClusters = 64;  // partial images reserved for the one-wave kernels (clusters, bulk scatters)
 static bool g_cluster_fused = false;  // opt-in (jscc_set_fused_cluster)
 
 // Co-resident clusters of the fused kernel for this device and shared-memory size (cached).
@@ -1656,7 +1910,9 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   int4* tpw = cv.take<int4>((size_t)M * vc);  // packed taps, weights only (row sums)
   float4* xsx = cv.take<float4>((size_t)2 * vc);  // ring stencil, x folded in
   float4* xsw = cv.take<float4>((size_t)2 * vc);  // ring stencil, weights only
-  float* part_cf = cv.take<float>((size_t)kCfMaxClusters * ldp);  // cluster path partial images
+  // partial images of the one-wave kernels (the cluster path or the bulk scatters), one per
+  // cluster or chunk of groups
+  float* part_cf = cv.take<float>((size_t)kCfMaxClusters * ldp);
   float* bq = cv.take<float>((size_t)n_groups * ldq);             // group adjoints b_g (bulk path)
   JSCC_REQUIRE(cv.ok(), "jscc_sparse_weight_grouped: workspace too small");
   // stride-4 ring stencil (checked by the caller against the tap table): centres multiples of 4
@@ -1910,11 +2166,35 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
                        ((size_t)taps.n_lf * sizeof(TE)) % 16 == 0 && taps.n_lf % kScVox == 0 && taps.n_lc % 4 == 0 &&
                        reinterpret_cast<uintptr_t>(q) % 16 == 0 && ldq % 4 == 0;
   int64_t n_part = chunks;
-  if (sc_bulk) {
-    const int tiles = (int)(vf / taps.n_lf) * ((taps.n_lf + kScTile - 1) / kScTile);
-    // one wave: tiles x chunks <= two CTAs per SM (fewer chunks than the workspace allows)
+  float* part_out = part;
+  // the stride-4 ring stencil's scatter: sixteen voxels per thread (the kernel checks that every
+  // run of four interpolates between two coarse voxels and reads the taps itself otherwise)
+  const uint32_t sp_a = (uint32_t)align_up((size_t)kSpTile * sizeof(TE), 128);
+  const bool sc_pair = sc_bulk && ring_stride == 4 && ring_len >= 8 && ring_len % 4 == 0 &&
+                       taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf &&
+                       sc_space >= 2 * (sp_a + (n_zc > 1 ? 2u : 1u) * kSpSeg * 4u);
+  if (sc_pair) {
+    const int tiles = (int)(vf / taps.n_lf) * ((taps.n_lf + kSpTile - 1) / kSpTile);
+    // one wave: tiles x chunks <= two CTAs per SM, partial images in the one-wave slots
     int64_t sc_chunks = 2 * (int64_t)num_sms() / tiles;
-    if (sc_chunks > chunks) sc_chunks = chunks;
+    if (sc_chunks > kCfMaxClusters) sc_chunks = kCfMaxClusters;
+    if (sc_chunks > n_groups) sc_chunks = n_groups;
+    if (sc_chunks < 1) sc_chunks = 1;
+    const int sc_gpc = (int)((n_groups + sc_chunks - 1) / sc_chunks);
+    JSCC_CUDA_CHECK(cudaFuncSetAttribute(sparse_group_scatter_pair_kernel<TE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sc_smem));
+    JSCC_TIMED("sparse_group_scatter", st,
+               (sparse_group_scatter_pair_kernel<TE><<<dim3((unsigned)tiles, (unsigned)sc_chunks), kScThreads,
+                                                       sc_smem, st>>>(q, ldq, grow, n_groups, sc_gpc, eff, ld_eff,
+                                                                      rows.n_det, taps, part_cf, ldp, sc_space, sp_a)));
+    n_part = sc_chunks;
+    part_out = part_cf;
+  } else if (sc_bulk) {
+    const int tiles = (int)(vf / taps.n_lf) * ((taps.n_lf + kScTile - 1) / kScTile);
+    // one wave: tiles x chunks <= two CTAs per SM, partial images in the one-wave slots
+    int64_t sc_chunks = 2 * (int64_t)num_sms() / tiles;
+    if (sc_chunks > kCfMaxClusters) sc_chunks = kCfMaxClusters;
+    if (sc_chunks > n_groups) sc_chunks = n_groups;
     if (sc_chunks < 1) sc_chunks = 1;
     const int sc_gpc = (int)((n_groups + sc_chunks - 1) / sc_chunks);
     JSCC_CUDA_CHECK(cudaFuncSetAttribute(sparse_group_scatter_bulk_kernel<TE>,
@@ -1922,8 +2202,9 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
     JSCC_TIMED("sparse_group_scatter", st,
                (sparse_group_scatter_bulk_kernel<TE><<<dim3((unsigned)tiles, (unsigned)sc_chunks), kScThreads,
                                                        sc_smem, st>>>(q, ldq, grow, n_groups, sc_gpc, eff, ld_eff,
-                                                                      rows.n_det, taps, part, ldp, sc_space, sc_a)));
+                                                                      rows.n_det, taps, part_cf, ldp, sc_space, sc_a)));
     n_part = sc_chunks;
+    part_out = part_cf;
   } else {
     dim3 sgrid((unsigned)((vf + 255) / 256), (unsigned)chunks);
     JSCC_TIMED("sparse_group_scatter", st,
@@ -1935,7 +2216,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   if (blocks > (int64_t)num_sms() * 16) blocks = (int64_t)num_sms() * 16;
   const int has_scale = scale != 1.0f;
   JSCC_TIMED("sparse_reduce", st,
-             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part, ldp, (int)n_part, rotmat_inv, ld_rot, vf,
+             (sparse_reduce_kernel<<<(unsigned)blocks, 256, 0, st>>>(part_out, ldp, (int)n_part, rotmat_inv, ld_rot, vf,
                                                                      has_scale, scale, weight)));
   JSCC_LAUNCH_CHECK();
   return JSCC_OK;
