@@ -80,7 +80,11 @@ JSCC_API int jscc_kernel_timing_collect(char* buf, size_t buf_bytes);
 /* ------------------------------------------------ single-photon (SC) path */
 
 /*
- * Workspace bytes needed by jscc_sc_weight for the given sizes.
+ * Workspace bytes for jscc_sc_weight at the given sizes: the two-pass kernels' scratch
+ * (forward split, ratio, back-projection partials: the minimum jscc_sc_weight accepts)
+ * plus, for one rotation, one partial image per cluster of the fused single-read kernel,
+ * which jscc_sc_weight runs instead of the two passes when the workspace holds them (the
+ * image read directly, no rotation tables, 16-byte-aligned rows, at most 38,400 voxels).
  */
 JSCC_API size_t jscc_sc_weight_workspace_bytes(int64_t n_bins, int64_t n_vox, int32_t n_rot);
 
@@ -170,10 +174,12 @@ JSCC_API int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, co
  *
  * Scratch lives in one fixed device array of JSCC_SC_NOALLOC_SCRATCH_BYTES (16 MiB)
  * inside this library; every GPU that loads the library holds it until the process
- * exits. Problems whose scratch need (jscc_sc_weight_workspace_bytes) exceeds it are
- * rejected with JSCC_ERR_INVALID and a message; use jscc_sc_weight for those. The
- * 16 MiB covers e.g. a 10,240-bin x 36,000-voxel subset block with one rotation
- * (about 5 MiB); scratch grows with the rotations handled per pass (up to 8).
+ * exits. Problems whose two-pass scratch need exceeds it are rejected with
+ * JSCC_ERR_INVALID and a message; use jscc_sc_weight for those. The 16 MiB covers e.g. a
+ * 10,240-bin x 36,000-voxel subset block with one rotation (about 5 MiB for the two
+ * passes); scratch grows with the rotations handled per pass (up to 8). The fused
+ * single-read kernel runs when the scratch also holds its partial images (see
+ * jscc_sc_weight_workspace_bytes).
  * The first call on each device looks up the array's device address (with that
  * device current); make that first call before any stream capture. The address is
  * kept for the life of the process: after cudaDeviceReset on a device, do not call this

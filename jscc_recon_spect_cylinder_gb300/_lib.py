@@ -302,8 +302,9 @@ def check_wait_timeouts() -> None:
     bulk, gemm = take_wait_timeout_count(), take_gemm_timeout_count()
     if bulk or gemm:
         timeout_epoch += 1
-        raise RuntimeError(f"device pipeline waits gave up: {bulk} in the sparse bulk kernels, {gemm} in the "
-                           "tensor-core GEMM; the results computed since the last check are invalid")
+        raise RuntimeError(f"device pipeline waits gave up: {bulk} in the bulk-copy kernels (grouped sparse "
+                           f"weight, fused SC weight), {gemm} in the tensor-core GEMM; the results computed since "
+                           "the last check are invalid")
 
 
 def take_bad_index_count() -> int:

@@ -189,4 +189,89 @@ __device__ __forceinline__ float load_elem(const __nv_bfloat16* p, int64_t i) {
   return __bfloat162float(p[i]);
 }
 
+// ---------------------------------------------------------------- pipeline roles
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// named barrier `id` over `count` threads (the warps of one role)
+__device__ __forceinline__ void role_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// named barrier returning the OR of every participant's `v` (the same value in all of them,
+// so a decision taken on it is uniform within the role)
+__device__ __forceinline__ bool role_sync_or(int id, int count, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
+// bounded wait that also gives up once another thread has flagged an abort
+__device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 31u) == 31u && *abort_flag) return false;
+  }
+  return false;
+}
+
+// ------------------------------------------------------------------ cluster primitives
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_id_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t n_clusters_x() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// all threads of every CTA of the cluster
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// the address of this CTA's shared variable at `p` in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t map_to_rank(const void* p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+// 16 bytes into another CTA's shared memory, completing 16 transaction bytes on that CTA's
+// mbarrier (no fence: the receiver's wait on its own mbarrier sees the data)
+__device__ __forceinline__ void st_async_v4(uint32_t addr, float a, float b, float c, float d, uint32_t bar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(
+                   addr),
+               "f"(a), "f"(b), "f"(c), "f"(d), "r"(bar)
+               : "memory");
+}
+// a wait that sees arrivals (and the stores before them) from other CTAs of the cluster
+__device__ __forceinline__ bool mbar_try_wait_cluster(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool cf_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                uint32_t polls) {
+  for (uint32_t i = 0; i < polls; ++i) {
+    if (mbar_try_wait_cluster(bar, parity)) return true;
+    if ((i & 31u) == 31u && *abort_flag) return false;
+  }
+  return false;
+}
+
 }  // namespace jscc

@@ -80,6 +80,7 @@ void timing_end(const char* name, cudaStream_t st) {
 
 int set_bulk_poll_limit(uint32_t polls, bool reset);  // sparse_ops.cu
 int set_gemm_poll_limit(uint32_t polls, bool reset);  // batched_gemm.cu
+int set_sc_poll_limit(uint32_t polls, bool reset);    // sc_projector.cu
 
 }  // namespace jscc
 
@@ -90,6 +91,8 @@ int jscc_set_wait_limit(int64_t polls) {
   const bool reset = polls < 0;
   const uint32_t v = reset ? 0u : (uint32_t)polls;
   int rc = jscc::set_bulk_poll_limit(v, reset);
+  if (rc != JSCC_OK) return rc;
+  rc = jscc::set_sc_poll_limit(v, reset);
   if (rc != JSCC_OK) return rc;
   return jscc::set_gemm_poll_limit(v, reset);
 }

@@ -21,6 +21,8 @@
 
 #include <mutex>
 
+#include "sc_fused.cuh"
+
 namespace jscc {
 
 constexpr int kRotBlock = 8;          // rotations handled per pass over A
@@ -557,7 +559,9 @@ struct ScPlan {
   int64_t rows_per_chunk;
   int64_t fwd_warps;       // forward pass: warps of the persistent grid (32 per SM)
   int fwd_maxp;            // forward pass: row pieces per warp (upper bound)
-  size_t ws_bytes;
+  size_t ws_bytes;         // the two-pass kernels' workspace (the minimum)
+  int64_t fs_clusters;     // fused single-read path (one rotation): clusters of two CTAs
+  size_t fs_bytes;         // its partial images, after the two-pass carve
 };
 
 static int pow2_block(int n_rot) {
@@ -589,7 +593,32 @@ static ScPlan plan_sc(int64_t n_bins, int64_t V, int32_t n_rot) {
   bytes += align_up((size_t)(n_bins > 0 ? n_bins : 1) * p.rb * sizeof(float), 256);  // ratio
   bytes += align_up((size_t)p.chunks * p.rb * p.ldx * sizeof(float), 256);          // partials
   p.ws_bytes = bytes + 256;
+  p.fs_clusters = n_rot == 1 ? (int64_t)num_sms() / 2 : 0;
+  if (p.fs_clusters > n_bins) p.fs_clusters = n_bins;
+  p.fs_bytes = p.fs_clusters > 0 ? align_up((size_t)p.fs_clusters * p.ldx * sizeof(float), 256) + 256 : 0;
   return p;
+}
+
+int set_sc_poll_limit(uint32_t polls, bool reset) {
+  const uint32_t v = reset ? kFsMaxPolls : polls;
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_sc_poll_limit, &v, sizeof(v)));
+  return JSCC_OK;
+}
+
+int take_sc_timeout_count(unsigned int* out) {
+  unsigned int h = 0, zero = 0;
+  JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_sc_timeout_count, sizeof(h)));
+  JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_sc_timeout_count, &zero, sizeof(zero)));
+  *out = h;
+  return JSCC_OK;
+}
+
+// The fused single-read path's partial images: after the two-pass carve `cv` when the
+// workspace holds them, else nullptr (the two-pass kernels run).
+static float* fused_partials(const ScPlan& p, Carver cv) {
+  if (p.fs_bytes == 0) return nullptr;
+  float* f = cv.take<float>((size_t)p.fs_clusters * p.ldx);
+  return cv.ok() ? f : nullptr;
 }
 
 template <typename T, int RB>
@@ -600,12 +629,42 @@ static int launch_sc_block(const T* A, int64_t lda, const int64_t* row_idx, int6
                            float* weight, const ScPlan& p, float* xr, float* ratio, float* part,
                            float* fpart, const float* xsrc_direct, cudaStream_t st, int stage = 0,
                            float* fout = nullptr, int64_t ld_fout = 0, const float* gin = nullptr,
-                           int64_t ld_gin = 0) {
+                           int64_t ld_gin = 0, float* fs_part = nullptr) {
   // stage 0: forward, ratio, back (the weight); 1: forward only into fout; 2: back-project gin
   constexpr int NV = VecTraits<T>::kVec;
   const bool vec_ok = ((lda * (int64_t)sizeof(T)) % 16 == 0) &&
                       (reinterpret_cast<uintptr_t>(A) % 16 == 0);
   const int sms = num_sms();
+  // fused single-read path: the weight of one rotation read directly, halves of 16-byte rows
+  // that fit the consumer registers, at least two stages of a row half
+  if (RB == 1 && stage == 0 && nr == 1 && xsrc_direct != nullptr && rotinv == nullptr && fs_part != nullptr &&
+      vec_ok && V % (16 / (int64_t)sizeof(T)) == 0 && p.fs_clusters > 0) {
+    const int64_t el = 16 / (int64_t)sizeof(T);
+    const int64_t split = (V / 2 + el - 1) / el * el;
+    const uint32_t stride = (uint32_t)align_up((size_t)split * sizeof(T), 128);
+    int stages = (int)((227u * 1024u - kFsHeader) / stride);
+    if (stages > kFsMaxStages) stages = kFsMaxStages;
+    int batch = stages / 2 < kFsMaxBatch ? stages / 2 : kFsMaxBatch;
+    if (split <= kFsHalfMax && V - split <= kFsHalfMax && V - split > 0 && stages >= 2 && batch >= 1 &&
+        reinterpret_cast<uintptr_t>(xsrc_direct) % 16 == 0) {
+      const size_t smem = kFsHeader + (size_t)stages * stride;
+      JSCC_CUDA_CHECK(cudaFuncSetAttribute(sc_fused_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      JSCC_TIMED("sc_fused", st,
+                 (sc_fused_kernel<T><<<(unsigned)(2 * p.fs_clusters), kFsThreads, smem, st>>>(
+                     A, lda, row_idx, n_bins, V, split, xsrc_direct, proj, ld_proj, r0, use_floor, floor_v, fs_part,
+                     p.ldx, stages, batch, stride)));
+      JSCC_LAUNCH_CHECK();
+      int64_t blocks = (V + 255) / 256;
+      if (blocks > (int64_t)sms * 16) blocks = (int64_t)sms * 16;
+      if (blocks < 1) blocks = 1;
+      JSCC_TIMED("sc_reduce_scatter", st,
+                 sc_reduce_scatter_kernel<<<(unsigned)blocks, 256, 0, st>>>(fs_part, p.ldx, (int)p.fs_clusters, 1, 1,
+                                                                            nullptr, ld_rot, r0, V, has_scale, scale,
+                                                                            weight));
+      JSCC_LAUNCH_CHECK();
+      return JSCC_OK;
+    }
+  }
   // forward: balanced contiguous split over warps, then fixed-order row finish
   if (stage == 2) {
     int64_t blocks = (n_bins * RB + 255) / 256;
@@ -707,7 +766,8 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
                            const int64_t* rotinv, int64_t ld_rot, int use_floor, float floor_v, int has_scale,
                            float scale, float* weight, const ScPlan& p, float* xr, float* ratio,
                            float* part, float* fpart, cudaStream_t st, int stage = 0, float* fout = nullptr,
-                           int64_t ld_fout = 0, const float* gin = nullptr, int64_t ld_gin = 0) {
+                           int64_t ld_fout = 0, const float* gin = nullptr, int64_t ld_gin = 0,
+                           float* fs_part = nullptr) {
   const int sms = num_sms();
   for (int r0 = 0; r0 < n_rot; r0 += p.rb) {
     const int nr = (n_rot - r0) < p.rb ? (n_rot - r0) : p.rb;
@@ -731,7 +791,7 @@ static int sc_weight_typed(const T* A, int64_t lda, const int64_t* row_idx, int6
       case 1:
         rc = launch_sc_block<T, 1>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
                                    use_floor, floor_v, has_scale, scale, weight, p, xr, ratio, part,
-                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin);
+                                   fpart, direct, st, stage, fout, ld_fout, gin, ld_gin, fs_part);
         break;
       case 2:
         rc = launch_sc_block<T, 2>(A, lda, row_idx, n_bins, V, proj, ld_proj, ld_rot, r0, nr, rotinv,
@@ -892,7 +952,8 @@ int jscc_sc_sensitivity(const void* A, int32_t a_dtype, int64_t lda, const int64
 }
 
 size_t jscc_sc_weight_workspace_bytes(int64_t n_bins, int64_t n_vox, int32_t n_rot) {
-  return plan_sc(n_bins, n_vox, n_rot).ws_bytes;
+  const ScPlan p = plan_sc(n_bins, n_vox, n_rot);
+  return p.ws_bytes + p.fs_bytes;
 }
 
 int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* row_idx,
@@ -923,17 +984,20 @@ int jscc_sc_weight(const void* A, int32_t a_dtype, int64_t lda, const int64_t* r
   float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
   float* fpart = cv.take<float>((size_t)p.fwd_warps * p.fwd_maxp * p.rb);
   JSCC_REQUIRE(cv.ok(), "jscc_sc_weight: workspace carve overflow");
+  float* fs_part = fused_partials(p, cv);
   const int has_scale = scale != 1.0f;
   cudaStream_t st = as_stream(stream);
   if (a_dtype == JSCC_DTYPE_F32)
     return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, proj,
                                   ld_proj,
                                   n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor, floor_v, has_scale,
-                                  scale, weight, p, xr, ratio, part, fpart, st);
+                                  scale, weight, p, xr, ratio, part, fpart, st, 0, nullptr, 0, nullptr, 0,
+                                  fs_part);
   return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins,
                                         n_vox,
                                         proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
-                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st);
+                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st, 0, nullptr,
+                                        0, nullptr, 0, fs_part);
 }
 
 // The two halves of jscc_sc_weight on their own (the differentiable projector's forward and
@@ -1151,13 +1215,15 @@ extern "C" int jscc_sc_weight_noalloc(const void* A, int32_t a_dtype, int64_t ld
   float* part = cv.take<float>((size_t)p.chunks * p.rb * p.ldx);
   float* fpart = cv.take<float>((size_t)p.fwd_warps * p.fwd_maxp * p.rb);
   JSCC_REQUIRE(cv.ok(), "jscc_sc_weight_noalloc: scratch carve overflow");
+  float* fs_part = fused_partials(p, cv);
   const int has_scale = scale != 1.0f;
   cudaStream_t st = as_stream(stream);
   if (a_dtype == JSCC_DTYPE_F32)
     return sc_weight_typed<float>(static_cast<const float*>(A), lda, row_idx, n_bins, n_vox, proj, ld_proj,
                                   n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor, floor_v, has_scale, scale,
-                                  weight, p, xr, ratio, part, fpart, st);
+                                  weight, p, xr, ratio, part, fpart, st, 0, nullptr, 0, nullptr, 0, fs_part);
   return sc_weight_typed<__nv_bfloat16>(static_cast<const __nv_bfloat16*>(A), lda, row_idx, n_bins, n_vox,
                                         proj, ld_proj, n_rot, img, rotmat, rotmat_inv, ld_rot, use_floor,
-                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st);
+                                        floor_v, has_scale, scale, weight, p, xr, ratio, part, fpart, st, 0, nullptr,
+                                        0, nullptr, 0, fs_part);
 }

@@ -702,36 +702,6 @@ __device__ unsigned int g_wait_timeout_count = 0;
 // give-up path while every copy still completes. The drains keep their own fixed bound.
 __device__ uint32_t g_bk_poll_limit = kBkMaxPolls;
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-// named barrier `id` over `count` threads (the warps of one role)
-__device__ __forceinline__ void role_sync(int id, int count) {
-  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
-
-// named barrier returning the OR of every participant's `v` (the same value in all of them,
-// so a decision taken on it is uniform within the role)
-__device__ __forceinline__ bool role_sync_or(int id, int count, bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(r)
-      : "r"((uint32_t)v), "r"(id), "r"(count)
-      : "memory");
-  return r != 0;
-}
-
-// bounded wait that also gives up once another thread has flagged an abort
-__device__ __forceinline__ bool bk_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, uint32_t polls) {
-  for (uint32_t i = 0; i < polls; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 31u) == 31u && *abort_flag) return false;
-  }
-  return false;
-}
-
 // eight consecutive sysmat-row values from shared memory starting at p (p 8-byte aligned for
 // BF16, 16-byte aligned for float)
 __device__ __forceinline__ void smem8(const __nv_bfloat16* p, float (&v)[8]) {
@@ -2484,16 +2454,19 @@ int set_bulk_poll_limit(uint32_t polls, bool reset) {
   JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_bk_poll_limit, &v, sizeof(v)));
   return JSCC_OK;
 }
+int take_sc_timeout_count(unsigned int* out);  // sc_projector.cu
 }  // namespace jscc
 
 extern "C" {
 
 int jscc_take_wait_timeout_count(unsigned int* out) {
   JSCC_REQUIRE(out, "jscc_take_wait_timeout_count: null pointer argument");
-  unsigned int h = 0, zero = 0;
+  unsigned int h = 0, zero = 0, hs = 0;
   JSCC_CUDA_CHECK(cudaMemcpyFromSymbol(&h, g_wait_timeout_count, sizeof(h)));
   JSCC_CUDA_CHECK(cudaMemcpyToSymbol(g_wait_timeout_count, &zero, sizeof(zero)));
-  *out = h;
+  const int rc = jscc::take_sc_timeout_count(&hs);  // the fused SC kernel's give-ups
+  if (rc != JSCC_OK) return rc;
+  *out = h + hs;
   return JSCC_OK;
 }
 
