@@ -174,7 +174,8 @@ class Sc3Workload:
     def kernel_bytes(self, dtype):
         b = 2 if dtype == "bf16" else 4
         rows = self.B / self.subsets
-        return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4}
+        return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4,
+                "sc_fused": rows * self.V * b + self.V * 4 + rows * 4}
 
     def config(self):
         return {"workload": self.name, "bins": self.B, "voxels": self.V, "subsets": self.subsets,

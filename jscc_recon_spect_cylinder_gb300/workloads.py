@@ -190,9 +190,13 @@ class JointWorkload:
         return 2 * self.n_events * self.V
 
     def sc_kernel_bytes(self, dtype):
+        """Algorithmic bytes of one subset's SC launches: the two-pass forward (rows + image)
+        and back (rows + ratios), or the fused single-read kernel (rows once + image +
+        projections)."""
         b = 2 if dtype == "bf16" else 4
         rows = self.B / self.subsets
-        return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4}
+        return {"sc_forward_split": rows * self.V * b + self.V * 4, "sc_back_partial": rows * self.V * b + rows * 4,
+                "sc_fused": rows * self.V * b + self.V * 4 + rows * 4}
 
     def sparse_kernel_bytes(self, dtype):
         """Algorithmic bytes of one launch of the grouped sparse kernels (one subset, the
