@@ -939,12 +939,14 @@ class JointBench:
 
     storage = "bf16 system matrix + bf16 sparse rows (int32 ids split out); fp32 arm: fp32 matrix + fp32 sparse rows (the same split layout and kernels)"
 
-    def __init__(self, dev, small=False):
+    def __init__(self, dev, small=False, radial_stride=1):
         from jscc_recon_spect_cylinder_gb300 import workloads
 
         kw = dict(views=2, n_events=60000, subsets=2) if small else {}
-        self.w = workloads.JointWorkload(dev, **kw)
+        self.w = workloads.JointWorkload(dev, radial_stride=radial_stride, **kw)
         self.name = "jsccsd-config3" if not small else "jsccsd-small"
+        if radial_stride > 1:
+            self.name += f"-radial{radial_stride}"
         self.metric = JOINT_METRIC
         self.traffic_file = "traffic_jsccsd3.json"
         self.dev = dev
@@ -1123,6 +1125,8 @@ def make_workload(name, dev):
         return JointBench(dev)
     if name == "jsccsd-small":
         return JointBench(dev, small=True)
+    if name == "jsccsd3-radial":  # the Compton T on the radially coarsened 25 x 90 grid (an extension)
+        return JointBench(dev, radial_stride=4)
     if name == "sparse-launch":
         return SparseLaunchBench(dev)
     if name == "cone2":
@@ -1335,7 +1339,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "sc3", "sc3-small", "sparse-launch", "cone2", "map5", "batch4",
+    ap.add_argument("--workload", choices=["jsccsd3", "jsccsd-small", "jsccsd3-radial", "sc3", "sc3-small", "sparse-launch", "cone2", "map5", "batch4",
                              "batch4-small", "batch4-joint"],
                     default="jsccsd3")
     ap.add_argument("--no-cpu-baseline", action="store_true")

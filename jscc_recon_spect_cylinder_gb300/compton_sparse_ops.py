@@ -220,6 +220,65 @@ def build_compton_sparse_projector(coor_full, theta_stride=2, z_stride=2, rotate
                                   layer_reduce, z_reduce, layer_expand, z_expand, coor_coarse)
 
 
+@dataclass
+class RadialComptonSparseProjector(ComptonSparseProjector):
+    """A projector that also coarsens the rings of each z plane (an extension: the
+    reference's builder coarsens theta and z only). The separable pair keeps the reference's
+    fields with the (z plane, ring) index in the z slot and one ring's theta in the layer
+    slot, so every operator of this module and every kernel take it unchanged:
+    fine_layer_num is the ring length, fine_z_num the planes x rings (coarse likewise)."""
+
+    radial_stride: int = 1
+    ring_num: int = 0
+
+    def to(self, device):
+        base = ComptonSparseProjector.to(self, device)
+        out = RadialComptonSparseProjector(**{f: getattr(base, f) for f in base.__dataclass_fields__},
+                                           radial_stride=self.radial_stride, ring_num=self.ring_num)
+        if getattr(base, "_jscc_tables", None):
+            out._jscc_tables = base._jscc_tables
+        return out
+
+
+def build_compton_sparse_projector_radial(coor_full, radial_stride=4, theta_stride=4, dtype=torch.float32):
+    """Radially and angularly coarsened projector of a polar grid whose rings all have one
+    length L (e.g. 100 x 360 -> 25 x 90 with strides 4 and 4): each z plane's rings are
+    coarsened by `radial_stride` with the reference's linear reduce / expand along the ring
+    index (its z convention: samples at (c + 1/2) s - 1/2, two-tap interpolation between
+    them, clamped at the ends), each ring's theta by `theta_stride` with its periodic maps.
+    The coarse coordinates: radius = the linear reduce of the ring radii, angle
+    th_c * s_theta * 2 pi / L, the plane's z. With radial_stride 1 the upsample and the
+    coarse coordinates equal build_compton_sparse_projector(..., theta_stride, z_stride=1)'s."""
+    if radial_stride <= 0 or theta_stride <= 0:
+        raise ValueError("radial_stride and theta_stride must be positive.")
+    layout = _infer_polar_layout(coor_full)
+    lengths = layout["ring_lengths"]
+    L = lengths[0]
+    if any(n != L for n in lengths):
+        raise ValueError("radial coarsening needs rings of one length.")
+    n_rings, nz = len(lengths), layout["fine_z_num"]
+    if n_rings % radial_stride != 0:
+        raise ValueError(f"ring count {n_rings} is not divisible by radial_stride={radial_stride}.")
+    ring_reduce = _build_linear_reduce_matrix(n_rings, radial_stride, dtype)
+    ring_expand = _build_linear_expand_matrix(n_rings, radial_stride, dtype)
+    planes = torch.eye(nz, dtype=dtype)
+    z_reduce = torch.kron(planes, ring_reduce)
+    z_expand = torch.kron(planes, ring_expand)
+    layer_reduce = _build_periodic_reduce_matrix(L, theta_stride, dtype)
+    layer_expand = _build_periodic_expand_matrix(L, theta_stride, dtype)
+    n_thc = L // theta_stride
+    radii = torch.matmul(ring_reduce.double(), layout["ring_radii"].double()).to(dtype)
+    ang = torch.arange(n_thc, dtype=dtype) * theta_stride * (2.0 * math.pi / L)
+    plane = torch.cat([torch.stack((r * torch.cos(ang), r * torch.sin(ang)), dim=1) for r in radii], dim=0)
+    z_values = layout["z_values"].to(dtype=dtype)
+    coor_coarse = torch.cat([torch.cat((plane, torch.full((plane.size(0), 1), z.item(), dtype=dtype)), dim=1)
+                             for z in z_values], dim=0)
+    n_rc = n_rings // radial_stride
+    return RadialComptonSparseProjector(theta_stride, 1, (theta_stride,) * n_rings, L, nz * n_rings, n_thc, nz * n_rc,
+                                        nz * n_rings * L, nz * n_rc * n_thc, layer_reduce, z_reduce, layer_expand,
+                                        z_expand, coor_coarse, radial_stride=radial_stride, ring_num=n_rings)
+
+
 # ----------------------------------------------------------------------------- operators (GPU)
 def _tables_for(t, projector):
     return tables(projector, t.device)

@@ -26,13 +26,21 @@ N_PHI, N_AXIAL, AXIAL_PITCH = 128, 32, 2.0
 
 
 def _upsample_sparse(tables, device):
-    """The fine <- coarse upsample of a one-plane projector as a float64 torch sparse
-    matrix [V_f, V_c] (z maps are the identity for one plane)."""
-    ptr, idx, w = (t.cpu() for t in tables.up[1])
-    if tables.n_zf != 1:
-        raise ValueError("the float64 reference supports one-plane grids")
-    rows = torch.repeat_interleave(torch.arange(ptr.numel() - 1), (ptr[1:] - ptr[:-1]).long())
-    U = torch.sparse_coo_tensor(torch.stack((rows, idx.long())), w.double(), (tables.n_lf, tables.n_lc))
+    """The fine <- coarse upsample U = Z (x) L of a projector's separable pair (the z map
+    and the layer map, CSR on the host) as a float64 torch sparse matrix [V_f, V_c]:
+    U[zf * n_lf + lf, zc * n_lc + lc] = Z[zf, zc] * L[lf, lc]."""
+    def coo(csr):
+        ptr, idx, w = (t.cpu() for t in csr)
+        rows = torch.repeat_interleave(torch.arange(ptr.numel() - 1), (ptr[1:] - ptr[:-1]).long())
+        return rows, idx.long(), w.double()
+
+    zr, zc, zw = coo(tables.up[0])
+    lr, lc, lw = coo(tables.up[1])
+    rows = (zr[:, None] * tables.n_lf + lr[None, :]).reshape(-1)
+    cols = (zc[:, None] * tables.n_lc + lc[None, :]).reshape(-1)
+    vals = (zw[:, None] * lw[None, :]).reshape(-1)
+    U = torch.sparse_coo_tensor(torch.stack((rows, cols)), vals,
+                                (tables.n_zf * tables.n_lf, tables.n_zc * tables.n_lc))
     return U.coalesce().to(device)
 
 
@@ -42,7 +50,7 @@ SCAT_R, ABS_R = 120.0, 150.0
 class JointWorkload:
     def __init__(self, device, views=20, n_events=1_000_000, subsets=8, alpha=0.5, theta_stride=4, e0=0.662,
                  res_662=0.08, delta_r=1.0, n_r=100, n_theta=360, radius=100.0, sc_counts=1e7, seed=synthetic.SEED,
-                 with_fp32=True, sort_events=True):
+                 with_fp32=True, sort_events=True, radial_stride=1):
         self.dev = device
         self.subsets = subsets
         self.alpha = alpha
@@ -93,8 +101,11 @@ class JointWorkload:
         for k, col in ((0, 1), (1, 3)):
             e = lst[:, col]
             lst[:, col] = e + (e * res / 2.355 * (e0 / e) ** 0.5) * noise[:, k]
-        self.projector = cso.build_compton_sparse_projector(grid.coor.cpu(), theta_stride=theta_stride, z_stride=1,
-                                                            rotate_num=1)
+        if radial_stride > 1:  # the radially coarsened extension (e.g. 25 x 90 for strides 4 x 4)
+            self.projector = cso.build_compton_sparse_projector_radial(grid.coor.cpu(), radial_stride, theta_stride)
+        else:
+            self.projector = cso.build_compton_sparse_projector(grid.coor.cpu(), theta_stride=theta_stride, z_stride=1,
+                                                                rotate_num=1)
         self.tables = cso.tables(self.projector, device)
         thr_max = 2 * e0 ** 2 / (0.511 + 2 * e0) - 0.001
         rows = build_sparse_rows_from_smeared(A, self.detector, self.projector, lst, delta_r, delta_r, e0, res,

@@ -197,6 +197,40 @@ def build_projector(coor_full, theta_stride=2, z_stride=2, rotate_num=None):
                      layer.shape[0] * zc.size, lr, zr, le, ze, coor)
 
 
+def build_radial_projector(coor_full, radial_stride=4, theta_stride=4):
+    """Radially coarsened projector (an extension: the reference's builder coarsens theta and
+    z only, compton_sparse_ops.py:212-290). Every ring of the grid has the same length L; the
+    rings of each z plane are coarsened by `radial_stride` with the reference's linear
+    reduce / expand along the ring index (its z convention, :109-129 / :157-185: samples at
+    the centres (c + 1/2) s - 1/2, two-tap interpolation between centres, clamped at the
+    ends) and each ring's theta by `theta_stride` with its periodic maps (:95-106 /
+    :132-154). Stored as the reference's separable pair with the (z plane, ring) index in the
+    z slot and theta in the layer slot: the fine index z * n_rings * L + r * L + th is the
+    reference's ring-major layout. Coarse coordinates: radius = the linear reduce of the ring
+    radii, angle th_c * s_theta * 2 pi / L, the plane's z."""
+    if radial_stride <= 0 or theta_stride <= 0:
+        raise ValueError("radial_stride and theta_stride must be positive.")
+    z_vals, nz, nl, lengths, ring_r = infer_polar_layout(coor_full)
+    L = lengths[0]
+    if any(n != L for n in lengths):
+        raise ValueError("radial coarsening needs rings of one length.")
+    nr = len(lengths)
+    if nr % radial_stride:
+        raise ValueError(f"ring count {nr} is not divisible by radial_stride={radial_stride}.")
+    th_r, th_e = periodic_reduce(L, theta_stride), periodic_expand(L, theta_stride)
+    r_r, r_e = linear_reduce(nr, radial_stride), linear_expand(nr, radial_stride)
+    eye = np.eye(nz, dtype=np.float32)
+    zr, ze = np.kron(eye, r_r).astype(np.float32), np.kron(eye, r_e).astype(np.float32)
+    nrc, nthc = nr // radial_stride, L // theta_stride
+    rad = (r_r.astype(np.float64) @ np.asarray(ring_r, dtype=np.float64)).astype(np.float32)
+    th = (np.arange(nthc, dtype=np.float32) * np.float32(theta_stride)) * np.float32(2.0 * math.pi / L)
+    plane = np.concatenate([np.stack((R * np.cos(th), R * np.sin(th)), axis=1) for R in rad], axis=0)
+    coor = np.concatenate([np.concatenate((plane, np.full((plane.shape[0], 1), z, np.float32)), axis=1)
+                           for z in z_vals.astype(np.float32)], axis=0).astype(np.float32)
+    return Projector(theta_stride, 1, (theta_stride,) * nr, L, nz * nr, nthc, nz * nrc, nz * nr * L,
+                     nz * nrc * nthc, th_r, zr, th_e, ze, coor)
+
+
 def _rows3(rows, nz, nl):
     return np.asarray(rows).reshape(rows.shape[0], nz, nl)
 
