@@ -1055,6 +1055,11 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       for (int u = 0; u < kBkQ; ++u) {
         const int c = et * 4 + u * (kBkEvents * 4);
         bv[u] = c < vc ? *reinterpret_cast<const float4*>(b + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < vc && c + 4 > vc) {  // a coarse grid that is not a multiple of four: the tail is padding
+          if (c + 1 >= vc) bv[u].y = 0.f;
+          if (c + 2 >= vc) bv[u].z = 0.f;
+          bv[u].w = 0.f;
+        }
         qa[u] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
       __syncwarp();
@@ -1091,6 +1096,11 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
             for (int k = 0; k < NE; ++k) {
               float v[4];
               smem4(slot(sl[k]), c, v);
+              if (c + 4 > vc) {  // padding past the row (any value) must not reach the dot
+#pragma unroll
+                for (int e = 1; e < 4; ++e)
+                  if (c + e >= vc) v[e] = 0.f;
+              }
               ffma4(acc[k], v, bv[u]);
             }
           }
@@ -1365,9 +1375,16 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
       rb[v] = in && b != a ? (l0[v] == b ? w0[v] : 0.f) + (l1[v] == b ? w1[v] : 0.f) : 0.f;
     }
   }
-  const bool staged = seg_len <= kScSeg;
+  // the q segment of z tap t starts at the flat coarse index z_t n_lc + cs0, copied from the
+  // 16-byte boundary below it (sh_t values earlier) and clamped to the q row
+  const int64_t f0 = (int64_t)z0 * n_lc + cs0, f1 = (int64_t)z1 * n_lc + cs0;
+  const int sh0 = (int)(f0 & 3), sh1 = (int)(f1 & 3);
+  const int seg_slot = (seg_len + 3 + 3) & ~3;  // a segment and its shift, in whole 16-byte units
+  const bool staged = seg_slot <= kScSeg;
   const uint32_t a_bytes = (uint32_t)((l_end - l_begin) * sizeof(TE));
-  const uint32_t seg_bytes = (uint32_t)seg_len * 4u;
+  const uint32_t seg_bytes = (uint32_t)seg_slot * 4u;
+  const uint32_t cp0 = (uint32_t)min((int64_t)seg_slot, ldq - (f0 - sh0)) * 4u;
+  const uint32_t cp1 = (uint32_t)min((int64_t)seg_slot, ldq - (f1 - sh1)) * 4u;
   // stages sized to this tile's segment: the sysmat tile (seg_off bytes) and one q segment per
   // z tap, as many as the shared memory holds
   const uint32_t stage_bytes = (seg_off + seg_bytes * (two_z ? 2u : 1u) + 127u) & ~127u;
@@ -1395,10 +1412,10 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
             if (ok) {
               unsigned char* st = stage(s);
               const float* qg = q + (int64_t)(w + k) * ldq;
-              mbar_arrive_expect_tx(full + s, a_bytes + seg_bytes * (two_z ? 2u : 1u));
+              mbar_arrive_expect_tx(full + s, a_bytes + cp0 + (two_z ? cp1 : 0u));
               bulk_copy_g2s(st, eff + clamp_row(row, n_det) * ld_eff + j0, a_bytes, full + s);
-              bulk_copy_g2s(st + seg_off, qg + (int64_t)z0 * n_lc + cs0, seg_bytes, full + s);
-              if (two_z) bulk_copy_g2s(st + seg_off + seg_bytes, qg + (int64_t)z1 * n_lc + cs0, seg_bytes, full + s);
+              bulk_copy_g2s(st + seg_off, qg + (f0 - sh0), cp0, full + s);
+              if (two_z) bulk_copy_g2s(st + seg_off + seg_bytes, qg + (f1 - sh1), cp1, full + s);
               *issued = kk + 1;
             }
           }
@@ -1485,8 +1502,8 @@ sparse_group_scatter_bulk_kernel(const float* __restrict__ q, int64_t ldq, const
           const TE* at = reinterpret_cast<const TE*>(st) + (lf0 - l_begin);
           float a[kScVox];
           load4x2(at, a);
-          accumulate(a, reinterpret_cast<const float*>(st + seg_off) - cs0,
-                     reinterpret_cast<const float*>(st + seg_off + seg_bytes) - cs0);
+          accumulate(a, reinterpret_cast<const float*>(st + seg_off) - cs0 + sh0,
+                     reinterpret_cast<const float*>(st + seg_off + seg_bytes) - cs0 + sh1);
         }
         __syncwarp();
         if (lane == 0) {
@@ -1856,7 +1873,10 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   // bulk-copy pipeline when every row start and length is 16-byte aligned (split storage),
   // b and q fit the event threads' registers and b plus at least two coarse rows fit in
   // shared memory
-  const uint32_t row_bytes = (uint32_t)((size_t)vc * sizeof(TC)), b_bytes = (uint32_t)((size_t)vc * 4);
+  // rows and b_g move in whole 16-byte units: a row's storage (its leading dimension) must
+  // cover the rounded-up length; the kernel masks the values past vc
+  const uint32_t row_bytes = (uint32_t)align_up((size_t)vc * sizeof(TC), 16);
+  const uint32_t b_bytes = (uint32_t)align_up((size_t)vc * 4, 16);
   const uint32_t slot_off = (uint32_t)align_up(kBkHeader + align_up(b_bytes, 128), 128);
   const uint32_t slot_stride = (uint32_t)align_up(row_bytes, 128);
   const size_t bk_limit = 227 * 1024;
@@ -1870,7 +1890,7 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   while (batch * 2 <= kBkMaxBatch && batch * 2 <= n_slots / 2) batch *= 2;
   const bool bulk = rows.packed == nullptr && n_slots >= 2 && vc <= kBkMaxCoarse &&
                     reinterpret_cast<uintptr_t>(rows.tc) % 16 == 0 && (rows.ld * sizeof(TC)) % 16 == 0 &&
-                    row_bytes % 16 == 0 && reinterpret_cast<uintptr_t>(eff) % 16 == 0 &&
+                    (size_t)rows.ld * sizeof(TC) >= row_bytes && reinterpret_cast<uintptr_t>(eff) % 16 == 0 &&
                     (ld_eff * sizeof(TE)) % 16 == 0 && ((size_t)vf * sizeof(TE)) % 16 == 0 && ldq % 4 == 0;
   const size_t bk_smem = (size_t)slot_off + (size_t)n_slots * slot_stride;
   int64_t bk_grid = num_sms();
@@ -2133,14 +2153,15 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   const size_t sc_smem = 110u * 1024u;
   const uint32_t sc_space = (uint32_t)(sc_smem - kScHeader);
   const bool sc_bulk = sc_space >= 2 * sc_stage && reinterpret_cast<uintptr_t>(eff) % 16 == 0 && (ld_eff * sizeof(TE)) % 16 == 0 &&
-                       ((size_t)taps.n_lf * sizeof(TE)) % 16 == 0 && taps.n_lf % kScVox == 0 && taps.n_lc % 4 == 0 &&
+                       ((size_t)taps.n_lf * sizeof(TE)) % 16 == 0 && taps.n_lf % kScVox == 0 &&
+                       taps.n_lf >= kScTile / 2 &&  // tiles never span z planes: short planes idle them
                        reinterpret_cast<uintptr_t>(q) % 16 == 0 && ldq % 4 == 0;
   int64_t n_part = chunks;
   float* part_out = part;
   // the stride-4 ring stencil's scatter: sixteen voxels per thread (the kernel checks that every
   // run of four interpolates between two coarse voxels and reads the taps itself otherwise)
   const uint32_t sp_a = (uint32_t)align_up((size_t)kSpTile * sizeof(TE), 128);
-  const bool sc_pair = sc_bulk && ring_stride == 4 && ring_len >= 8 && ring_len % 4 == 0 &&
+  const bool sc_pair = sc_bulk && taps.n_lc % 4 == 0 && ring_stride == 4 && ring_len >= 8 && ring_len % 4 == 0 &&
                        taps.n_lf % ring_len == 0 && taps.n_lc * 4 == taps.n_lf &&
                        sc_space >= 2 * (sp_a + (n_zc > 1 ? 2u : 1u) * kSpSeg * 4u);
   if (sc_pair) {

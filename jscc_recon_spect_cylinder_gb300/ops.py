@@ -870,9 +870,19 @@ def sparse_weight(rows, sysmat, tables: SparseTables, img, grouped=False, rotmat
 
 
 def split_sparse_rows(rows, dtype=torch.bfloat16):
-    """Packed rows [E, 1 + V_c] -> (row_id int32 0-based, coarse rows [E, V_c] of ``dtype``)."""
+    """Packed rows [E, 1 + V_c] -> (row_id int32 0-based, coarse rows [E, V_c] of ``dtype``).
+    The coarse rows are a view of a buffer whose leading dimension is a whole number of
+    16-byte units (zero padding past V_c), so the bulk-copy kernels move whole rows for any
+    coarse grid."""
     ids = (sparse_unpack_ids(rows) - 1).to(torch.int32)
-    return ids, rows[:, 1:].to(dtype).contiguous()
+    vc = rows.size(1) - 1
+    per16 = 16 // torch.empty((), dtype=dtype).element_size()
+    ld = (vc + per16 - 1) // per16 * per16
+    if ld == vc:
+        return ids, rows[:, 1:].to(dtype).contiguous()
+    buf = torch.zeros((rows.size(0), ld), dtype=dtype, device=rows.device)
+    buf[:, :vc] = rows[:, 1:]
+    return ids, buf[:, :vc]
 
 
 def sparse_weight_split(row_id, t_coarse, sysmat, tables: SparseTables, img, grouped=False, rotmat=None,

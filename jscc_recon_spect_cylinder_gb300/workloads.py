@@ -125,7 +125,7 @@ class JointWorkload:
         split = [ops.split_sparse_rows(p, torch.bfloat16) for p in parts]
         self.ids = [s[0] for s in split]
         self.tc_bf16 = [s[1] for s in split]
-        self.tc_f32 = [p[:, 1:].contiguous() for p in parts] if with_fp32 else None
+        self.tc_f32 = [ops.split_sparse_rows(p, torch.float32)[1] for p in parts] if with_fp32 else None
         del rows, parts
         # ---------------- sensitivities: s (SC column sums), d (Compton, build_sparse_sensi_d
         # rescaling: sum(d) = sum(s) * E_C / E_S), joint s_j = alpha s + (2 - alpha) d

@@ -5,7 +5,8 @@ tests/test_radial_projector.py): on the golden sparse problem's grid (4 planes o
 24 theta) coarsened by 2 radially and 4 in theta, the sparse T builder's rows, the four
 separable operators and both weight semantics against the FP64 oracle; on a 16-ring x
 96-theta grid coarsened 4 x 4, the bulk split-row path (BF16 and float32 rows) against the
-oracle and against the per-event kernel."""
+oracle and against the per-event kernel; and the bulk kernels on coarse grids that are not
+16-byte multiples (padded rows, shifted q segments)."""
 from __future__ import annotations
 
 import numpy as np
@@ -80,3 +81,37 @@ def test_radial_bulk_split_rows(cuda, dtype):
     assert rel_l2(bulk.cpu(), want) < TOL_W
     assert rel_l2(event.cpu(), want) < TOL_W
     assert rel_l2(bulk.cpu(), event.cpu()) < TOL_W
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float32])
+def test_bulk_paths_on_unaligned_coarse_grids(cuda, dtype):
+    """Six planes of 3 rings x 360 theta coarsened 4 in theta and 2 in z: 810 coarse voxels
+    (coarse rows that are not a whole number of 16-byte units: padded split storage, masked
+    row tails in the coefficient kernel) and 270 coarse voxels per plane (q segments that start
+    off a 16-byte boundary: copied from the boundary below in the bulk scatter, two z taps).
+    The bulk kernels match the per-event kernel, both semantics, and no wait gives up."""
+    from jscc_recon_spect_cylinder_gb300 import _lib, ops, synthetic
+    from jscc_recon_spect_cylinder_gb300 import compton_sparse_ops as cso
+
+    plane = synthetic.polar_grid(3, 360, 30.0).coor
+    coor = torch.cat([torch.cat((plane[:, :2], torch.full((plane.size(0), 1), 2.0 * k)), dim=1) for k in range(6)])
+    p = cso.build_compton_sparse_projector(coor, 4, 2, rotate_num=1)
+    tb = cso.tables(p, cuda)
+    vc, n_lc = p.coarse_pixel_num, p.coarse_layer_num
+    assert vc % 4 != 0 and n_lc % 4 != 0 and p.fine_layer_num >= 1024
+    g = torch.Generator().manual_seed(31)
+    n_det, n = 250, 2200
+    V = p.fine_pixel_num
+    A = (torch.rand((n_det, V), generator=g) + 0.05).to(dtype).to(cuda)
+    cp1 = torch.randint(1, n_det + 1, (n,), generator=g)
+    rows = torch.cat((cp1.float().unsqueeze(1), torch.rand((n, vc), generator=g) ** 3), dim=1).to(cuda)
+    ids, tcd = ops.split_sparse_rows(rows, dtype)
+    assert tcd.stride(0) * tcd.element_size() % 16 == 0 and tcd.stride(0) > vc  # padded
+    x = (torch.rand((V, 1), generator=g) + 0.2).to(cuda)
+    _lib.take_wait_timeout_count()
+    for grouped in (False, True):
+        a = ops.sparse_weight_split(ids, tcd, A, tb, x, grouped=grouped, method="event")
+        b = ops.sparse_weight_split(ids, tcd, A, tb, x, grouped=grouped)
+        torch.cuda.synchronize()
+        assert rel_l2(b.cpu(), a.cpu()) < TOL_W
+    assert _lib.take_wait_timeout_count() == 0
