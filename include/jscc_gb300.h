@@ -418,10 +418,13 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * and only read when have_sums != 0 (S_i depends on the rows, the sysmat and the grouping
  * only, so callers keep it across iterations with the same `order`). The coarse grid must fit in
  * shared memory (V_c floats <= 227 KB). Deterministic (fixed-order reductions).
- * With split rows whose starts and lengths are 16-byte aligned (and a 16-byte aligned
- * sysmat row pitch) the per-group step streams the sysmat row and the coarse rows into
- * shared memory with bulk copies; its waits are bounded and a wait that gives up is
- * counted (jscc_take_wait_timeout_count), the weight of that call then being invalid.
+ * With split rows whose starts are 16-byte aligned and whose pitch (ld_tc) covers the row
+ * rounded up to a whole number of 16-byte units (the values past V_c may be anything), and a
+ * 16-byte aligned sysmat row pitch, the weight runs as three bulk-copy pipelines: the group
+ * adjoints b_g (sysmat row segments streamed into shared memory), the event coefficients and
+ * q_g (b_g and the coarse rows streamed in), and the scatter (sysmat tiles and q segments
+ * streamed in); their waits are bounded and a wait that gives up is counted
+ * (jscc_take_wait_timeout_count), the weight of that call then being invalid.
  * ring_len / ring_stride (0 / 0: no claim) state that the adjoint table is a stride-4 ring
  * stencil: z the identity, each fine plane made of rings of ring_len theta voxels, coarse
  * voxel lc = r * (ring_len / 4) + th with taps r * ring_len + (4 th + d) mod ring_len,
@@ -433,7 +436,7 @@ JSCC_API int jscc_sparse_weight_split(const int32_t* row_id, const void* t_coars
  * GROUPED, or MATERIALIZE with have_sums) runs as one kernel on clusters of four CTAs that
  * split the rings: each event row and each group's sysmat row is read from HBM once and the
  * per-group coarse sums stay on chip (the per-event sums of MATERIALIZE are computed
- * beforehand by the two-kernel pipeline when have_sums == 0).
+ * beforehand by the separate kernels when have_sums == 0).
  */
 /*
  * Number of bounded device waits that gave up since the last call (then reset to 0).
@@ -444,15 +447,16 @@ JSCC_API int jscc_take_wait_timeout_count(unsigned int* out);
 
 /*
  * Whether jscc_sparse_weight_grouped uses the fused cluster kernel where it applies
- * (enable != 0) or the two-kernel pipeline (coefficients, then the scatter; the default, as it
- * is the faster of the two on GB300 at the joint configuration's sizes). Process-wide. No
+ * (enable != 0) or the separate kernels (adjoints, coefficients, scatter; the default, as they
+ * are the faster form on GB300 at the joint configuration's sizes). Process-wide. No
  * counterpart in the reference.
  */
 JSCC_API int jscc_set_fused_cluster(int32_t enable);
 
 /*
  * Poll bound of every bounded pipeline wait on the current device: the bulk sparse kernels
- * (jscc_sparse_weight_grouped) and the tensor-core GEMM (jscc_bf16_gemm_nt). polls < 0
+ * (jscc_sparse_weight_grouped), the fused single-read SC kernel (jscc_sc_weight,
+ * jscc_sc_weight_noalloc) and the tensor-core GEMM (jscc_bf16_gemm_nt). polls < 0
  * restores the default (2^22 polls per wait); 0 makes each such wait give up at once. A CTA
  * that gives up still waits, with a fixed bound of its own, for the copies and MMAs it has
  * in flight, frees its tensor memory and is counted (jscc_take_wait_timeout_count,

@@ -290,7 +290,7 @@ timeout_epoch = 0
 
 def set_fused_cluster(enable: bool) -> None:
     """Let the grouped sparse weight use its fused cluster kernel where it applies, or (the
-    default) the two-kernel pipeline."""
+    default) the separate adjoint, coefficient and scatter kernels."""
     check(load().jscc_set_fused_cluster(1 if enable else 0), "jscc_set_fused_cluster")
 
 

@@ -6,7 +6,7 @@
 //   b_g = adj(A_g . x)          f_i = t_i . b_g          c_i = coefficient of f_i
 //   q_g = sum_i c_i t_i         w  += A_g . up(q_g)
 // Each byte of the event rows and of the group's sysmat row is read from HBM once, and q never
-// leaves the chip (the two-kernel form writes q and reads every sysmat row a second time).
+// leaves the chip (the separate kernels write b and q and read every sysmat row a second time).
 //
 // Data split: a cluster of kCfCluster CTAs (one per SM) works on the same groups; CTA r owns
 // the rings [R0, R1) of the polar grid (one z plane, the stride-4 ring stencil: coarse voxel

@@ -702,18 +702,6 @@ __device__ unsigned int g_wait_timeout_count = 0;
 // give-up path while every copy still completes. The drains keep their own fixed bound.
 __device__ uint32_t g_bk_poll_limit = kBkMaxPolls;
 
-// eight consecutive sysmat-row values from shared memory starting at p (p 8-byte aligned for
-// BF16, 16-byte aligned for float)
-__device__ __forceinline__ void smem8(const __nv_bfloat16* p, float (&v)[8]) {
-  const uint2 a = *reinterpret_cast<const uint2*>(p), b = *reinterpret_cast<const uint2*>(p + 4);
-  v[0] = bf16_lo(a.x); v[1] = bf16_hi(a.x); v[2] = bf16_lo(a.y); v[3] = bf16_hi(a.y);
-  v[4] = bf16_lo(b.x); v[5] = bf16_hi(b.x); v[6] = bf16_lo(b.y); v[7] = bf16_hi(b.y);
-}
-__device__ __forceinline__ void smem8(const float* p, float (&v)[8]) {
-  const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 4);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-}
-
 // acc.xyzw += v[0..3] * b.xyzw as two packed f32x2 FMAs: per lane the same round-to-nearest FMA
 // as fmaf, in half the issued instructions
 __device__ __forceinline__ void ffma4(float4& acc, const float (&v)[4], const float4& b) {
