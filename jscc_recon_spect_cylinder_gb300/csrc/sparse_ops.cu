@@ -907,8 +907,9 @@ sparse_group_adjoint_taps_kernel(const int32_t* __restrict__ grow, int n_groups,
   }
 }
 
-// ---- sparse_group_coef (bulk): MODE 0 materialise coefficients, 1 grouped, 2 event sums
-template <int MODE, typename TC>
+// ---- sparse_group_coef (bulk): MODE 0 materialise coefficients, 1 grouped, 2 event sums;
+// RAGGED: vc is not a multiple of four, so the last four-value chunk is masked
+template <int MODE, typename TC, bool RAGGED>
 __global__ void __launch_bounds__(kBkThreads, 1)
 sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order, const int32_t* __restrict__ goff,
                               int n_groups, int vc, const float* __restrict__ bq, float* __restrict__ s_ev,
@@ -1043,7 +1044,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
       for (int u = 0; u < kBkQ; ++u) {
         const int c = et * 4 + u * (kBkEvents * 4);
         bv[u] = c < vc ? *reinterpret_cast<const float4*>(b + c) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (c < vc && c + 4 > vc) {  // a coarse grid that is not a multiple of four: the tail is padding
+        if (RAGGED && c < vc && c + 4 > vc) {  // the tail past vc is padding
           if (c + 1 >= vc) bv[u].y = 0.f;
           if (c + 2 >= vc) bv[u].z = 0.f;
           bv[u].w = 0.f;
@@ -1084,7 +1085,7 @@ sparse_group_coef_bulk_kernel(SpRows<TC> rows, const int32_t* __restrict__ order
             for (int k = 0; k < NE; ++k) {
               float v[4];
               smem4(slot(sl[k]), c, v);
-              if (c + 4 > vc) {  // padding past the row (any value) must not reach the dot
+              if (RAGGED && c + 4 > vc) {  // padding past the row (any value) must not reach the dot
 #pragma unroll
                 for (int e = 1; e < 4; ++e)
                   if (c + e >= vc) v[e] = 0.f;
@@ -1992,14 +1993,27 @@ static int grouped_launch(const SpRows<TC>& rows, bool vec_rows, int64_t n_event
   do {                                                                                                           \
     JSCC_GA(TP, XS);                                                                                             \
     if (attr == cudaSuccess) attr = cudaGetLastError();                                                          \
-    if (attr == cudaSuccess)                                                                                     \
-      attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, TC>,                                       \
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                    \
-    if (attr == cudaSuccess)                                                                                     \
-      JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                    \
-                 (sparse_group_coef_bulk_kernel<MODE, TC><<<(unsigned)bk_grid, kBkThreads, bk_smem, st>>>(       \
-                     rows, order, goff, n_groups, (int)vc, bq, s_ev, q, ldq, n_slots, batch, b_bytes, row_bytes, \
-                     slot_off, slot_stride)));                                                                   \
+    if (vc % 4 == 0) {                                                                                           \
+      if (attr == cudaSuccess)                                                                                   \
+        attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, TC, false>,                              \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                  \
+      if (attr == cudaSuccess)                                                                                   \
+        JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                  \
+                   (sparse_group_coef_bulk_kernel<MODE, TC, false><<<(unsigned)bk_grid, kBkThreads, bk_smem,     \
+                                                                     st>>>(                                     \
+                       rows, order, goff, n_groups, (int)vc, bq, s_ev, q, ldq, n_slots, batch, b_bytes,         \
+                       row_bytes, slot_off, slot_stride)));                                                     \
+    } else {                                                                                                     \
+      if (attr == cudaSuccess)                                                                                   \
+        attr = cudaFuncSetAttribute(sparse_group_coef_bulk_kernel<MODE, TC, true>,                               \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bk_smem);                  \
+      if (attr == cudaSuccess)                                                                                   \
+        JSCC_TIMED(MODE == 2 ? "sparse_group_rowsum" : "sparse_group_coef", st,                                  \
+                   (sparse_group_coef_bulk_kernel<MODE, TC, true><<<(unsigned)bk_grid, kBkThreads, bk_smem,      \
+                                                                    st>>>(                                      \
+                       rows, order, goff, n_groups, (int)vc, bq, s_ev, q, ldq, n_slots, batch, b_bytes,         \
+                       row_bytes, slot_off, slot_stride)));                                                     \
+    }                                                                                                            \
   } while (0)
 #define JSCC_GC_K(MODE, KT, TW)                                                                                  \
   do {                                                                                                           \
