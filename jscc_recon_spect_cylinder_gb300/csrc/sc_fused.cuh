@@ -9,17 +9,20 @@
 //     columns' image values and back-projection sums in registers (c = 4 t + 1,920 u);
 //   * a producer warp streams every row's column half into a ring of shared-memory stages
 //     (cp.async.bulk on mbarriers);
-//   * per batch of up to `batch` rows the consumers form their partial dots, reduce them per
-//     warp and then over the warps in warp order after one named barrier, exchange the CTA's
-//     partials with the peer CTA (one 16-byte st.async completing on the peer's mbarrier),
-//     and form f = partial(rank 0) + partial(rank 1) (the same sum, so the same ratio, in both
-//     CTAs), r = proj / max(f, floor), then add r * row to their sums, rows in order;
+//   * per batch of up to `batch` rows (a body compiled per row count) the consumers form their
+//     partial dots, reduce them per warp and then over the warps in warp order after one
+//     named barrier, exchange the CTA's partials with the peer CTA (one 16-byte st.async
+//     completing on the peer's mbarrier), and form f = partial(rank 0) + partial(rank 1) (the
+//     same sum, so the same ratio, in both CTAs), r = proj / max(f, floor), then add r * row
+//     to their sums, rows in order;
 //   * every cluster writes one partial image; sc_reduce_scatter_kernel adds the clusters'
 //     images in cluster order (scaled) to the weight.
 // Every wait is bounded (jscc_set_wait_limit): a CTA that gives up counts it
 // (jscc_take_wait_timeout_count), waits (bounded) for what it still has in flight and leaves
 // through the final cluster barrier with its peer.
 #pragma once
+
+#include <type_traits>
 
 namespace jscc {
 
@@ -134,55 +137,52 @@ sc_fused_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict_
     }
     bool bad = false, aborted = false;
     int par = 0, i = 0;
-    for (int bs = 0; bs < n_rows; bs += batch, par ^= 1, ++i) {
-      const int n = n_rows - bs < batch ? n_rows - bs : batch;
+    // One batch of NB rows from row bs; false when a wait gave up. The body is compiled once
+    // per row count, so a batch issues no instructions for rows it does not hold.
+    auto run_batch = [&](auto nb_tag, int bs) -> bool {
+      constexpr int NB = decltype(nb_tag)::value;
       // this lane's row of the batch: its projection value, read before the dots
       float y_lane = 0.f;
-      if (lane < n) {
+      if (lane < NB) {
         const int64_t b = b0 + bs + lane;
         const int64_t pb = row_idx ? row_idx[b] : b;
         y_lane = proj[pb * ld_proj + r0];
       }
-      int sl[kFsMaxBatch];
+      int sl[NB];
 #pragma unroll
-      for (int k = 0; k < kFsMaxBatch; ++k) sl[k] = (bs + k) % n_stages;
+      for (int k = 0; k < NB; ++k) sl[k] = (bs + k) % n_stages;
 #pragma unroll
-      for (int k = 0; k < kFsMaxBatch; ++k)
-        if (k < n && !bk_wait(full + sl[k], (uint32_t)((bs + k) / n_stages) & 1u, abort_flag, polls)) bad = true;
+      for (int k = 0; k < NB; ++k)
+        if (!bk_wait(full + sl[k], (uint32_t)((bs + k) / n_stages) & 1u, abort_flag, polls)) bad = true;
       // ---- partial dots over this CTA's columns
-      float4 pd[kFsMaxBatch];
+      float4 pd[NB];
 #pragma unroll
-      for (int k = 0; k < kFsMaxBatch; ++k) pd[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < NB; ++k) pd[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
       for (int u = 0; u < kFsQ; ++u) {
         const int c = tid * 4 + u * (kFsConsumers * 4);
         if (c < ncol) {
 #pragma unroll
-          for (int k = 0; k < kFsMaxBatch; ++k)
-            if (k < n) {
-              float v[4];
-              FsRow<T>::get(stage(sl[k]), c, v);
-              const float2 lo = __ffma2_rn(make_float2(v[0], v[1]), make_float2(xv[u].x, xv[u].y),
-                                           make_float2(pd[k].x, pd[k].y));
-              const float2 hi = __ffma2_rn(make_float2(v[2], v[3]), make_float2(xv[u].z, xv[u].w),
-                                           make_float2(pd[k].z, pd[k].w));
-              pd[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
-            }
+          for (int k = 0; k < NB; ++k) {
+            float v[4];
+            FsRow<T>::get(stage(sl[k]), c, v);
+            const float2 lo = __ffma2_rn(make_float2(v[0], v[1]), make_float2(xv[u].x, xv[u].y),
+                                         make_float2(pd[k].x, pd[k].y));
+            const float2 hi = __ffma2_rn(make_float2(v[2], v[3]), make_float2(xv[u].z, xv[u].w),
+                                         make_float2(pd[k].z, pd[k].w));
+            pd[k] = make_float4(lo.x, lo.y, hi.x, hi.y);
+          }
         }
       }
 #pragma unroll
-      for (int k = 0; k < kFsMaxBatch; ++k)
-        if (k < n) {
-          const float f = warp_sum((pd[k].x + pd[k].y) + (pd[k].z + pd[k].w));
-          if (lane == 0) red[(par * kFsConsumerWarps + warp) * kFsMaxBatch + k] = f;
-        }
-      if (role_sync_or(1, kFsConsumers, bad)) {
-        aborted = true;
-        break;
+      for (int k = 0; k < NB; ++k) {
+        const float f = warp_sum((pd[k].x + pd[k].y) + (pd[k].z + pd[k].w));
+        if (lane == 0) red[(par * kFsConsumerWarps + warp) * kFsMaxBatch + k] = f;
       }
+      if (role_sync_or(1, kFsConsumers, bad)) return false;
       // ---- this CTA's partial of row k in lane k (warps in order), to the peer
       float mine = 0.f;
-      if (lane < n)
+      if (lane < NB)
         for (int w = 0; w < kFsConsumerWarps; ++w) mine += red[(par * kFsConsumerWarps + w) * kFsMaxBatch + lane];
       if (warp == 0) {
         const float m0 = __shfl_sync(0xffffffffu, mine, 0), m1 = __shfl_sync(0xffffffffu, mine, 1);
@@ -197,12 +197,9 @@ sc_fused_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict_
       // ---- the peer's partials; f = partial(rank 0) + partial(rank 1) in both CTAs
       const bool got = cf_wait_cluster(xfull + par, (uint32_t)(i >> 1) & 1u, abort_flag, polls);
       if (warp == 0 && lane == 0 && got) waited[par] += 1;
-      if (!__all_sync(0xffffffffu, got)) {
-        aborted = true;
-        break;
-      }
+      if (!__all_sync(0xffffffffu, got)) return false;
       float r_lane = 0.f;
-      if (lane < n) {
+      if (lane < NB) {
         const float theirs = xbuf[par * kFsMaxBatch + lane];
         float f = h == 0 ? mine + theirs : theirs + mine;
         if (use_floor) f = fmaxf(f, floor_v);
@@ -210,29 +207,45 @@ sc_fused_kernel(const T* __restrict__ A, int64_t lda, const int64_t* __restrict_
       }
       // ---- back-projection: acc += r_k * row_k over this thread's columns, rows in order
 #pragma unroll
-      for (int k = 0; k < kFsMaxBatch; ++k)
-        if (k < n) {
-          const float rk = __shfl_sync(0xffffffffu, r_lane, k);
+      for (int k = 0; k < NB; ++k) {
+        const float rk = __shfl_sync(0xffffffffu, r_lane, k);
 #pragma unroll
-          for (int u = 0; u < kFsQ; ++u) {
-            const int c = tid * 4 + u * (kFsConsumers * 4);
-            if (c < ncol) {
-              float v[4];
-              FsRow<T>::get(stage(sl[k]), c, v);
-              const float2 rr = make_float2(rk, rk);
-              const float2 lo = __ffma2_rn(rr, make_float2(v[0], v[1]), make_float2(acc[u].x, acc[u].y));
-              const float2 hi = __ffma2_rn(rr, make_float2(v[2], v[3]), make_float2(acc[u].z, acc[u].w));
-              acc[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
-            }
+        for (int u = 0; u < kFsQ; ++u) {
+          const int c = tid * 4 + u * (kFsConsumers * 4);
+          if (c < ncol) {
+            float v[4];
+            FsRow<T>::get(stage(sl[k]), c, v);
+            const float2 rr = make_float2(rk, rk);
+            const float2 lo = __ffma2_rn(rr, make_float2(v[0], v[1]), make_float2(acc[u].x, acc[u].y));
+            const float2 hi = __ffma2_rn(rr, make_float2(v[2], v[3]), make_float2(acc[u].z, acc[u].w));
+            acc[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
           }
         }
+      }
       // ---- this warp is past its reads of the batch's stages
       __syncwarp();
       if (lane == 0) {
-        if (warp == 0) *used = bs + n;
+        if (warp == 0) *used = bs + NB;
 #pragma unroll
-        for (int k = 0; k < kFsMaxBatch; ++k)
-          if (k < n) mbar_arrive(empty + sl[k]);
+        for (int k = 0; k < NB; ++k) mbar_arrive(empty + sl[k]);
+      }
+      return true;
+    };
+    for (int bs = 0; bs < n_rows; bs += batch, par ^= 1, ++i) {
+      const int n = n_rows - bs < batch ? n_rows - bs : batch;
+      bool ok;
+      if (n == 1) {
+        ok = run_batch(std::integral_constant<int, 1>{}, bs);
+      } else if (n == 2) {
+        ok = run_batch(std::integral_constant<int, 2>{}, bs);
+      } else if (n == 3) {
+        ok = run_batch(std::integral_constant<int, 3>{}, bs);
+      } else {
+        ok = run_batch(std::integral_constant<int, kFsMaxBatch>{}, bs);
+      }
+      if (!ok) {
+        aborted = true;
+        break;
       }
     }
     if (aborted) {
