@@ -1002,7 +1002,11 @@ class JointBench:
         land in are allocated once before the job (a service keeps them resident); the
         matrix, projections and sensitivity are copied first, each subset's sparse rows on a
         second stream, and the first iteration's update of subset k waits for subset k's
-        rows only."""
+        rows only. One untimed job into the same buffers comes first (a service's pinned
+        staging buffers are reused across jobs; the first DMA out of freshly pinned host
+        memory is not representative), then the median of three timed jobs. Every job copies
+        all inputs again, and the copies bump the device buffers' versions, so the group
+        plans and event sums cached on them are rebuilt inside each timed job."""
         from jscc_recon_spect_cylinder_gb300 import ops
 
         w = self.w
@@ -1026,37 +1030,46 @@ class JointBench:
         side = torch.cuda.Stream(self.dev)
         landed = [torch.cuda.Event() for _ in range(w.subsets)]
         main = torch.cuda.current_stream(self.dev)
-        torch.cuda.synchronize(self.dev)
-        t0 = time.perf_counter()
-        for d, h in ((A, hA), (y, hy), (s, hs), (x0, hx0)):
-            d.copy_(h, non_blocking=True)
-        for d, h in zip(sub, hsub):
-            d.copy_(h, non_blocking=True)
-        side.wait_stream(main)
-        with torch.cuda.stream(side):
-            for k in range(w.subsets):
-                ids[k].copy_(hids[k], non_blocking=True)
-                tc[k].copy_(htc[k], non_blocking=True)
-                landed[k].record(side)
-        img = x0
-        for it in range(iters):
-            for k in range(w.subsets):
-                if it == 0:
-                    main.wait_event(landed[k])
-                wt = torch.zeros_like(img)
-                ops.sc_weight(A, y, img, floor=1e-12, scale=w.alpha, out=wt, row_idx=sub[k])
-                ops.sparse_weight_split(ids[k], tc[k], A, w.tables, img, grouped=False, scale=2 - w.alpha, out=wt)
-                img = ops.em_update(img, wt, s, safe=True)
-        out.copy_(img, non_blocking=True)
-        torch.cuda.synchronize(self.dev)
-        sec = time.perf_counter() - t0
+
+        def job():
+            torch.cuda.synchronize(self.dev)
+            t0 = time.perf_counter()
+            for d, h in ((A, hA), (y, hy), (s, hs), (x0, hx0)):
+                d.copy_(h, non_blocking=True)
+            for d, h in zip(sub, hsub):
+                d.copy_(h, non_blocking=True)
+            side.wait_stream(main)
+            with torch.cuda.stream(side):
+                for k in range(w.subsets):
+                    ids[k].copy_(hids[k], non_blocking=True)
+                    tc[k].copy_(htc[k], non_blocking=True)
+                    landed[k].record(side)
+            img = x0
+            for it in range(iters):
+                for k in range(w.subsets):
+                    if it == 0:
+                        main.wait_event(landed[k])
+                    wt = torch.zeros_like(img)
+                    ops.sc_weight(A, y, img, floor=1e-12, scale=w.alpha, out=wt, row_idx=sub[k])
+                    ops.sparse_weight_split(ids[k], tc[k], A, w.tables, img, grouped=False, scale=2 - w.alpha,
+                                            out=wt)
+                    img = ops.em_update(img, wt, s, safe=True)
+            out.copy_(img, non_blocking=True)
+            torch.cuda.synchronize(self.dev)
+            return time.perf_counter() - t0
+
+        job()  # untimed: first use of the pinned staging buffers
+        secs = [job() for _ in range(3)]
+        sec = sorted(secs)[1]
         for t in ids + tc:
             t.record_stream(side)
         return {"value": iters * w.subsets / sec, "unit": "subset-iters/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(w.V * 4),
                 "step": (f"one job: stage inputs into resident device buffers (sparse rows on a second stream, "
                          f"overlapping the first iteration) + {iters} iterations + read image (the sparse T rows "
-                         "are built beforehand by the GPU T builder, outside the timed job)"), "seconds": sec}
+                         "are built beforehand by the GPU T builder, outside the timed job); median of 3 jobs "
+                         "after one untimed job into the same buffers"), "seconds": sec,
+                "seconds_per_job": secs}
 
     def cpu_rate(self, steps=2, warmup=1):
         """The reference's own functions on the host cores (oracle.reference_timing): whole-
