@@ -51,7 +51,9 @@ def _c_weight(A, y, x, row_idx, floor, scale, shrink):
 @pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float32])
 @pytest.mark.parametrize("V,n_det,subset,floor", [
     (36000, 2000, 700, 1e-12),    # the joint configuration's image, a row subset
+    (36000, 2000, 608, None),     # eight rows per cluster: BF16 batches of three, three, two
     (4800, 1500, None, None),     # config-1 image, every row, no floor
+    (4800, 150, None, 1e-12),     # two rows per cluster: one two-row batch each
     (4800, 7, None, 1e-12),       # fewer rows than clusters
     (4804, 300, 150, None),       # not a multiple of the vector width: two-pass kernels
 ])
